@@ -1,0 +1,115 @@
+"""ctypes binding of librq.so (include/rq.h).
+
+The library is the product: there is no Python or CPU implementation of any query behind this
+module.  Importing succeeds without a GPU (the tests check the exports on CPU), but every call
+that needs the device fails with RQ_ECUDA when there is none, and a missing librq.so raises
+ImportError instead of falling back to anything.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "librq.so"
+
+RQ_OK, RQ_EINVAL, RQ_ENOMEM, RQ_ECUDA, RQ_EBUDGET, RQ_ENOTSUP, RQ_ESTATE = range(7)
+LAYOUT_DEFAULT, LAYOUT_STACK, LAYOUT_STACKLESS, LAYOUT_BVH8Q = range(4)
+MODE_STRICT, MODE_FAST = 0, 1
+TIE_LOWER_INDEX, TIE_FIRST_FOUND = 0, 1
+FLAG_REF_COMPAT, FLAG_IGNORE_TRANSPARENT, FLAG_HOST_BUFFERS, FLAG_NO_PERSISTENT = 1, 2, 4, 8
+
+VERTEX_DTYPE = np.dtype([("pos", "<f4", (4,)), ("packed", "<u4", (4,))])
+TRI_DTYPE = np.dtype(("<i4", (4,)))
+STACK_NODE_DTYPE = np.dtype(("<f4", (16,)))
+STACKLESS_NODE_DTYPE = np.dtype(("<f4", (8,)))
+ENTITY_DTYPE = np.dtype([("model", "<f4", (16,)), ("inverse", "<f4", (16,)),
+                         ("node_offset", "<i4"), ("node_count", "<i4"), ("data", "<i4", (14,))])
+RAY_DTYPE = np.dtype([("o", "<f4", (3,)), ("tmin", "<f4"), ("d", "<f4", (3,)), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("w", "<f4"),
+                      ("tri", "<i4"), ("mesh", "<i4"), ("entity", "<i4"), ("iters", "<i4")])
+assert ENTITY_DTYPE.itemsize == 192 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 32
+
+
+class RqOpts(C.Structure):
+    _fields_ = [("layout", C.c_int32), ("mode", C.c_int32), ("tie", C.c_int32),
+                ("flags", C.c_int32), ("block_size", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class RqBuildOpts(C.Structure):
+    _fields_ = [("leaf_size", C.c_int32), ("swap_children", C.c_int32),
+                ("swap_seed", C.c_uint32), ("n_threads", C.c_int32)]
+
+
+class RqBvhInfo(C.Structure):
+    _fields_ = [("n_nodes", C.c_int64), ("n_nodes_used", C.c_int64), ("n_tris", C.c_int64),
+                ("node_bytes", C.c_int32), ("layout", C.c_int32), ("leaf_count", C.c_int64),
+                ("split_fails", C.c_int64), ("build_ms", C.c_double)]
+
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_I32 = C.c_int32
+_S = C.c_int
+
+# name -> (restype, argtypes).  Every symbol declared in include/rq.h appears here.
+SIGNATURES = {
+    "rq_abi_version": (C.c_int, []),
+    "rq_status_string": (C.c_char_p, [_S]),
+    "rq_create": (_S, [C.c_int, C.POINTER(_P)]),
+    "rq_destroy": (_S, [_P]),
+    "rq_last_error": (C.c_char_p, [_P]),
+    "rq_build_bvh": (_S, [_P, _I64, _P, _I64, _P, _I32, _S, C.POINTER(RqBuildOpts), C.POINTER(_P)]),
+    "rq_bvh_info_get": (_S, [_P, C.POINTER(RqBvhInfo)]),
+    "rq_bvh_nodes": (_S, [_P, C.POINTER(_P), C.POINTER(_I64)]),
+    "rq_bvh_triangles": (_S, [_P, C.POINTER(_P), C.POINTER(_I64)]),
+    "rq_bvh_free": (None, [_P]),
+    "rq_scene_validate": (_S, [_S, _P, _I64, _P, _I64, _P, _I64, _P, _I32, C.c_char_p, C.c_size_t]),
+    "rq_scene_create": (_S, [_P, _S, _P, _I64, _P, _I64, _P, _I64, _P, _I32, C.POINTER(_P)]),
+    "rq_scene_set_entities": (_S, [_P, _P, _I32]),
+    "rq_scene_bytes": (_S, [_P, C.POINTER(_I64)]),
+    "rq_scene_destroy": (_S, [_P]),
+    "rq_closest": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
+    "rq_anyhit": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads librq.so once.  Raises ImportError when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run candela_gb300._build.build() "
+                              "(the engine has no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class RqError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+def check(status: int, ctx=None) -> None:
+    if status != RQ_OK:
+        m = lib().rq_last_error(ctx)
+        raise RqError(status, (m or b"").decode() or lib().rq_status_string(status).decode())
+
+
+def ptr(a) -> int:
+    """Address of a numpy array's data or of a torch tensor's storage."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+        return a.ctypes.data
+    return a.data_ptr()

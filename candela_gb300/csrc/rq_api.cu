@@ -1,0 +1,440 @@
+// C ABI implementation: contexts, BVH construction, scene upload and validation, query dispatch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/rq.h"
+#include "bvh_build.h"
+#include "rq_internal.h"
+#include "rq_validate.h"
+
+struct rq_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;       // default stream of the context
+    cudaStream_t pipe[2] = {nullptr, nullptr};  // host-buffer staging pipeline
+    cudaEvent_t ev = nullptr;
+    void* stage_in[2] = {nullptr, nullptr};
+    void* stage_out[2] = {nullptr, nullptr};
+    size_t stage_in_bytes[2] = {0, 0};
+    size_t stage_out_bytes[2] = {0, 0};
+    int* counters = nullptr;  // device work counters for persistent kernels (64 ints)
+    std::string err;
+};
+
+struct rq_bvh {
+    rq::BuildOutput out;
+    int32_t layout = RQ_LAYOUT_BVH2_STACK;
+};
+
+struct rq_scene {
+    rq_ctx* ctx = nullptr;
+    int32_t layout = RQ_LAYOUT_BVH2_STACK;
+    std::vector<float> h_nodes;  // host copy, used to validate entity lists
+    int64_t n_nodes = 0, n_tris = 0, n_verts = 0;
+    float4* d_nodes = nullptr;
+    int4* d_tris = nullptr;
+    float4* d_verts = nullptr;
+    rq_entity* d_ents = nullptr;
+    int32_t n_ents = 0;
+    int32_t ents_cap = 0;
+    int64_t bytes = 0;
+    rq::SceneView view{};
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+rq_status fail(rq_ctx* ctx, rq_status s, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    g_err = msg;
+    return s;
+}
+
+rq_status cuda_fail(rq_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, RQ_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define RQ_CUDA(ctx, call)                                        \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+bool is_identity(const float* m) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            const float want = (c == r) ? 1.0f : 0.0f;
+            uint32_t a, b;
+            std::memcpy(&a, &m[c * 4 + r], 4);
+            std::memcpy(&b, &want, 4);
+            if (a != b) return false;
+        }
+    return true;
+}
+
+rq_status ensure_stage(rq_ctx* ctx, int k, size_t in_bytes, size_t out_bytes) {
+    if (ctx->stage_in_bytes[k] < in_bytes) {
+        if (ctx->stage_in[k]) cudaFree(ctx->stage_in[k]);
+        ctx->stage_in[k] = nullptr;
+        ctx->stage_in_bytes[k] = 0;
+        if (cudaMalloc(&ctx->stage_in[k], in_bytes) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "staging buffer allocation failed");
+        ctx->stage_in_bytes[k] = in_bytes;
+    }
+    if (ctx->stage_out_bytes[k] < out_bytes) {
+        if (ctx->stage_out[k]) cudaFree(ctx->stage_out[k]);
+        ctx->stage_out[k] = nullptr;
+        ctx->stage_out_bytes[k] = 0;
+        if (cudaMalloc(&ctx->stage_out[k], out_bytes) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "staging buffer allocation failed");
+        ctx->stage_out_bytes[k] = out_bytes;
+    }
+    return RQ_OK;
+}
+
+rq_status resolve(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, rq::QueryConfig& q) {
+    rq_opts d{};
+    if (!o) o = &d;
+    q.layout = o->layout == RQ_LAYOUT_DEFAULT ? sc->layout : o->layout;
+    q.mode = o->mode;
+    q.tie_lower = o->tie == RQ_TIE_LOWER_INDEX ? 1 : 0;
+    q.flags = o->flags;
+    q.block = o->block_size;
+    if (o->tie != RQ_TIE_LOWER_INDEX && o->tie != RQ_TIE_FIRST_FOUND)
+        return fail(ctx, RQ_EINVAL, "unknown tie rule");
+    if (q.mode != RQ_MODE_STRICT && q.mode != RQ_MODE_FAST)
+        return fail(ctx, RQ_EINVAL, "unknown mode");
+    if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
+    if (q.mode == RQ_MODE_FAST) return fail(ctx, RQ_ENOTSUP, "fast mode not available");
+    return RQ_OK;
+}
+
+// Host-buffer pipeline: chunks alternate between two streams so that the copy of one chunk
+// overlaps the traversal of the previous one (H2D and D2H use separate copy engines).
+template <class Launch>
+rq_status staged(rq_ctx* ctx, const void* h_in, size_t in_stride, void* h_out, size_t out_stride,
+                 int64_t n, cudaStream_t user, Launch launch) {
+    const int64_t chunk = int64_t(1) << 20;
+    for (int k = 0; k < 2; ++k) {
+        rq_status s = ensure_stage(ctx, k, std::min<int64_t>(n, chunk) * in_stride,
+                                   std::min<int64_t>(n, chunk) * out_stride);
+        if (s != RQ_OK) return s;
+    }
+    RQ_CUDA(ctx, cudaEventRecord(ctx->ev, user));
+    RQ_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[0], ctx->ev, 0));
+    RQ_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[1], ctx->ev, 0));
+    int k = 0;
+    for (int64_t off = 0; off < n; off += chunk, k ^= 1) {
+        const int64_t m = std::min(chunk, n - off);
+        cudaStream_t st = ctx->pipe[k];
+        RQ_CUDA(ctx, cudaMemcpyAsync(ctx->stage_in[k], static_cast<const char*>(h_in) + off * in_stride,
+                                     m * in_stride, cudaMemcpyHostToDevice, st));
+        RQ_CUDA(ctx, launch(ctx->stage_in[k], ctx->stage_out[k], m, st));
+        RQ_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(h_out) + off * out_stride, ctx->stage_out[k],
+                                     m * out_stride, cudaMemcpyDeviceToHost, st));
+    }
+    RQ_CUDA(ctx, cudaStreamSynchronize(ctx->pipe[0]));
+    RQ_CUDA(ctx, cudaStreamSynchronize(ctx->pipe[1]));
+    return RQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rq_abi_version(void) { return RQ_ABI_VERSION; }
+
+const char* rq_status_string(rq_status s) {
+    switch (s) {
+        case RQ_OK: return "ok";
+        case RQ_EINVAL: return "invalid argument";
+        case RQ_ENOMEM: return "out of memory";
+        case RQ_ECUDA: return "CUDA error";
+        case RQ_EBUDGET: return "iteration budget exhausted";
+        case RQ_ENOTSUP: return "not supported";
+        case RQ_ESTATE: return "invalid state";
+    }
+    return "unknown status";
+}
+
+const char* rq_last_error(const rq_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+rq_status rq_create(int device, rq_ctx** out) {
+    if (!out) return fail(nullptr, RQ_EINVAL, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, RQ_ECUDA, "no CUDA device available (the engine has no CPU path)");
+    if (device < 0 || device >= n) return fail(nullptr, RQ_EINVAL, "device index out of range");
+    auto* ctx = new (std::nothrow) rq_ctx;
+    if (!ctx) return fail(nullptr, RQ_ENOMEM, "context allocation failed");
+    ctx->device = device;
+    if ((e = cudaSetDevice(device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->pipe[0], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->pipe[1], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->counters, 64 * sizeof(int))) != cudaSuccess) {
+        rq_status s = cuda_fail(nullptr, e, "context setup");
+        rq_destroy(ctx);
+        return s;
+    }
+    *out = ctx;
+    return RQ_OK;
+}
+
+rq_status rq_destroy(rq_ctx* ctx) {
+    if (!ctx) return RQ_OK;
+    cudaSetDevice(ctx->device);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->stage_in[k]) cudaFree(ctx->stage_in[k]);
+        if (ctx->stage_out[k]) cudaFree(ctx->stage_out[k]);
+        if (ctx->pipe[k]) cudaStreamDestroy(ctx->pipe[k]);
+    }
+    if (ctx->counters) cudaFree(ctx->counters);
+    if (ctx->ev) cudaEventDestroy(ctx->ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RQ_OK;
+}
+
+// ---- BVH construction ----------------------------------------------------------------------
+
+rq_status rq_build_bvh(const rq_vertex* verts, int64_t n_verts, const uint32_t* indices,
+                       int64_t n_indices, const int32_t* mesh_ids, int32_t tri_offset,
+                       rq_layout layout, const rq_build_opts* opts, rq_bvh** out) {
+    if (!out) return fail(nullptr, RQ_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (!verts || !indices || n_verts <= 0 || n_indices <= 0 || n_indices % 3 != 0)
+        return fail(nullptr, RQ_EINVAL, "vertex/index arrays empty or not a multiple of 3");
+    if (layout != RQ_LAYOUT_BVH2_STACK && layout != RQ_LAYOUT_BVH2_STACKLESS)
+        return fail(nullptr, RQ_EINVAL, "layout must be BVH2_STACK or BVH2_STACKLESS");
+    if (tri_offset < 0) return fail(nullptr, RQ_EINVAL, "tri_offset < 0");
+    rq_build_opts d{};
+    if (!opts) opts = &d;
+    rq::BuildInput in{};
+    in.vert_records = reinterpret_cast<const float*>(verts);
+    in.n_verts = n_verts;
+    in.indices = indices;
+    in.n_tris = n_indices / 3;
+    in.mesh_ids = mesh_ids;
+    in.tri_offset = tri_offset;
+    in.leaf_size = opts->leaf_size == 0 ? 2 : opts->leaf_size;
+    in.layout = layout == RQ_LAYOUT_BVH2_STACK ? 0 : 1;
+    in.swap_children = opts->swap_children;
+    in.swap_seed = opts->swap_seed;
+    in.n_threads = opts->n_threads;
+    auto* b = new (std::nothrow) rq_bvh;
+    if (!b) return fail(nullptr, RQ_ENOMEM, "bvh allocation failed");
+    b->layout = layout;
+    int r;
+    try {
+        r = rq::build_bvh(in, b->out);
+    } catch (const std::bad_alloc&) {
+        delete b;
+        return fail(nullptr, RQ_ENOMEM, "host allocation failed during BVH build");
+    }
+    if (r != 0) {
+        delete b;
+        return fail(nullptr, RQ_EINVAL,
+                    "invalid build input (leaf size 1..15, index < n_verts, < 2^27 triangles, "
+                    "stack layout needs more triangles than one leaf)");
+    }
+    *out = b;
+    return RQ_OK;
+}
+
+rq_status rq_bvh_info_get(const rq_bvh* b, rq_bvh_info* info) {
+    if (!b || !info) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    info->n_nodes = b->out.n_nodes;
+    info->n_nodes_used = b->out.n_nodes_used;
+    info->n_tris = static_cast<int64_t>(b->out.tris.size() / 4);
+    info->node_bytes = b->layout == RQ_LAYOUT_BVH2_STACK ? 64 : 32;
+    info->layout = b->layout;
+    info->leaf_count = b->out.leaf_count;
+    info->split_fails = b->out.split_fails;
+    info->build_ms = b->out.build_ms;
+    return RQ_OK;
+}
+
+rq_status rq_bvh_nodes(const rq_bvh* b, const void** nodes, int64_t* n_nodes) {
+    if (!b || !nodes || !n_nodes) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    *nodes = b->out.nodes.data();
+    *n_nodes = b->out.n_nodes;
+    return RQ_OK;
+}
+
+rq_status rq_bvh_triangles(const rq_bvh* b, const rq_triangle** tris, int64_t* n_tris) {
+    if (!b || !tris || !n_tris) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    *tris = reinterpret_cast<const rq_triangle*>(b->out.tris.data());
+    *n_tris = static_cast<int64_t>(b->out.tris.size() / 4);
+    return RQ_OK;
+}
+
+void rq_bvh_free(rq_bvh* b) { delete b; }
+
+// ---- Scene -----------------------------------------------------------------------------------
+
+rq_status rq_scene_validate(rq_layout layout, const rq_vertex* verts, int64_t n_verts,
+                            const rq_triangle* tris, int64_t n_tris, const void* nodes,
+                            int64_t n_nodes, const rq_entity* ents, int32_t n_ents, char* msg,
+                            size_t msg_len) {
+    std::string why;
+    const bool ok = rq::validate_scene(layout, verts, n_verts, tris, n_tris, nodes, n_nodes, ents,
+                                       n_ents, why);
+    if (msg && msg_len) {
+        std::snprintf(msg, msg_len, "%s", why.c_str());
+    }
+    if (!ok) return fail(nullptr, RQ_EINVAL, why);
+    return RQ_OK;
+}
+
+rq_status rq_scene_create(rq_ctx* ctx, rq_layout layout, const rq_vertex* verts, int64_t n_verts,
+                          const rq_triangle* tris, int64_t n_tris, const void* nodes,
+                          int64_t n_nodes, const rq_entity* ents, int32_t n_ents,
+                          rq_scene** out) {
+    if (!ctx || !out) return fail(ctx, RQ_EINVAL, "NULL context or out");
+    *out = nullptr;
+    std::string why;
+    if (!rq::validate_scene(layout, verts, n_verts, tris, n_tris, nodes, n_nodes, ents, n_ents, why))
+        return fail(ctx, RQ_EINVAL, why);
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    auto* sc = new (std::nothrow) rq_scene;
+    if (!sc) return fail(ctx, RQ_ENOMEM, "scene allocation failed");
+    sc->ctx = ctx;
+    sc->layout = layout;
+    sc->n_nodes = n_nodes;
+    sc->n_tris = n_tris;
+    sc->n_verts = n_verts;
+    const size_t node_bytes = layout == RQ_LAYOUT_BVH2_STACK ? 64 : 32;
+    sc->h_nodes.assign(static_cast<const float*>(nodes),
+                       static_cast<const float*>(nodes) + n_nodes * (node_bytes / 4));
+    const size_t nb = node_bytes * n_nodes, tb = 16 * n_tris, vb = 32 * n_verts;
+    cudaError_t e;
+    if ((e = cudaMalloc(&sc->d_nodes, nb)) != cudaSuccess || (e = cudaMalloc(&sc->d_tris, tb)) != cudaSuccess ||
+        (e = cudaMalloc(&sc->d_verts, vb)) != cudaSuccess) {
+        rq_scene_destroy(sc);
+        return fail(ctx, RQ_ENOMEM, std::string("scene device allocation: ") + cudaGetErrorString(e));
+    }
+    sc->bytes = static_cast<int64_t>(nb + tb + vb);
+    if ((e = cudaMemcpy(sc->d_nodes, nodes, nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(sc->d_tris, tris, tb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(sc->d_verts, verts, vb, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        rq_scene_destroy(sc);
+        return cuda_fail(ctx, e, "scene upload");
+    }
+    sc->view.nodes = sc->d_nodes;
+    sc->view.n_nodes = n_nodes;
+    sc->view.tris = sc->d_tris;
+    sc->view.n_tris = n_tris;
+    sc->view.verts = sc->d_verts;
+    sc->view.n_verts = n_verts;
+    sc->view.layout = layout;
+    rq_status s = rq_scene_set_entities(sc, ents, n_ents);
+    if (s != RQ_OK) {
+        rq_scene_destroy(sc);
+        return s;
+    }
+    *out = sc;
+    return RQ_OK;
+}
+
+rq_status rq_scene_set_entities(rq_scene* sc, const rq_entity* ents, int32_t n_ents) {
+    if (!sc) return fail(nullptr, RQ_EINVAL, "NULL scene");
+    rq_ctx* ctx = sc->ctx;
+    std::string why;
+    if (!rq::validate_entities(sc->layout, sc->h_nodes.data(), sc->n_nodes, sc->n_tris, ents,
+                               n_ents, why))
+        return fail(ctx, RQ_EINVAL, why);
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n_ents > sc->ents_cap) {
+        if (sc->d_ents) cudaFree(sc->d_ents);
+        sc->d_ents = nullptr;
+        sc->ents_cap = 0;
+        if (cudaMalloc(&sc->d_ents, sizeof(rq_entity) * n_ents) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "entity buffer allocation failed");
+        sc->ents_cap = n_ents;
+    }
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_ents, ents, sizeof(rq_entity) * n_ents, cudaMemcpyHostToDevice));
+    sc->n_ents = n_ents;
+    sc->view.ents = sc->d_ents;
+    sc->view.n_ents = n_ents;
+    bool ident = true;
+    for (int i = 0; i < n_ents; ++i) ident = ident && is_identity(ents[i].inverse);
+    sc->view.all_identity = ident ? 1 : 0;
+    return RQ_OK;
+}
+
+rq_status rq_scene_bytes(const rq_scene* sc, int64_t* bytes) {
+    if (!sc || !bytes) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap;
+    return RQ_OK;
+}
+
+rq_status rq_scene_destroy(rq_scene* sc) {
+    if (!sc) return RQ_OK;
+    if (sc->ctx) cudaSetDevice(sc->ctx->device);
+    if (sc->d_nodes) cudaFree(sc->d_nodes);
+    if (sc->d_tris) cudaFree(sc->d_tris);
+    if (sc->d_verts) cudaFree(sc->d_verts);
+    if (sc->d_ents) cudaFree(sc->d_ents);
+    delete sc;
+    return RQ_OK;
+}
+
+// ---- Queries --------------------------------------------------------------------------------
+
+rq_status rq_closest(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t n, rq_hit* hits,
+                     const rq_opts* opts, void* stream) {
+    if (!ctx || !sc) return fail(ctx, RQ_EINVAL, "NULL context or scene");
+    if (n < 0 || (n > 0 && (!rays || !hits))) return fail(ctx, RQ_EINVAL, "bad ray/hit arrays");
+    if (sc->ctx != ctx) return fail(ctx, RQ_EINVAL, "scene belongs to another context");
+    rq::QueryConfig q{};
+    rq_status s = resolve(ctx, sc, opts, q);
+    if (s != RQ_OK) return s;
+    if (n == 0) return RQ_OK;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const rq::SceneView view = sc->view;
+    if (q.flags & RQ_FLAG_HOST_BUFFERS) {
+        return staged(ctx, rays, sizeof(rq_ray), hits, sizeof(rq_hit), n, st,
+                      [&](void* din, void* dout, int64_t m, cudaStream_t cs) {
+                          return rq::launch_closest(view, q, static_cast<const rq_ray*>(din), m,
+                                                    static_cast<rq_hit*>(dout), nullptr, cs);
+                      });
+    }
+    RQ_CUDA(ctx, rq::launch_closest(view, q, rays, n, hits, ctx->counters, st));
+    return RQ_OK;
+}
+
+rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t n,
+                    uint8_t* occluded, const rq_opts* opts, void* stream) {
+    if (!ctx || !sc) return fail(ctx, RQ_EINVAL, "NULL context or scene");
+    if (n < 0 || (n > 0 && (!rays || !occluded))) return fail(ctx, RQ_EINVAL, "bad ray/result arrays");
+    if (sc->ctx != ctx) return fail(ctx, RQ_EINVAL, "scene belongs to another context");
+    rq::QueryConfig q{};
+    rq_status s = resolve(ctx, sc, opts, q);
+    if (s != RQ_OK) return s;
+    if (n == 0) return RQ_OK;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const rq::SceneView view = sc->view;
+    if (q.flags & RQ_FLAG_HOST_BUFFERS) {
+        return staged(ctx, rays, sizeof(rq_ray), occluded, 1, n, st,
+                      [&](void* din, void* dout, int64_t m, cudaStream_t cs) {
+                          return rq::launch_anyhit(view, q, static_cast<const rq_ray*>(din), m,
+                                                   static_cast<uint8_t*>(dout), nullptr, cs);
+                      });
+    }
+    RQ_CUDA(ctx, rq::launch_anyhit(view, q, rays, n, occluded, ctx->counters, st));
+    return RQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,44 @@
+// Internal types shared by the host API (rq_api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/rq.h"
+
+namespace rq {
+
+// Device view of an uploaded scene.  All buffers keep the reference byte layouts; derived
+// layouts (compact triangle records, BVH8) are added next to them.
+struct SceneView {
+    const float4* nodes;      // stack: 4 float4 per node; stackless: 2 float4 per node
+    int64_t n_nodes;
+    const int4* tris;         // {i0, i1, i2, mesh}
+    int64_t n_tris;
+    const float4* verts;      // 2 float4 per vertex; .xyz of the first = position
+    int64_t n_verts;
+    const rq_entity* ents;
+    int32_t n_ents;
+    int32_t layout;           // RQ_LAYOUT_BVH2_STACK / RQ_LAYOUT_BVH2_STACKLESS
+    int32_t all_identity;     // every entity's inverse matrix is exactly the identity
+    int32_t pad;
+    // Fast-mode triangle records in leaf order: {v0.xyz, mesh}, {e1.xyz, i0}, {e2.xyz, 0}.
+    const float4* tri_fast;
+};
+
+// Query configuration resolved by the host API.
+struct QueryConfig {
+    int32_t layout;
+    int32_t mode;
+    int32_t tie_lower;   // 1 = lower-index rule
+    int32_t flags;
+    int32_t block;
+};
+
+// Kernel launchers (rq_kernels.cu).  Return cudaGetLastError() after the launch.
+cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
+                           rq_hit* hits, int* work_counter, cudaStream_t st);
+cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
+                          uint8_t* occluded, int* work_counter, cudaStream_t st);
+
+}  // namespace rq

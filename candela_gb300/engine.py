@@ -1,0 +1,262 @@
+"""Python host side of the ray-query engine, over the C ABI (include/rq.h).
+
+`RayIntersector` mirrors the reference's host wrapper `Candela::RayIntersector<T>`
+(Source/Core/BVH/Intersector.h:60-451): objects are added one at a time (AddObject builds the
+object's BVH and appends its nodes / triangles / vertices to global buffers, rebasing vertex
+indices, :169-198), entities instance objects with a model matrix (PushEntity, :200-216),
+BufferEntities / BufferData upload (:226-351), and queries run on the device.  Queries accept
+device tensors (torch, resident in HBM) or host numpy arrays (copied inside the call).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import (ENTITY_DTYPE, HIT_DTYPE, RAY_DTYPE, STACK_NODE_DTYPE, STACKLESS_NODE_DTYPE,
+                   TRI_DTYPE, VERTEX_DTYPE, check, lib, ptr)
+
+STACK, STACKLESS, BVH8Q = L.LAYOUT_STACK, L.LAYOUT_STACKLESS, L.LAYOUT_BVH8Q
+
+
+@dataclass
+class BVH:
+    """Host buffers of one object's BVH, in the reference's byte layout."""
+    layout: int
+    nodes: np.ndarray       # STACK_NODE_DTYPE or STACKLESS_NODE_DTYPE
+    tris: np.ndarray        # TRI_DTYPE
+    n_nodes_used: int
+    leaf_count: int
+    split_fails: int
+    build_ms: float
+
+
+def build_bvh(vertices: np.ndarray, indices: np.ndarray, mesh_ids=None, tri_offset: int = 0,
+              layout: int = STACK, leaf_size: int = 2, swap_children: bool = False,
+              swap_seed: int = 0, n_threads: int = 0) -> BVH:
+    """BVH::BuildBVH for one object (BVHConstructor.cpp:951-1108) via rq_build_bvh."""
+    v = np.ascontiguousarray(vertices, dtype=VERTEX_DTYPE)
+    idx = np.ascontiguousarray(indices, dtype=np.uint32).ravel()
+    mid = None if mesh_ids is None else np.ascontiguousarray(mesh_ids, dtype=np.int32)
+    opts = L.RqBuildOpts(leaf_size, int(swap_children), swap_seed & 0xFFFFFFFF, n_threads)
+    h = C.c_void_p()
+    check(lib().rq_build_bvh(ptr(v), v.shape[0], ptr(idx), idx.size, ptr(mid), tri_offset, layout,
+                             C.byref(opts), C.byref(h)))
+    try:
+        info = L.RqBvhInfo()
+        check(lib().rq_bvh_info_get(h, C.byref(info)))
+        np_ = C.c_void_p()
+        nn = C.c_int64()
+        check(lib().rq_bvh_nodes(h, C.byref(np_), C.byref(nn)))
+        dt = STACK_NODE_DTYPE if layout == STACK else STACKLESS_NODE_DTYPE
+        nodes = np.frombuffer(C.string_at(np_.value, nn.value * dt.itemsize), dtype=np.float32)
+        nodes = nodes.reshape(nn.value, dt.itemsize // 4).copy()
+        tp = C.c_void_p()
+        nt = C.c_int64()
+        check(lib().rq_bvh_triangles(h, C.byref(tp), C.byref(nt)))
+        tris = np.frombuffer(C.string_at(tp.value, nt.value * 16), dtype=np.int32).reshape(-1, 4).copy()
+        return BVH(layout, nodes, tris, info.n_nodes_used, info.leaf_count, info.split_fails,
+                   info.build_ms)
+    finally:
+        lib().rq_bvh_free(h)
+
+
+def validate_scene(layout, vertices, tris, nodes, entities) -> tuple[bool, str]:
+    """rq_scene_validate: host-only check of the buffers a scene upload would receive."""
+    msg = C.create_string_buffer(512)
+    v = np.ascontiguousarray(vertices)
+    t = np.ascontiguousarray(tris, dtype=np.int32)
+    n = np.ascontiguousarray(nodes, dtype=np.float32)
+    e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
+    s = lib().rq_scene_validate(layout, ptr(v), v.shape[0], ptr(t), t.shape[0], ptr(n), n.shape[0],
+                                ptr(e), e.shape[0], msg, 512)
+    return s == L.RQ_OK, msg.value.decode()
+
+
+def identity_entity(node_offset: int, node_count: int, emissive: float = 0.0,
+                    alpha: float = 1.0, model=None) -> np.ndarray:
+    """A BVHEntity record (Intersector.h:43-49, PushEntity :200-216)."""
+    e = np.zeros(1, dtype=ENTITY_DTYPE)
+    m = np.eye(4, dtype=np.float32) if model is None else np.asarray(model, dtype=np.float32)
+    inv = np.linalg.inv(m.astype(np.float64)).astype(np.float32) if model is not None else m
+    e["model"] = m.T.ravel()      # glm column-major
+    e["inverse"] = inv.T.ravel()
+    e["node_offset"] = node_offset
+    e["node_count"] = node_count
+    e["data"][0, 0] = np.float32(emissive).view(np.int32)
+    e["data"][0, 1] = np.float32(alpha).view(np.int32)
+    return e
+
+
+class Context:
+    """rq_ctx on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.handle = C.c_void_p()
+        check(lib().rq_create(device, C.byref(self.handle)))
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            lib().rq_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def scene(self, layout, vertices, tris, nodes, entities) -> "Scene":
+        return Scene(self, layout, vertices, tris, nodes, entities)
+
+
+def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0) -> L.RqOpts:
+    return L.RqOpts(layout, mode, tie, flags, block_size, (C.c_int32 * 3)())
+
+
+class Scene:
+    """Device-resident scene (rq_scene): global vertex / triangle / node buffers + entities."""
+
+    def __init__(self, ctx: Context, layout, vertices, tris, nodes, entities):
+        self.ctx = ctx
+        self.layout = layout
+        v = np.ascontiguousarray(vertices)
+        t = np.ascontiguousarray(tris, dtype=np.int32)
+        n = np.ascontiguousarray(nodes, dtype=np.float32)
+        e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
+        self.handle = C.c_void_p()
+        check(lib().rq_scene_create(ctx.handle, layout, ptr(v), v.shape[0], ptr(t), t.shape[0],
+                                    ptr(n), n.shape[0], ptr(e), e.shape[0], C.byref(self.handle)),
+              ctx.handle)
+
+    def set_entities(self, entities):
+        e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
+        check(lib().rq_scene_set_entities(self.handle, ptr(e), e.shape[0]), self.ctx.handle)
+
+    def device_bytes(self) -> int:
+        b = C.c_int64()
+        check(lib().rq_scene_bytes(self.handle, C.byref(b)))
+        return b.value
+
+    def close(self):
+        if self.handle:
+            lib().rq_scene_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- queries -----------------------------------------------------------------------------
+    def closest(self, rays, hits=None, *, layout=0, mode=0, tie=0, flags=0, block_size=0,
+                stream=None):
+        """Closest hit.  `rays` is a numpy RAY_DTYPE array (host path, copies inside the call)
+        or a torch uint8/float tensor on the device holding 32-byte rays."""
+        host = isinstance(rays, np.ndarray)
+        n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
+        if hits is None:
+            if host:
+                hits = np.empty(n, dtype=HIT_DTYPE)
+            else:
+                import torch
+                hits = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
+        f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
+        o = _opts(layout, mode, tie, f, block_size)
+        check(lib().rq_closest(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), C.byref(o),
+                               stream), self.ctx.handle)
+        return hits
+
+    def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, stream=None):
+        host = isinstance(rays, np.ndarray)
+        n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
+        if out is None:
+            if host:
+                out = np.empty(n, dtype=np.uint8)
+            else:
+                import torch
+                out = torch.empty(n, dtype=torch.uint8, device=rays.device)
+        f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
+        o = _opts(layout, mode, 0, f, block_size)
+        check(lib().rq_anyhit(self.ctx.handle, self.handle, ptr(rays), n, ptr(out), C.byref(o),
+                              stream), self.ctx.handle)
+        return out
+
+
+class RayIntersector:
+    """Mirror of Candela::RayIntersector<T> (Intersector.h:60-451) over the C ABI.
+
+    layout: STACK (RayIntersector<FlattenedStackNode>) or STACKLESS
+    (RayIntersector<FlattenedNode>)."""
+
+    def __init__(self, layout: int = STACK, leaf_size: int = 2, swap_children: bool = False,
+                 swap_seed: int = 0):
+        self.layout = layout
+        self.leaf_size = leaf_size
+        self.swap_children = swap_children
+        self.swap_seed = swap_seed
+        self.nodes = []          # m_BVHNodes
+        self.vertices = []       # m_BVHVertices
+        self.triangles = []      # m_BVHTriangles
+        self._n_nodes = 0
+        self._n_tris = 0
+        self._index_offset = 0   # m_IndexOffset
+        self.object_data = {}    # m_ObjectData: id -> (tri offset, vertex offset, node offset, count)
+        self._pending = []       # m_Entities
+        self.entities = np.zeros(0, dtype=ENTITY_DTYPE)  # m_BVHEntities
+        self.scene: Scene | None = None
+
+    def add_object(self, object_id: int, meshes) -> None:
+        """AddObject (:169-198).  `meshes`: list of scenes.Mesh (merged like BuildBVH :981-1002:
+        indices offset by the running vertex count, one mesh id per triangle)."""
+        verts, idx, mids, off = [], [], [], 0
+        for m in meshes:
+            verts.append(m.vertices)
+            idx.append(m.indices.astype(np.uint64) + off)
+            mids.append(m.mesh_ids)
+            off += m.vertices.shape[0]
+        v = np.concatenate(verts)
+        bvh = build_bvh(v, np.concatenate(idx).astype(np.uint32), np.concatenate(mids),
+                        tri_offset=self._n_tris, layout=self.layout, leaf_size=self.leaf_size,
+                        swap_children=self.swap_children, swap_seed=self.swap_seed)
+        self.object_data[object_id] = (self._n_tris, sum(x.shape[0] for x in self.vertices),
+                                       self._n_nodes, bvh.nodes.shape[0])
+        tris = bvh.tris.copy()
+        tris[:, :3] += self._index_offset
+        self.vertices.append(v)
+        self.nodes.append(bvh.nodes)
+        self.triangles.append(tris)
+        self._n_nodes += bvh.nodes.shape[0]
+        self._n_tris += tris.shape[0]
+        self._index_offset += v.shape[0]
+
+    def push_entity(self, object_id: int, model=None, emissive: float = 0.0,
+                    translucency: float = 0.0) -> None:
+        """PushEntity (:200-216).  Raises like the reference when the object was never added."""
+        if object_id not in self.object_data:
+            raise KeyError("Trying to push entity whose parent object hasn't been added to global BVH")
+        _, _, noff, ncount = self.object_data[object_id]
+        self._pending.append(identity_entity(noff, ncount, emissive, 1.0 - translucency, model))
+
+    def buffer_entities(self) -> None:
+        """BufferEntities (:226-239)."""
+        self.entities = (np.concatenate(self._pending) if self._pending
+                         else np.zeros(0, dtype=ENTITY_DTYPE))
+        self._pending = []
+        if self.scene is not None:
+            self.scene.set_entities(self.entities)
+
+    def buffer_data(self, ctx: Context) -> Scene:
+        """BufferData (:321-351): uploads the global buffers (and the current entities)."""
+        self.scene = ctx.scene(self.layout, np.concatenate(self.vertices),
+                               np.concatenate(self.triangles), np.concatenate(self.nodes),
+                               self.entities)
+        return self.scene
+
+    def global_buffers(self):
+        return (np.concatenate(self.vertices), np.concatenate(self.triangles),
+                np.concatenate(self.nodes), self.entities)

@@ -1,0 +1,235 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY.
+
+ctypes wrappers of the checkers built by oracle/Makefile:
+  * liboracle.so  — CPU restatement of the reference traversal (rq_oracle.cpp);
+  * librefbvh.so  — the reference BVH constructor compiled unmodified (only where the reference
+                    source tree is mounted; absent on the GPU hosts).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liboracle.so"
+REF_SO = HERE / "_ref" / "librefbvh.so"
+REF_LEAF4_SO = HERE / "_ref" / "librefbvh_leaf4.so"
+REFERENCE_ROOT = Path(os.environ.get("RQ_REFERENCE_ROOT", "/root/reference"))
+
+RAY_DTYPE = np.dtype([("o", "<f4", (3,)), ("tmin", "<f4"), ("d", "<f4", (3,)), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("w", "<f4"),
+                      ("tri", "<i4"), ("mesh", "<i4"), ("entity", "<i4"), ("iters", "<i4")])
+
+ORC_STACK, ORC_STACKLESS = 0, 1
+ORC_TIE_FIRST_FOUND, ORC_TIE_LOWER_INDEX = 0, 1
+ORC_FLAG_REF_COMPAT, ORC_FLAG_IGNORE_TRANSPARENT = 1, 2
+
+
+def build(reference: bool | None = None) -> None:
+    """Builds liboracle.so; also the reference-builder harness when the reference is present."""
+    targets = ["oracle"]
+    if reference is None:
+        reference = (REFERENCE_ROOT / "Source" / "Core" / "BVH" / "BVHConstructor.cpp").exists()
+    if reference:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", str(HERE), f"REF={REFERENCE_ROOT}", *targets], check=True)
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("n_nodes", C.c_int64), ("tris", C.c_void_p),
+                ("verts", C.c_void_p), ("ents", C.c_void_p), ("n_ents", C.c_int32),
+                ("layout", C.c_int32)]
+
+
+_orc = None
+
+
+def orc() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        if not ORACLE_SO.exists():
+            build(reference=False)
+        L = C.CDLL(str(ORACLE_SO))
+        P, I64, I32 = C.c_void_p, C.c_int64, C.c_int32
+        sp = C.POINTER(OrcScene)
+        L.orc_closest.argtypes = [sp, P, I64, P, C.c_int, C.c_int, C.c_int, P]
+        L.orc_anyhit.argtypes = [sp, P, I64, P, C.c_int, P, P]
+        L.orc_ray_triangle.argtypes = [P] * 6
+        L.orc_ray_bounds_stack.argtypes = [P, P, P, P, C.c_float]
+        L.orc_ray_bounds_stack.restype = C.c_float
+        L.orc_ray_bounds_stackless.argtypes = [P, P, P, P, C.c_float, C.c_float]
+        L.orc_ray_bounds_stackless.restype = C.c_float
+        L.orc_barycentrics.argtypes = [P] * 5
+        L.orc_gi_raygen.argtypes = [sp, P, P, I64, I32, C.c_uint32, C.c_float, C.c_float, I32,
+                                    C.c_int, P]
+        L.orc_shade.argtypes = [sp, P, P, I64, P, P, I32, P, P, P, I32, C.c_int, P]
+        L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
+        L.orc_pcg_hash.argtypes = [C.c_uint32]
+        L.orc_pcg_hash.restype = C.c_uint32
+        L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        _orc = L
+    return _orc
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleScene:
+    """Keeps the numpy buffers alive for the C struct that points into them."""
+
+    def __init__(self, layout: int, vertices, tris, nodes, entities):
+        self.vertices = np.ascontiguousarray(vertices)
+        self.tris = np.ascontiguousarray(tris, dtype=np.int32)
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float32)
+        self.entities = np.ascontiguousarray(entities)
+        self.layout = layout  # ORC_STACK / ORC_STACKLESS
+        self.s = OrcScene(_p(self.nodes), self.nodes.shape[0], _p(self.tris), _p(self.vertices),
+                          _p(self.entities), self.entities.shape[0], layout)
+
+    def closest(self, rays, tie=ORC_TIE_LOWER_INDEX, flags=0, nthreads=None, tri_tests=False):
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.empty(rays.shape[0], dtype=HIT_DTYPE)
+        tt = np.empty(rays.shape[0], dtype=np.int32) if tri_tests else None
+        orc().orc_closest(C.byref(self.s), _p(rays), rays.shape[0], _p(hits), tie, flags,
+                          nthreads or os.cpu_count() or 1, _p(tt))
+        return (hits, tt) if tri_tests else hits
+
+    def anyhit(self, rays, nthreads=None, counters=False):
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        occ = np.empty(rays.shape[0], dtype=np.uint8)
+        it = np.empty(rays.shape[0], dtype=np.int32) if counters else None
+        tt = np.empty(rays.shape[0], dtype=np.int32) if counters else None
+        orc().orc_anyhit(C.byref(self.s), _p(rays), rays.shape[0], _p(occ),
+                         nthreads or os.cpu_count() or 1, _p(it), _p(tt))
+        return (occ, it, tt) if counters else occ
+
+    def gi_raygen(self, primary, hits, spp, seed, origin_offset, ray_tmax=1000000.0,
+                  normal_mode=0, nthreads=None):
+        primary = np.ascontiguousarray(primary, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.empty(primary.shape[0] * spp, dtype=RAY_DTYPE)
+        orc().orc_gi_raygen(C.byref(self.s), _p(primary), _p(hits), primary.shape[0], spp,
+                            seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode,
+                            nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def shadow_raygen(self, rays, hits, sun_dir, origin_offset, normal_mode=0, nthreads=None):
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.empty(rays.shape[0], dtype=RAY_DTYPE)
+        sd = np.asarray(sun_dir, dtype=np.float32)
+        orc().orc_shadow_raygen(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(sd),
+                                origin_offset, normal_mode, nthreads or os.cpu_count() or 1,
+                                _p(out))
+        return out
+
+    def shade(self, rays, hits, shadow_lit, albedo, sun_dir, sun_color, sky_color,
+              normal_mode=0, nthreads=None):
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        alb = np.ascontiguousarray(albedo, dtype=np.float32).reshape(-1, 3)
+        lit = None if shadow_lit is None else np.ascontiguousarray(shadow_lit, dtype=np.uint8)
+        out = np.empty((rays.shape[0], 4), dtype=np.float32)
+        f3 = lambda x: np.asarray(x, dtype=np.float32)  # noqa: E731
+        sd, sc, sk = f3(sun_dir), f3(sun_color), f3(sky_color)
+        orc().orc_shade(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(lit), _p(alb),
+                        alb.shape[0], _p(sd), _p(sc), _p(sk), normal_mode,
+                        nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+
+def ray_triangle(ro, rd, v0, v1, v2):
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float32)  # noqa: E731
+    a = [f(x) for x in (ro, rd, v0, v1, v2)]
+    out = np.zeros(3, dtype=np.float32)
+    orc().orc_ray_triangle(*[_p(x) for x in a], _p(out))
+    return out
+
+
+def ray_bounds_stack(ro, invdir, bmin, bmax, maxt):
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float32)  # noqa: E731
+    a = [f(x) for x in (ro, invdir, bmin, bmax)]
+    return orc().orc_ray_bounds_stack(*[_p(x) for x in a], maxt)
+
+
+def ray_bounds_stackless(bmin, bmax, ro, invdir, t_min, t_max):
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float32)  # noqa: E731
+    a = [f(x) for x in (bmin, bmax, ro, invdir)]
+    return orc().orc_ray_bounds_stackless(*[_p(x) for x in a], t_min, t_max)
+
+
+def barycentrics(p, a, b, c):
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float32)  # noqa: E731
+    x = [f(v) for v in (p, a, b, c)]
+    out = np.zeros(3, dtype=np.float32)
+    orc().orc_barycentrics(*[_p(v) for v in x], _p(out))
+    return out
+
+
+def pcg_hash(x: int) -> int:
+    return orc().orc_pcg_hash(x & 0xFFFFFFFF)
+
+
+def sincos_turns(x: float):
+    s, c = C.c_float(), C.c_float()
+    orc().orc_sincos_turns(x, C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+# ---- reference BVH constructor (compiled from the mounted reference tree) -----------------
+
+_ref = {}
+
+
+def ref_available(leaf4: bool = False) -> bool:
+    so = REF_LEAF4_SO if leaf4 else REF_SO
+    if not so.exists() and (REFERENCE_ROOT / "Source").exists():
+        try:
+            build(reference=True)
+        except Exception:
+            return False
+    return so.exists()
+
+
+def _refl(leaf4: bool) -> C.CDLL:
+    key = "leaf4" if leaf4 else "leaf2"
+    if key not in _ref:
+        L = C.CDLL(str(REF_LEAF4_SO if leaf4 else REF_SO))
+        L.refbvh_build.restype = C.c_void_p
+        L.refbvh_build.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                   C.c_void_p, C.c_int32, C.c_int, C.c_uint32]
+        L.refbvh_info.argtypes = [C.c_void_p] + [C.POINTER(C.c_int64)] * 6
+        L.refbvh_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.refbvh_free.argtypes = [C.c_void_p]
+        _ref[key] = L
+    return _ref[key]
+
+
+def ref_build_bvh(vertices, indices, mesh_ids=None, tri_offset=0, stackless=False,
+                  swap_mode=0, swap_seed=0, leaf4=False):
+    """Runs the reference constructor; returns (nodes float32 (N,16|8), tris int32 (T,4), info)."""
+    L = _refl(leaf4)
+    v = np.ascontiguousarray(vertices)
+    idx = np.ascontiguousarray(indices, dtype=np.uint32).ravel()
+    mid = None if mesh_ids is None else np.ascontiguousarray(mesh_ids, dtype=np.int32)
+    h = L.refbvh_build(1 if stackless else 0, _p(v), v.shape[0], _p(idx), idx.size, _p(mid),
+                       tri_offset, swap_mode, swap_seed)
+    if not h:
+        raise ValueError("reference builder rejected the input")
+    try:
+        vals = [C.c_int64() for _ in range(6)]
+        L.refbvh_info(h, *[C.byref(x) for x in vals])
+        n_nodes, n_tris, last, leaves, fails, depth = (x.value for x in vals)
+        nodes = np.zeros((n_nodes, 8 if stackless else 16), dtype=np.float32)
+        tris = np.zeros((n_tris, 4), dtype=np.int32)
+        L.refbvh_copy(h, _p(nodes), _p(tris))
+        return nodes, tris, dict(last_node_index=last, leaf_count=leaves, split_fails=fails,
+                                 max_depth=depth)
+    finally:
+        L.refbvh_free(h)

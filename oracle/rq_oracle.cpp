@@ -1,0 +1,705 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the reference's ray-query path, used as the parity checker for the CUDA
+// kernels and as the timed CPU baseline.  The reference implements this path only as GLSL compute
+// shaders; there is no CPU intersector in it (BVH/Intersector.h:353-357 is a stub), so this file
+// restates the GLSL arithmetic statement by statement in C++.  Every function cites the lines it
+// follows.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+//
+// Arithmetic conventions (the definition that the strict GPU kernels must reproduce bit for bit):
+//  * IEEE binary32, round to nearest, no contraction (built with -ffp-contract=off);
+//  * GLSL min/max as specified: min(x,y) = y < x ? y : x, max(x,y) = x < y ? y : x;
+//  * dot(a,b) = (a.x*b.x + a.y*b.y) + a.z*b.z;  cross(a,b) = (a.y*b.z - a.z*b.y, ...);
+//  * mat4*vec4 (column-major) = ((M[0]*v.x + M[1]*v.y) + M[2]*v.z) + M[3]*v.w, per row;
+//  * 1.0/x and a/b are IEEE divisions; normalize(v) = v / sqrt(dot(v,v)).
+#include "rq_oracle.h"
+
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct V3 {
+    float x, y, z;
+};
+
+inline float gmin(float x, float y) { return y < x ? y : x; }  // GLSL min
+inline float gmax(float x, float y) { return x < y ? y : x; }  // GLSL max
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 mul(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline V3 muls(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 neg(V3 a) { return {-a.x, -a.y, -a.z}; }
+inline float dot(V3 a, V3 b) {
+    float r = a.x * b.x;
+    r = r + a.y * b.y;
+    r = r + a.z * b.z;
+    return r;
+}
+inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 vmin(V3 a, V3 b) { return {gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)}; }
+inline V3 vmax(V3 a, V3 b) { return {gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)}; }
+inline V3 normalize(V3 v) {
+    float l = std::sqrt(dot(v, v));
+    return {v.x / l, v.y / l, v.z / l};
+}
+inline float clamp01(float x) { return gmin(gmax(x, 0.0f), 1.0f); }
+
+inline int32_t f2i(float f) {
+    int32_t i;
+    std::memcpy(&i, &f, 4);
+    return i;
+}
+inline V3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+
+// glm/GLSL column-major mat4 * vec4, returning xyz.
+inline V3 xform(const float* m, V3 v, float w) {
+    V3 r;
+    r.x = m[0] * v.x;
+    r.x = r.x + m[4] * v.y;
+    r.x = r.x + m[8] * v.z;
+    r.x = r.x + m[12] * w;
+    r.y = m[1] * v.x;
+    r.y = r.y + m[5] * v.y;
+    r.y = r.y + m[9] * v.z;
+    r.y = r.y + m[13] * w;
+    r.z = m[2] * v.x;
+    r.z = r.z + m[6] * v.y;
+    r.z = r.z + m[10] * v.z;
+    r.z = r.z + m[14] * w;
+    return r;
+}
+
+struct Scene {
+    const float* nodes;  // 16 floats per stack node, 8 per stackless node
+    int64_t n_nodes;
+    const int32_t* tris;
+    const float* verts;  // 8 words per vertex; position = first 3
+    const orc_entity* ents;
+    int n_ents;
+    int layout;
+};
+
+inline V3 vpos(const Scene& s, int32_t vi) { return ld3(s.verts + (int64_t)vi * 8); }
+
+// RayTriangle, Include/TraverseBVHStack.glsl:87-105 (identical in TraverseBVHStackless.glsl:79-97).
+inline void ray_triangle(V3 ro, V3 rd, V3 v0, V3 v1, V3 v2, float& t, float& u, float& v) {
+    V3 v1v0 = sub(v1, v0);
+    V3 v2v0 = sub(v2, v0);
+    V3 rov0 = sub(ro, v0);
+    V3 n = cross(v1v0, v2v0);
+    V3 q = cross(rov0, rd);
+    float d = 1.0f / dot(rd, n);
+    u = d * dot(neg(q), v2v0);
+    v = d * dot(q, v1v0);
+    t = d * dot(neg(n), rov0);
+    if (u < 0.0f || v < 0.0f || (u + v) > 1.0f) t = -1.0f;
+}
+
+// RayBounds (stack), Include/TraverseBVHStack.glsl:107-116.
+inline float ray_bounds_stack(V3 ro, V3 invdir, V3 bmin, V3 bmax, float maxt) {
+    V3 f = mul(sub(bmax, ro), invdir);
+    V3 n = mul(sub(bmin, ro), invdir);
+    V3 tmax = vmax(f, n);
+    V3 tmin = vmin(f, n);
+    float t1 = gmin(gmin(tmax.x, gmin(tmax.y, tmax.z)), maxt);
+    float t0 = gmax(gmax(tmin.x, gmax(tmin.y, tmin.z)), 0.0f);
+    return (t1 >= t0) ? (t0 > 0.0f ? t0 : t1) : -1.0f;
+}
+
+// RayBounds (stackless), Include/TraverseBVHStackless.glsl:67-75 (max3/min3) and 100-109.
+inline float ray_bounds_stackless(V3 bmin, V3 bmax, V3 ro, V3 invdir, float t_min, float t_max) {
+    V3 t0 = mul(sub(bmin, ro), invdir);
+    V3 t1 = mul(sub(bmax, ro), invdir);
+    V3 a = vmin(t0, t1);
+    V3 b = vmax(t0, t1);
+    float tmin = gmax(gmax(gmax(a.x, a.y), a.z), t_min);
+    float tmax = gmin(gmin(b.x, gmin(b.y, b.z)), t_max);
+    return (tmax >= tmin) ? tmin : -1.0f;
+}
+
+// ComputeBarycentrics, Include/TraverseBVHStack.glsl:150-166.
+inline void barycentrics(V3 p, V3 a, V3 b, V3 c, float& u, float& v, float& w) {
+    V3 v0 = sub(b, a), v1 = sub(c, a), v2 = sub(p, a);
+    float d00 = dot(v0, v0);
+    float d01 = dot(v0, v1);
+    float d11 = dot(v1, v1);
+    float d20 = dot(v2, v0);
+    float d21 = dot(v2, v1);
+    float denom = d00 * d11 - d01 * d01;
+    v = (d11 * d20 - d01 * d21) / denom;
+    w = (d00 * d21 - d01 * d20) / denom;
+    u = 1.0f - v - w;
+}
+
+struct Best {
+    float tmax;     // running TMax
+    float closest;  // ClosestTraversal
+    int32_t tri;
+    int32_t mesh;
+};
+
+// Triangle acceptance: the reference keeps the first hit found (`t > 0 && t < TMax`,
+// TraverseBVHStack.glsl:239); the lower-index rule also accepts an exact tie in t when the
+// triangle index is lower, which makes the result independent of traversal order.
+inline bool accept(float t, float tmin, int32_t idx, const Best& b, int tie) {
+    if (!(t > tmin)) return false;
+    if (t < b.tmax) return true;
+    return tie == ORC_TIE_LOWER_INDEX && t == b.tmax && idx < b.tri;
+}
+
+inline void test_leaf(const Scene& s, V3 ro, V3 rd, int32_t start, int32_t len, float tmin,
+                      Best& b, int tie, int32_t& tests) {
+    for (int32_t idx = start; idx < start + len; ++idx) {
+        const int32_t* tr = s.tris + (int64_t)idx * 4;
+        float t, u, v;
+        ray_triangle(ro, rd, vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), t, u, v);
+        ++tests;
+        if (accept(t, tmin, idx, b, tie)) {
+            b.tmax = t;
+            b.closest = t;
+            b.mesh = tr[3];
+            b.tri = idx;
+        }
+    }
+}
+
+// IntersectBVHStack, Include/TraverseBVHStack.glsl:168-324.  `b` carries TMax in and the best
+// hit out.  Returns the iteration count.
+int32_t bvh_stack_closest(const Scene& s, V3 ro, V3 rd, int32_t start, int32_t count, float tmin,
+                          Best& b, int tie, int32_t& tests) {
+    V3 inv = {1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z};
+    int32_t stack[64];
+    int32_t sp = 0;
+    int32_t iters = 0;
+    int32_t cur = start;
+    const int64_t total = s.n_nodes;
+    while (iters < 1024) {
+        // Bounds guard, TraverseBVHStack.glsl:201-205.  `cur >= total` replaces the reference's
+        // `cur > u_TotalNodes`, whose equality case reads one node past the buffer.
+        if (sp >= 64 || sp < 0 || cur < start || cur > start + count || cur < 0 || cur >= total)
+            break;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)cur * 16;
+        const int32_t lw = f2i(nd[3]), rw = f2i(nd[11]);
+        const bool lleaf = lw != -1, rleaf = rw != -1;
+        float lt = lleaf ? -1.0f : ray_bounds_stack(ro, inv, ld3(nd + 0), ld3(nd + 4), b.tmax);
+        float rt = rleaf ? -1.0f : ray_bounds_stack(ro, inv, ld3(nd + 8), ld3(nd + 12), b.tmax);
+        if (lleaf) test_leaf(s, ro, rd, lw >> 4, lw & 0xF, tmin, b, tie, tests);
+        if (rleaf) test_leaf(s, ro, rd, rw >> 4, rw & 0xF, tmin, b, tie, tests);
+        if (lt > 0.0f && rt > 0.0f) {
+            cur = f2i(nd[7]) + start;
+            int32_t post = f2i(nd[15]) + start;
+            if (rt < lt) {
+                int32_t tmp = cur;
+                cur = post;
+                post = tmp;
+            }
+            if (sp >= 63) break;
+            stack[sp++] = post;
+            continue;
+        } else if (lt > 0.0f) {
+            cur = f2i(nd[7]) + start;
+            continue;
+        } else if (rt > 0.0f) {
+            cur = f2i(nd[15]) + start;
+            continue;
+        }
+        if (sp <= 0) break;
+        cur = stack[--sp];
+    }
+    return iters;
+}
+
+// IntersectBVHStackless, Include/TraverseBVHStackless.glsl:175-278.
+int32_t bvh_stackless_closest(const Scene& s, V3 ro, V3 rd, int32_t start, int32_t count,
+                              float tmin, Best& b, int tie, int32_t& tests) {
+    V3 inv = {1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z};
+    int32_t iters = 0;
+    int32_t ptr = start;
+    const int64_t total = s.n_nodes;
+    while (ptr >= 0 && iters < 1024) {
+        if (ptr < start || ptr > start + count || ptr < 0 || ptr >= total) break;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)ptr * 8;
+        float bt = ray_bounds_stackless(ld3(nd), ld3(nd + 4), ro, inv, 0.0001f, b.tmax);
+        if (bt > 0.0f && bt < b.tmax) {
+            const int32_t packed = f2i(nd[3]);
+            if (packed != -1) {
+                test_leaf(s, ro, rd, packed >> 4, packed & 0xF, tmin, b, tie, tests);
+                ptr = f2i(nd[7]);
+                if (ptr < 0) break;
+                ptr += start;
+                continue;
+            }
+            ptr++;
+            continue;
+        }
+        ptr = f2i(nd[7]);
+        if (ptr < 0) break;
+        ptr += start;
+    }
+    return iters;
+}
+
+// IntersectBVHStackOcclusion, Include/TraverseBVHStack.glsl:509-657.  Returns hit t or -1.
+float bvh_stack_any(const Scene& s, V3 ro, V3 rd, int32_t start, int32_t count, float tmin,
+                    float tmax, int32_t& iters, int32_t& tests) {
+    V3 inv = {1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z};
+    int32_t stack[64];
+    int32_t sp = 0;
+    int32_t cur = start;
+    const int64_t total = s.n_nodes;
+    int32_t it = 0;
+    while (it < 1024) {
+        if (sp >= 64 || sp < 0 || cur < start || cur > start + count || cur < 0 || cur >= total)
+            break;
+        ++it;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)cur * 16;
+        const int32_t lw = f2i(nd[3]), rw = f2i(nd[11]);
+        const bool lleaf = lw != -1, rleaf = rw != -1;
+        float lt = lleaf ? -1.0f : ray_bounds_stack(ro, inv, ld3(nd + 0), ld3(nd + 4), tmax);
+        float rt = rleaf ? -1.0f : ray_bounds_stack(ro, inv, ld3(nd + 8), ld3(nd + 12), tmax);
+        for (int side = 0; side < 2; ++side) {
+            const bool leaf = side == 0 ? lleaf : rleaf;
+            if (!leaf) continue;
+            const int32_t w = side == 0 ? lw : rw;
+            for (int32_t idx = w >> 4; idx < (w >> 4) + (w & 0xF); ++idx) {
+                const int32_t* tr = s.tris + (int64_t)idx * 4;
+                float t, u, v;
+                ray_triangle(ro, rd, vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), t, u, v);
+                ++tests;
+                if (t > tmin && t < tmax) return t;
+            }
+        }
+        if (lt > 0.0f && rt > 0.0f) {
+            cur = f2i(nd[7]) + start;
+            int32_t post = f2i(nd[15]) + start;
+            if (rt < lt) {
+                int32_t tmp = cur;
+                cur = post;
+                post = tmp;
+            }
+            if (sp >= 63) break;
+            stack[sp++] = post;
+            continue;
+        } else if (lt > 0.0f) {
+            cur = f2i(nd[7]) + start;
+            continue;
+        } else if (rt > 0.0f) {
+            cur = f2i(nd[15]) + start;
+            continue;
+        }
+        if (sp <= 0) break;
+        cur = stack[--sp];
+    }
+    return -1.0f;
+}
+
+// IntersectBVHStacklessOcclusion, Include/TraverseBVHStackless.glsl:463-556.
+float bvh_stackless_any(const Scene& s, V3 ro, V3 rd, int32_t start, int32_t count, float tmin,
+                        float tmax, int32_t& iters, int32_t& tests) {
+    V3 inv = {1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z};
+    int32_t ptr = start;
+    int32_t it = 0;
+    const int64_t total = s.n_nodes;
+    while (ptr >= 0 && it < 1024) {
+        if (ptr < start || ptr > start + count || ptr < 0 || ptr >= total) break;
+        ++it;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)ptr * 8;
+        float bt = ray_bounds_stackless(ld3(nd), ld3(nd + 4), ro, inv, 0.0001f, tmax);
+        if (bt > 0.0f && bt < tmax) {
+            const int32_t packed = f2i(nd[3]);
+            if (packed != -1) {
+                for (int32_t idx = packed >> 4; idx < (packed >> 4) + (packed & 0xF); ++idx) {
+                    const int32_t* tr = s.tris + (int64_t)idx * 4;
+                    float t, u, v;
+                    ray_triangle(ro, rd, vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), t, u,
+                                 v);
+                    ++tests;
+                    if (t > tmin && t < tmax) return t;
+                }
+                ptr = f2i(nd[7]);
+                if (ptr < 0) break;
+                ptr += start;
+                continue;
+            }
+            ptr++;
+            continue;
+        }
+        ptr = f2i(nd[7]);
+        if (ptr < 0) break;
+        ptr += start;
+    }
+    return -1.0f;
+}
+
+inline float ent_alpha(const orc_entity& e) {
+    float a;
+    std::memcpy(&a, &e.data[1], 4);
+    return a;
+}
+
+// IntersectScene / IntersectSceneIgnoreTransparent, Include/TraverseBVHStack.glsl:327-413
+// (stackless: Include/TraverseBVHStackless.glsl:280-366).
+void scene_closest(const Scene& s, const orc_ray& r, orc_hit& h, int tie, int flags,
+                   int32_t& tests) {
+    h.t = h.u = h.v = h.w = -1.0f;
+    h.tri = h.mesh = h.entity = -1;
+    h.iters = 0;
+    if (!(r.tmax > r.tmin)) return;  // inactive ray
+    const V3 o = ld3(r.o), d = ld3(r.d);
+    float tmax = r.tmax;  // scene TMax (1000000.0 in the reference, :331)
+    float closest = -1.0f;
+    int32_t mesh = -1, tri = -1, ent = -1;
+    for (int i = 0; i < s.n_ents; ++i) {
+        const orc_entity& e = s.ents[i];
+        if ((flags & ORC_FLAG_IGNORE_TRANSPARENT) && ent_alpha(e) < 0.99f) continue;
+        V3 ro = xform(e.inverse, o, 1.0f);
+        V3 rd = xform(e.inverse, d, 0.0f);
+        // Per-BVH call: TMax is the running scene TMax and ClosestTraversal starts at -1, so T
+        // is this BVH's closest hit only.  Under the lower-index rule the best triangle so far
+        // seeds the tie comparison.
+        Best bb{tmax, -1.0f, tie == ORC_TIE_LOWER_INDEX ? tri : -1, -1};
+        int32_t it = s.layout == ORC_STACK
+                         ? bvh_stack_closest(s, ro, rd, e.node_offset, e.node_count, r.tmin, bb,
+                                             tie, tests)
+                         : bvh_stackless_closest(s, ro, rd, e.node_offset, e.node_count, r.tmin,
+                                                 bb, tie, tests);
+        h.iters += it;
+        const float T = bb.closest;
+        if (T > 0.0f && (T < tmax || (tie == ORC_TIE_LOWER_INDEX && T == tmax && bb.tri < tri))) {
+            tmax = T;
+            closest = T;
+            mesh = bb.mesh;
+            tri = bb.tri;
+            ent = i;
+        }
+    }
+    if (closest > 0.0f) {
+        h.tri = tri;
+        h.mesh = mesh;
+        h.entity = ent;
+        const bool report = (flags & ORC_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
+        if (report) {
+            const orc_entity& e = s.ents[ent];
+            V3 ro = xform(e.inverse, o, 1.0f);
+            V3 rd = xform(e.inverse, d, 0.0f);
+            const int32_t* tr = s.tris + (int64_t)tri * 4;
+            V3 p = add(ro, muls(rd, closest));
+            float u, v, w;
+            barycentrics(p, vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), u, v, w);
+            h.t = closest;
+            h.u = u;
+            h.v = v;
+            h.w = w;
+        }
+    }
+}
+
+// IntersectSceneOcclusion, Include/TraverseBVHStack.glsl:659-676 (stackless: :558-575), with the
+// per-ray TMax passed to every BVH (the per-BVH functions take TMax, :509).
+bool scene_any(const Scene& s, const orc_ray& r, int32_t& iters, int32_t& tests) {
+    if (!(r.tmax > r.tmin)) return false;
+    const V3 o = ld3(r.o), d = ld3(r.d);
+    for (int i = 0; i < s.n_ents; ++i) {
+        const orc_entity& e = s.ents[i];
+        V3 ro = xform(e.inverse, o, 1.0f);
+        V3 rd = xform(e.inverse, d, 0.0f);
+        float T = s.layout == ORC_STACK
+                      ? bvh_stack_any(s, ro, rd, e.node_offset, e.node_count, r.tmin, r.tmax,
+                                      iters, tests)
+                      : bvh_stackless_any(s, ro, rd, e.node_offset, e.node_count, r.tmin,
+                                          r.tmax, iters, tests);
+        if (T > 0.0f) return true;
+    }
+    return false;
+}
+
+Scene make_scene(const orc_scene* s) {
+    return Scene{static_cast<const float*>(s->nodes), s->n_nodes, s->tris,
+                 static_cast<const float*>(s->verts), s->ents, s->n_ents, s->layout};
+}
+
+template <class F>
+void parallel_for(int64_t n, int nthreads, F f) {
+    if (nthreads <= 1 || n < 4096) {
+        f(int64_t(0), n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; ++t) {
+        const int64_t b = t * chunk, e = std::min<int64_t>(n, b + chunk);
+        if (b >= e) break;
+        th.emplace_back([=] { f(b, e); });
+    }
+    for (auto& x : th) x.join();
+}
+
+// ---- GI ray generation and shading ---------------------------------------------------------
+
+// Exact binary16 -> binary32 conversion (GLSL unpackHalf2x16 component).
+float half_to_float(uint32_t h) {
+    const uint32_t sign = (h >> 15) & 1u, exp = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+    uint32_t bits;
+    if (exp == 0) {
+        if (man == 0) {
+            bits = sign << 31;
+        } else {  // subnormal: normalise
+            int e = -1;
+            uint32_t m = man;
+            do {
+                ++e;
+                m <<= 1;
+            } while ((m & 0x400u) == 0);
+            bits = (sign << 31) | (uint32_t(127 - 15 - e) << 23) | ((m & 0x3FFu) << 13);
+        }
+    } else if (exp == 31) {
+        bits = (sign << 31) | 0x7F800000u | (man << 13);
+    } else {
+        bits = (sign << 31) | ((exp + 112u) << 23) | (man << 13);
+    }
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+
+// UnpackNormal, Include/TraverseBVHStack.glsl:417-420.
+V3 unpack_normal(const Scene& s, int32_t vi) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(s.verts + (int64_t)vi * 8) + 4;
+    return {half_to_float(w[0] & 0xFFFFu), half_to_float(w[0] >> 16), half_to_float(w[1] & 0xFFFFu)};
+}
+
+// Shading normal at a hit: GetData's interpolated vertex normal (TraverseBVHStack.glsl:438) or the
+// geometric normal.
+V3 hit_normal(const Scene& s, const orc_hit& h, int mode) {
+    const int32_t* tr = s.tris + (int64_t)h.tri * 4;
+    if (mode == 0) {
+        V3 a = muls(unpack_normal(s, tr[0]), h.u);
+        V3 b = muls(unpack_normal(s, tr[1]), h.v);
+        V3 c = muls(unpack_normal(s, tr[2]), h.w);
+        return normalize(add(add(a, b), c));
+    }
+    V3 A = vpos(s, tr[0]), B = vpos(s, tr[1]), C = vpos(s, tr[2]);
+    return normalize(cross(sub(B, A), sub(C, A)));
+}
+
+float u01(uint32_t h) { return float(h >> 8) * (1.0f / 16777216.0f); }
+
+uint32_t pcg_hash(uint32_t x) {
+    uint32_t state = x * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+
+// sin(2*pi*x), cos(2*pi*x) for x in [0,1): quadrant reduction, reflection to [0, pi/4], then
+// Taylor polynomials (sin to x^9, cos to x^10) evaluated by Horner without contraction.
+void sincos_turns(float x, float& so, float& co) {
+    const float x4 = x * 4.0f;
+    const float q = std::floor(x4);
+    float f = x4 - q;
+    const int quad = int(q) & 3;
+    const bool refl = f > 0.5f;
+    if (refl) f = 1.0f - f;
+    const float th = f * 1.57079637f;
+    const float t2 = th * th;
+    float sp = 2.75573192e-06f;
+    sp = sp * t2 + -1.98412698e-04f;
+    sp = sp * t2 + 8.33333333e-03f;
+    sp = sp * t2 + -1.66666667e-01f;
+    sp = sp * t2 + 1.0f;
+    float S = th * sp;
+    float cp = -2.75573192e-07f;
+    cp = cp * t2 + 2.48015873e-05f;
+    cp = cp * t2 + -1.38888889e-03f;
+    cp = cp * t2 + 4.16666667e-02f;
+    cp = cp * t2 + -0.5f;
+    cp = cp * t2 + 1.0f;
+    float C = cp;
+    if (refl) {
+        float tmp = S;
+        S = C;
+        C = tmp;
+    }
+    switch (quad) {
+        case 0: so = S; co = C; break;
+        case 1: so = C; co = -S; break;
+        case 2: so = -S; co = -C; break;
+        default: so = -C; co = S; break;
+    }
+}
+
+// CosWeightedHemisphere, Include/Sampling.glsl:1-12, with cos/sin(2*pi*r.x) from sincos_turns.
+V3 cos_weighted_hemisphere(V3 n, float rx_, float ry_) {
+    V3 uu = normalize(cross(n, V3{0.0f, 1.0f, 1.0f}));
+    V3 vv = cross(uu, n);
+    float ra = std::sqrt(ry_);
+    float s, c;
+    sincos_turns(rx_, s, c);
+    float rx = ra * c;
+    float ry = ra * s;
+    float rz = std::sqrt(1.0f - ry_);
+    V3 rr = add(add(muls(uu, rx), muls(vv, ry)), muls(n, rz));
+    return normalize(rr);
+}
+
+uint32_t sample_key(uint32_t seed, uint32_t ray, uint32_t dim) {
+    return pcg_hash(pcg_hash(pcg_hash(seed) + ray) + dim);
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_closest(const orc_scene* sc, const orc_ray* rays, int64_t n, orc_hit* hits, int tie,
+                 int flags, int nthreads, int32_t* tri_tests) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            int32_t tests = 0;
+            scene_closest(s, rays[i], hits[i], tie, flags, tests);
+            if (tri_tests) tri_tests[i] = tests;
+        }
+    });
+}
+
+void orc_anyhit(const orc_scene* sc, const orc_ray* rays, int64_t n, uint8_t* occluded,
+                int nthreads, int32_t* iters, int32_t* tri_tests) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            int32_t it = 0, tests = 0;
+            occluded[i] = scene_any(s, rays[i], it, tests) ? 1 : 0;
+            if (iters) iters[i] = it;
+            if (tri_tests) tri_tests[i] = tests;
+        }
+    });
+}
+
+void orc_ray_triangle(const float ro[3], const float rd[3], const float v0[3], const float v1[3],
+                      const float v2[3], float out[3]) {
+    ray_triangle(ld3(ro), ld3(rd), ld3(v0), ld3(v1), ld3(v2), out[0], out[1], out[2]);
+}
+
+float orc_ray_bounds_stack(const float ro[3], const float invdir[3], const float bmin[3],
+                           const float bmax[3], float maxt) {
+    return ray_bounds_stack(ld3(ro), ld3(invdir), ld3(bmin), ld3(bmax), maxt);
+}
+
+float orc_ray_bounds_stackless(const float bmin[3], const float bmax[3], const float ro[3],
+                               const float invdir[3], float t_min, float t_max) {
+    return ray_bounds_stackless(ld3(bmin), ld3(bmax), ld3(ro), ld3(invdir), t_min, t_max);
+}
+
+void orc_barycentrics(const float p[3], const float a[3], const float b[3], const float c[3],
+                      float out[3]) {
+    barycentrics(ld3(p), ld3(a), ld3(b), ld3(c), out[0], out[1], out[2]);
+}
+
+uint32_t orc_pcg_hash(uint32_t x) { return pcg_hash(x); }
+void orc_sincos_turns(float x, float* s, float* c) { sincos_turns(x, *s, *c); }
+
+void orc_gi_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit* hits, int64_t n,
+                   int32_t spp, uint32_t seed, float origin_offset, float ray_tmax,
+                   int32_t normal_mode, int nthreads, orc_ray* out) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const orc_hit& h = hits[i];
+            for (int k = 0; k < spp; ++k) {
+                orc_ray& o = out[i * spp + k];
+                if (!(h.t > 0.0f)) {
+                    o = orc_ray{{0, 0, 0}, 0.0f, {0, 0, 1}, -1.0f};
+                    continue;
+                }
+                const V3 ro = ld3(primary[i].o), rd = ld3(primary[i].d);
+                V3 P = add(ro, muls(rd, h.t));
+                V3 N = hit_normal(s, h, normal_mode);
+                // Face the normal toward the incoming ray (DiffuseTrace.glsl:486-488).
+                if (dot(N, rd) > 0.0001f) N = neg(N);
+                const uint32_t rid = uint32_t(i * spp + k);
+                float r0 = u01(sample_key(seed, rid, 0u));
+                float r1 = u01(sample_key(seed, rid, 1u));
+                V3 dir = cos_weighted_hemisphere(N, r0, r1);
+                V3 org = add(P, muls(N, origin_offset));  // DiffuseTrace.glsl:445
+                o.o[0] = org.x; o.o[1] = org.y; o.o[2] = org.z;
+                o.d[0] = dir.x; o.d[1] = dir.y; o.d[2] = dir.z;
+                o.tmin = 0.0f;
+                o.tmax = ray_tmax;
+            }
+        }
+    });
+}
+
+void orc_shadow_raygen(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n,
+                       const float sun_dir[3], float origin_offset, int32_t normal_mode,
+                       int nthreads, orc_ray* out) {
+    const Scene s = make_scene(sc);
+    const V3 L = neg(ld3(sun_dir));
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const orc_hit& h = hits[i];
+            orc_ray& o = out[i];
+            if (!(h.t > 0.0f) || !(rays[i].tmax > rays[i].tmin)) {
+                o = orc_ray{{0, 0, 0}, 0.0f, {0, 0, 1}, -1.0f};
+                continue;
+            }
+            const V3 ro = ld3(rays[i].o), rd = ld3(rays[i].d);
+            V3 P = add(ro, muls(rd, h.t));
+            V3 N = hit_normal(s, h, normal_mode);
+            if (dot(N, rd) > 0.0001f) N = neg(N);
+            V3 org = add(P, muls(N, origin_offset));
+            o.o[0] = org.x; o.o[1] = org.y; o.o[2] = org.z;
+            o.d[0] = L.x; o.d[1] = L.y; o.d[2] = L.z;
+            o.tmin = 0.0f;
+            o.tmax = 1000000.0f;
+        }
+    });
+}
+
+void orc_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n,
+               const uint8_t* shadow_lit, const float* albedo, int32_t n_albedo,
+               const float sun_dir[3], const float sun_color[3], const float sky_color[3],
+               int32_t normal_mode, int nthreads, float* out4) {
+    const Scene s = make_scene(sc);
+    const V3 sd = ld3(sun_dir), sunc = ld3(sun_color), sky = ld3(sky_color);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const orc_hit& h = hits[i];
+            float* o = out4 + i * 4;
+            if (!(rays[i].tmax > rays[i].tmin)) {
+                o[0] = o[1] = o[2] = 0.0f;
+                o[3] = 0.0f;
+                continue;
+            }
+            if (!(h.t > 0.0f)) {  // sky (DiffuseTrace.glsl:490) and unoccluded AO (:494)
+                o[0] = sky.x; o[1] = sky.y; o[2] = sky.z;
+                o[3] = 1.0f;
+                continue;
+            }
+            const V3 rd = ld3(rays[i].d);
+            V3 N = hit_normal(s, h, normal_mode);
+            if (dot(N, rd) > 0.0001f) N = neg(N);
+            V3 alb = (h.mesh >= 0 && h.mesh < n_albedo) ? ld3(albedo + 3 * h.mesh)
+                                                        : V3{0.8f, 0.8f, 0.8f};
+            float em;
+            std::memcpy(&em, &s.ents[h.entity].data[0], 4);
+            const float lit = shadow_lit ? (shadow_lit[i] ? 1.0f : 0.0f) : 1.0f;
+            // GetDirect, DiffuseTrace.glsl:368-372, plus Albedo*emissive (:491).
+            const float ndl = clamp01(dot(N, neg(sd)));
+            V3 direct = muls(muls(mul(alb, sunc), lit), ndl);
+            V3 rad = add(direct, muls(alb, em));
+            o[0] = rad.x; o[1] = rad.y; o[2] = rad.z;
+            o[3] = std::pow(clamp01(h.t / 2.4f), 1.23f);  // DiffuseTrace.glsl:494
+        }
+    });
+}
+
+}  // extern "C"
