@@ -1,0 +1,339 @@
+#!/usr/bin/env python3
+"""Ray-query engine benchmark (one JSON line on rank 0).
+
+Workload (default): 64 displaced subdivision-5 icospheres + ground plane, 1,310,722 triangles,
+SAH BVH (leaf 2, stack layout); 1920x1080 pinhole primary closest-hit rays plus 4 cosine-weighted
+diffuse-GI closest-hit rays per primary hit, Lambert shading and per-pixel accumulation.  One
+"step" is that whole pass (rq_gi_frame).  Metric: Mrays/s = (primary + active secondary rays) per
+second.  Synthetic seeded scene and rays (no dataset).
+
+  value      device-resident inputs, CUDA-event time per step, L2 flushed between steps
+  e2e        same pass through the C ABI with host buffers: pinned primary rays copied in and the
+             pixel buffer copied out inside the timed region
+  roofline   the dominant kernel (secondary closest-hit traversal): algorithmic bytes per launch
+             (64 B per node visit + 64 B per triangle test, counted on the device) / its
+             CUDA-event launch time, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU restatement of the reference traversal (the reference has no CPU
+             intersector) on the host cores, on a bounded sample of the same workload
+
+--impl reference times that CPU path alone (the reference's ray-query path restated on the host
+cores) on the same workload and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s closest/any-hit on 1 GB300: batched+BVH8q vs plain FP32, CPU ref beside"
+UNIT = "Mrays/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--cpu-seconds", type=float, default=8.0,
+                    help="wall-clock bound of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(config: str):
+    import candela_gb300 as R
+    from candela_gb300 import scenes as S
+    if config == "c1":
+        mesh = S.c1_heightfield_scene()
+        rays = S.camera_rays(512, 512, **S.C1_CAMERA)
+        params = dict(spp=1, seed=1, origin_offset=1e-3, ray_tmax=0.25, query=1)
+        name = ("heightfield 256x256 (131,072 tris), 512x512 primary closest-hit + 1 cosine AO "
+                "any-hit ray per hit (tmax 0.25), stack BVH leaf 2, strict")
+    else:
+        mesh = S.c2_icosphere_scene()
+        rays = S.camera_rays(1920, 1080, **S.C2_CAMERA)
+        params = dict(spp=4, seed=1, origin_offset=1e-3, ray_tmax=1000000.0, query=0)
+        name = ("64 displaced subdiv-5 icospheres + ground (1,310,722 tris), 1920x1080 primary "
+                "closest-hit + 4 cosine diffuse-GI closest-hit rays per hit, Lambert shading, "
+                "stack BVH leaf 2, strict")
+    t0 = time.perf_counter()
+    bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
+    build_s = time.perf_counter() - t0
+    ent = R.identity_entity(0, bvh.nodes.shape[0])
+    n_mesh = int(mesh.mesh_ids.max()) + 1
+    albedo = (0.25 + 0.65 * S.uniform(17, 5, n_mesh * 3)).astype(np.float32).reshape(-1, 3)
+    return dict(mesh=mesh, bvh=bvh, ent=ent, rays=rays, params=params, name=name,
+                albedo=albedo, build_s=build_s)
+
+
+def cpu_baseline(wl, seconds: float):
+    """The CPU restatement of the reference path on all host cores, on a bounded sample:
+    repeated whole-pass runs over a prefix of the primary rays until `seconds` elapse."""
+    from oracle import oracle as O
+    nthreads = os.cpu_count() or 1
+    osc = O.OracleScene(O.ORC_STACK, wl["mesh"].vertices, wl["bvh"].tris, wl["bvh"].nodes,
+                        wl["ent"])
+    p = wl["params"]
+    n = min(len(wl["rays"]), 1 << 18)
+    prim = wl["rays"][:: max(1, len(wl["rays"]) // n)][:n]
+    rays_done = 0
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        h = osc.closest(prim, nthreads=nthreads)
+        sec = osc.gi_raygen(prim, h, p["spp"], p["seed"], p["origin_offset"], p["ray_tmax"], 0,
+                            nthreads=nthreads)
+        act = int((sec["tmax"] > 0).sum())
+        if p["query"] == 1:
+            osc.anyhit(sec, nthreads=nthreads)
+        else:
+            sh = osc.closest(sec, nthreads=nthreads)
+            sd = np.array([0.3, 0.4, -0.866], dtype=np.float32)
+            osc.shade(sec, sh, None, wl["albedo"], sd / np.sqrt((sd * sd).sum()),
+                      np.array([4.0, 3.8, 3.5], np.float32), np.array([0.5, 0.7, 1.0], np.float32),
+                      nthreads=nthreads)
+        rays_done += len(prim) + act
+        reps += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": rays_done / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{reps} whole GI passes over {len(prim)} of the primary rays (every "
+                      f"{max(1, len(wl['rays']) // n)}th pixel), same scene/BVH/params, "
+                      f"{dt:.1f} s on {nthreads} threads"}
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    res = cpu_baseline(wl, max(args.cpu_seconds, 1.0) * max(1, args.steps) / 10.0)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": wl["name"]},
+            "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle as O
+        O.build(reference=False)
+        wl = make_workload(args.config)
+        run_reference(args, wl, rank, world)
+        return
+
+    import torch
+    import candela_gb300 as R
+    from candela_gb300 import _lib as L
+    from candela_gb300.engine import gi_params
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    wl = make_workload(args.config)
+    ctx = R.Context(local)
+    sc = ctx.scene(R.STACK, wl["mesh"].vertices, wl["bvh"].tris, wl["bvh"].nodes, wl["ent"])
+    sc.set_materials(wl["albedo"])
+    p = gi_params(**wl["params"])
+    rays = wl["rays"]
+    n = len(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).to(dev)
+    d_pix = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    # ray counts of one pass (untimed)
+    _, st = sc.gi_frame(d_rays, p, out=d_pix, stats=True, stream=sptr)
+    rays_per_step = st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
+    launches_per_step = 5 + (2 if wl["params"].get("shadow_rays") else 0)
+
+    for _ in range(args.warmup):
+        sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = rays_per_step * args.steps * world / (total_ms / 1e3) / 1e6
+
+    # e2e: host buffers through the C ABI (pinned in, pinned out), host clock, sync per step
+    h_rays = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
+    h_pix = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
+    for _ in range(max(1, args.warmup)):
+        sc.gi_frame(h_rays, p, out=h_pix)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sc.gi_frame(h_rays, p, out=h_pix)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": rays_per_step * args.steps / e2e_s / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_rays.nbytes), "d2h_bytes_per_step": int(h_pix.nbytes)}
+
+    # roofline of the dominant kernel: secondary closest-hit (or AO any-hit) traversal
+    d_hits = sc.closest(d_rays, stream=sptr)
+    d_sec = sc.gi_raygen(d_rays, d_hits, p, stream=sptr)
+    q_any = wl["params"]["query"] == 1
+    run = (lambda: sc.anyhit(d_sec, stream=sptr)) if q_any else (lambda: sc.closest(d_sec, stream=sptr))
+    torch.cuda.synchronize()
+    ctx.read_counters(reset=True)
+    if q_any:
+        sc.anyhit(d_sec, flags=L.FLAG_COUNT, stream=sptr)
+    else:
+        sc.closest(d_sec, flags=L.FLAG_COUNT, stream=sptr)
+    cnt = ctx.read_counters(reset=True)
+    algo_bytes = 64 * cnt["node_visits"] + 64 * cnt["triangle_tests"]
+    for _ in range(3):
+        run()
+    kev = []
+    for i in range(max(3, args.steps)):
+        flush.fill_(i & 0xFF)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run()
+        b.record(stream)
+        kev.append((a, b))
+    torch.cuda.synchronize()
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+    peak, peak_kind = load_peaks()
+    achieved = algo_bytes / (k_ms / 1e3) / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(args.config)
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_kind": peak_kind, "kernel": "secondary " + ("any-hit" if q_any else "closest-hit") + " traversal (strict, stack BVH2)",
+                "kernel_ms": round(k_ms, 4), "algorithmic_bytes_per_launch": int(algo_bytes),
+                "node_visits": int(cnt["node_visits"]), "triangle_tests": int(cnt["triangle_tests"]),
+                "active_rays": int(st["secondary_rays"])}
+
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene and camera rays)",
+            "config": {"workload": wl["name"], "rays_per_step": int(rays_per_step),
+                       "primary_rays": int(st["primary_rays"]),
+                       "secondary_rays": int(st["secondary_rays"]),
+                       "l2": "flushed between timed steps (512 MB write)",
+                       "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
+                       "bvh_build_s": round(wl["build_s"], 3)},
+            "e2e": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in e2e.items()},
+            "roofline": roofline, "clocks": clk.summary(),
+            "gpu_launches": launches_per_step * args.steps}
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

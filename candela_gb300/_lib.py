@@ -19,6 +19,7 @@ LAYOUT_DEFAULT, LAYOUT_STACK, LAYOUT_STACKLESS, LAYOUT_BVH8Q = range(4)
 MODE_STRICT, MODE_FAST = 0, 1
 TIE_LOWER_INDEX, TIE_FIRST_FOUND = 0, 1
 FLAG_REF_COMPAT, FLAG_IGNORE_TRANSPARENT, FLAG_HOST_BUFFERS, FLAG_NO_PERSISTENT = 1, 2, 4, 8
+FLAG_COUNT = 16
 
 VERTEX_DTYPE = np.dtype([("pos", "<f4", (4,)), ("packed", "<u4", (4,))])
 TRI_DTYPE = np.dtype(("<i4", (4,)))
@@ -48,6 +49,20 @@ class RqBvhInfo(C.Structure):
                 ("split_fails", C.c_int64), ("build_ms", C.c_double)]
 
 
+class RqGiParams(C.Structure):
+    _fields_ = [("spp", C.c_int32), ("seed", C.c_uint32), ("origin_offset", C.c_float),
+                ("ray_tmax", C.c_float), ("normal_mode", C.c_int32), ("query", C.c_int32),
+                ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
+                ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3),
+                ("sky_color", C.c_float * 3), ("reserved", C.c_int32 * 3)]
+
+
+class RqFrameStats(C.Structure):
+    _fields_ = [("primary_rays", C.c_int64), ("primary_hits", C.c_int64),
+                ("secondary_rays", C.c_int64), ("secondary_hits", C.c_int64),
+                ("shadow_rays", C.c_int64), ("shadow_occluded", C.c_int64)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -72,6 +87,13 @@ SIGNATURES = {
     "rq_scene_destroy": (_S, [_P]),
     "rq_closest": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_anyhit": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
+    "rq_counters_read": (_S, [_P, C.POINTER(C.c_int64 * 2), C.c_int]),
+    "rq_scene_set_materials": (_S, [_P, _P, _I32]),
+    "rq_gi_raygen": (_S, [_P, _P, _P, _P, _I64, C.POINTER(RqGiParams), _P, _P]),
+    "rq_shadow_raygen": (_S, [_P, _P, _P, _P, _I64, C.POINTER(RqGiParams), _P, _P]),
+    "rq_shade": (_S, [_P, _P, _P, _P, _I64, _P, C.POINTER(RqGiParams), _P, _P]),
+    "rq_gi_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
+                         C.POINTER(RqFrameStats), _P]),
 }
 
 _lib = None

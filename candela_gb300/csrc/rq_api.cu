@@ -11,42 +11,10 @@
 #include "../../include/rq.h"
 #include "bvh_build.h"
 #include "rq_internal.h"
+#include "rq_objects.h"
 #include "rq_validate.h"
 
-struct rq_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;       // default stream of the context
-    cudaStream_t pipe[2] = {nullptr, nullptr};  // host-buffer staging pipeline
-    cudaEvent_t ev = nullptr;
-    void* stage_in[2] = {nullptr, nullptr};
-    void* stage_out[2] = {nullptr, nullptr};
-    size_t stage_in_bytes[2] = {0, 0};
-    size_t stage_out_bytes[2] = {0, 0};
-    int* counters = nullptr;  // device work counters for persistent kernels (64 ints)
-    std::string err;
-};
-
-struct rq_bvh {
-    rq::BuildOutput out;
-    int32_t layout = RQ_LAYOUT_BVH2_STACK;
-};
-
-struct rq_scene {
-    rq_ctx* ctx = nullptr;
-    int32_t layout = RQ_LAYOUT_BVH2_STACK;
-    std::vector<float> h_nodes;  // host copy, used to validate entity lists
-    int64_t n_nodes = 0, n_tris = 0, n_verts = 0;
-    float4* d_nodes = nullptr;
-    int4* d_tris = nullptr;
-    float4* d_verts = nullptr;
-    rq_entity* d_ents = nullptr;
-    int32_t n_ents = 0;
-    int32_t ents_cap = 0;
-    int64_t bytes = 0;
-    rq::SceneView view{};
-};
-
-namespace {
+namespace rq {
 
 thread_local std::string g_err;
 
@@ -60,11 +28,46 @@ rq_status cuda_fail(rq_ctx* ctx, cudaError_t e, const char* what) {
     return fail(ctx, RQ_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define RQ_CUDA(ctx, call)                                        \
-    do {                                                          \
-        cudaError_t e_ = (call);                                  \
-        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
-    } while (0)
+rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out) {
+    if (slot < 0 || slot >= kScratchSlots) return fail(ctx, RQ_EINVAL, "bad scratch slot");
+    if (bytes == 0) bytes = 256;
+    if (ctx->scratch_bytes[slot] < bytes) {
+        if (ctx->scratch[slot]) cudaFree(ctx->scratch[slot]);
+        ctx->scratch[slot] = nullptr;
+        ctx->scratch_bytes[slot] = 0;
+        const size_t want = bytes + bytes / 8;  // headroom so small growth does not reallocate
+        if (cudaMalloc(&ctx->scratch[slot], want) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "scratch allocation failed");
+        ctx->scratch_bytes[slot] = want;
+    }
+    *out = ctx->scratch[slot];
+    return RQ_OK;
+}
+
+rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, QueryConfig& q) {
+    rq_opts d{};
+    if (!o) o = &d;
+    q.layout = o->layout == RQ_LAYOUT_DEFAULT ? sc->layout : o->layout;
+    q.mode = o->mode;
+    q.tie_lower = o->tie == RQ_TIE_LOWER_INDEX ? 1 : 0;
+    q.flags = o->flags;
+    q.block = o->block_size;
+    q.counters = (o->flags & RQ_FLAG_COUNT) ? work_counters(ctx) : nullptr;
+    if (o->tie != RQ_TIE_LOWER_INDEX && o->tie != RQ_TIE_FIRST_FOUND)
+        return fail(ctx, RQ_EINVAL, "unknown tie rule");
+    if (q.mode != RQ_MODE_STRICT && q.mode != RQ_MODE_FAST)
+        return fail(ctx, RQ_EINVAL, "unknown mode");
+    if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
+    if (q.mode == RQ_MODE_FAST) return fail(ctx, RQ_ENOTSUP, "fast mode not available");
+    return RQ_OK;
+}
+
+}  // namespace rq
+
+namespace {
+
+using rq::fail;
+using rq::cuda_fail;
 
 bool is_identity(const float* m) {
     for (int c = 0; c < 4; ++c)
@@ -95,23 +98,6 @@ rq_status ensure_stage(rq_ctx* ctx, int k, size_t in_bytes, size_t out_bytes) {
             return fail(ctx, RQ_ENOMEM, "staging buffer allocation failed");
         ctx->stage_out_bytes[k] = out_bytes;
     }
-    return RQ_OK;
-}
-
-rq_status resolve(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, rq::QueryConfig& q) {
-    rq_opts d{};
-    if (!o) o = &d;
-    q.layout = o->layout == RQ_LAYOUT_DEFAULT ? sc->layout : o->layout;
-    q.mode = o->mode;
-    q.tie_lower = o->tie == RQ_TIE_LOWER_INDEX ? 1 : 0;
-    q.flags = o->flags;
-    q.block = o->block_size;
-    if (o->tie != RQ_TIE_LOWER_INDEX && o->tie != RQ_TIE_FIRST_FOUND)
-        return fail(ctx, RQ_EINVAL, "unknown tie rule");
-    if (q.mode != RQ_MODE_STRICT && q.mode != RQ_MODE_FAST)
-        return fail(ctx, RQ_EINVAL, "unknown mode");
-    if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
-    if (q.mode == RQ_MODE_FAST) return fail(ctx, RQ_ENOTSUP, "fast mode not available");
     return RQ_OK;
 }
 
@@ -163,7 +149,7 @@ const char* rq_status_string(rq_status s) {
     return "unknown status";
 }
 
-const char* rq_last_error(const rq_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+const char* rq_last_error(const rq_ctx* ctx) { return ctx ? ctx->err.c_str() : rq::g_err.c_str(); }
 
 rq_status rq_create(int device, rq_ctx** out) {
     if (!out) return fail(nullptr, RQ_EINVAL, "out is NULL");
@@ -181,7 +167,8 @@ rq_status rq_create(int device, rq_ctx** out) {
         (e = cudaStreamCreateWithFlags(&ctx->pipe[0], cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ctx->pipe[1], cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->counters, 64 * sizeof(int))) != cudaSuccess) {
+        (e = cudaMalloc(&ctx->counters, 64 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMemset(ctx->counters, 0, 64 * sizeof(int))) != cudaSuccess) {
         rq_status s = cuda_fail(nullptr, e, "context setup");
         rq_destroy(ctx);
         return s;
@@ -199,9 +186,23 @@ rq_status rq_destroy(rq_ctx* ctx) {
         if (ctx->pipe[k]) cudaStreamDestroy(ctx->pipe[k]);
     }
     if (ctx->counters) cudaFree(ctx->counters);
+    for (int k = 0; k < kScratchSlots; ++k)
+        if (ctx->scratch[k]) cudaFree(ctx->scratch[k]);
     if (ctx->ev) cudaEventDestroy(ctx->ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+    return RQ_OK;
+}
+
+rq_status rq_counters_read(rq_ctx* ctx, rq_counters* out, int reset) {
+    if (!ctx || !out) return fail(ctx, RQ_EINVAL, "NULL argument");
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    RQ_CUDA(ctx, cudaDeviceSynchronize());
+    unsigned long long c[2];
+    RQ_CUDA(ctx, cudaMemcpy(c, rq::work_counters(ctx), sizeof(c), cudaMemcpyDeviceToHost));
+    out->node_visits = static_cast<int64_t>(c[0]);
+    out->triangle_tests = static_cast<int64_t>(c[1]);
+    if (reset) RQ_CUDA(ctx, cudaMemset(rq::work_counters(ctx), 0, sizeof(c)));
     return RQ_OK;
 }
 
@@ -385,6 +386,7 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_tris) cudaFree(sc->d_tris);
     if (sc->d_verts) cudaFree(sc->d_verts);
     if (sc->d_ents) cudaFree(sc->d_ents);
+    if (sc->d_albedo) cudaFree(sc->d_albedo);
     delete sc;
     return RQ_OK;
 }
@@ -397,11 +399,11 @@ rq_status rq_closest(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_
     if (n < 0 || (n > 0 && (!rays || !hits))) return fail(ctx, RQ_EINVAL, "bad ray/hit arrays");
     if (sc->ctx != ctx) return fail(ctx, RQ_EINVAL, "scene belongs to another context");
     rq::QueryConfig q{};
-    rq_status s = resolve(ctx, sc, opts, q);
+    rq_status s = rq::resolve_query(ctx, sc, opts, q);
     if (s != RQ_OK) return s;
     if (n == 0) return RQ_OK;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
     const rq::SceneView view = sc->view;
     if (q.flags & RQ_FLAG_HOST_BUFFERS) {
         return staged(ctx, rays, sizeof(rq_ray), hits, sizeof(rq_hit), n, st,
@@ -420,11 +422,11 @@ rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t
     if (n < 0 || (n > 0 && (!rays || !occluded))) return fail(ctx, RQ_EINVAL, "bad ray/result arrays");
     if (sc->ctx != ctx) return fail(ctx, RQ_EINVAL, "scene belongs to another context");
     rq::QueryConfig q{};
-    rq_status s = resolve(ctx, sc, opts, q);
+    rq_status s = rq::resolve_query(ctx, sc, opts, q);
     if (s != RQ_OK) return s;
     if (n == 0) return RQ_OK;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
     const rq::SceneView view = sc->view;
     if (q.flags & RQ_FLAG_HOST_BUFFERS) {
         return staged(ctx, rays, sizeof(rq_ray), occluded, 1, n, st,

@@ -1,0 +1,365 @@
+// Diffuse-GI / RTAO pass: secondary ray generation, shading and per-pixel accumulation, plus the
+// C ABI entry points that drive the whole pass (rq_gi_frame).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "rq_gi.cuh"
+#include "rq_objects.h"
+
+namespace rq {
+namespace {
+
+using strict::f3;
+
+struct GiArgs {
+    int32_t spp;
+    uint32_t seed;
+    float origin_offset;
+    float ray_tmax;
+    int32_t normal_mode;
+    float shadow_offset;
+    f3 sun_dir, sun_color, sky;
+};
+
+GiArgs to_args(const rq_gi_params& p) {
+    GiArgs a;
+    a.spp = p.spp;
+    a.seed = p.seed;
+    a.origin_offset = p.origin_offset;
+    a.ray_tmax = p.ray_tmax;
+    a.normal_mode = p.normal_mode;
+    a.shadow_offset = p.shadow_offset;
+    a.sun_dir = {p.sun_dir[0], p.sun_dir[1], p.sun_dir[2]};
+    a.sun_color = {p.sun_color[0], p.sun_color[1], p.sun_color[2]};
+    a.sky = {p.sky_color[0], p.sky_color[1], p.sky_color[2]};
+    return a;
+}
+
+__device__ __forceinline__ void put_ray(rq_ray* out, int64_t j, f3 o, float tmin, f3 d, float tmax) {
+    float4* p = reinterpret_cast<float4*>(out) + 2 * j;
+    p[0] = make_float4(o.x, o.y, o.z, tmin);
+    p[1] = make_float4(d.x, d.y, d.z, tmax);
+}
+
+__device__ __forceinline__ void get_hit(const rq_hit* hits, int64_t i, float4& a, int4& b) {
+    const float4* p = reinterpret_cast<const float4*>(hits) + 2 * i;
+    a = __ldg(p);
+    const float4 q = __ldg(p + 1);
+    b = make_int4(__float_as_int(q.x), __float_as_int(q.y), __float_as_int(q.z), __float_as_int(q.w));
+}
+
+// One thread per secondary ray j = i*spp + k (DiffuseTrace.glsl:439-446, 486-488).
+__global__ void k_gi_raygen(SceneView s, const rq_ray* __restrict__ prim,
+                            const rq_hit* __restrict__ hits, int64_t n, GiArgs a,
+                            rq_ray* __restrict__ out, unsigned long long* active) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = n * a.spp;
+    bool act = false;
+    if (j < total) {
+        const int64_t i = j / a.spp;
+        float4 h0;
+        int4 h1;
+        get_hit(hits, i, h0, h1);
+        if (h0.x > 0.0f) {
+            const float4* pr = reinterpret_cast<const float4*>(prim) + 2 * i;
+            const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+            const uint32_t rid = static_cast<uint32_t>(j);
+            const float u0 = gi::u01(gi::sample_key(a.seed, rid, 0u));
+            const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
+            const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
+            const f3 org = strict::add(P, strict::muls(N, a.origin_offset));
+            put_ray(out, j, org, 0.0f, dir, a.ray_tmax);
+            act = true;
+        } else {
+            put_ray(out, j, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
+        }
+    }
+    if (active) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
+    }
+}
+
+__global__ void k_shadow_raygen(SceneView s, const rq_ray* __restrict__ rays,
+                                const rq_hit* __restrict__ hits, int64_t n, GiArgs a,
+                                rq_ray* __restrict__ out, unsigned long long* active) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool act = false;
+    if (j < n) {
+        float4 h0;
+        int4 h1;
+        get_hit(hits, j, h0, h1);
+        const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * j;
+        const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+        if (h0.x > 0.0f && r1.w > r0.w) {
+            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+            const f3 org = strict::add(P, strict::muls(N, a.shadow_offset));
+            put_ray(out, j, org, 0.0f, strict::neg(a.sun_dir), 1000000.0f);
+            act = true;
+        } else {
+            put_ray(out, j, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
+        }
+    }
+    if (active) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
+    }
+}
+
+// GetDirect (DiffuseTrace.glsl:368-372) + emissive (:491) + AO (:494).
+__global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
+                        int64_t n, const uint8_t* __restrict__ lit, int lit_is_occlusion,
+                        const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                        float4* __restrict__ out) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * j;
+    const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+    if (!(r1.w > r0.w)) {
+        out[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    float4 h0;
+    int4 h1;
+    get_hit(hits, j, h0, h1);
+    if (!(h0.x > 0.0f)) {
+        out[j] = make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
+        return;
+    }
+    const f3 rd = strict::xyz(r1);
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    f3 alb{0.8f, 0.8f, 0.8f};
+    if (h1.y >= 0 && h1.y < n_albedo)
+        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
+    const float em = __int_as_float(s.ents[h1.z].data[0]);
+    // lit[j] = 1 means the sun is visible; an occlusion buffer (1 = blocked) is read inverted.
+    const float l = lit ? ((lit[j] != 0) != (lit_is_occlusion != 0) ? 1.0f : 0.0f) : 1.0f;
+    const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
+    const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
+    const f3 rad = strict::add(direct, strict::muls(alb, em));
+    const float ao = powf(strict::gmin(strict::gmax(__fdiv_rn(h0.x, 2.4f), 0.0f), 1.0f), 1.23f);
+    out[j] = make_float4(rad.x, rad.y, rad.z, ao);
+}
+
+// AO query: visibility 1 - occluded for active rays, 0 for inactive ones.
+__global__ void k_ao_shade(const rq_ray* __restrict__ rays, const uint8_t* __restrict__ occ, int64_t n,
+                           float4* __restrict__ out) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * j;
+    const float tmin = __ldg(pr).w, tmax = __ldg(pr + 1).w;
+    const float vis = (tmax > tmin) ? (occ[j] ? 0.0f : 1.0f) : 0.0f;
+    out[j] = make_float4(0.0f, 0.0f, 0.0f, vis);
+}
+
+// Per-pixel mean over the spp secondary samples (summed in sample order).
+__global__ void k_accumulate(const float4* __restrict__ shaded, int64_t n, int32_t spp,
+                             float4* __restrict__ pixels) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < spp; ++k) {
+        const float4 v = __ldg(shaded + i * spp + k);
+        acc.x = __fadd_rn(acc.x, v.x);
+        acc.y = __fadd_rn(acc.y, v.y);
+        acc.z = __fadd_rn(acc.z, v.z);
+        acc.w = __fadd_rn(acc.w, v.w);
+    }
+    const float inv = __fdiv_rn(1.0f, static_cast<float>(spp));
+    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                            __fmul_rn(acc.w, inv));
+}
+
+__global__ void k_count_hits(const rq_hit* __restrict__ hits, int64_t n, unsigned long long* cnt) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool h = i < n && __ldg(reinterpret_cast<const float*>(hits) + 8 * i) > 0.0f;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
+}
+
+__global__ void k_count_bytes(const uint8_t* __restrict__ b, int64_t n, unsigned long long* cnt) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool h = i < n && b[i] != 0;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
+}
+
+inline unsigned grid(int64_t n, int b) { return static_cast<unsigned>((n + b - 1) / b); }
+
+rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
+    if (!p) return fail(ctx, RQ_EINVAL, "NULL gi params");
+    if (p->spp < 1 || p->spp > 1024) return fail(ctx, RQ_EINVAL, "spp must be 1..1024");
+    if (p->normal_mode != 0 && p->normal_mode != 1) return fail(ctx, RQ_EINVAL, "bad normal_mode");
+    if (p->query != 0 && p->query != 1) return fail(ctx, RQ_EINVAL, "bad query kind");
+    return RQ_OK;
+}
+
+}  // namespace
+}  // namespace rq
+
+using rq::fail;
+
+extern "C" {
+
+rq_status rq_scene_set_materials(rq_scene* sc, const float* albedo_rgb, int32_t n_meshes) {
+    if (!sc || n_meshes < 0 || (n_meshes > 0 && !albedo_rgb))
+        return fail(sc ? sc->ctx : nullptr, RQ_EINVAL, "bad material arguments");
+    rq_ctx* ctx = sc->ctx;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (sc->d_albedo) cudaFree(sc->d_albedo);
+    sc->d_albedo = nullptr;
+    sc->n_albedo = 0;
+    if (n_meshes == 0) return RQ_OK;
+    if (cudaMalloc(&sc->d_albedo, sizeof(float) * 3 * n_meshes) != cudaSuccess)
+        return fail(ctx, RQ_ENOMEM, "material buffer allocation failed");
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_albedo, albedo_rgb, sizeof(float) * 3 * n_meshes,
+                            cudaMemcpyHostToDevice));
+    sc->n_albedo = n_meshes;
+    return RQ_OK;
+}
+
+rq_status rq_gi_raygen(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, const rq_hit* hits,
+                       int64_t n, const rq_gi_params* p, rq_ray* out, void* stream) {
+    if (!ctx || !sc || n < 0 || (n > 0 && (!primary || !hits || !out)))
+        return fail(ctx, RQ_EINVAL, "bad arguments");
+    rq_status s = rq::check_params(ctx, p);
+    if (s != RQ_OK || n == 0) return s;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
+    const int64_t total = n * p->spp;
+    rq::k_gi_raygen<<<rq::grid(total, 256), 256, 0, st>>>(sc->view, primary, hits, n, rq::to_args(*p),
+                                                          out, nullptr);
+    RQ_CUDA(ctx, cudaGetLastError());
+    return RQ_OK;
+}
+
+rq_status rq_shadow_raygen(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, const rq_hit* hits,
+                           int64_t n, const rq_gi_params* p, rq_ray* out, void* stream) {
+    if (!ctx || !sc || n < 0 || (n > 0 && (!rays || !hits || !out)))
+        return fail(ctx, RQ_EINVAL, "bad arguments");
+    rq_status s = rq::check_params(ctx, p);
+    if (s != RQ_OK || n == 0) return s;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
+    rq::k_shadow_raygen<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, rays, hits, n, rq::to_args(*p),
+                                                          out, nullptr);
+    RQ_CUDA(ctx, cudaGetLastError());
+    return RQ_OK;
+}
+
+rq_status rq_shade(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, const rq_hit* hits,
+                   int64_t n, const uint8_t* lit, const rq_gi_params* p, float* out4, void* stream) {
+    if (!ctx || !sc || n < 0 || (n > 0 && (!rays || !hits || !out4)))
+        return fail(ctx, RQ_EINVAL, "bad arguments");
+    rq_status s = rq::check_params(ctx, p);
+    if (s != RQ_OK || n == 0) return s;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
+    rq::k_shade<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, rays, hits, n, lit, 0, sc->d_albedo,
+                                                  sc->n_albedo, rq::to_args(*p),
+                                                  reinterpret_cast<float4*>(out4));
+    RQ_CUDA(ctx, cudaGetLastError());
+    return RQ_OK;
+}
+
+rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, int64_t n,
+                      const rq_gi_params* p, const rq_opts* opts, float* pixels4,
+                      rq_frame_stats* stats, void* stream) {
+    if (!ctx || !sc || n < 0 || (n > 0 && (!primary || !pixels4)))
+        return fail(ctx, RQ_EINVAL, "bad arguments");
+    rq_status s = rq::check_params(ctx, p);
+    if (s != RQ_OK) return s;
+    rq::QueryConfig q{};
+    if ((s = rq::resolve_query(ctx, sc, opts, q)) != RQ_OK) return s;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return RQ_OK;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
+    const bool host = (q.flags & RQ_FLAG_HOST_BUFFERS) != 0;
+    q.flags &= ~RQ_FLAG_HOST_BUFFERS;
+    const int64_t m = n * p->spp;
+    void *d_prim = nullptr, *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr,
+         *d_shade = nullptr, *d_pix = nullptr, *d_shadow = nullptr, *d_lit = nullptr;
+    if ((s = rq::scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
+        (s = rq::scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
+        (s = rq::scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
+        (s = rq::scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
+        (s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK)
+        return s;
+    if (host) {
+        if ((s = rq::scratch(ctx, 0, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
+            (s = rq::scratch(ctx, 6, 16 * n, &d_pix)) != RQ_OK)
+            return s;
+        RQ_CUDA(ctx, cudaMemcpyAsync(d_prim, primary, sizeof(rq_ray) * n, cudaMemcpyHostToDevice, st));
+    } else {
+        d_prim = const_cast<rq_ray*>(primary);
+        d_pix = pixels4;
+    }
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
+    if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
+    const rq::GiArgs a = rq::to_args(*p);
+    const rq_ray* prim = static_cast<const rq_ray*>(d_prim);
+    rq_hit* phit = static_cast<rq_hit*>(d_phit);
+    rq_ray* sec = static_cast<rq_ray*>(d_sec);
+    rq_hit* shit = static_cast<rq_hit*>(d_shit);
+    float4* shade = static_cast<float4*>(d_shade);
+    RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, ctx->counters + 32, st));
+    if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
+    rq::k_gi_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
+                                                      stats ? cnt + 1 : nullptr);
+    RQ_CUDA(ctx, cudaGetLastError());
+    if (p->query == 1) {
+        uint8_t* occ = static_cast<uint8_t*>(d_occ);
+        RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sec, m, occ, ctx->counters + 40, st));
+        if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 2);
+        rq::k_ao_shade<<<rq::grid(m, 256), 256, 0, st>>>(sec, occ, m, shade);
+    } else {
+        RQ_CUDA(ctx, rq::launch_closest(sc->view, q, sec, m, shit, ctx->counters + 40, st));
+        if (stats) rq::k_count_hits<<<rq::grid(m, 256), 256, 0, st>>>(shit, m, cnt + 2);
+        const uint8_t* lit = nullptr;
+        if (p->shadow_rays) {
+            if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK ||
+                (s = rq::scratch(ctx, 8, m, &d_lit)) != RQ_OK)
+                return s;
+            rq_ray* sh = static_cast<rq_ray*>(d_shadow);
+            uint8_t* occ = static_cast<uint8_t*>(d_lit);
+            rq::k_shadow_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh,
+                                                                  stats ? cnt + 3 : nullptr);
+            RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sh, m, occ, ctx->counters + 48, st));
+            if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 4);
+            lit = occ;  // occlusion bytes: k_shade reads them inverted
+        }
+        rq::k_shade<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, lit, lit ? 1 : 0,
+                                                      sc->d_albedo, sc->n_albedo, a, shade);
+    }
+    rq::k_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(shade, n, p->spp, static_cast<float4*>(d_pix));
+    RQ_CUDA(ctx, cudaGetLastError());
+    if (host) {
+        RQ_CUDA(ctx, cudaMemcpyAsync(pixels4, d_pix, 16 * n, cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+    if (stats) {
+        unsigned long long c[8];
+        RQ_CUDA(ctx, cudaMemcpyAsync(c, cnt, sizeof(c), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(ctx, cudaStreamSynchronize(st));
+        stats->primary_rays = n;
+        stats->primary_hits = static_cast<int64_t>(c[0]);
+        stats->secondary_rays = static_cast<int64_t>(c[1]);
+        stats->secondary_hits = static_cast<int64_t>(c[2]);
+        stats->shadow_rays = static_cast<int64_t>(c[3]);
+        stats->shadow_occluded = static_cast<int64_t>(c[4]);
+    }
+    return RQ_OK;
+}
+
+}  // extern "C"

@@ -33,6 +33,7 @@ struct QueryConfig {
     int32_t tie_lower;   // 1 = lower-index rule
     int32_t flags;
     int32_t block;
+    unsigned long long* counters;  // non-null: accumulate node visits / triangle tests here
 };
 
 // Kernel launchers (rq_kernels.cu).  Return cudaGetLastError() after the launch.

@@ -1,0 +1,70 @@
+// Library-internal object definitions shared by the C ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rq.h"
+#include "bvh_build.h"
+#include "rq_internal.h"
+
+constexpr int kScratchSlots = 16;
+
+struct rq_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;       // default stream of the context
+    cudaStream_t pipe[2] = {nullptr, nullptr};  // host-buffer staging pipeline
+    cudaEvent_t ev = nullptr;
+    void* stage_in[2] = {nullptr, nullptr};
+    void* stage_out[2] = {nullptr, nullptr};
+    size_t stage_in_bytes[2] = {0, 0};
+    size_t stage_out_bytes[2] = {0, 0};
+    int* counters = nullptr;  // device work counters for persistent kernels (64 ints)
+    void* scratch[kScratchSlots] = {};
+    size_t scratch_bytes[kScratchSlots] = {};
+    std::string err;
+};
+
+struct rq_bvh {
+    rq::BuildOutput out;
+    int32_t layout = RQ_LAYOUT_BVH2_STACK;
+};
+
+struct rq_scene {
+    rq_ctx* ctx = nullptr;
+    int32_t layout = RQ_LAYOUT_BVH2_STACK;
+    std::vector<float> h_nodes;  // host copy, used to validate entity lists
+    int64_t n_nodes = 0, n_tris = 0, n_verts = 0;
+    float4* d_nodes = nullptr;
+    int4* d_tris = nullptr;
+    float4* d_verts = nullptr;
+    rq_entity* d_ents = nullptr;
+    int32_t n_ents = 0;
+    int32_t ents_cap = 0;
+    int64_t bytes = 0;
+    rq::SceneView view{};
+    float* d_albedo = nullptr;  // 3 floats per mesh id
+    int32_t n_albedo = 0;
+};
+
+namespace rq {
+
+rq_status fail(rq_ctx* ctx, rq_status s, const std::string& msg);
+rq_status cuda_fail(rq_ctx* ctx, cudaError_t e, const char* what);
+// Resolves rq_opts (NULL = defaults) against the scene into a kernel configuration.
+rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, QueryConfig& q);
+// Query work counters (2 x u64) inside the context's counter block.
+inline unsigned long long* work_counters(rq_ctx* ctx) {
+    return reinterpret_cast<unsigned long long*>(ctx->counters) + 8;
+}
+// Grow-only device scratch buffer of the context (slot < kScratchSlots).
+rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out);
+
+}  // namespace rq
+
+#define RQ_CUDA(ctx, call)                                            \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return rq::cuda_fail((ctx), e_, #call); \
+    } while (0)

@@ -139,8 +139,9 @@ __device__ __forceinline__ bool accept(float t, float tmin, int32_t idx, const B
 // accepted triangle.
 template <bool kAny, bool kTieLower>
 __device__ __forceinline__ bool test_leaf(const SceneView& s, f3 ro, f3 rd, int32_t start,
-                                          int32_t len, float tmin, Best& b) {
+                                          int32_t len, float tmin, Best& b, int32_t& tests) {
     for (int32_t idx = start; idx < start + len; ++idx) {
+        ++tests;
         const int4 tr = ldg4i(s.tris + idx);
         const float t = ray_triangle(ro, rd, vpos(s, tr.x), vpos(s, tr.y), vpos(s, tr.z));
         if (kAny) {
@@ -162,7 +163,7 @@ __device__ __forceinline__ bool test_leaf(const SceneView& s, f3 ro, f3 rd, int3
 // lives in local memory.  Returns the iteration count.
 template <bool kAny, bool kTieLower>
 __device__ int32_t bvh_stack(const SceneView& s, f3 ro, f3 rd, int32_t start, int32_t count,
-                             float tmin, Best& b) {
+                             float tmin, Best& b, int32_t& tests) {
     const f3 inv = rcp3(rd);
     int32_t stack[64];
     int32_t sp = 0;
@@ -180,8 +181,8 @@ __device__ int32_t bvh_stack(const SceneView& s, f3 ro, f3 rd, int32_t start, in
         const bool lleaf = lw != -1, rleaf = rw != -1;
         const float lt = lleaf ? -1.0f : ray_bounds_stack(ro, inv, lmin, lmax, b.tmax);
         const float rt = rleaf ? -1.0f : ray_bounds_stack(ro, inv, rmin, rmax, b.tmax);
-        if (lleaf && test_leaf<kAny, kTieLower>(s, ro, rd, lw >> 4, lw & 0xF, tmin, b)) break;
-        if (rleaf && test_leaf<kAny, kTieLower>(s, ro, rd, rw >> 4, rw & 0xF, tmin, b)) break;
+        if (lleaf && test_leaf<kAny, kTieLower>(s, ro, rd, lw >> 4, lw & 0xF, tmin, b, tests)) break;
+        if (rleaf && test_leaf<kAny, kTieLower>(s, ro, rd, rw >> 4, rw & 0xF, tmin, b, tests)) break;
         if (lt > 0.0f && rt > 0.0f) {
             cur = __float_as_int(lmax.w) + start;
             int32_t post = __float_as_int(rmax.w) + start;
@@ -209,7 +210,7 @@ __device__ int32_t bvh_stack(const SceneView& s, f3 ro, f3 rd, int32_t start, in
 // IntersectBVHStackless (:175-278) and IntersectBVHStacklessOcclusion (:463-556).
 template <bool kAny, bool kTieLower>
 __device__ int32_t bvh_stackless(const SceneView& s, f3 ro, f3 rd, int32_t start, int32_t count,
-                                 float tmin, Best& b) {
+                                 float tmin, Best& b, int32_t& tests) {
     const f3 inv = rcp3(rd);
     int32_t iters = 0;
     int32_t ptr = start;
@@ -222,7 +223,7 @@ __device__ int32_t bvh_stackless(const SceneView& s, f3 ro, f3 rd, int32_t start
         if (bt > 0.0f && bt < b.tmax) {
             const int32_t packed = __float_as_int(bmin.w);
             if (packed != -1) {
-                if (test_leaf<kAny, kTieLower>(s, ro, rd, packed >> 4, packed & 0xF, tmin, b))
+                if (test_leaf<kAny, kTieLower>(s, ro, rd, packed >> 4, packed & 0xF, tmin, b, tests))
                     break;
                 ptr = __float_as_int(bmax.w);
                 if (ptr < 0) break;
@@ -244,7 +245,7 @@ __device__ __forceinline__ float ent_alpha(const rq_entity& e) { return __int_as
 // IntersectScene / IntersectSceneIgnoreTransparent (:327-413; stackless :280-366).
 template <bool kStackless, bool kTieLower>
 __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 r1, int flags,
-                              rq_hit& h) {
+                              rq_hit& h, int32_t& tests) {
     h.t = h.u = h.v = h.w = -1.0f;
     h.tri = h.mesh = h.entity = -1;
     h.iters = 0;
@@ -261,8 +262,8 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
         const f3 rd = xform(e.inverse, d, 0.0f);
         Best bb{tmax, -1.0f, kTieLower ? tri : -1, -1};
         const int32_t it =
-            kStackless ? bvh_stackless<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb)
-                       : bvh_stack<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb);
+            kStackless ? bvh_stackless<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests)
+                       : bvh_stack<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests);
         h.iters += it;
         const float T = bb.closest;
         if (T > 0.0f && (T < tmax || (kTieLower && T == tmax && bb.tri < tri))) {
@@ -296,7 +297,8 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
 
 // IntersectSceneOcclusion (:659-676; stackless :558-575) with the per-ray TMax.
 template <bool kStackless>
-__device__ bool scene_any(const SceneView& s, const float4 r0, const float4 r1) {
+__device__ bool scene_any(const SceneView& s, const float4 r0, const float4 r1, int32_t& iters,
+                          int32_t& tests) {
     const float rtmin = r0.w, rtmax = r1.w;
     if (!(rtmax > rtmin)) return false;
     const f3 o = xyz(r0), d = xyz(r1);
@@ -305,10 +307,9 @@ __device__ bool scene_any(const SceneView& s, const float4 r0, const float4 r1) 
         const f3 ro = xform(e.inverse, o, 1.0f);
         const f3 rd = xform(e.inverse, d, 0.0f);
         Best bb{rtmax, -1.0f, -1, -1};
-        if (kStackless)
-            bvh_stackless<true, false>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb);
-        else
-            bvh_stack<true, false>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb);
+        iters += kStackless
+                     ? bvh_stackless<true, false>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests)
+                     : bvh_stack<true, false>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests);
         if (bb.closest > 0.0f) return true;
     }
     return false;

@@ -109,8 +109,23 @@ class Context:
         except Exception:
             pass
 
+    def read_counters(self, reset: bool = True) -> dict:
+        """Node visits / triangle tests accumulated by queries run with FLAG_COUNT."""
+        c = (C.c_int64 * 2)()
+        check(lib().rq_counters_read(self.handle, C.byref(c), int(reset)), self.handle)
+        return {"node_visits": c[0], "triangle_tests": c[1]}
+
     def scene(self, layout, vertices, tris, nodes, entities) -> "Scene":
         return Scene(self, layout, vertices, tris, nodes, entities)
+
+
+def _stream(t, stream):
+    """Stream for a device-tensor call: the caller's, else torch's current stream on the
+    tensor's device, so results are ordered with the torch work that consumes them."""
+    if stream is not None or t is None or isinstance(t, np.ndarray):
+        return stream
+    import torch
+    return torch.cuda.current_stream(t.device).cuda_stream
 
 
 def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0) -> L.RqOpts:
@@ -168,7 +183,7 @@ class Scene:
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
         o = _opts(layout, mode, tie, f, block_size)
         check(lib().rq_closest(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), C.byref(o),
-                               stream), self.ctx.handle)
+                               _stream(rays, stream)), self.ctx.handle)
         return hits
 
     def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, stream=None):
@@ -183,8 +198,84 @@ class Scene:
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
         o = _opts(layout, mode, 0, f, block_size)
         check(lib().rq_anyhit(self.ctx.handle, self.handle, ptr(rays), n, ptr(out), C.byref(o),
-                              stream), self.ctx.handle)
+                              _stream(rays, stream)), self.ctx.handle)
         return out
+
+
+def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode=0, query=0,
+              shadow_rays=False, shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866),
+              sun_color=(4.0, 3.8, 3.5), sky_color=(0.5, 0.7, 1.0)) -> L.RqGiParams:
+    """rq_gi_params for the diffuse-GI (query=0) or RTAO (query=1) pass."""
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
+    return L.RqGiParams(spp, seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode, query,
+                        int(shadow_rays), shadow_offset, f3(sd), f3(sun_color), f3(sky_color),
+                        (C.c_int32 * 3)())
+
+
+def _empty_like_dev(ref, shape, dtype):
+    import torch
+    return torch.empty(shape, dtype=dtype, device=ref.device)
+
+
+class _GiMixin:
+    def set_materials(self, albedo_rgb):
+        a = np.ascontiguousarray(albedo_rgb, dtype=np.float32).reshape(-1, 3)
+        check(lib().rq_scene_set_materials(self.handle, ptr(a), a.shape[0]), self.ctx.handle)
+
+    def gi_raygen(self, primary, hits, params, out=None, stream=None):
+        """Device tensors: primary (n*32 bytes), hits (n, 8) -> secondary rays (n*spp*32 bytes)."""
+        import torch
+        n = primary.numel() * primary.element_size() // 32
+        if out is None:
+            out = torch.empty(n * params.spp * 32, dtype=torch.uint8, device=primary.device)
+        check(lib().rq_gi_raygen(self.ctx.handle, self.handle, ptr(primary), ptr(hits), n,
+                                 C.byref(params), ptr(out), _stream(primary, stream)), self.ctx.handle)
+        return out
+
+    def shadow_raygen(self, rays, hits, params, out=None, stream=None):
+        import torch
+        n = rays.numel() * rays.element_size() // 32
+        if out is None:
+            out = torch.empty(n * 32, dtype=torch.uint8, device=rays.device)
+        check(lib().rq_shadow_raygen(self.ctx.handle, self.handle, ptr(rays), ptr(hits), n,
+                                     C.byref(params), ptr(out), _stream(rays, stream)),
+              self.ctx.handle)
+        return out
+
+    def shade(self, rays, hits, params, lit=None, out=None, stream=None):
+        import torch
+        n = rays.numel() * rays.element_size() // 32
+        if out is None:
+            out = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+        check(lib().rq_shade(self.ctx.handle, self.handle, ptr(rays), ptr(hits), n, ptr(lit),
+                             C.byref(params), ptr(out), _stream(rays, stream)), self.ctx.handle)
+        return out
+
+    def gi_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0,
+                 stats=False, stream=None):
+        """Whole GI / AO pass.  numpy primary rays -> host path (copies inside the call)."""
+        host = isinstance(primary, np.ndarray)
+        n = primary.shape[0] if host else primary.numel() * primary.element_size() // 32
+        if out is None:
+            if host:
+                out = np.empty((n, 4), dtype=np.float32)
+            else:
+                out = _empty_like_dev(primary, (n, 4), __import__("torch").float32)
+        st = L.RqFrameStats() if stats else None
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        check(lib().rq_gi_frame(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params),
+                                C.byref(o), ptr(out), C.byref(st) if st is not None else None,
+                                _stream(primary, stream)), self.ctx.handle)
+        if stats:
+            return out, {k: getattr(st, k) for k, _ in L.RqFrameStats._fields_}
+        return out
+
+
+for _name, _fn in list(vars(_GiMixin).items()):
+    if callable(_fn) and not _name.startswith("__"):
+        setattr(Scene, _name, _fn)
 
 
 class RayIntersector:

@@ -4,7 +4,7 @@
  * constructor, its flattened node / triangle / vertex buffers and the closest-hit / any-hit ray
  * API.  Every entry point names the reference interface it replaces.  Plain C types only: no
  * CUDA, C++ or torch types cross this boundary; `stream` arguments are cudaStream_t passed as
- * void* (NULL = the context's own stream).
+ * void* (NULL = the CUDA default stream, as everywhere in the CUDA runtime).
  *
  * Conventions
  *  - Every call returns rq_status.  On failure rq_last_error(ctx) holds a message.
@@ -124,7 +124,9 @@ enum {
     RQ_FLAG_IGNORE_TRANSPARENT = 2,  /* IntersectSceneIgnoreTransparent: skip entities with
                                         alpha < 0.99 (TraverseBVHStack.glsl:368-413) */
     RQ_FLAG_HOST_BUFFERS = 4,        /* ray/hit pointers are host memory */
-    RQ_FLAG_NO_PERSISTENT = 8        /* one thread per ray instead of the persistent kernel */
+    RQ_FLAG_NO_PERSISTENT = 8,       /* one thread per ray instead of the persistent kernel */
+    RQ_FLAG_COUNT = 16               /* accumulate node visits and triangle tests into the
+                                        context's work counters (rq_counters_read) */
 };
 
 typedef struct rq_opts {
@@ -147,6 +149,15 @@ const char* rq_status_string(rq_status s);
 rq_status rq_create(int device, rq_ctx** out);
 rq_status rq_destroy(rq_ctx* ctx);
 const char* rq_last_error(const rq_ctx* ctx);
+
+/* Work counters accumulated by queries run with RQ_FLAG_COUNT (the reference has only a
+ * per-ray iteration count, TraverseBVHStack.glsl:319).  Synchronises the context's stream.
+ * reset != 0 zeroes them after reading. */
+typedef struct rq_counters {
+    int64_t node_visits;
+    int64_t triangle_tests;
+} rq_counters;
+rq_status rq_counters_read(rq_ctx* ctx, rq_counters* out, int reset);
 
 /* ---- BVH construction (host) ------------------------------------------------------------ */
 
@@ -225,6 +236,63 @@ rq_status rq_closest(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int
  * 509-682; stackless :463-579), with the per-ray tmax the per-BVH functions accept. */
 rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
                     uint8_t* occluded, const rq_opts* opts, void* stream);
+
+/* ---- Diffuse GI / RTAO ------------------------------------------------------------------ */
+
+/* Parameters of the GI / AO pass that consumes the queries (Shaders/DiffuseTrace.glsl:386-662). */
+typedef struct rq_gi_params {
+    int32_t spp;           /* secondary rays per primary hit */
+    uint32_t seed;         /* sample-hash seed (e.g. the frame index) */
+    float origin_offset;   /* secondary origin = P + N * offset (DiffuseTrace.glsl:445 uses 0.05) */
+    float ray_tmax;        /* secondary tmax: 1e6 for GI, the AO radius for RTAO */
+    int32_t normal_mode;   /* 0 = interpolated half-packed vertex normal (GetData), 1 = geometric */
+    int32_t query;         /* 0 = closest-hit GI rays + Lambert shading, 1 = any-hit AO rays */
+    int32_t shadow_rays;   /* GI only: 1 = sun visibility from an any-hit shadow ray per GI hit
+                              (the reference reads a cascaded shadow map, DiffuseTrace.glsl:
+                              325-366); 0 = unshadowed */
+    float shadow_offset;   /* shadow origin = hit + N * offset */
+    float sun_dir[3];      /* u_SunDirection: direction the light travels */
+    float sun_color[3];    /* SUN_COLOR_DIFF */
+    float sky_color[3];    /* radiance returned by a miss (the reference samples u_Skymap) */
+    int32_t reserved[3];
+} rq_gi_params;
+
+typedef struct rq_frame_stats {
+    int64_t primary_rays, primary_hits;
+    int64_t secondary_rays, secondary_hits;  /* active secondary rays and their hits (or occluded) */
+    int64_t shadow_rays, shadow_occluded;
+} rq_frame_stats;
+
+/* Per-mesh albedo (rgb floats, indexed by the triangle's mesh id), the ModelColor of the
+ * reference's TextureReferences buffer (Intersector.h:373-418, GetData :440-451).  Meshes without
+ * an entry shade with albedo 0.8. */
+rq_status rq_scene_set_materials(rq_scene* scene, const float* albedo_rgb, int32_t n_meshes);
+
+/* Cosine-weighted secondary rays from primary hits: for primary ray i with a hit and k < spp,
+ * out[i*spp + k] = {P + N*offset, 0, CosWeightedHemisphere(N, hash(seed, i*spp + k)), ray_tmax}
+ * with N faced toward the incoming ray (DiffuseTrace.glsl:439-446, 486-488; Sampling.glsl:1-12);
+ * other slots are inactive (tmax = -1).  Device buffers. */
+rq_status rq_gi_raygen(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary,
+                       const rq_hit* hits, int64_t n, const rq_gi_params* params, rq_ray* out,
+                       void* stream);
+/* Shadow rays toward -sun_dir from the hits of `rays` (inactive where there is no hit). */
+rq_status rq_shadow_raygen(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays,
+                           const rq_hit* hits, int64_t n, const rq_gi_params* params, rq_ray* out,
+                           void* stream);
+/* Lambert shading of secondary hits: out4[j] = (albedo*sun*lit*clamp(dot(N,-sun),0,1) +
+ * albedo*emissive, AO) with AO = pow(clamp(t/2.4,0,1),1.23) (GetDirect DiffuseTrace.glsl:368-372,
+ * :490-494); a miss gives (sky, 1); an inactive ray (0,0,0,0).  lit may be NULL (all lit). */
+rq_status rq_shade(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, const rq_hit* hits,
+                   int64_t n, const uint8_t* lit, const rq_gi_params* params, float* out4,
+                   void* stream);
+/* Whole GI / RTAO pass for n primary rays (pixels): primary closest hit, secondary ray
+ * generation, secondary queries (closest + optional shadow any-hit, or AO any-hit), shading, and
+ * the per-pixel mean over spp written to pixels4 (rgb radiance, AO or visibility).  With
+ * RQ_FLAG_HOST_BUFFERS in opts, `primary` and `pixels4` are host memory.  `stats` (nullable)
+ * synchronises the stream to read the ray counts. */
+rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,
+                      const rq_gi_params* params, const rq_opts* opts, float* pixels4,
+                      rq_frame_stats* stats, void* stream);
 
 #ifdef __cplusplus
 }
