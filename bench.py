@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--config", default="c2", choices=["c1", "c2"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
+    ap.add_argument("--profile", action="store_true",
+                    help="run one GI pass and exit (the case the ncu captures use: the 2nd "
+                         "traversal launch is the full-size secondary closest-hit launch)")
     return ap.parse_args()
 
 
@@ -233,6 +236,12 @@ def main():
     sptr = stream.cuda_stream
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
+    if args.profile:
+        sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": wl["name"], "pixels": n}))
+        return
+
     # ray counts of one pass (untimed)
     _, st = sc.gi_frame(d_rays, p, out=d_pix, stats=True, stream=sptr)
     rays_per_step = st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
@@ -301,12 +310,12 @@ def main():
     peak, peak_kind = load_peaks()
     achieved = algo_bytes / (k_ms / 1e3) / 1e9
     traffic = None
-    prof = ROOT / "profiles" / "traffic.json"
+    prof = ROOT / "profiles" / "ncu_traffic.txt"
     if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get(args.config)
-        except Exception:
-            traffic = None
+        for ln in prof.read_text().splitlines():
+            f = ln.split()
+            if len(f) == 3 and not ln.startswith("#") and f[0] == args.config:
+                traffic = int(f[2])
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_kind": peak_kind, "kernel": "secondary " + ("any-hit" if q_any else "closest-hit") + " traversal (strict, stack BVH2)",
