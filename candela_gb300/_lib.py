@@ -94,7 +94,11 @@ SIGNATURES = {
     "rq_shade": (_S, [_P, _P, _P, _P, _I64, _P, C.POINTER(RqGiParams), _P, _P]),
     "rq_gi_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                          C.POINTER(RqFrameStats), _P]),
+    "rq_gi_frame_noalloc": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
+                                 _P]),
 }
+
+NOALLOC_MAX_RAYS = 65536
 
 _lib = None
 

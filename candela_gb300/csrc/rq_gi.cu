@@ -205,6 +205,41 @@ rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
 }
 
 }  // namespace
+
+// The GI pass over caller-provided intermediate buffers: the kernel sequence of rq_gi_frame
+// without its ray-count statistics.  Used by the no-allocation entry point (rq_noalloc.cu).
+cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
+                               const float* albedo, int32_t n_albedo, const rq_ray* prim,
+                               int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st) {
+    const GiArgs a = to_args(p);
+    const int64_t m = n * p.spp;
+    cudaError_t e = launch_closest(s, q, prim, n, b.primary_hits, nullptr, st);
+    if (e != cudaSuccess) return e;
+    k_gi_raygen<<<grid(m, 256), 256, 0, st>>>(s, prim, b.primary_hits, n, a, b.secondary, nullptr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (p.query == 1) {
+        if ((e = launch_anyhit(s, q, b.secondary, m, b.occluded, nullptr, st)) != cudaSuccess) return e;
+        k_ao_shade<<<grid(m, 256), 256, 0, st>>>(b.secondary, b.occluded, m, b.shaded);
+    } else {
+        if ((e = launch_closest(s, q, b.secondary, m, b.secondary_hits, nullptr, st)) != cudaSuccess)
+            return e;
+        const uint8_t* lit = nullptr;
+        if (p.shadow_rays) {
+            k_shadow_raygen<<<grid(m, 256), 256, 0, st>>>(s, b.secondary, b.secondary_hits, m, a,
+                                                          b.shadow, nullptr);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if ((e = launch_anyhit(s, q, b.shadow, m, b.occluded, nullptr, st)) != cudaSuccess)
+                return e;
+            lit = b.occluded;
+        }
+        k_shade<<<grid(m, 256), 256, 0, st>>>(s, b.secondary, b.secondary_hits, m, lit, lit ? 1 : 0,
+                                              albedo, n_albedo, a, b.shaded);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_accumulate<<<grid(n, 256), 256, 0, st>>>(b.shaded, n, p.spp, reinterpret_cast<float4*>(pixels4));
+    return cudaGetLastError();
+}
+
 }  // namespace rq
 
 using rq::fail;

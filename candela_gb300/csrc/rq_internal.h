@@ -42,4 +42,19 @@ cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ra
 cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                           uint8_t* occluded, int* work_counter, cudaStream_t st);
 
+// Intermediate buffers of one GI pass (n primary rays, n*spp secondary rays).
+struct GiBuffers {
+    rq_hit* primary_hits;    // n
+    rq_ray* secondary;       // n*spp
+    rq_hit* secondary_hits;  // n*spp
+    uint8_t* occluded;       // n*spp (AO or shadow any-hit results)
+    float4* shaded;          // n*spp
+    rq_ray* shadow;          // n*spp (shadow rays, GI with shadow_rays only)
+};
+
+// The GI pass over caller-provided intermediate buffers (rq_gi.cu).
+cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
+                               const float* albedo, int32_t n_albedo, const rq_ray* prim,
+                               int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st);
+
 }  // namespace rq

@@ -294,6 +294,31 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary,
                       const rq_gi_params* params, const rq_opts* opts, float* pixels4,
                       rq_frame_stats* stats, void* stream);
 
+/* ---- Allocation-free GI pass ------------------------------------------------------------ */
+
+/* Capacity of the fixed scratch used by rq_gi_frame_noalloc: at most this many primary rays, and
+ * at most this many secondary rays (n * spp). */
+#define RQ_NOALLOC_MAX_RAYS 65536
+
+/* The GI / RTAO pass of rq_gi_frame for callers that cannot allocate device memory while they
+ * render.  No counterpart in the reference (its GI pass is a GLSL dispatch over preallocated
+ * images).  cudaMalloc can synchronise the device and can fail under memory pressure, so frame
+ * loops that must keep their timing, and host applications that own all device memory through
+ * their own allocator and forbid plugins from allocating, cannot call rq_gi_frame, which grows
+ * its scratch on demand.  This variant allocates nothing: its intermediates live in one fixed
+ * __device__ array (about 9 MiB, held by every GPU that loads librq.so until the process exits).
+ *  - Device buffers only (RQ_FLAG_HOST_BUFFERS is rejected); no statistics.
+ *  - n > RQ_NOALLOC_MAX_RAYS or n * spp > RQ_NOALLOC_MAX_RAYS is rejected with RQ_EINVAL.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+ *    that device current; make that first call before any stream capture.
+ *  - All calls share the array: calls whose work overlaps on the GPU (different streams or host
+ *    threads) race and must be serialised by the caller.  Each call overwrites everything it
+ *    reads, so nothing from an earlier call leaks into its result.
+ * Results equal rq_gi_frame's for the same inputs. */
+rq_status rq_gi_frame_noalloc(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,
+                              const rq_gi_params* params, const rq_opts* opts, float* pixels4,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif
