@@ -120,6 +120,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def combine_ranks(total_ms: float, rays_per_step: int, steps: int, world: int, dist=None,
+                  device=None):
+    """N independent replicas (weak scaling): the job time is the slowest rank's, the value counts
+    every rank's rays.  Returns (max_ms, Mrays/s)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, rays_per_step * steps * world / (total_ms / 1e3) / 1e6
+
+
 def make_workload(config: str):
     import candela_gb300 as R
     from candela_gb300 import scenes as S
@@ -263,12 +275,8 @@ def main():
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = rays_per_step * args.steps * world / (total_ms / 1e3) / 1e6
+    total_ms, value = combine_ranks(float(sum(step_ms)), rays_per_step, args.steps, world, dist,
+                                    dev)
 
     # e2e: host buffers through the C ABI (pinned in, pinned out), host clock, sync per step
     h_rays = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)

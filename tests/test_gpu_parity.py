@@ -157,3 +157,19 @@ def test_leaf4_bvh(ctx):
     sc = ctx.scene(layout, *bufs)
     assert_hits_identical(hits_from_device(sc.closest(rays_to_device(rays))),
                           oracle_scene(bufs, layout).closest(rays), "leaf 4")
+
+
+@pytest.mark.parametrize("depth", [40, 70])
+def test_push_cap_on_gpu(ctx, depth):
+    """The reference's 63-push cap (TraverseBVHStack.glsl:293-295) on a hand-made chain BVH."""
+    from .test_oracle import _chain_bvh
+    v, t, n, e = _chain_bvh(depth)
+    rays = np.zeros(3, dtype=R.RAY_DTYPE)
+    rays["o"] = [[0, 0, 0.5], [0.1, -0.2, 0.7], [0.0, 0.3, -0.5]]
+    rays["d"] = [[0, 0, -1], [0, 0, -1], [0, 0, 1]]
+    rays["tmax"] = 1e6
+    osc = O.OracleScene(O.ORC_STACK, v, t, n, e)
+    sc = ctx.scene(R.STACK, v, t, n, e)
+    assert_hits_identical(hits_from_device(sc.closest(rays_to_device(rays))), osc.closest(rays),
+                          f"chain depth {depth}")
+    np.testing.assert_array_equal(sc.anyhit(rays_to_device(rays)).cpu().numpy(), osc.anyhit(rays))
