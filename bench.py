@@ -331,6 +331,39 @@ def main():
                 "node_visits": int(cnt["node_visits"]), "triangle_tests": int(cnt["triangle_tests"]),
                 "active_rays": int(st["secondary_rays"])}
 
+    # per-query breakdown (device-resident rays, L2 flushed before each timed launch)
+    def timed(fn, reps=max(3, min(args.steps, 10))):
+        for _ in range(2):
+            fn()
+        evs = []
+        for i in range(reps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    n_sec = int(st["secondary_rays"])
+    n_sec_slots = int(d_sec.numel() // 32)
+    breakdown = {}
+    cases = [
+        ("primary_closest_strict_stack", lambda: sc.closest(d_rays, stream=sptr), n),
+        ("secondary_closest_strict_stack", lambda: sc.closest(d_sec, stream=sptr), n_sec),
+        ("secondary_closest_strict_stack_one_thread_per_ray",
+         lambda: sc.closest(d_sec, flags=L.FLAG_NO_PERSISTENT, stream=sptr), n_sec),
+        ("secondary_anyhit_strict_stack", lambda: sc.anyhit(d_sec, stream=sptr), n_sec),
+    ]
+    for name, fn, rays_n in cases:
+        ms = timed(fn)
+        breakdown[name] = {"mrays_s": round(rays_n / (ms / 1e3) / 1e6, 1), "ms": round(ms, 4),
+                           "rays": rays_n}
+    breakdown["note"] = (f"secondary launches cover {n_sec_slots} ray slots of which {n_sec} are "
+                         "active (pixels whose primary ray missed give inactive slots); Mrays/s "
+                         "counts active rays")
+
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -342,7 +375,7 @@ def main():
                        "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
                        "bvh_build_s": round(wl["build_s"], 3)},
             "e2e": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in e2e.items()},
-            "roofline": roofline, "clocks": clk.summary(),
+            "roofline": roofline, "breakdown": breakdown, "clocks": clk.summary(),
             "gpu_launches": launches_per_step * args.steps}
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)

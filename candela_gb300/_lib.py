@@ -49,6 +49,11 @@ class RqBvhInfo(C.Structure):
                 ("split_fails", C.c_int64), ("build_ms", C.c_double)]
 
 
+class RqBvh8Info(C.Structure):
+    _fields_ = [("nodes", C.c_int64), ("triangles", C.c_int64), ("bytes", C.c_int64),
+                ("bvh2_nodes", C.c_int64), ("build_ms", C.c_double)]
+
+
 class RqGiParams(C.Structure):
     _fields_ = [("spp", C.c_int32), ("seed", C.c_uint32), ("origin_offset", C.c_float),
                 ("ray_tmax", C.c_float), ("normal_mode", C.c_int32), ("query", C.c_int32),
@@ -88,6 +93,11 @@ SIGNATURES = {
     "rq_closest": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_anyhit": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_counters_read": (_S, [_P, C.POINTER(C.c_int64 * 2), C.c_int]),
+    "rq_device_status": (_S, [_P, C.POINTER(C.c_uint32), C.c_int]),
+    "rq_scene_build_bvh8": (_S, [_P, C.POINTER(RqBvh8Info)]),
+    "rq_build_bvh8": (_S, [_S, _P, _I64, _P, _I64, _P, _I64, _I32, _I32, C.POINTER(_P)]),
+    "rq_bvh8_buffers": (_S, [_P, C.POINTER(_P), C.POINTER(_I64), C.POINTER(_P), C.POINTER(_I64)]),
+    "rq_bvh8_free": (None, [_P]),
     "rq_scene_set_materials": (_S, [_P, _P, _I32]),
     "rq_gi_raygen": (_S, [_P, _P, _P, _P, _I64, C.POINTER(RqGiParams), _P, _P]),
     "rq_shadow_raygen": (_S, [_P, _P, _P, _P, _I64, C.POINTER(RqGiParams), _P, _P]),

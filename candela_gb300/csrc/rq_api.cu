@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/rq.h"
+#include "bvh8.h"
 #include "bvh_build.h"
 #include "rq_internal.h"
 #include "rq_objects.h"
@@ -57,6 +58,13 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
         return fail(ctx, RQ_EINVAL, "unknown tie rule");
     if (q.mode != RQ_MODE_STRICT && q.mode != RQ_MODE_FAST)
         return fail(ctx, RQ_EINVAL, "unknown mode");
+    q.status = status_word(ctx);
+    if (q.layout == RQ_LAYOUT_BVH8Q) {
+        if (!sc->bvh8) return fail(ctx, RQ_ENOTSUP, "BVH8 not built: call rq_scene_build_bvh8");
+        if (q.mode != RQ_MODE_STRICT || !q.tie_lower)
+            return fail(ctx, RQ_ENOTSUP, "BVH8 queries use strict leaf tests and lower-index ties");
+        return RQ_OK;
+    }
     if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
     if (q.mode == RQ_MODE_FAST) return fail(ctx, RQ_ENOTSUP, "fast mode not available");
     return RQ_OK;
@@ -68,6 +76,7 @@ namespace {
 
 using rq::fail;
 using rq::cuda_fail;
+using rq::status_word;
 
 bool is_identity(const float* m) {
     for (int c = 0; c < 4; ++c)
@@ -121,7 +130,7 @@ rq_status staged(rq_ctx* ctx, const void* h_in, size_t in_stride, void* h_out, s
         cudaStream_t st = ctx->pipe[k];
         RQ_CUDA(ctx, cudaMemcpyAsync(ctx->stage_in[k], static_cast<const char*>(h_in) + off * in_stride,
                                      m * in_stride, cudaMemcpyHostToDevice, st));
-        RQ_CUDA(ctx, launch(ctx->stage_in[k], ctx->stage_out[k], m, st));
+        RQ_CUDA(ctx, launch(ctx->stage_in[k], ctx->stage_out[k], m, st, rq::queue_counter(ctx, 4 + k)));
         RQ_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(h_out) + off * out_stride, ctx->stage_out[k],
                                      m * out_stride, cudaMemcpyDeviceToHost, st));
     }
@@ -281,6 +290,51 @@ rq_status rq_bvh_triangles(const rq_bvh* b, const rq_triangle** tris, int64_t* n
 
 void rq_bvh_free(rq_bvh* b) { delete b; }
 
+// ---- BVH8 (host) ---------------------------------------------------------------------------
+
+struct rq_bvh8 {
+    rq::Bvh8Out out;
+};
+
+rq_status rq_build_bvh8(rq_layout layout, const void* nodes, int64_t n_nodes, const rq_triangle* tris,
+                        int64_t n_tris, const rq_vertex* verts, int64_t n_verts, int32_t node_offset,
+                        int32_t node_count, rq_bvh8** out) {
+    if (!out || !nodes || !tris || !verts) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    *out = nullptr;
+    auto* b = new (std::nothrow) rq_bvh8;
+    if (!b) return fail(nullptr, RQ_ENOMEM, "allocation failed");
+    std::string why;
+    std::vector<rq::Bvh8Range> r{{node_offset, node_count}};
+    bool ok;
+    try {
+        ok = rq::build_bvh8(layout, static_cast<const float*>(nodes), n_nodes,
+                            reinterpret_cast<const int32_t*>(tris), n_tris,
+                            reinterpret_cast<const float*>(verts), n_verts, r, b->out, why);
+    } catch (const std::bad_alloc&) {
+        delete b;
+        return fail(nullptr, RQ_ENOMEM, "host allocation failed");
+    }
+    if (!ok) {
+        delete b;
+        return fail(nullptr, RQ_EINVAL, "BVH8 build: " + why);
+    }
+    *out = b;
+    return RQ_OK;
+}
+
+rq_status rq_bvh8_buffers(const rq_bvh8* b, const uint32_t** nodes, int64_t* n_nodes,
+                          const float** tri_records, int64_t* n_records) {
+    if (!b || !nodes || !n_nodes || !tri_records || !n_records)
+        return fail(nullptr, RQ_EINVAL, "NULL argument");
+    *nodes = b->out.nodes.data();
+    *n_nodes = b->out.n_nodes;
+    *tri_records = b->out.tris.data();
+    *n_records = b->out.n_tris;
+    return RQ_OK;
+}
+
+void rq_bvh8_free(rq_bvh8* b) { delete b; }
+
 // ---- Scene -----------------------------------------------------------------------------------
 
 rq_status rq_scene_validate(rq_layout layout, const rq_vertex* verts, int64_t n_verts,
@@ -317,6 +371,10 @@ rq_status rq_scene_create(rq_ctx* ctx, rq_layout layout, const rq_vertex* verts,
     const size_t node_bytes = layout == RQ_LAYOUT_BVH2_STACK ? 64 : 32;
     sc->h_nodes.assign(static_cast<const float*>(nodes),
                        static_cast<const float*>(nodes) + n_nodes * (node_bytes / 4));
+    sc->h_tris.assign(reinterpret_cast<const int32_t*>(tris),
+                      reinterpret_cast<const int32_t*>(tris) + 4 * n_tris);
+    sc->h_verts.assign(reinterpret_cast<const float*>(verts),
+                       reinterpret_cast<const float*>(verts) + 8 * n_verts);
     const size_t nb = node_bytes * n_nodes, tb = 16 * n_tris, vb = 32 * n_verts;
     cudaError_t e;
     if ((e = cudaMalloc(&sc->d_nodes, nb)) != cudaSuccess || (e = cudaMalloc(&sc->d_tris, tb)) != cudaSuccess ||
@@ -370,12 +428,78 @@ rq_status rq_scene_set_entities(rq_scene* sc, const rq_entity* ents, int32_t n_e
     bool ident = true;
     for (int i = 0; i < n_ents; ++i) ident = ident && is_identity(ents[i].inverse);
     sc->view.all_identity = ident ? 1 : 0;
+    sc->h_ents.assign(ents, ents + n_ents);
+    if (sc->bvh8) return rq_scene_build_bvh8(sc, nullptr);
+    return RQ_OK;
+}
+
+rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
+    if (!sc) return fail(nullptr, RQ_EINVAL, "NULL scene");
+    rq_ctx* ctx = sc->ctx;
+    std::vector<rq::Bvh8Range> ranges;
+    for (const rq_entity& e : sc->h_ents) ranges.push_back({e.node_offset, e.node_count});
+    rq::Bvh8Out b;
+    std::string why;
+    bool ok;
+    try {
+        ok = rq::build_bvh8(sc->layout, sc->h_nodes.data(), sc->n_nodes, sc->h_tris.data(), sc->n_tris,
+                            sc->h_verts.data(), sc->n_verts, ranges, b, why);
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, RQ_ENOMEM, "host allocation failed during BVH8 build");
+    }
+    if (!ok) return fail(ctx, RQ_ENOTSUP, "BVH8 build: " + why);
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (sc->d_b8nodes) cudaFree(sc->d_b8nodes);
+    if (sc->d_b8tris) cudaFree(sc->d_b8tris);
+    sc->d_b8nodes = nullptr;
+    sc->d_b8tris = nullptr;
+    sc->bvh8 = false;
+    const size_t nb = b.nodes.size() * 4, tb = std::max<size_t>(16, b.tris.size() * 4);
+    if (cudaMalloc(&sc->d_b8nodes, nb) != cudaSuccess || cudaMalloc(&sc->d_b8tris, tb) != cudaSuccess)
+        return fail(ctx, RQ_ENOMEM, "BVH8 device allocation failed");
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_b8nodes, b.nodes.data(), nb, cudaMemcpyHostToDevice));
+    if (!b.tris.empty())
+        RQ_CUDA(ctx, cudaMemcpy(sc->d_b8tris, b.tris.data(), b.tris.size() * 4, cudaMemcpyHostToDevice));
+    const int32_t ne = static_cast<int32_t>(b.roots.size());
+    if (ne > sc->b8roots_cap) {
+        if (sc->d_b8roots) cudaFree(sc->d_b8roots);
+        sc->d_b8roots = nullptr;
+        sc->b8roots_cap = 0;
+        if (cudaMalloc(&sc->d_b8roots, sizeof(int32_t) * ne) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "BVH8 root table allocation failed");
+        sc->b8roots_cap = ne;
+    }
+    if (ne) RQ_CUDA(ctx, cudaMemcpy(sc->d_b8roots, b.roots.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
+    sc->b8_nodes = b.n_nodes;
+    sc->b8_tris = b.n_tris;
+    sc->b8_bytes = static_cast<int64_t>(nb + tb + sizeof(int32_t) * sc->b8roots_cap);
+    sc->b8_build_ms = b.build_ms;
+    sc->view.b8_nodes = sc->d_b8nodes;
+    sc->view.b8_tris = sc->d_b8tris;
+    sc->view.b8_roots = sc->d_b8roots;
+    sc->bvh8 = true;
+    if (info) {
+        info->nodes = b.n_nodes;
+        info->triangles = b.n_tris;
+        info->bytes = sc->b8_bytes;
+        info->bvh2_nodes = b.bvh2_nodes;
+        info->build_ms = b.build_ms;
+    }
+    return RQ_OK;
+}
+
+rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset) {
+    if (!ctx || !bits) return fail(ctx, RQ_EINVAL, "NULL argument");
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    RQ_CUDA(ctx, cudaDeviceSynchronize());
+    RQ_CUDA(ctx, cudaMemcpy(bits, rq::status_word(ctx), sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (reset) RQ_CUDA(ctx, cudaMemset(rq::status_word(ctx), 0, sizeof(uint32_t)));
     return RQ_OK;
 }
 
 rq_status rq_scene_bytes(const rq_scene* sc, int64_t* bytes) {
     if (!sc || !bytes) return fail(nullptr, RQ_EINVAL, "NULL argument");
-    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap;
+    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap + sc->b8_bytes;
     return RQ_OK;
 }
 
@@ -387,6 +511,9 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_verts) cudaFree(sc->d_verts);
     if (sc->d_ents) cudaFree(sc->d_ents);
     if (sc->d_albedo) cudaFree(sc->d_albedo);
+    if (sc->d_b8nodes) cudaFree(sc->d_b8nodes);
+    if (sc->d_b8tris) cudaFree(sc->d_b8tris);
+    if (sc->d_b8roots) cudaFree(sc->d_b8roots);
     delete sc;
     return RQ_OK;
 }
@@ -407,12 +534,12 @@ rq_status rq_closest(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_
     const rq::SceneView view = sc->view;
     if (q.flags & RQ_FLAG_HOST_BUFFERS) {
         return staged(ctx, rays, sizeof(rq_ray), hits, sizeof(rq_hit), n, st,
-                      [&](void* din, void* dout, int64_t m, cudaStream_t cs) {
+                      [&](void* din, void* dout, int64_t m, cudaStream_t cs, unsigned long long* qc) {
                           return rq::launch_closest(view, q, static_cast<const rq_ray*>(din), m,
-                                                    static_cast<rq_hit*>(dout), nullptr, cs);
+                                                    static_cast<rq_hit*>(dout), qc, cs);
                       });
     }
-    RQ_CUDA(ctx, rq::launch_closest(view, q, rays, n, hits, ctx->counters, st));
+    RQ_CUDA(ctx, rq::launch_closest(view, q, rays, n, hits, rq::queue_counter(ctx, 0), st));
     return RQ_OK;
 }
 
@@ -430,12 +557,12 @@ rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t
     const rq::SceneView view = sc->view;
     if (q.flags & RQ_FLAG_HOST_BUFFERS) {
         return staged(ctx, rays, sizeof(rq_ray), occluded, 1, n, st,
-                      [&](void* din, void* dout, int64_t m, cudaStream_t cs) {
+                      [&](void* din, void* dout, int64_t m, cudaStream_t cs, unsigned long long* qc) {
                           return rq::launch_anyhit(view, q, static_cast<const rq_ray*>(din), m,
-                                                   static_cast<uint8_t*>(dout), nullptr, cs);
+                                                   static_cast<uint8_t*>(dout), qc, cs);
                       });
     }
-    RQ_CUDA(ctx, rq::launch_anyhit(view, q, rays, n, occluded, ctx->counters, st));
+    RQ_CUDA(ctx, rq::launch_anyhit(view, q, rays, n, occluded, rq::queue_counter(ctx, 0), st));
     return RQ_OK;
 }
 

@@ -348,18 +348,18 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     rq_ray* sec = static_cast<rq_ray*>(d_sec);
     rq_hit* shit = static_cast<rq_hit*>(d_shit);
     float4* shade = static_cast<float4*>(d_shade);
-    RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, ctx->counters + 32, st));
+    RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, rq::queue_counter(ctx, 0), st));
     if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
     rq::k_gi_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
                                                       stats ? cnt + 1 : nullptr);
     RQ_CUDA(ctx, cudaGetLastError());
     if (p->query == 1) {
         uint8_t* occ = static_cast<uint8_t*>(d_occ);
-        RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sec, m, occ, ctx->counters + 40, st));
+        RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sec, m, occ, rq::queue_counter(ctx, 1), st));
         if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 2);
         rq::k_ao_shade<<<rq::grid(m, 256), 256, 0, st>>>(sec, occ, m, shade);
     } else {
-        RQ_CUDA(ctx, rq::launch_closest(sc->view, q, sec, m, shit, ctx->counters + 40, st));
+        RQ_CUDA(ctx, rq::launch_closest(sc->view, q, sec, m, shit, rq::queue_counter(ctx, 1), st));
         if (stats) rq::k_count_hits<<<rq::grid(m, 256), 256, 0, st>>>(shit, m, cnt + 2);
         const uint8_t* lit = nullptr;
         if (p->shadow_rays) {
@@ -370,7 +370,7 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
             uint8_t* occ = static_cast<uint8_t*>(d_lit);
             rq::k_shadow_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh,
                                                                   stats ? cnt + 3 : nullptr);
-            RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sh, m, occ, ctx->counters + 48, st));
+            RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sh, m, occ, rq::queue_counter(ctx, 2), st));
             if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 4);
             lit = occ;  // occlusion bytes: k_shade reads them inverted
         }

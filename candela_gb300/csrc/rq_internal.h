@@ -22,8 +22,11 @@ struct SceneView {
     int32_t layout;           // RQ_LAYOUT_BVH2_STACK / RQ_LAYOUT_BVH2_STACKLESS
     int32_t all_identity;     // every entity's inverse matrix is exactly the identity
     int32_t pad;
-    // Fast-mode triangle records in leaf order: {v0.xyz, mesh}, {e1.xyz, i0}, {e2.xyz, 0}.
-    const float4* tri_fast;
+    // BVH8 with quantised child boxes (rq_scene_build_bvh8): nodes (5 x uint4), triangle records
+    // (4 x float4), BVH8 root per entity (-1: none).
+    const uint4* b8_nodes;
+    const float4* b8_tris;
+    const int32_t* b8_roots;
 };
 
 // Query configuration resolved by the host API.
@@ -34,13 +37,16 @@ struct QueryConfig {
     int32_t flags;
     int32_t block;
     unsigned long long* counters;  // non-null: accumulate node visits / triangle tests here
+    unsigned* status;              // device status bits (stack overflow, iteration budget)
 };
 
 // Kernel launchers (rq_kernels.cu).  Return cudaGetLastError() after the launch.
+// `queue` (nullable) is a device ray counter for the persistent kernels; without one (or with
+// RQ_FLAG_NO_PERSISTENT) one thread runs per ray.
 cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
-                           rq_hit* hits, int* work_counter, cudaStream_t st);
+                           rq_hit* hits, unsigned long long* queue, cudaStream_t st);
 cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
-                          uint8_t* occluded, int* work_counter, cudaStream_t st);
+                          uint8_t* occluded, unsigned long long* queue, cudaStream_t st);
 
 // Intermediate buffers of one GI pass (n primary rays, n*spp secondary rays).
 struct GiBuffers {

@@ -1,7 +1,14 @@
 // Ray-query kernels and their launchers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include <mutex>
+#include <unordered_map>
+
 #include "rq_internal.h"
+#include "rq_bvh8.cuh"
+#include "rq_persistent.cuh"
 #include "rq_strict.cuh"
 
 namespace rq {
@@ -63,16 +70,188 @@ __global__ void __launch_bounds__(128) k_anyhit_strict(SceneView s, const rq_ray
     if (counters) count_work(counters, iters, tests);
 }
 
+// Persistent strict traversal (closest or any hit): see rq_persistent.cuh.
+template <bool kAny, bool kStackless, bool kTieLower>
+__global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq_ray* __restrict__ rays,
+                                                           int64_t n, rq_hit* __restrict__ hits,
+                                                           uint8_t* __restrict__ occ, int flags,
+                                                           unsigned long long* queue,
+                                                           unsigned long long* counters) {
+    persist::StrictRay<kAny, kStackless, kTieLower> R;
+    int32_t stack[kStackless ? 1 : 64];
+    int64_t id = -1;
+    bool need = true;
+    int32_t tests = 0, nodes = 0;
+    while (true) {
+        const int64_t nid = persist::fetch(queue, need);
+        if (need) {
+            id = nid;
+            if (id >= n) break;
+            float4 r0, r1;
+            load_ray(rays, id, r0, r1);
+            if (!R.init(s, r0, r1, flags)) {
+                if (kAny) {
+                    occ[id] = 0;
+                } else {
+                    rq_hit h;
+                    R.finish(s, flags, h);
+                    store_hit(hits, id, h);
+                }
+                continue;
+            }
+            need = false;
+        }
+        if (R.step(s, stack, tests) && !R.end_entity(s, flags)) {
+            nodes += R.iters_total;
+            if (kAny) {
+                occ[id] = R.occluded ? 1 : 0;
+            } else {
+                rq_hit h;
+                R.finish(s, flags, h);
+                store_hit(hits, id, h);
+            }
+            need = true;
+        }
+    }
+    if (counters) count_work(counters, nodes, tests);
+}
+
+// BVH8 traversal, one thread per ray, with the strict scene loop around it.
+template <bool kAny>
+__global__ void __launch_bounds__(128) k_bvh8(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
+                                              rq_hit* __restrict__ hits, uint8_t* __restrict__ occ,
+                                              int flags, unsigned* status_out,
+                                              unsigned long long* counters) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int32_t visits = 0, tests = 0;
+    unsigned status = 0;
+    if (i < n) {
+        float4 r0, r1;
+        load_ray(rays, i, r0, r1);
+        const float rtmin = r0.w, rtmax = r1.w;
+        const strict::f3 o = strict::xyz(r0), d = strict::xyz(r1);
+        float tmax = rtmax, closest = -1.0f;
+        int32_t mesh = -1, tri = -1, ent = -1;
+        bool occluded = false;
+        if (rtmax > rtmin) {
+            for (int e = 0; e < s.n_ents; ++e) {
+                const rq_entity& E = s.ents[e];
+                if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f)
+                    continue;
+                const int32_t root = s.b8_roots[e];
+                if (root < 0) continue;
+                const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
+                                                    strict::xform(E.inverse, d, 0.0f));
+                bvh8::Hit8 h{kAny ? rtmax : tmax, -1.0f, kAny ? -1 : tri, -1};
+                visits += bvh8::traverse<kAny, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h,
+                                                     tests, status);
+                const float T = h.closest;
+                if (kAny) {
+                    if (T > 0.0f) {
+                        occluded = true;
+                        break;
+                    }
+                } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+                    tmax = T;
+                    closest = T;
+                    mesh = h.mesh;
+                    tri = h.tri;
+                    ent = e;
+                }
+            }
+        }
+        if (kAny) {
+            occ[i] = occluded ? 1 : 0;
+        } else {
+            rq_hit hh;
+            hh.t = hh.u = hh.v = hh.w = -1.0f;
+            hh.tri = hh.mesh = hh.entity = -1;
+            hh.iters = visits;
+            if (closest > 0.0f) {
+                hh.tri = tri;
+                hh.mesh = mesh;
+                hh.entity = ent;
+                const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
+                if (report) {
+                    const rq_entity& E = s.ents[ent];
+                    const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
+                    const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
+                    const int4 tr = strict::ldg4i(s.tris + tri);
+                    const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
+                    float u, v, w;
+                    strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y),
+                                         strict::vpos(s, tr.z), u, v, w);
+                    hh.t = closest;
+                    hh.u = u;
+                    hh.v = v;
+                    hh.w = w;
+                }
+            }
+            store_hit(hits, i, hh);
+        }
+    }
+    if (status) atomicOr(status_out, status);
+    if (counters) count_work(counters, visits, tests);
+}
+
 inline unsigned grid_for(int64_t n, int block) {
     return static_cast<unsigned>((n + block - 1) / block);
 }
 
 }  // namespace
 
+namespace {
+
+// Resident-grid size of a persistent kernel (SM count x resident blocks), cached per device.
+template <class K>
+int persistent_grid(K kernel, int block) {
+    static std::mutex mu;
+    static std::unordered_map<long long, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long long key = (reinterpret_cast<long long>(reinterpret_cast<const void*>(kernel)) << 6) ^ dev;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    const int g = sms * (per_sm > 0 ? per_sm : 1);
+    cache[key] = g;
+    return g;
+}
+
+template <bool kAny, bool kStackless, bool kTieLower>
+cudaError_t launch_persistent(const SceneView& s, const QueryConfig& q, const rq_ray* rays,
+                              int64_t n, rq_hit* hits, uint8_t* occ, unsigned long long* queue,
+                              cudaStream_t st) {
+    const int block = 128;
+    auto k = k_persistent_strict<kAny, kStackless, kTieLower>;
+    const int64_t g = std::min<int64_t>(persistent_grid(k, block), (n + block - 1) / block);
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k<<<static_cast<unsigned>(g), block, 0, st>>>(s, rays, n, hits, occ, q.flags, queue, q.counters);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
-                           rq_hit* hits, int* /*work_counter*/, cudaStream_t st) {
+                           rq_hit* hits, unsigned long long* queue, cudaStream_t st) {
     unsigned long long* cnt = q.counters;
     if (n <= 0) return cudaSuccess;
+    if (q.layout == RQ_LAYOUT_BVH8Q) {
+        k_bvh8<false><<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, hits, nullptr, q.flags, q.status, cnt);
+        return cudaGetLastError();
+    }
+    if (queue && !(q.flags & RQ_FLAG_NO_PERSISTENT)) {
+        const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
+        if (sl)
+            return q.tie_lower ? launch_persistent<false, true, true>(s, q, rays, n, hits, nullptr, queue, st)
+                               : launch_persistent<false, true, false>(s, q, rays, n, hits, nullptr, queue, st);
+        return q.tie_lower ? launch_persistent<false, false, true>(s, q, rays, n, hits, nullptr, queue, st)
+                           : launch_persistent<false, false, false>(s, q, rays, n, hits, nullptr, queue, st);
+    }
     const int block = 128;
     const bool stackless = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
     if (stackless) {
@@ -90,9 +269,18 @@ cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ra
 }
 
 cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
-                          uint8_t* occluded, int* /*work_counter*/, cudaStream_t st) {
+                          uint8_t* occluded, unsigned long long* queue, cudaStream_t st) {
     unsigned long long* cnt = q.counters;
     if (n <= 0) return cudaSuccess;
+    if (q.layout == RQ_LAYOUT_BVH8Q) {
+        k_bvh8<true><<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, nullptr, occluded, q.flags, q.status, cnt);
+        return cudaGetLastError();
+    }
+    if (queue && !(q.flags & RQ_FLAG_NO_PERSISTENT)) {
+        if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
+            return launch_persistent<true, true, false>(s, q, rays, n, nullptr, occluded, queue, st);
+        return launch_persistent<true, false, false>(s, q, rays, n, nullptr, occluded, queue, st);
+    }
     const int block = 128;
     if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
         k_anyhit_strict<true><<<grid_for(n, block), block, 0, st>>>(s, rays, n, occluded, cnt);

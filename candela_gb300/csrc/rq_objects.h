@@ -46,6 +46,18 @@ struct rq_scene {
     rq::SceneView view{};
     float* d_albedo = nullptr;  // 3 floats per mesh id
     int32_t n_albedo = 0;
+    // host copies (validation and derived layouts)
+    std::vector<int32_t> h_tris;
+    std::vector<float> h_verts;
+    std::vector<rq_entity> h_ents;
+    // BVH8 with quantised boxes (built on request)
+    bool bvh8 = false;
+    uint4* d_b8nodes = nullptr;
+    float4* d_b8tris = nullptr;
+    int32_t* d_b8roots = nullptr;
+    int32_t b8roots_cap = 0;
+    int64_t b8_nodes = 0, b8_tris = 0, b8_bytes = 0;
+    double b8_build_ms = 0.0;
 };
 
 namespace rq {
@@ -57,6 +69,12 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
 // Query work counters (2 x u64) inside the context's counter block.
 inline unsigned long long* work_counters(rq_ctx* ctx) {
     return reinterpret_cast<unsigned long long*>(ctx->counters) + 8;
+}
+// Device status bits of the kernels (atomicOr), read by rq_device_status.
+inline unsigned* status_word(rq_ctx* ctx) { return reinterpret_cast<unsigned*>(ctx->counters) + 30; }
+// Ray-queue counter k (0..15) of the persistent kernels, inside the context's counter block.
+inline unsigned long long* queue_counter(rq_ctx* ctx, int k) {
+    return reinterpret_cast<unsigned long long*>(ctx->counters) + 16 + k;
 }
 // Grow-only device scratch buffer of the context (slot < kScratchSlots).
 rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out);

@@ -63,6 +63,27 @@ def build_bvh(vertices: np.ndarray, indices: np.ndarray, mesh_ids=None, tri_offs
         lib().rq_bvh_free(h)
 
 
+def build_bvh8_host(layout, nodes, tris, vertices, node_offset=0, node_count=None):
+    """rq_build_bvh8: host-side BVH8 of one object.  Returns (nodes uint32 (N, 20),
+    triangle records float32 (M, 16))."""
+    n = np.ascontiguousarray(nodes, dtype=np.float32)
+    t = np.ascontiguousarray(tris, dtype=np.int32)
+    v = np.ascontiguousarray(vertices)
+    node_count = n.shape[0] - node_offset if node_count is None else node_count
+    h = C.c_void_p()
+    check(lib().rq_build_bvh8(layout, ptr(n), n.shape[0], ptr(t), t.shape[0], ptr(v), v.shape[0],
+                              node_offset, node_count, C.byref(h)))
+    try:
+        np_, nn, tp, nt = C.c_void_p(), C.c_int64(), C.c_void_p(), C.c_int64()
+        check(lib().rq_bvh8_buffers(h, C.byref(np_), C.byref(nn), C.byref(tp), C.byref(nt)))
+        nodes8 = np.frombuffer(C.string_at(np_.value, nn.value * 80), dtype=np.uint32).reshape(-1, 20).copy()
+        recs = (np.frombuffer(C.string_at(tp.value, nt.value * 64), dtype=np.float32).reshape(-1, 16).copy()
+                if nt.value else np.zeros((0, 16), np.float32))
+        return nodes8, recs
+    finally:
+        lib().rq_bvh8_free(h)
+
+
 def validate_scene(layout, vertices, tris, nodes, entities) -> tuple[bool, str]:
     """rq_scene_validate: host-only check of the buffers a scene upload would receive."""
     msg = C.create_string_buffer(512)
@@ -109,6 +130,12 @@ class Context:
         except Exception:
             pass
 
+    def device_status(self, reset: bool = True) -> int:
+        """Kernel status bits since the last reset (1 = BVH8 stack overflow, 2 = visit budget)."""
+        b = C.c_uint32()
+        check(lib().rq_device_status(self.handle, C.byref(b), int(reset)), self.handle)
+        return b.value
+
     def read_counters(self, reset: bool = True) -> dict:
         """Node visits / triangle tests accumulated by queries run with FLAG_COUNT."""
         c = (C.c_int64 * 2)()
@@ -150,6 +177,12 @@ class Scene:
     def set_entities(self, entities):
         e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
         check(lib().rq_scene_set_entities(self.handle, ptr(e), e.shape[0]), self.ctx.handle)
+
+    def build_bvh8(self) -> dict:
+        """rq_scene_build_bvh8: enables RQ_LAYOUT_BVH8Q queries on this scene."""
+        info = L.RqBvh8Info()
+        check(lib().rq_scene_build_bvh8(self.handle, C.byref(info)), self.ctx.handle)
+        return {k: getattr(info, k) for k, _ in L.RqBvh8Info._fields_}
 
     def device_bytes(self) -> int:
         b = C.c_int64()

@@ -14,6 +14,8 @@
  *    With RQ_FLAG_HOST_BUFFERS the call synchronises before returning.
  *  - One rq_ctx per host thread.  One GPU per context.  There is no CPU fallback: a context can
  *    only be created on a CUDA device.
+ *  - Queries through one context share its device work counters: do not run them concurrently
+ *    on different streams (use one context per concurrent stream).
  */
 #ifndef RQ_H_
 #define RQ_H_
@@ -159,6 +161,11 @@ typedef struct rq_counters {
 } rq_counters;
 rq_status rq_counters_read(rq_ctx* ctx, rq_counters* out, int reset);
 
+/* Status bits raised by kernels since the last reset (synchronises the device): bit 0 = a BVH8
+ * traversal stack overflowed, bit 1 = a traversal exhausted its node-visit budget.  Such rays
+ * return the best hit found so far; the bits make that visible.  0 = clean. */
+rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset);
+
 /* ---- BVH construction (host) ------------------------------------------------------------ */
 
 typedef struct rq_bvh rq_bvh;
@@ -197,6 +204,19 @@ rq_status rq_bvh_nodes(const rq_bvh* bvh, const void** nodes, int64_t* n_nodes);
 rq_status rq_bvh_triangles(const rq_bvh* bvh, const rq_triangle** tris, int64_t* n_tris);
 void rq_bvh_free(rq_bvh* bvh);
 
+/* Host-side BVH8 derivation for one object (what rq_scene_build_bvh8 does per object), for
+ * inspection and offline use.  `nodes` is a BVH2 buffer of `layout`; the object occupies nodes
+ * [node_offset, node_offset + node_count).  Output: 80-byte nodes (root = node 0) and 64-byte
+ * triangle records {v0, tri}, {e1, mesh}, {e2, 0}, {n, 0}; the node format is documented in
+ * candela_gb300/csrc/bvh8.h.  No counterpart in the reference. */
+typedef struct rq_bvh8 rq_bvh8;
+rq_status rq_build_bvh8(rq_layout layout, const void* nodes, int64_t n_nodes,
+                        const rq_triangle* tris, int64_t n_tris, const rq_vertex* verts,
+                        int64_t n_verts, int32_t node_offset, int32_t node_count, rq_bvh8** out);
+rq_status rq_bvh8_buffers(const rq_bvh8* b, const uint32_t** nodes, int64_t* n_nodes,
+                          const float** tri_records, int64_t* n_records);
+void rq_bvh8_free(rq_bvh8* b);
+
 /* ---- Scene upload ----------------------------------------------------------------------- */
 
 typedef struct rq_scene rq_scene;
@@ -219,6 +239,17 @@ rq_status rq_scene_validate(rq_layout layout, const rq_vertex* verts, int64_t n_
                             size_t msg_len);
 /* Replaces RayIntersector<T>::PushEntities + BufferEntities (Intersector.h:200-239). */
 rq_status rq_scene_set_entities(rq_scene* scene, const rq_entity* ents, int32_t n_ents);
+/* Derives an 8-wide BVH with 8-bit conservatively quantised child boxes (RQ_LAYOUT_BVH8Q) from
+ * the scene's BVH2 buffers, for every object its entities reference, and uploads it.  Queries with
+ * RQ_LAYOUT_BVH8Q test leaves with the strict FP32 triangle arithmetic and the lower-index tie
+ * rule, so their hits equal RQ_LAYOUT_BVH2_STACK strict hits (iters then counts BVH8 nodes).
+ * Needs BVH2 leaves of at most 4 triangles (RQ_ENOTSUP otherwise).  Rebuilt automatically by
+ * rq_scene_set_entities once enabled.  No counterpart in the reference. */
+typedef struct rq_bvh8_info {
+    int64_t nodes, triangles, bytes, bvh2_nodes;
+    double build_ms;
+} rq_bvh8_info;
+rq_status rq_scene_build_bvh8(rq_scene* scene, rq_bvh8_info* info);
 /* Device bytes held by the scene (all layouts built so far). */
 rq_status rq_scene_bytes(const rq_scene* scene, int64_t* bytes);
 rq_status rq_scene_destroy(rq_scene* scene);

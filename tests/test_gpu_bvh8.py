@@ -1,0 +1,75 @@
+"""BVH8 with quantised boxes on the GPU: hits equal the strict BVH2 kernel's (t, barycentrics,
+triangle, mesh, entity; `iters` counts different nodes), any-hit bits equal, no status bits."""
+import numpy as np
+import pytest
+
+import candela_gb300 as R
+from candela_gb300 import _lib as L
+from candela_gb300 import scenes as S
+
+from .helpers import hits_from_device, mesh, oracle_scene, rays_to_device, single_object
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["t", "u", "v", "w", "tri", "mesh", "entity"]
+
+
+def _same(a, b):
+    ua = np.ascontiguousarray(a).view(np.uint32).reshape(len(a), 8)[:, :7]
+    ub = np.ascontiguousarray(b).view(np.uint32).reshape(len(b), 8)[:, :7]
+    return (ua == ub).all(1)
+
+
+@pytest.mark.parametrize("name,layout,leaf", [("c1", R.STACK, 2), ("c1", R.STACKLESS, 2),
+                                              ("ico2", R.STACK, 4), ("hf64", R.STACK, 2)])
+def test_bvh8_equals_strict(ctx, name, layout, leaf):
+    bufs = single_object(name, layout, leaf)
+    sc = ctx.scene(layout, *bufs)
+    info = sc.build_bvh8()
+    assert info["nodes"] > 0 and info["triangles"] == bufs[1].shape[0]
+    rays = np.concatenate([S.camera_rays(384, 256, **S.C1_CAMERA),
+                           S.sphere_rays(100_000, (-1.5, -1.5, -0.3), (1.5, 1.5, 1.2), seed=41)])
+    d = rays_to_device(rays)
+    strict = hits_from_device(sc.closest(d))
+    b8 = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q))
+    same = _same(strict, b8)
+    assert same.mean() >= 0.9999, f"{(~same).sum()} of {len(rays)} rays differ"
+    occ_s = sc.anyhit(d).cpu().numpy()
+    occ_8 = sc.anyhit(d, layout=L.LAYOUT_BVH8Q).cpu().numpy()
+    assert (occ_s == occ_8).mean() >= 0.9999
+    assert ctx.device_status() == 0
+
+
+def test_bvh8_multi_entity_and_oracle(ctx):
+    ri = R.RayIntersector(R.STACK)
+    ri.add_object(1, [mesh("hf32")])
+    ri.add_object(2, [mesh("ico2")])
+    T = np.eye(4)
+    T[:3, 3] = [0.25, -0.5, 0.125]
+    ri.push_entity(1)
+    ri.push_entity(2, model=T)
+    ri.push_entity(2)
+    ri.buffer_entities()
+    sc = ri.buffer_data(ctx)
+    sc.build_bvh8()
+    rays = S.sphere_rays(100_000, (-1.5, -1.5, -0.5), (1.5, 1.5, 1.5), seed=22)
+    from oracle import oracle as O
+    want = O.OracleScene(O.ORC_STACK, *ri.global_buffers()).closest(rays)
+    got = hits_from_device(sc.closest(rays_to_device(rays), layout=L.LAYOUT_BVH8Q))
+    assert _same(got, want).mean() >= 0.9999
+    # entities changed after the build: the BVH8 follows
+    ri.push_entity(1, model=T)
+    ri.buffer_entities()
+    want2 = O.OracleScene(O.ORC_STACK, *ri.global_buffers()).closest(rays)
+    got2 = hits_from_device(sc.closest(rays_to_device(rays), layout=L.LAYOUT_BVH8Q))
+    assert _same(got2, want2).mean() >= 0.9999
+    assert ctx.device_status() == 0
+
+
+def test_bvh8_requires_build_and_strict(ctx):
+    bufs = single_object("hf32", R.STACK)
+    sc = ctx.scene(R.STACK, *bufs)
+    rays = rays_to_device(S.camera_rays(16, 16, **S.C1_CAMERA))
+    with pytest.raises(R.RqError) as e:
+        sc.closest(rays, layout=L.LAYOUT_BVH8Q)
+    assert e.value.status == L.RQ_ENOTSUP
