@@ -356,10 +356,21 @@ def main():
          lambda: sc.closest(d_sec, flags=L.FLAG_NO_PERSISTENT, stream=sptr), n_sec),
         ("secondary_anyhit_strict_stack", lambda: sc.anyhit(d_sec, stream=sptr), n_sec),
     ]
+    b8 = sc.build_bvh8()
+    cases += [
+        ("primary_closest_bvh8q", lambda: sc.closest(d_rays, layout=L.LAYOUT_BVH8Q, stream=sptr), n),
+        ("secondary_closest_bvh8q", lambda: sc.closest(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr), n_sec),
+        ("secondary_anyhit_bvh8q", lambda: sc.anyhit(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr), n_sec),
+    ]
     for name, fn, rays_n in cases:
         ms = timed(fn)
         breakdown[name] = {"mrays_s": round(rays_n / (ms / 1e3) / 1e6, 1), "ms": round(ms, 4),
                            "rays": rays_n}
+    h_strict = sc.closest(d_sec, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
+    h_b8 = sc.closest(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
+    breakdown["bvh8q_vs_strict_identical_hits"] = float((h_strict == h_b8).all(1).mean())
+    breakdown["bvh8q_build"] = {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}
+    breakdown["bvh8q_status"] = ctx.device_status()
     breakdown["note"] = (f"secondary launches cover {n_sec_slots} ray slots of which {n_sec} are "
                          "active (pixels whose primary ray missed give inactive slots); Mrays/s "
                          "counts active rays")

@@ -333,7 +333,7 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
                         return false;
                     }
                     if (T[c].tri_count > 0)
-                        meta[s] = static_cast<uint8_t>(((T[c].tri_count - 1) << 5) | tri_off);
+                        meta[s] = static_cast<uint8_t>((T[c].tri_count << 5) | tri_off);
                     for (int32_t i = 0; i < T[c].tri_count; ++i) {
                         const int32_t t = T[c].tri_start + i;
                         const int32_t* tr = tris + static_cast<int64_t>(t) * 4;

@@ -13,8 +13,8 @@ namespace rq {
 //   w[4]     child_base: node index of the first internal child (internal children contiguous,
 //            in slot order)
 //   w[5]     tri_base: first record of this node's leaf triangles (contiguous, slot order)
-//   w[6..7]  meta[8]: slot s: 0 = empty or internal, else leaf = (count - 1) << 5 | offset with
-//            offset < 32 relative to tri_base and 1 <= count <= 4
+//   w[6..7]  meta[8]: slot s: 0 = empty or internal, else leaf = count << 5 | offset with
+//            offset < 32 relative to tri_base and 1 <= count <= 4 (never 0 for a leaf)
 //   w[8..19] quantised boxes: qlo_x[8] qlo_y[8] qlo_z[8] qhi_x[8] qhi_y[8] qhi_z[8] (bytes);
 //            child box = p + q * 2^(e-127) per axis, rounded outward so it contains the FP32 box
 // Children are placed in slots by octant (slot bit i set = child lies toward +axis i), so a ray

@@ -143,7 +143,7 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                         hits_oct |= 1u << (s ^ r.oct);
                     } else {
                         const uint32_t m = ((s < 4 ? meta0 : meta1) >> (8 * k)) & 0xFFu;
-                        if (m) tmask |= ((2u << (m >> 5)) - 1u) << (m & 31u);
+                        if (m) tmask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
                     }
                 }
             }

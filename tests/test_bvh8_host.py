@@ -38,7 +38,7 @@ def _walk(nodes8, recs, verts):
                 out.extend(tris_under(int(nd[4]) + k))
                 k += 1
             elif meta[s]:
-                cnt = int(meta[s] >> 5) + 1
+                cnt = int(meta[s] >> 5)
                 off = int(meta[s] & 31)
                 out.extend(range(int(nd[5]) + off, int(nd[5]) + off + cnt))
         below[i] = out
@@ -57,7 +57,7 @@ def _walk(nodes8, recs, verts):
                 ts = tris_under(int(nd[4]) + k)
                 k += 1
             elif meta[s]:
-                cnt = int(meta[s] >> 5) + 1
+                cnt = int(meta[s] >> 5)
                 off = int(meta[s] & 31)
                 ts = list(range(int(nd[5]) + off, int(nd[5]) + off + cnt))
             else:
@@ -87,11 +87,14 @@ def test_bvh8_conservative_and_complete(name, layout, leaf):
     # conservative boxes
     rec_tri_verts = np.stack([v0, v1, v2], 1).astype(np.float64)  # (M, 3, 3)
     checked = 0
+    reachable = set()
     for lo, hi, ts in _walk(nodes8, recs, v):
+        reachable.update(ts)
         pts = rec_tri_verts[ts].reshape(-1, 3)
         assert (pts >= lo[None, :]).all() and (pts <= hi[None, :]).all()
         checked += 1
     assert checked >= nodes8.shape[0]
+    assert reachable == set(range(recs.shape[0])), "a triangle record is not reachable via any slot"
 
 
 def test_bvh8_rejects_big_leaves():
