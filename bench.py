@@ -152,10 +152,12 @@ def make_workload(config: str):
     bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
     build_s = time.perf_counter() - t0
     ent = R.identity_entity(0, bvh.nodes.shape[0])
+    bvh_sl = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACKLESS)
+    ent_sl = R.identity_entity(0, bvh_sl.nodes.shape[0])
     n_mesh = int(mesh.mesh_ids.max()) + 1
     albedo = (0.25 + 0.65 * S.uniform(17, 5, n_mesh * 3)).astype(np.float32).reshape(-1, 3)
-    return dict(mesh=mesh, bvh=bvh, ent=ent, rays=rays, params=params, name=name,
-                albedo=albedo, build_s=build_s)
+    return dict(mesh=mesh, bvh=bvh, ent=ent, bvh_sl=bvh_sl, ent_sl=ent_sl, rays=rays,
+                params=params, name=name, albedo=albedo, build_s=build_s)
 
 
 def cpu_baseline(wl, seconds: float):
@@ -240,6 +242,7 @@ def main():
     sc = ctx.scene(R.STACK, wl["mesh"].vertices, wl["bvh"].tris, wl["bvh"].nodes, wl["ent"])
     sc.set_materials(wl["albedo"])
     p = gi_params(**wl["params"])
+    q_any = wl["params"]["query"] == 1
     rays = wl["rays"]
     n = len(rays)
     d_rays = torch.from_numpy(rays.view(np.uint8)).to(dev)
@@ -247,91 +250,68 @@ def main():
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    B8 = L.LAYOUT_BVH8Q
 
     if args.profile:
-        sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
+        # the launch the tuned bench uses (128 threads, 8 resident blocks: 64-register cap)
+        b8 = sc.build_bvh8()
+        sc.gi_frame(d_rays, p, out=d_pix, layout=B8, block_size=128, min_blocks=8, stream=sptr)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": wl["name"], "pixels": n}))
+        print(json.dumps({"profile_case": wl["name"], "pixels": n, "bvh8_nodes": b8["nodes"]}))
         return
 
-    # ray counts of one pass (untimed)
-    _, st = sc.gi_frame(d_rays, p, out=d_pix, stats=True, stream=sptr)
+    # ---- set-up (untimed): BVH8, secondary rays of one pass, autotuning, ray counts
+    b8 = sc.build_bvh8()
+    d_hits = sc.closest(d_rays, stream=sptr)
+    d_sec = sc.gi_raygen(d_rays, d_hits, p, stream=sptr)
+    tuning = {}
+    for lay, lname in ((B8, "bvh8q"), (R.STACK, "strict_stack")):
+        for qk, qname in ((0, "closest"), (1, "anyhit")):
+            tuning[f"{lname}_{qname}"] = sc.autotune(d_sec, query=qk, layout=lay)
+    _, st = sc.gi_frame(d_rays, p, out=d_pix, layout=B8, stats=True, stream=sptr)
     rays_per_step = st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
     launches_per_step = 5 + (2 if wl["params"].get("shadow_rays") else 0)
 
+    def timed_steps(layout, steps, warmup):
+        for _ in range(warmup):
+            sc.gi_frame(d_rays, p, out=d_pix, layout=layout, stream=sptr)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            sc.gi_frame(d_rays, p, out=d_pix, layout=layout, stream=sptr)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return float(sum(a.elapsed_time(b) for a, b in ev))
+
+    # ---- headline: GI pass on the tuned BVH8q path (hits identical to strict BVH2)
     for _ in range(args.warmup):
-        sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
+        sc.gi_frame(d_rays, p, out=d_pix, layout=B8, stream=sptr)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.fill_(i & 0xFF)
-            ev[i][0].record(stream)
-            sc.gi_frame(d_rays, p, out=d_pix, stream=sptr)
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms, value = combine_ranks(float(sum(step_ms)), rays_per_step, args.steps, world, dist,
-                                    dev)
+        total_ms = timed_steps(B8, args.steps, 0)
+    total_ms, value = combine_ranks(total_ms, rays_per_step, args.steps, world, dist, dev)
+    # the plain FP32 kernel (strict BVH2, default launch) on the same pass, for the ratio
+    plain_ms = timed_steps(R.STACK, args.steps, 1)
+    plain_value = rays_per_step * args.steps / (plain_ms / 1e3) / 1e6
 
-    # e2e: host buffers through the C ABI (pinned in, pinned out), host clock, sync per step
+    # ---- e2e: host buffers through the C ABI (pinned in, pinned out), host clock
     h_rays = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
     h_pix = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
     for _ in range(max(1, args.warmup)):
-        sc.gi_frame(h_rays, p, out=h_pix)
+        sc.gi_frame(h_rays, p, out=h_pix, layout=B8)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        sc.gi_frame(h_rays, p, out=h_pix)
+        sc.gi_frame(h_rays, p, out=h_pix, layout=B8)
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": rays_per_step * args.steps / e2e_s / 1e6, "unit": UNIT,
+    e2e = {"value": round(rays_per_step * args.steps / e2e_s / 1e6, 2), "unit": UNIT,
            "h2d_bytes_per_step": int(h_rays.nbytes), "d2h_bytes_per_step": int(h_pix.nbytes)}
 
-    # roofline of the dominant kernel: secondary closest-hit (or AO any-hit) traversal
-    d_hits = sc.closest(d_rays, stream=sptr)
-    d_sec = sc.gi_raygen(d_rays, d_hits, p, stream=sptr)
-    q_any = wl["params"]["query"] == 1
-    run = (lambda: sc.anyhit(d_sec, stream=sptr)) if q_any else (lambda: sc.closest(d_sec, stream=sptr))
-    torch.cuda.synchronize()
-    ctx.read_counters(reset=True)
-    if q_any:
-        sc.anyhit(d_sec, flags=L.FLAG_COUNT, stream=sptr)
-    else:
-        sc.closest(d_sec, flags=L.FLAG_COUNT, stream=sptr)
-    cnt = ctx.read_counters(reset=True)
-    algo_bytes = 64 * cnt["node_visits"] + 64 * cnt["triangle_tests"]
-    for _ in range(3):
-        run()
-    kev = []
-    for i in range(max(3, args.steps)):
-        flush.fill_(i & 0xFF)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        run()
-        b.record(stream)
-        kev.append((a, b))
-    torch.cuda.synchronize()
-    k_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
-    peak, peak_kind = load_peaks()
-    achieved = algo_bytes / (k_ms / 1e3) / 1e9
-    traffic = None
-    prof = ROOT / "profiles" / "ncu_traffic.txt"
-    if prof.exists():
-        for ln in prof.read_text().splitlines():
-            f = ln.split()
-            if len(f) == 3 and not ln.startswith("#") and f[0] == args.config:
-                traffic = int(f[2])
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic,
-                "peak_kind": peak_kind, "kernel": "secondary " + ("any-hit" if q_any else "closest-hit") + " traversal (strict, stack BVH2)",
-                "kernel_ms": round(k_ms, 4), "algorithmic_bytes_per_launch": int(algo_bytes),
-                "node_visits": int(cnt["node_visits"]), "triangle_tests": int(cnt["triangle_tests"]),
-                "active_rays": int(st["secondary_rays"])}
-
-    # per-query breakdown (device-resident rays, L2 flushed before each timed launch)
+    # ---- per-query breakdown (device rays, L2 flushed before each timed launch)
     def timed(fn, reps=max(3, min(args.steps, 10))):
         for _ in range(2):
             fn()
@@ -348,46 +328,95 @@ def main():
 
     n_sec = int(st["secondary_rays"])
     n_sec_slots = int(d_sec.numel() // 32)
-    breakdown = {}
+    V0 = dict(block_size=128, min_blocks=1)  # the untuned default launch
     cases = [
-        ("primary_closest_strict_stack", lambda: sc.closest(d_rays, stream=sptr), n),
-        ("secondary_closest_strict_stack", lambda: sc.closest(d_sec, stream=sptr), n_sec),
-        ("secondary_closest_strict_stack_one_thread_per_ray",
-         lambda: sc.closest(d_sec, flags=L.FLAG_NO_PERSISTENT, stream=sptr), n_sec),
-        ("secondary_anyhit_strict_stack", lambda: sc.anyhit(d_sec, stream=sptr), n_sec),
+        ("primary_closest_strict_stack", lambda: sc.closest(d_rays, stream=sptr, **V0), n, {}),
+        ("secondary_closest_strict_stack", lambda: sc.closest(d_sec, stream=sptr, **V0), n_sec, {}),
+        ("secondary_closest_strict_stack_persistent",
+         lambda: sc.closest(d_sec, stream=sptr, block_size=128, min_blocks=1, persistent=1), n_sec, None),
+        ("secondary_anyhit_strict_stack", lambda: sc.anyhit(d_sec, stream=sptr, **V0), n_sec, {}),
+        ("secondary_closest_strict_stackless",
+         lambda: sc.closest(d_sec_sl, stream=sptr), n_sec, None),
+        ("primary_closest_bvh8q", lambda: sc.closest(d_rays, layout=B8, stream=sptr), n, {"layout": B8}),
+        ("secondary_closest_bvh8q", lambda: sc.closest(d_sec, layout=B8, stream=sptr), n_sec, {"layout": B8}),
+        ("secondary_anyhit_bvh8q", lambda: sc.anyhit(d_sec, layout=B8, stream=sptr), n_sec, {"layout": B8}),
     ]
-    b8 = sc.build_bvh8()
-    cases += [
-        ("primary_closest_bvh8q", lambda: sc.closest(d_rays, layout=L.LAYOUT_BVH8Q, stream=sptr), n),
-        ("secondary_closest_bvh8q", lambda: sc.closest(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr), n_sec),
-        ("secondary_anyhit_bvh8q", lambda: sc.anyhit(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr), n_sec),
-    ]
-    for name, fn, rays_n in cases:
+    sc_sl = ctx.scene(R.STACKLESS, wl["mesh"].vertices, wl["bvh_sl"].tris, wl["bvh_sl"].nodes,
+                      wl["ent_sl"])
+    d_sec_sl = d_sec
+    cases[4] = ("secondary_closest_strict_stackless", lambda: sc_sl.closest(d_sec_sl, stream=sptr),
+                n_sec, None)
+    breakdown = {}
+    for name, fn, rays_n, count_kw in cases:
         ms = timed(fn)
-        breakdown[name] = {"mrays_s": round(rays_n / (ms / 1e3) / 1e6, 1), "ms": round(ms, 4),
-                           "rays": rays_n}
+        breakdown[name] = {"mrays_s": round(rays_n / (ms / 1e3) / 1e6, 1), "ms": round(ms, 4)}
+        if count_kw is not None:  # work per active ray (device counters, one untimed launch)
+            ctx.read_counters(reset=True)
+            src = d_rays if name.startswith("primary") else d_sec
+            if "anyhit" in name:
+                sc.anyhit(src, flags=L.FLAG_COUNT, stream=sptr, **count_kw)
+            else:
+                sc.closest(src, flags=L.FLAG_COUNT, stream=sptr, **count_kw)
+            c = ctx.read_counters(reset=True)
+            breakdown[name]["nodes_per_ray"] = round(c["node_visits"] / max(1, rays_n), 3)
+            breakdown[name]["tri_tests_per_ray"] = round(c["triangle_tests"] / max(1, rays_n), 3)
+            breakdown[name]["counts"] = c
     h_strict = sc.closest(d_sec, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
-    h_b8 = sc.closest(d_sec, layout=L.LAYOUT_BVH8Q, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
-    breakdown["bvh8q_vs_strict_identical_hits"] = float((h_strict == h_b8).all(1).mean())
-    breakdown["bvh8q_build"] = {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}
-    breakdown["bvh8q_status"] = ctx.device_status()
-    breakdown["note"] = (f"secondary launches cover {n_sec_slots} ray slots of which {n_sec} are "
-                         "active (pixels whose primary ray missed give inactive slots); Mrays/s "
-                         "counts active rays")
+    h_b8 = sc.closest(d_sec, layout=B8, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
+    o_strict = sc.anyhit(d_sec, stream=sptr).cpu().numpy()
+    o_b8 = sc.anyhit(d_sec, layout=B8, stream=sptr).cpu().numpy()
+    agreement = {"closest_hits_identical": float((h_strict == h_b8).all(1).mean()),
+                 "anyhit_identical": float((o_strict == o_b8).mean()),
+                 "rays": n_sec_slots, "device_status": ctx.device_status()}
+
+    # ---- roofline of the dominant kernel (secondary closest / AO any-hit on BVH8q)
+    dom = "secondary_anyhit_bvh8q" if q_any else "secondary_closest_bvh8q"
+    ref = "secondary_anyhit_strict_stack" if q_any else "secondary_closest_strict_stack"
+    c2 = breakdown[ref]["counts"]
+    algo_bytes = 64 * c2["node_visits"] + 64 * c2["triangle_tests"]  # BVH2-equivalent work
+    c8 = breakdown[dom]["counts"]
+    fetched8 = 80 * c8["node_visits"] + 64 * c8["triangle_tests"]
+    k_ms = breakdown[dom]["ms"]
+    peak, peak_kind = load_peaks()
+    achieved = algo_bytes / (k_ms / 1e3) / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "ncu_traffic.txt"
+    if prof.exists():
+        for ln in prof.read_text().splitlines():
+            f = ln.split()
+            if len(f) == 3 and not ln.startswith("#") and f[0] == args.config:
+                traffic = int(f[2])
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": dom.replace("_", " ") + " (k_bvh8)", "kernel_ms": k_ms,
+                "algorithmic_bytes_per_launch": int(algo_bytes),
+                "algorithmic_bytes_basis": "strict BVH2 work for the same rays: 64 B per node visit "
+                                           "+ 64 B per triangle test",
+                "bvh8_fetched_bytes_per_launch": int(fetched8),
+                "active_rays": n_sec}
+    for k in list(breakdown):
+        breakdown[k].pop("counts", None)
 
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene and camera rays)",
-            "config": {"workload": wl["name"], "rays_per_step": int(rays_per_step),
+            "config": {"workload": wl["name"], "traversal": "BVH8q, autotuned launch, strict FP32 "
+                                                            "leaf test (hits identical to strict BVH2)",
+                       "rays_per_step": int(rays_per_step),
                        "primary_rays": int(st["primary_rays"]),
                        "secondary_rays": int(st["secondary_rays"]),
                        "l2": "flushed between timed steps (512 MB write)",
                        "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
-                       "bvh_build_s": round(wl["build_s"], 3)},
-            "e2e": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in e2e.items()},
-            "roofline": roofline, "breakdown": breakdown, "clocks": clk.summary(),
-            "gpu_launches": launches_per_step * args.steps}
+                       "bvh_build_s": round(wl["build_s"], 3),
+                       "bvh8_build": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
+            "plain_fp32_bvh2": {"value": round(plain_value, 2), "unit": UNIT,
+                                "ms_per_step": round(plain_ms / args.steps, 4),
+                                "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},
+            "e2e": e2e, "roofline": roofline, "breakdown": breakdown, "bvh8q_vs_strict": agreement,
+            "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
+                             "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
+            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
         print(json.dumps(line), flush=True)

@@ -35,7 +35,15 @@ assert ENTITY_DTYPE.itemsize == 192 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.i
 
 class RqOpts(C.Structure):
     _fields_ = [("layout", C.c_int32), ("mode", C.c_int32), ("tie", C.c_int32),
-                ("flags", C.c_int32), ("block_size", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("flags", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
+                ("persistent", C.c_int32), ("reserved", C.c_int32)]
+
+
+class RqTuneResult(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
+                ("persistent", C.c_int32), ("n_variants", C.c_int32), ("ms", C.c_float * 8),
+                ("block", C.c_int32 * 8), ("min_blocks_of", C.c_int32 * 8),
+                ("persistent_of", C.c_int32 * 8)]
 
 
 class RqBuildOpts(C.Structure):
@@ -94,6 +102,7 @@ SIGNATURES = {
     "rq_anyhit": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_counters_read": (_S, [_P, C.POINTER(C.c_int64 * 2), C.c_int]),
     "rq_device_status": (_S, [_P, C.POINTER(C.c_uint32), C.c_int]),
+    "rq_autotune": (_S, [_P, _P, _P, _I64, _I32, _S, C.POINTER(RqTuneResult)]),
     "rq_scene_build_bvh8": (_S, [_P, C.POINTER(RqBvh8Info)]),
     "rq_build_bvh8": (_S, [_S, _P, _I64, _P, _I64, _P, _I64, _I32, _I32, C.POINTER(_P)]),
     "rq_bvh8_buffers": (_S, [_P, C.POINTER(_P), C.POINTER(_I64), C.POINTER(_P), C.POINTER(_I64)]),

@@ -54,6 +54,24 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
     q.flags = o->flags;
     q.block = o->block_size;
     q.counters = (o->flags & RQ_FLAG_COUNT) ? work_counters(ctx) : nullptr;
+    q.variant_closest = q.variant_any = -1;
+    if (o->block_size || o->min_blocks || o->persistent) {
+        int found = -1;
+        for (int v = 0; v < kNumLaunchVariants; ++v)
+            if (kLaunchVariants[v].block == o->block_size &&
+                kLaunchVariants[v].min_blocks == o->min_blocks &&
+                kLaunchVariants[v].persistent == (o->persistent ? 1 : 0))
+                found = v;
+        if (found < 0) return fail(ctx, RQ_EINVAL, "no compiled launch variant with that block size / min_blocks");
+        q.variant_closest = q.variant_any = found;
+    } else if (q.layout >= 0 && q.layout < 4) {
+        q.variant_closest = sc->tuned[q.layout][0];
+        q.variant_any = sc->tuned[q.layout][1];
+    }
+    if (o->flags & RQ_FLAG_NO_PERSISTENT) {
+        if (q.variant_closest >= 0 && kLaunchVariants[q.variant_closest].persistent) q.variant_closest = 0;
+        if (q.variant_any >= 0 && kLaunchVariants[q.variant_any].persistent) q.variant_any = 0;
+    }
     if (o->tie != RQ_TIE_LOWER_INDEX && o->tie != RQ_TIE_FIRST_FOUND)
         return fail(ctx, RQ_EINVAL, "unknown tie rule");
     if (q.mode != RQ_MODE_STRICT && q.mode != RQ_MODE_FAST)
@@ -77,6 +95,8 @@ namespace {
 using rq::fail;
 using rq::cuda_fail;
 using rq::status_word;
+using rq::kLaunchVariants;
+using rq::kNumLaunchVariants;
 
 bool is_identity(const float* m) {
     for (int c = 0; c < 4; ++c)
@@ -485,6 +505,62 @@ rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
         info->bvh2_nodes = b.bvh2_nodes;
         info->build_ms = b.build_ms;
     }
+    return RQ_OK;
+}
+
+rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, int32_t query,
+                      rq_layout layout, rq_tune_result* out) {
+    if (!ctx || !sc || !out || !rays || n <= 0 || (query != 0 && query != 1))
+        return fail(ctx, RQ_EINVAL, "bad autotune arguments");
+    rq_opts o{};
+    o.layout = layout;
+    rq::QueryConfig q{};
+    rq_status s = rq::resolve_query(ctx, sc, &o, q);
+    if (s != RQ_OK) return s;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    void* out_buf = nullptr;
+    if ((s = rq::scratch(ctx, 9, query == 0 ? sizeof(rq_hit) * n : n, &out_buf)) != RQ_OK) return s;
+    cudaEvent_t a, b;
+    RQ_CUDA(ctx, cudaEventCreate(&a));
+    RQ_CUDA(ctx, cudaEventCreate(&b));
+    std::memset(out, 0, sizeof(*out));
+    out->n_variants = kNumLaunchVariants;
+    float best = 1e30f;
+    int best_v = 0;
+    cudaStream_t st = ctx->stream;
+    for (int v = 0; v < kNumLaunchVariants; ++v) {
+        out->block[v] = kLaunchVariants[v].block;
+        out->min_blocks_of[v] = kLaunchVariants[v].min_blocks;
+        out->persistent_of[v] = kLaunchVariants[v].persistent;
+        out->ms[v] = -1.0f;
+        if (kLaunchVariants[v].persistent && q.layout == RQ_LAYOUT_BVH8Q) continue;
+        q.variant_closest = q.variant_any = v;
+        float vbest = 1e30f;
+        for (int rep = 0; rep < 4; ++rep) {
+            RQ_CUDA(ctx, cudaEventRecord(a, st));
+            cudaError_t e = query == 0
+                ? rq::launch_closest(sc->view, q, rays, n, static_cast<rq_hit*>(out_buf), rq::queue_counter(ctx, 8), st)
+                : rq::launch_anyhit(sc->view, q, rays, n, static_cast<uint8_t*>(out_buf), rq::queue_counter(ctx, 8), st);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune launch");
+            RQ_CUDA(ctx, cudaEventRecord(b, st));
+            RQ_CUDA(ctx, cudaEventSynchronize(b));
+            float ms = 0.0f;
+            RQ_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+            if (rep > 0) vbest = std::min(vbest, ms);  // rep 0 is the warm-up
+        }
+        out->ms[v] = vbest;
+        if (vbest < best) {
+            best = vbest;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    sc->tuned[q.layout][query] = static_cast<int8_t>(best_v);
+    out->variant = best_v;
+    out->block_size = kLaunchVariants[best_v].block;
+    out->min_blocks = kLaunchVariants[best_v].min_blocks;
+    out->persistent = kLaunchVariants[best_v].persistent;
     return RQ_OK;
 }
 

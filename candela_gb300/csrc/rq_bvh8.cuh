@@ -4,8 +4,9 @@
 // scale) and o = (p - ro) * inv, so a child's slab distances are fma(q, inv_s, o).  The near and
 // far planes are chosen per axis from the sign of the direction, so each child costs six FMAs and
 // two 3-way min/max.  The FMA form rounds; its error is bounded by a few ulps of the node's extent
-// in t, so o is widened by 8 ulps of 255*|inv_s| + |o| on each side, which keeps the test
-// conservative: every child box the ray meets in exact arithmetic is entered.  Zero direction
+// in t plus half a grid step (from folding the 2^23 bias of the byte-to-float trick into o), so o
+// is widened by that much on each side, which keeps the test conservative: every child box the ray
+// meets in exact arithmetic is entered.  Zero direction
 // components use a +-1e30 reciprocal for the boxes (the triangle test still uses the exact ray).
 //
 // Leaf test: the strict RayTriangle arithmetic (TraverseBVHStack.glsl:87-105) on precomputed
@@ -37,8 +38,9 @@ __device__ __forceinline__ float max3f(float a, float b, float c) {
     asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
 }
-__device__ __forceinline__ float ubyte(uint32_t w, int k) {
-    return __uint2float_rn((w >> (8 * k)) & 0xFFu);
+// Byte k of w as the float 2^23 + byte (one byte permute, no int-to-float conversion).
+__device__ __forceinline__ float ubyte_biased(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | static_cast<unsigned>(k)));
 }
 
 struct Ray8 {
@@ -108,9 +110,13 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
             const float ox = (p.x - r.ro.x) * r.binv.x;
             const float oy = (p.y - r.ro.y) * r.binv.y;
             const float oz = (p.z - r.ro.z) * r.binv.z;
-            const float px = kUlp8 * (255.0f * fabsf(isx) + fabsf(ox));
-            const float py = kUlp8 * (255.0f * fabsf(isy) + fabsf(oy));
-            const float pz = kUlp8 * (255.0f * fabsf(isz) + fabsf(oz));
+            // Quantised coordinates arrive as 2^23 + q, so the origin term absorbs -2^23 * inv_s;
+            // rounding that sum costs at most half a grid step, which the padding also covers.
+            const float bx = ox - 8388608.0f * isx, by = oy - 8388608.0f * isy;
+            const float bz = oz - 8388608.0f * isz;
+            const float px = 0.5f * fabsf(isx) + kUlp8 * (255.0f * fabsf(isx) + fabsf(ox));
+            const float py = 0.5f * fabsf(isy) + kUlp8 * (255.0f * fabsf(isy) + fabsf(oy));
+            const float pz = 0.5f * fabsf(isz) + kUlp8 * (255.0f * fabsf(isz) + fabsf(oz));
             // near plane = lo for a positive direction, hi for a negative one
             const uint32_t loxy0 = w2.x, loxy1 = w2.y, loy0 = w2.z, loy1 = w2.w;
             const uint32_t loz0 = w3.x, loz1 = w3.y, hix0 = w3.z, hix1 = w3.w;
@@ -122,8 +128,8 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
             const uint32_t fY0 = ny ? loy0 : hiy0, fY1 = ny ? loy1 : hiy1;
             const uint32_t nZ0 = nz ? hiz0 : loz0, nZ1 = nz ? hiz1 : loz1;
             const uint32_t fZ0 = nz ? loz0 : hiz0, fZ1 = nz ? loz1 : hiz1;
-            const float onx = ox - px, ofx = ox + px, ony = oy - py, ofy = oy + py;
-            const float onz = oz - pz, ofz = oz + pz;
+            const float onx = bx - px, ofx = bx + px, ony = by - py, ofy = by + py;
+            const float onz = bz - pz, ofz = bz + pz;
             uint32_t hits_oct = 0;  // internal children hit, bit (slot ^ oct)
             uint32_t tmask = 0;     // triangles of leaf children hit
             const uint32_t meta0 = w1.z, meta1 = w1.w;
@@ -133,9 +139,12 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                 const uint32_t a = s < 4 ? nX0 : nX1, b = s < 4 ? fX0 : fX1;
                 const uint32_t c = s < 4 ? nY0 : nY1, d = s < 4 ? fY0 : fY1;
                 const uint32_t e = s < 4 ? nZ0 : nZ1, f = s < 4 ? fZ0 : fZ1;
-                const float tnx = fmaf(ubyte(a, k), isx, onx), tfx = fmaf(ubyte(b, k), isx, ofx);
-                const float tny = fmaf(ubyte(c, k), isy, ony), tfy = fmaf(ubyte(d, k), isy, ofy);
-                const float tnz = fmaf(ubyte(e, k), isz, onz), tfz = fmaf(ubyte(f, k), isz, ofz);
+                const float tnx = fmaf(ubyte_biased(a, k), isx, onx);
+                const float tfx = fmaf(ubyte_biased(b, k), isx, ofx);
+                const float tny = fmaf(ubyte_biased(c, k), isy, ony);
+                const float tfy = fmaf(ubyte_biased(d, k), isy, ofy);
+                const float tnz = fmaf(ubyte_biased(e, k), isz, onz);
+                const float tfz = fmaf(ubyte_biased(f, k), isz, ofz);
                 const float tn = fmaxf(max3f(tnx, tny, tnz), tmin);
                 const float tf = fminf(min3f(tfx, tfy, tfz), h.tmax);
                 if (tn <= tf) {
@@ -157,9 +166,12 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                 ++tests;
                 const float t = ray_triangle_rec(r.ro, r.rd, A, B, C, D);
                 if (kAny) {
-                    if (t > tmin && t < h.tmax) {
+                    if (t > tmin && t < h.tmax) {  // first hit ends the walk
                         h.closest = t;
-                        return visits;
+                        tmask = 0;
+                        hits_oct = 0;
+                        group = 0;
+                        sp = 0;
                     }
                 } else {
                     const int32_t idx = __float_as_int(A.w);

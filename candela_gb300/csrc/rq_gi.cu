@@ -115,6 +115,156 @@ __global__ void k_shadow_raygen(SceneView s, const rq_ray* __restrict__ rays,
     }
 }
 
+// Compacting variant of k_gi_raygen: active secondary rays are appended to `out` (block-aggregated
+// atomic, so only the order of blocks varies between runs), with slot_of[c] = slot j of compact
+// ray c and comp_of[j] = c (or -1 for an inactive slot).  Results are scattered back by slot, so
+// per-pixel sums keep their sample order; only the assignment of rays to threads changes.
+__global__ void __launch_bounds__(256) k_gi_raygen_compact(
+    SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
+    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of,
+    unsigned long long* count) {
+    __shared__ unsigned warp_count[8];
+    __shared__ unsigned long long block_base;
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = n * a.spp;
+    bool act = false;
+    f3 org{0.0f, 0.0f, 0.0f}, dir{0.0f, 0.0f, 1.0f};
+    if (j < total) {
+        const int64_t i = j / a.spp;
+        float4 h0;
+        int4 h1;
+        get_hit(hits, i, h0, h1);
+        if (h0.x > 0.0f) {
+            const float4* pr = reinterpret_cast<const float4*>(prim) + 2 * i;
+            const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+            const uint32_t rid = static_cast<uint32_t>(j);
+            const float u0 = gi::u01(gi::sample_key(a.seed, rid, 0u));
+            const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
+            dir = gi::cos_weighted_hemisphere(N, u0, u1);
+            org = strict::add(P, strict::muls(N, a.origin_offset));
+            act = true;
+        }
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+    if (lane == 0) warp_count[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (unsigned w = 0; w < blockDim.x / 32; ++w) {
+            const unsigned c = warp_count[w];
+            warp_count[w] = tot;
+            tot += c;
+        }
+        block_base = tot ? atomicAdd(count, static_cast<unsigned long long>(tot)) : 0ull;
+    }
+    __syncthreads();
+    if (j < total) {
+        if (act) {
+            const int64_t c = static_cast<int64_t>(block_base) + warp_count[warp] +
+                              __popc(m & ((1u << lane) - 1u));
+            put_ray(out, c, org, 0.0f, dir, a.ray_tmax);
+            slot_of[c] = static_cast<int32_t>(j);
+            comp_of[j] = static_cast<int32_t>(c);
+        } else {
+            comp_of[j] = -1;
+        }
+    }
+}
+
+// Shadow rays for the first *count compact secondary hits.
+__global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
+                                  const rq_hit* __restrict__ hits, int64_t n_max, GiArgs a,
+                                  rq_ray* __restrict__ out, const unsigned long long* count,
+                                  unsigned long long* active) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool act = false;
+    if (j < n) {
+        float4 h0;
+        int4 h1;
+        get_hit(hits, j, h0, h1);
+        const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * j;
+        const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+        if (h0.x > 0.0f && r1.w > r0.w) {
+            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+            const f3 org = strict::add(P, strict::muls(N, a.shadow_offset));
+            put_ray(out, j, org, 0.0f, strict::neg(a.sun_dir), 1000000.0f);
+            act = true;
+        } else {
+            put_ray(out, j, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
+        }
+    }
+    if (active) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
+    }
+}
+
+// Shading per slot from compact rays / hits / visibility (comp_of[j] < 0: inactive slot).
+__global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
+                          const int32_t* __restrict__ comp_of, int64_t m,
+                          const uint8_t* __restrict__ occl, int query, const float* __restrict__ albedo,
+                          int32_t n_albedo, GiArgs a, float4* __restrict__ out) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int32_t c = comp_of[j];
+    if (c < 0) {
+        out[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    if (query == 1) {  // AO: visibility of the compact any-hit ray
+        out[j] = make_float4(0.0f, 0.0f, 0.0f, occl[c] ? 0.0f : 1.0f);
+        return;
+    }
+    float4 h0;
+    int4 h1;
+    get_hit(hits, c, h0, h1);
+    if (!(h0.x > 0.0f)) {
+        out[j] = make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
+        return;
+    }
+    const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * static_cast<int64_t>(c);
+    const f3 rd = strict::xyz(__ldg(pr + 1));
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    f3 alb{0.8f, 0.8f, 0.8f};
+    if (h1.y >= 0 && h1.y < n_albedo)
+        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
+    const float em = __int_as_float(s.ents[h1.z].data[0]);
+    const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
+    const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
+    const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
+    const f3 rad = strict::add(direct, strict::muls(alb, em));
+    const float ao = powf(strict::gmin(strict::gmax(__fdiv_rn(h0.x, 2.4f), 0.0f), 1.0f), 1.23f);
+    out[j] = make_float4(rad.x, rad.y, rad.z, ao);
+}
+
+__global__ void k_count_hits_c(const rq_hit* __restrict__ hits, int64_t n_max,
+                               const unsigned long long* count, unsigned long long* cnt) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool h = i < n && __ldg(reinterpret_cast<const float*>(hits) + 8 * i) > 0.0f;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
+}
+
+__global__ void k_count_bytes_c(const uint8_t* __restrict__ b, int64_t n_max,
+                                const unsigned long long* count, unsigned long long* cnt) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool h = i < n && b[i] != 0;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
+}
+
 // GetDirect (DiffuseTrace.glsl:368-372) + emissive (:491) + AO (:494).
 __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                         int64_t n, const uint8_t* __restrict__ lit, int lit_is_occlusion,
@@ -324,12 +474,15 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     q.flags &= ~RQ_FLAG_HOST_BUFFERS;
     const int64_t m = n * p->spp;
     void *d_prim = nullptr, *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr,
-         *d_shade = nullptr, *d_pix = nullptr, *d_shadow = nullptr, *d_lit = nullptr;
+         *d_shade = nullptr, *d_pix = nullptr, *d_shadow = nullptr, *d_slot = nullptr,
+         *d_comp = nullptr;
     if ((s = rq::scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
         (s = rq::scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
         (s = rq::scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
         (s = rq::scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
-        (s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK)
+        (s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK ||
+        (s = rq::scratch(ctx, 10, 4 * m, &d_slot)) != RQ_OK ||
+        (s = rq::scratch(ctx, 11, 4 * m, &d_comp)) != RQ_OK)
         return s;
     if (host) {
         if ((s = rq::scratch(ctx, 0, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
@@ -341,42 +494,46 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
         d_pix = pixels4;
     }
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
+    unsigned long long* count = rq::frame_counter(ctx);  // active (compact) secondary rays
+    RQ_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
     if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
     const rq::GiArgs a = rq::to_args(*p);
     const rq_ray* prim = static_cast<const rq_ray*>(d_prim);
     rq_hit* phit = static_cast<rq_hit*>(d_phit);
     rq_ray* sec = static_cast<rq_ray*>(d_sec);
     rq_hit* shit = static_cast<rq_hit*>(d_shit);
+    uint8_t* occ = static_cast<uint8_t*>(d_occ);
     float4* shade = static_cast<float4*>(d_shade);
+    int32_t* slot_of = static_cast<int32_t*>(d_slot);
+    int32_t* comp_of = static_cast<int32_t*>(d_comp);
     RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, rq::queue_counter(ctx, 0), st));
     if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
-    rq::k_gi_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
-                                                      stats ? cnt + 1 : nullptr);
+    rq::k_gi_raygen_compact<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
+                                                              slot_of, comp_of, count);
     RQ_CUDA(ctx, cudaGetLastError());
+    rq::SceneView cv = sc->view;  // secondary launches cover only the compact prefix
+    cv.ray_count = count;
+    const uint8_t* vis = nullptr;
     if (p->query == 1) {
-        uint8_t* occ = static_cast<uint8_t*>(d_occ);
-        RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sec, m, occ, rq::queue_counter(ctx, 1), st));
-        if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 2);
-        rq::k_ao_shade<<<rq::grid(m, 256), 256, 0, st>>>(sec, occ, m, shade);
+        RQ_CUDA(ctx, rq::launch_anyhit(cv, q, sec, m, occ, rq::queue_counter(ctx, 1), st));
+        if (stats) rq::k_count_bytes_c<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 2);
+        vis = occ;
     } else {
-        RQ_CUDA(ctx, rq::launch_closest(sc->view, q, sec, m, shit, rq::queue_counter(ctx, 1), st));
-        if (stats) rq::k_count_hits<<<rq::grid(m, 256), 256, 0, st>>>(shit, m, cnt + 2);
-        const uint8_t* lit = nullptr;
+        RQ_CUDA(ctx, rq::launch_closest(cv, q, sec, m, shit, rq::queue_counter(ctx, 1), st));
+        if (stats) rq::k_count_hits_c<<<rq::grid(m, 256), 256, 0, st>>>(shit, m, count, cnt + 2);
         if (p->shadow_rays) {
-            if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK ||
-                (s = rq::scratch(ctx, 8, m, &d_lit)) != RQ_OK)
-                return s;
+            if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
             rq_ray* sh = static_cast<rq_ray*>(d_shadow);
-            uint8_t* occ = static_cast<uint8_t*>(d_lit);
-            rq::k_shadow_raygen<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh,
-                                                                  stats ? cnt + 3 : nullptr);
-            RQ_CUDA(ctx, rq::launch_anyhit(sc->view, q, sh, m, occ, rq::queue_counter(ctx, 2), st));
-            if (stats) rq::k_count_bytes<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, cnt + 4);
-            lit = occ;  // occlusion bytes: k_shade reads them inverted
+            rq::k_shadow_raygen_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count,
+                                                                    stats ? cnt + 3 : nullptr);
+            RQ_CUDA(ctx, cudaGetLastError());
+            RQ_CUDA(ctx, rq::launch_anyhit(cv, q, sh, m, occ, rq::queue_counter(ctx, 2), st));
+            if (stats) rq::k_count_bytes_c<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 4);
+            vis = occ;
         }
-        rq::k_shade<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, lit, lit ? 1 : 0,
-                                                      sc->d_albedo, sc->n_albedo, a, shade);
     }
+    rq::k_shade_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p->query,
+                                                    sc->d_albedo, sc->n_albedo, a, shade);
     rq::k_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(shade, n, p->spp, static_cast<float4*>(d_pix));
     RQ_CUDA(ctx, cudaGetLastError());
     if (host) {
@@ -384,12 +541,13 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
     }
     if (stats) {
-        unsigned long long c[8];
+        unsigned long long c[8], act = 0;
         RQ_CUDA(ctx, cudaMemcpyAsync(c, cnt, sizeof(c), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(ctx, cudaMemcpyAsync(&act, count, sizeof(act), cudaMemcpyDeviceToHost, st));
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
         stats->primary_rays = n;
         stats->primary_hits = static_cast<int64_t>(c[0]);
-        stats->secondary_rays = static_cast<int64_t>(c[1]);
+        stats->secondary_rays = static_cast<int64_t>(act);
         stats->secondary_hits = static_cast<int64_t>(c[2]);
         stats->shadow_rays = static_cast<int64_t>(c[3]);
         stats->shadow_occluded = static_cast<int64_t>(c[4]);

@@ -27,6 +27,9 @@ struct SceneView {
     const uint4* b8_nodes;
     const float4* b8_tris;
     const int32_t* b8_roots;
+    // Optional device-side ray count: when set, a launch over n rays processes only the first
+    // min(n, *ray_count) (used for compacted secondary rays whose count is known on the device).
+    const unsigned long long* ray_count;
 };
 
 // Query configuration resolved by the host API.
@@ -38,7 +41,17 @@ struct QueryConfig {
     int32_t block;
     unsigned long long* counters;  // non-null: accumulate node visits / triangle tests here
     unsigned* status;              // device status bits (stack overflow, iteration budget)
+    int32_t variant_closest;       // index into kLaunchVariants (-1 = default)
+    int32_t variant_any;
 };
+
+// Compiled launch variants of the traversal kernels: threads per block, minimum resident blocks
+// per SM (the register cap follows from it), and the persistent ray-queue form.
+struct LaunchVariant {
+    int32_t block, min_blocks, persistent;
+};
+constexpr int kNumLaunchVariants = 7;
+extern const LaunchVariant kLaunchVariants[kNumLaunchVariants];
 
 // Kernel launchers (rq_kernels.cu).  Return cudaGetLastError() after the launch.
 // `queue` (nullable) is a device ray counter for the persistent kernels; without one (or with

@@ -39,10 +39,11 @@ __device__ __forceinline__ void count_work(unsigned long long* counters, int32_t
 }
 
 // One thread per ray, strict arithmetic and reference traversal order.
-template <bool kStackless, bool kTieLower>
-__global__ void __launch_bounds__(128) k_closest_strict(SceneView s, const rq_ray* __restrict__ rays,
+template <bool kStackless, bool kTieLower, int kB, int kM>
+__global__ void __launch_bounds__(kB, kM) k_closest_strict(SceneView s, const rq_ray* __restrict__ rays,
                                                         int64_t n, rq_hit* __restrict__ hits,
                                                         int flags, unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     rq_hit h;
     int32_t tests = 0;
@@ -56,10 +57,11 @@ __global__ void __launch_bounds__(128) k_closest_strict(SceneView s, const rq_ra
     if (counters) count_work(counters, h.iters, tests);
 }
 
-template <bool kStackless>
-__global__ void __launch_bounds__(128) k_anyhit_strict(SceneView s, const rq_ray* __restrict__ rays,
+template <bool kStackless, int kB, int kM>
+__global__ void __launch_bounds__(kB, kM) k_anyhit_strict(SceneView s, const rq_ray* __restrict__ rays,
                                                        int64_t n, uint8_t* __restrict__ occ,
                                                        unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     int32_t iters = 0, tests = 0;
     if (i < n) {
@@ -77,6 +79,7 @@ __global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq
                                                            uint8_t* __restrict__ occ, int flags,
                                                            unsigned long long* queue,
                                                            unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
     persist::StrictRay<kAny, kStackless, kTieLower> R;
     int32_t stack[kStackless ? 1 : 64];
     int64_t id = -1;
@@ -117,11 +120,12 @@ __global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq
 }
 
 // BVH8 traversal, one thread per ray, with the strict scene loop around it.
-template <bool kAny>
-__global__ void __launch_bounds__(128) k_bvh8(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
+template <bool kAny, int kB, int kM>
+__global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
                                               rq_hit* __restrict__ hits, uint8_t* __restrict__ occ,
                                               int flags, unsigned* status_out,
                                               unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     int32_t visits = 0, tests = 0;
     unsigned status = 0;
@@ -236,57 +240,84 @@ cudaError_t launch_persistent(const SceneView& s, const QueryConfig& q, const rq
 
 }  // namespace
 
+namespace {
+
+template <int kB, int kM>
+cudaError_t closest_variant(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
+                            rq_hit* hits, cudaStream_t st) {
+    unsigned long long* cnt = q.counters;
+    const unsigned g = grid_for(n, kB);
+    if (q.layout == RQ_LAYOUT_BVH8Q)
+        k_bvh8<false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, nullptr, q.flags, q.status, cnt);
+    else if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
+        q.tie_lower ? k_closest_strict<true, true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt)
+                    : k_closest_strict<true, false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt);
+    else
+        q.tie_lower ? k_closest_strict<false, true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt)
+                    : k_closest_strict<false, false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt);
+    return cudaGetLastError();
+}
+
+template <int kB, int kM>
+cudaError_t anyhit_variant(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
+                           uint8_t* occ, cudaStream_t st) {
+    unsigned long long* cnt = q.counters;
+    const unsigned g = grid_for(n, kB);
+    if (q.layout == RQ_LAYOUT_BVH8Q)
+        k_bvh8<true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, nullptr, occ, q.flags, q.status, cnt);
+    else if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
+        k_anyhit_strict<true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, occ, cnt);
+    else
+        k_anyhit_strict<false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, occ, cnt);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+const LaunchVariant kLaunchVariants[kNumLaunchVariants] = {
+    {128, 1, 0}, {128, 4, 0}, {128, 6, 0}, {128, 8, 0}, {256, 3, 0}, {64, 12, 0}, {128, 1, 1}};
+
 cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                            rq_hit* hits, unsigned long long* queue, cudaStream_t st) {
-    unsigned long long* cnt = q.counters;
     if (n <= 0) return cudaSuccess;
-    if (q.layout == RQ_LAYOUT_BVH8Q) {
-        k_bvh8<false><<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, hits, nullptr, q.flags, q.status, cnt);
-        return cudaGetLastError();
+    int v = q.variant_closest < 0 ? 0 : q.variant_closest;
+    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q)) v = 0;
+    switch (v) {
+        case 1: return closest_variant<128, 4>(s, q, rays, n, hits, st);
+        case 2: return closest_variant<128, 6>(s, q, rays, n, hits, st);
+        case 3: return closest_variant<128, 8>(s, q, rays, n, hits, st);
+        case 4: return closest_variant<256, 3>(s, q, rays, n, hits, st);
+        case 5: return closest_variant<64, 12>(s, q, rays, n, hits, st);
+        case 6: {
+            const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
+            if (sl)
+                return q.tie_lower ? launch_persistent<false, true, true>(s, q, rays, n, hits, nullptr, queue, st)
+                                   : launch_persistent<false, true, false>(s, q, rays, n, hits, nullptr, queue, st);
+            return q.tie_lower ? launch_persistent<false, false, true>(s, q, rays, n, hits, nullptr, queue, st)
+                               : launch_persistent<false, false, false>(s, q, rays, n, hits, nullptr, queue, st);
+        }
+        default: return closest_variant<128, 1>(s, q, rays, n, hits, st);
     }
-    if (queue && !(q.flags & RQ_FLAG_NO_PERSISTENT)) {
-        const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
-        if (sl)
-            return q.tie_lower ? launch_persistent<false, true, true>(s, q, rays, n, hits, nullptr, queue, st)
-                               : launch_persistent<false, true, false>(s, q, rays, n, hits, nullptr, queue, st);
-        return q.tie_lower ? launch_persistent<false, false, true>(s, q, rays, n, hits, nullptr, queue, st)
-                           : launch_persistent<false, false, false>(s, q, rays, n, hits, nullptr, queue, st);
-    }
-    const int block = 128;
-    const bool stackless = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
-    if (stackless) {
-        if (q.tie_lower)
-            k_closest_strict<true, true><<<grid_for(n, block), block, 0, st>>>(s, rays, n, hits, q.flags, cnt);
-        else
-            k_closest_strict<true, false><<<grid_for(n, block), block, 0, st>>>(s, rays, n, hits, q.flags, cnt);
-    } else {
-        if (q.tie_lower)
-            k_closest_strict<false, true><<<grid_for(n, block), block, 0, st>>>(s, rays, n, hits, q.flags, cnt);
-        else
-            k_closest_strict<false, false><<<grid_for(n, block), block, 0, st>>>(s, rays, n, hits, q.flags, cnt);
-    }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                           uint8_t* occluded, unsigned long long* queue, cudaStream_t st) {
-    unsigned long long* cnt = q.counters;
     if (n <= 0) return cudaSuccess;
-    if (q.layout == RQ_LAYOUT_BVH8Q) {
-        k_bvh8<true><<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, nullptr, occluded, q.flags, q.status, cnt);
-        return cudaGetLastError();
+    int v = q.variant_any < 0 ? 0 : q.variant_any;
+    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q)) v = 0;
+    switch (v) {
+        case 1: return anyhit_variant<128, 4>(s, q, rays, n, occluded, st);
+        case 2: return anyhit_variant<128, 6>(s, q, rays, n, occluded, st);
+        case 3: return anyhit_variant<128, 8>(s, q, rays, n, occluded, st);
+        case 4: return anyhit_variant<256, 3>(s, q, rays, n, occluded, st);
+        case 5: return anyhit_variant<64, 12>(s, q, rays, n, occluded, st);
+        case 6: {
+            if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
+                return launch_persistent<true, true, false>(s, q, rays, n, nullptr, occluded, queue, st);
+            return launch_persistent<true, false, false>(s, q, rays, n, nullptr, occluded, queue, st);
+        }
+        default: return anyhit_variant<128, 1>(s, q, rays, n, occluded, st);
     }
-    if (queue && !(q.flags & RQ_FLAG_NO_PERSISTENT)) {
-        if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
-            return launch_persistent<true, true, false>(s, q, rays, n, nullptr, occluded, queue, st);
-        return launch_persistent<true, false, false>(s, q, rays, n, nullptr, occluded, queue, st);
-    }
-    const int block = 128;
-    if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
-        k_anyhit_strict<true><<<grid_for(n, block), block, 0, st>>>(s, rays, n, occluded, cnt);
-    else
-        k_anyhit_strict<false><<<grid_for(n, block), block, 0, st>>>(s, rays, n, occluded, cnt);
-    return cudaGetLastError();
 }
 
 }  // namespace rq

@@ -58,6 +58,8 @@ struct rq_scene {
     int32_t b8roots_cap = 0;
     int64_t b8_nodes = 0, b8_tris = 0, b8_bytes = 0;
     double b8_build_ms = 0.0;
+    // autotuned launch variant per [layout][query kind] (-1 = default)
+    int8_t tuned[4][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
 };
 
 namespace rq {
@@ -69,6 +71,10 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
 // Query work counters (2 x u64) inside the context's counter block.
 inline unsigned long long* work_counters(rq_ctx* ctx) {
     return reinterpret_cast<unsigned long long*>(ctx->counters) + 8;
+}
+// Device counter of compact (active) secondary rays in a GI pass.
+inline unsigned long long* frame_counter(rq_ctx* ctx) {
+    return reinterpret_cast<unsigned long long*>(ctx->counters) + 12;
 }
 // Device status bits of the kernels (atomicOr), read by rq_device_status.
 inline unsigned* status_word(rq_ctx* ctx) { return reinterpret_cast<unsigned*>(ctx->counters) + 30; }

@@ -155,8 +155,8 @@ def _stream(t, stream):
     return torch.cuda.current_stream(t.device).cuda_stream
 
 
-def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0) -> L.RqOpts:
-    return L.RqOpts(layout, mode, tie, flags, block_size, (C.c_int32 * 3)())
+def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0, min_blocks=0, persistent=0) -> L.RqOpts:
+    return L.RqOpts(layout, mode, tie, flags, block_size, min_blocks, persistent, 0)
 
 
 class Scene:
@@ -177,6 +177,18 @@ class Scene:
     def set_entities(self, entities):
         e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
         check(lib().rq_scene_set_entities(self.handle, ptr(e), e.shape[0]), self.ctx.handle)
+
+    def autotune(self, rays, query: int = 0, layout: int = 0) -> dict:
+        """rq_autotune on device rays: times each launch variant, keeps the fastest."""
+        n = rays.numel() * rays.element_size() // 32
+        r = L.RqTuneResult()
+        check(lib().rq_autotune(self.ctx.handle, self.handle, ptr(rays), n, query,
+                                layout or self.layout, C.byref(r)), self.ctx.handle)
+        variants = [dict(block=r.block[i], min_blocks=r.min_blocks_of[i],
+                         persistent=r.persistent_of[i], ms=round(r.ms[i], 4))
+                    for i in range(r.n_variants)]
+        return dict(variant=r.variant, block_size=r.block_size, min_blocks=r.min_blocks,
+                    persistent=r.persistent, variants=variants)
 
     def build_bvh8(self) -> dict:
         """rq_scene_build_bvh8: enables RQ_LAYOUT_BVH8Q queries on this scene."""
@@ -202,7 +214,7 @@ class Scene:
 
     # -- queries -----------------------------------------------------------------------------
     def closest(self, rays, hits=None, *, layout=0, mode=0, tie=0, flags=0, block_size=0,
-                stream=None):
+                min_blocks=0, persistent=0, stream=None):
         """Closest hit.  `rays` is a numpy RAY_DTYPE array (host path, copies inside the call)
         or a torch uint8/float tensor on the device holding 32-byte rays."""
         host = isinstance(rays, np.ndarray)
@@ -214,12 +226,13 @@ class Scene:
                 import torch
                 hits = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
-        o = _opts(layout, mode, tie, f, block_size)
+        o = _opts(layout, mode, tie, f, block_size, min_blocks, persistent)
         check(lib().rq_closest(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), C.byref(o),
                                _stream(rays, stream)), self.ctx.handle)
         return hits
 
-    def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, stream=None):
+    def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, min_blocks=0,
+               persistent=0, stream=None):
         host = isinstance(rays, np.ndarray)
         n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
         if out is None:
@@ -229,7 +242,7 @@ class Scene:
                 import torch
                 out = torch.empty(n, dtype=torch.uint8, device=rays.device)
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
-        o = _opts(layout, mode, 0, f, block_size)
+        o = _opts(layout, mode, 0, f, block_size, min_blocks, persistent)
         check(lib().rq_anyhit(self.ctx.handle, self.handle, ptr(rays), n, ptr(out), C.byref(o),
                               _stream(rays, stream)), self.ctx.handle)
         return out
@@ -287,7 +300,7 @@ class _GiMixin:
         return out
 
     def gi_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0,
-                 stats=False, stream=None):
+                 block_size=0, min_blocks=0, persistent=0, stats=False, stream=None):
         """Whole GI / AO pass.  numpy primary rays -> host path (copies inside the call)."""
         host = isinstance(primary, np.ndarray)
         n = primary.shape[0] if host else primary.numel() * primary.element_size() // 32
@@ -297,7 +310,8 @@ class _GiMixin:
             else:
                 out = _empty_like_dev(primary, (n, 4), __import__("torch").float32)
         st = L.RqFrameStats() if stats else None
-        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size,
+                  min_blocks, persistent)
         check(lib().rq_gi_frame(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params),
                                 C.byref(o), ptr(out), C.byref(st) if st is not None else None,
                                 _stream(primary, stream)), self.ctx.handle)

@@ -136,8 +136,13 @@ typedef struct rq_opts {
     int32_t mode;        /* rq_mode */
     int32_t tie;         /* rq_tie */
     int32_t flags;       /* RQ_FLAG_* */
-    int32_t block_size;  /* 0 = tuned default */
-    int32_t reserved[3];
+    /* Launch variant: (block_size, min_blocks, persistent) must name one of the compiled variants
+     * listed by rq_autotune; all zero = the variant rq_autotune picked for this scene, layout and
+     * query kind, else the default (128 threads, one thread per ray). */
+    int32_t block_size;
+    int32_t min_blocks;  /* minimum resident blocks per SM the kernel was compiled for */
+    int32_t persistent;  /* 1 = persistent ray-queue kernel (BVH2 layouts only) */
+    int32_t reserved;
 } rq_opts;
 
 /* ---- Context ---------------------------------------------------------------------------- */
@@ -261,6 +266,20 @@ rq_status rq_scene_destroy(rq_scene* scene);
  * TraverseBVHStackless.glsl:280-319).  opts may be NULL (strict, lower-index ties). */
 rq_status rq_closest(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
                      rq_hit* hits, const rq_opts* opts, void* stream);
+
+/* Autotuner: times every compiled launch variant of the traversal kernel for `query` (0 =
+ * closest hit, 1 = any hit) and `layout` on the caller's device rays (3 timed launches each, after
+ * one warm-up), and records the fastest for the scene; later queries with an all-zero variant in
+ * rq_opts use it.  out->ms[i] is variant i's best time in ms (-1 = not applicable to the layout). */
+#define RQ_MAX_VARIANTS 8
+typedef struct rq_tune_result {
+    int32_t variant, block_size, min_blocks, persistent;
+    int32_t n_variants;
+    float ms[RQ_MAX_VARIANTS];
+    int32_t block[RQ_MAX_VARIANTS], min_blocks_of[RQ_MAX_VARIANTS], persistent_of[RQ_MAX_VARIANTS];
+} rq_tune_result;
+rq_status rq_autotune(rq_ctx* ctx, rq_scene* scene, const rq_ray* rays, int64_t n, int32_t query,
+                      rq_layout layout, rq_tune_result* out);
 
 /* Any hit (occlusion) for n rays: occluded[i] = 1 when a triangle with tmin < t < tmax lies on the
  * ray.  Replaces float IntersectRay(o, d) / IntersectSceneOcclusion (TraverseBVHStack.glsl:
