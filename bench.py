@@ -253,9 +253,14 @@ def main():
     B8 = L.LAYOUT_BVH8Q
 
     if args.profile:
-        # the launch the tuned bench uses (128 threads, 8 resident blocks: 64-register cap)
+        # One k_bvh8 launch: the secondary closest-hit launch of the roofline below (8,294,400 ray
+        # slots of one GI pass), with the launch variant the autotuner picks on GB300 (128 threads,
+        # 8 resident blocks).  Earlier kernels: k_closest_strict (primary) and k_gi_raygen.
         b8 = sc.build_bvh8()
-        sc.gi_frame(d_rays, p, out=d_pix, layout=B8, block_size=128, min_blocks=8, stream=sptr)
+        h = sc.closest(d_rays, stream=sptr)
+        sec = sc.gi_raygen(d_rays, h, p, stream=sptr)
+        fn = sc.anyhit if q_any else sc.closest
+        fn(sec, layout=B8, block_size=128, min_blocks=8, stream=sptr)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": wl["name"], "pixels": n, "bvh8_nodes": b8["nodes"]}))
         return
