@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
@@ -211,6 +211,121 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_c5(args):
+    """Differentiation workload: heightfield 512x512 (524,288 tris, vertex z = parameters), 1024x1024
+    depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a second-seed
+    heightfield; timed step = rq_fwd + rq_bwd; central FD check (h = 1e-3) on 256 random vertices
+    whose pixels do not switch triangles; 100 Adam steps (lr 1e-3) with BVH refit per step."""
+    import torch
+    import candela_gb300 as R
+    from candela_gb300 import scenes as S
+    from candela_gb300.engine import diff_params
+    torch.cuda.set_device(0)
+    mesh = S.c5_heightfield_scene(5)
+    tmesh = S.c5_heightfield_scene(6)
+    bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
+    tb = R.build_bvh(tmesh.vertices, tmesh.indices, tmesh.mesh_ids, 0, layout=R.STACK)
+    ctx = R.Context(0)
+    sc = ctx.scene(R.STACK, mesh.vertices, bvh.tris, bvh.nodes, R.identity_entity(0, bvh.nodes.shape[0]))
+    tsc = ctx.scene(R.STACK, tmesh.vertices, tb.tris, tb.nodes, R.identity_entity(0, tb.nodes.shape[0]))
+    rays = S.camera_rays(1024, 1024, **S.C5_CAMERA)
+    n = len(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    p = diff_params(shadow_rays=True)
+    target, _, t0 = tsc.forward(d_rays, torch.zeros((n, 2), device="cuda"), p)
+    t0.close()
+    grad = torch.empty((mesh.vertices.shape[0], 3), dtype=torch.float32, device="cuda")
+    image = torch.empty((n, 2), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        _, _, tape = sc.forward(d_rays, target, p, image=image, want_loss=False)
+        tape.backward(grad)
+        tape.close()
+    torch.cuda.synchronize()
+    evs = []
+    for i in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _, _, tape = sc.forward(d_rays, target, p, image=image, want_loss=False)
+        tape.backward(grad)
+        b.record(stream)
+        evs.append((a, b, tape))
+    torch.cuda.synchronize()
+    step_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in evs)
+    for _, _, t in evs:
+        t.close()
+    # central finite differences on 256 vertices away from triangle switches
+    _, loss0, tape = sc.forward(d_rays, target, p)
+    gz = tape.backward().cpu().numpy()[:, 2]
+    tape.close()
+    tgt = target.cpu().numpy().astype(np.float64)
+    base = torch.from_numpy(mesh.vertices["pos"][:, :3].copy()).cuda()
+    h = 1e-3
+
+    def render(dz, v):
+        xyz = base.clone()
+        xyz[v, 2] += dz
+        sc.update_positions(xyz)
+        img, _, t = sc.forward(d_rays, target, p, image=image, want_loss=False)
+        t.close()
+        tri = sc.closest(d_rays).cpu().numpy().view(R.HIT_DTYPE)["tri"]
+        im = img.cpu().numpy().astype(np.float64)
+        l = np.where(im[:, 0] > 0, (im[:, 0] - tgt[:, 0]) ** 2 + (im[:, 1] - tgt[:, 1]) ** 2, 0.0)
+        return l, tri
+
+    rng = np.random.default_rng(11)
+    cand = np.nonzero(np.abs(gz) > 1e-3 * np.abs(gz).max())[0]
+    rng.shuffle(cand)
+    rels, tried = [], 0
+    for v in cand:
+        tried += 1
+        lp, tp = render(+h, v)
+        lm, tm = render(-h, v)
+        if not np.array_equal(tp, tm):
+            continue
+        fd = (lp - lm).sum() / (2 * h)
+        rels.append(abs(fd - gz[v]) / max(abs(fd), 1e-12))
+        if len(rels) == 256 or tried > 2000:
+            break
+    sc.update_positions(base)
+    rels = np.array(rels)
+    # 100 Adam steps on vertex z with refit
+    z = base[:, 2].clone().requires_grad_(False)
+    m1 = torch.zeros_like(z)
+    m2 = torch.zeros_like(z)
+    lr, b1, b2, eps = 1e-3, 0.9, 0.999, 1e-8
+    losses = []
+    t_adam = time.perf_counter()
+    for k in range(1, 101):
+        xyz = base.clone()
+        xyz[:, 2] = z
+        sc.update_positions(xyz)
+        _, l, tape = sc.forward(d_rays, target, p, image=image)
+        g = tape.backward(grad)[:, 2]
+        tape.close()
+        losses.append(l)
+        m1.mul_(b1).add_(g, alpha=1 - b1)
+        m2.mul_(b2).addcmul_(g, g, value=1 - b2)
+        z -= lr * (m1 / (1 - b1 ** k)) / ((m2 / (1 - b2 ** k)).sqrt() + eps)
+    torch.cuda.synchronize()
+    adam_s = time.perf_counter() - t_adam
+    line = {"metric": METRIC, "value": round(n / (step_ms / 1e3) / 1e6, 2), "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded heightfields and camera rays)",
+            "config": {"workload": "differentiation: heightfield 512x512 (524,288 tris), 1024x1024 "
+                                   "depth + Lambert + shadow any-hit, L2 vs second-seed image; step = "
+                                   "rq_fwd + rq_bwd (primary rays counted)"},
+            "fd_check": {"vertices": int(len(rels)), "h": h,
+                         "median_rel_err": float(np.median(rels)) if len(rels) else None,
+                         "max_rel_err": float(rels.max()) if len(rels) else None,
+                         "frac_within_1e-3": float((rels <= 1e-3).mean()) if len(rels) else None},
+            "adam": {"steps": 100, "lr": lr, "loss_first": losses[0], "loss_last": losses[-1],
+                     "seconds": round(adam_s, 3)},
+            "initial_loss": loss0}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -223,6 +338,11 @@ def main():
         O.build(reference=False)
         wl = make_workload(args.config)
         run_reference(args, wl, rank, world)
+        return
+
+    if args.config == "c5":
+        if rank == 0:
+            run_c5(args)
         return
 
     import torch

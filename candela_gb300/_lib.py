@@ -62,6 +62,12 @@ class RqBvh8Info(C.Structure):
                 ("bvh2_nodes", C.c_int64), ("build_ms", C.c_double)]
 
 
+class RqDiffParams(C.Structure):
+    _fields_ = [("sun_dir", C.c_float * 3), ("sun_color", C.c_float), ("albedo", C.c_float),
+                ("w_depth", C.c_float), ("w_radiance", C.c_float), ("shadow_rays", C.c_int32),
+                ("shadow_offset", C.c_float), ("recompute", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+
 class RqGiParams(C.Structure):
     _fields_ = [("spp", C.c_int32), ("seed", C.c_uint32), ("origin_offset", C.c_float),
                 ("ray_tmax", C.c_float), ("normal_mode", C.c_int32), ("query", C.c_int32),
@@ -113,6 +119,12 @@ SIGNATURES = {
     "rq_shade": (_S, [_P, _P, _P, _P, _I64, _P, C.POINTER(RqGiParams), _P, _P]),
     "rq_gi_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                          C.POINTER(RqFrameStats), _P]),
+    "rq_fwd": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqDiffParams), _P, C.POINTER(C.c_double),
+                    C.POINTER(_P), _P]),
+    "rq_bwd": (_S, [_P, _P, _P, _P]),
+    "rq_tape_free": (_S, [_P]),
+    "rq_tape_bytes": (_S, [_P, C.POINTER(_I64)]),
+    "rq_scene_update_positions": (_S, [_P, _P, _P]),
     "rq_gi_frame_noalloc": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                                  _P]),
 }

@@ -456,6 +456,13 @@ rq_status rq_scene_set_entities(rq_scene* sc, const rq_entity* ents, int32_t n_e
 rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
     if (!sc) return fail(nullptr, RQ_EINVAL, "NULL scene");
     rq_ctx* ctx = sc->ctx;
+    if (sc->host_stale) {  // positions were updated on the device: refresh the host copies
+        RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+        RQ_CUDA(ctx, cudaDeviceSynchronize());
+        RQ_CUDA(ctx, cudaMemcpy(sc->h_nodes.data(), sc->d_nodes, sc->h_nodes.size() * 4, cudaMemcpyDeviceToHost));
+        RQ_CUDA(ctx, cudaMemcpy(sc->h_verts.data(), sc->d_verts, sc->h_verts.size() * 4, cudaMemcpyDeviceToHost));
+        sc->host_stale = false;
+    }
     std::vector<rq::Bvh8Range> ranges;
     for (const rq_entity& e : sc->h_ents) ranges.push_back({e.node_offset, e.node_count});
     rq::Bvh8Out b;
@@ -590,6 +597,9 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_b8nodes) cudaFree(sc->d_b8nodes);
     if (sc->d_b8tris) cudaFree(sc->d_b8tris);
     if (sc->d_b8roots) cudaFree(sc->d_b8roots);
+    if (sc->d_refit) cudaFree(sc->d_refit);
+    if (sc->d_adj_off) cudaFree(sc->d_adj_off);
+    if (sc->d_adj) cudaFree(sc->d_adj);
     delete sc;
     return RQ_OK;
 }

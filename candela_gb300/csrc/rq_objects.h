@@ -9,7 +9,7 @@
 #include "bvh_build.h"
 #include "rq_internal.h"
 
-constexpr int kScratchSlots = 16;
+constexpr int kScratchSlots = 32;
 
 struct rq_ctx {
     int device = 0;
@@ -58,6 +58,12 @@ struct rq_scene {
     int32_t b8roots_cap = 0;
     int64_t b8_nodes = 0, b8_tris = 0, b8_bytes = 0;
     double b8_build_ms = 0.0;
+    // refit plan (node, object offset) bottom-up by level, and vertex -> (triangle, corner) lists
+    bool refit_ready = false, adj_ready = false, host_stale = false;
+    std::vector<int64_t> refit_level_off;
+    int2* d_refit = nullptr;
+    int32_t* d_adj_off = nullptr;
+    int32_t* d_adj = nullptr;
     // autotuned launch variant per [layout][query kind] (-1 = default)
     int8_t tuned[4][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
 };

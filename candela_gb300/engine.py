@@ -170,6 +170,7 @@ class Scene:
         n = np.ascontiguousarray(nodes, dtype=np.float32)
         e = np.ascontiguousarray(entities, dtype=ENTITY_DTYPE)
         self.handle = C.c_void_p()
+        self.n_verts = v.shape[0]
         check(lib().rq_scene_create(ctx.handle, layout, ptr(v), v.shape[0], ptr(t), t.shape[0],
                                     ptr(n), n.shape[0], ptr(e), e.shape[0], C.byref(self.handle)),
               ctx.handle)
@@ -323,6 +324,72 @@ class _GiMixin:
 for _name, _fn in list(vars(_GiMixin).items()):
     if callable(_fn) and not _name.startswith("__"):
         setattr(Scene, _name, _fn)
+
+
+def diff_params(sun_dir=(0.4, 0.3, -0.866), sun_color=3.0, albedo=0.7, w_depth=1.0,
+                w_radiance=1.0, shadow_rays=True, shadow_offset=1e-3, recompute=False):
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
+    return L.RqDiffParams((C.c_float * 3)(*[float(x) for x in sd]), sun_color, albedo, w_depth,
+                          w_radiance, int(shadow_rays), shadow_offset, int(recompute),
+                          (C.c_int32 * 2)())
+
+
+class Tape:
+    """rq_tape: what rq_fwd saved for rq_bwd."""
+
+    def __init__(self, scene, handle, rays):
+        self.scene, self.handle, self.rays = scene, handle, rays
+
+    def nbytes(self) -> int:
+        b = C.c_int64()
+        check(lib().rq_tape_bytes(self.handle, C.byref(b)))
+        return b.value
+
+    def backward(self, grad=None, stream=None):
+        """dloss/dposition for every vertex as an (n_verts, 3) float32 device tensor."""
+        import torch
+        sc = self.scene
+        if grad is None:
+            grad = torch.empty((sc.n_verts, 3), dtype=torch.float32, device=self.rays.device)
+        check(lib().rq_bwd(sc.ctx.handle, self.handle, ptr(grad), _stream(self.rays, stream)),
+              sc.ctx.handle)
+        return grad
+
+    def close(self):
+        if self.handle:
+            lib().rq_tape_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _scene_forward(self, rays, target, params, image=None, want_loss=True, stream=None):
+    """rq_fwd: returns (image (n, 2) device tensor, loss float or None, Tape)."""
+    import torch
+    n = rays.numel() * rays.element_size() // 32
+    if image is None:
+        image = torch.empty((n, 2), dtype=torch.float32, device=rays.device)
+    loss = C.c_double(0.0)
+    h = C.c_void_p()
+    check(lib().rq_fwd(self.ctx.handle, self.handle, ptr(rays), n, ptr(target), C.byref(params),
+                       ptr(image), C.byref(loss) if want_loss else None, C.byref(h),
+                       _stream(rays, stream)), self.ctx.handle)
+    return image, (loss.value if want_loss else None), Tape(self, h, rays)
+
+
+def _scene_update_positions(self, xyz, stream=None):
+    """rq_scene_update_positions: xyz is an (n_verts, 3) float32 device tensor; refits the BVH."""
+    check(lib().rq_scene_update_positions(self.handle, ptr(xyz), _stream(xyz, stream)),
+          self.ctx.handle)
+
+
+Scene.forward = _scene_forward
+Scene.update_positions = _scene_update_positions
 
 
 class RayIntersector:

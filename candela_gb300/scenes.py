@@ -339,3 +339,11 @@ def c1_heightfield_scene() -> Mesh:
 def c2_icosphere_scene(n_spheres: int = 64) -> Mesh:
     """64 displaced subdivision-5 icospheres + 2-triangle ground plane (1,310,722 triangles)."""
     return icosphere_set(n_spheres=n_spheres, subdiv=5, seed=2)
+
+
+C5_CAMERA = dict(eye=(0.0, -1.6, 2.2), target=(0.0, 0.0, 0.0), vfov_deg=60.0)
+
+
+def c5_heightfield_scene(seed: int = 5) -> Mesh:
+    """Heightfield 512x512 (524,288 triangles) over [-1,1]^2; vertex z are the parameters."""
+    return heightfield(512, seed=seed)

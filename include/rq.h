@@ -344,6 +344,47 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary,
                       const rq_gi_params* params, const rq_opts* opts, float* pixels4,
                       rq_frame_stats* stats, void* stream);
 
+/* ---- Differentiation: depth + Lambert adjoint w.r.t. vertex positions ---------------------- */
+
+/* No counterpart in the reference (its GI is not differentiable).  Per primary ray i the forward
+ * pass renders image[i] = (depth, radiance): depth = closest-hit t (strict traversal), radiance =
+ * albedo * sun_color * lit * max(dot(N, -sun_dir), 0) with N the geometric normal of the hit
+ * triangle faced toward the ray and lit from an optional any-hit shadow ray (visibility is
+ * treated as constant).  The loss is sum over hit pixels of w_depth*(depth - target.x)^2 +
+ * w_radiance*(radiance - target.y)^2, reduced in FP64 in a fixed order; misses contribute 0.
+ * rq_bwd writes dloss/dposition for every vertex: per-hit closed-form derivatives of t and of the
+ * Lambert term, reduced deterministically (pixels sorted by triangle with an integer counting
+ * sort, per-triangle sums in pixel order, per-vertex sums over a fixed vertex->triangle list): no
+ * floating-point atomics, so gradients are bit-reproducible.  Entities must be identities. */
+typedef struct rq_diff_params {
+    float sun_dir[3];
+    float sun_color;
+    float albedo;
+    float w_depth, w_radiance;
+    int32_t shadow_rays;
+    float shadow_offset;
+    int32_t recompute;  /* 1 = keep no hit records: rq_bwd re-traces the primary (and shadow) rays */
+    int32_t reserved[2];
+} rq_diff_params;
+
+typedef struct rq_tape rq_tape;
+
+/* rays: n device rays (must stay valid until rq_tape_free when recompute = 1); target2 / image2:
+ * n x 2 device floats (image2 written); loss: host double (nullable; reading it synchronises). */
+rq_status rq_fwd(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
+                 const float* target2, const rq_diff_params* params, float* image2, double* loss,
+                 rq_tape** tape, void* stream);
+/* grad_xyz: n_verts x 3 device floats, overwritten with dloss/dposition. */
+rq_status rq_bwd(rq_ctx* ctx, rq_tape* tape, float* grad_xyz, void* stream);
+rq_status rq_tape_free(rq_tape* tape);
+/* Device bytes the tape holds (hit records unless recompute, plus dloss/dimage). */
+rq_status rq_tape_bytes(const rq_tape* tape, int64_t* bytes);
+
+/* Replaces every vertex position (xyz: n_verts x 3 device floats) and refits the BVH2 boxes with
+ * the topology kept (exact min/max per level, bottom-up).  Stack layout scenes; the BVH8 is
+ * dropped (rebuild with rq_scene_build_bvh8). */
+rq_status rq_scene_update_positions(rq_scene* scene, const float* xyz, void* stream);
+
 /* ---- Allocation-free GI pass ------------------------------------------------------------ */
 
 /* Capacity of the fixed scratch used by rq_gi_frame_noalloc: at most this many primary rays, and
