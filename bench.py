@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
@@ -211,6 +211,127 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def c3_workload(seed: int = 3):
+    """8 seeded scenes (heightfields and icosphere sets, 10k-2M triangles log-uniform) and 64
+    queries (1k-2M rays log-uniform; half camera rays, half uniform-sphere rays; half closest,
+    half any hit)."""
+    import math
+    import candela_gb300 as R
+    from candela_gb300 import scenes as S
+    u = S.uniform(seed, 900, 8 + 64 * 4)
+    scenes = []
+    for k in range(8):
+        tris = math.exp(math.log(1e4) + u[k] * (math.log(2e6) - math.log(1e4)))
+        if k % 2 == 0:
+            n = max(8, int(round(math.sqrt(tris / 2))))
+            mesh = S.heightfield(n, seed=50 + k)
+            lo, hi = (-1.2, -1.2, -0.4), (1.2, 1.2, 0.6)
+        else:
+            sub = 2 if tris < 2e5 else 3
+            per = 20 * 4 ** sub
+            cnt = max(1, int(round(tris / per)))
+            mesh = S.icosphere_set(n_spheres=cnt, subdiv=sub, seed=60 + k, ground=6.0)
+            lo, hi = (-4.5, -4.5, -0.2), (4.5, 4.5, 2.5)
+        bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
+        scenes.append(dict(mesh=mesh, bvh=bvh, lo=lo, hi=hi, tris=int(mesh.n_tris)))
+    queries = []
+    for q in range(64):
+        a, b, c, d = u[8 + 4 * q: 12 + 4 * q]
+        n = int(math.exp(math.log(1e3) + a * (math.log(2e6) - math.log(1e3))))
+        sc = int(b * 8) % 8
+        coherent = q % 2 == 0
+        kind = 0 if (q // 2) % 2 == 0 else 1
+        lo, hi = scenes[sc]["lo"], scenes[sc]["hi"]
+        if coherent:
+            w = max(1, int(math.sqrt(n * 16 / 9)))
+            h = max(1, n // w)
+            ang = 2 * math.pi * c
+            eye = (3.5 * math.cos(ang) * hi[0] / 1.2, 3.5 * math.sin(ang) * hi[1] / 1.2, 1.5 + hi[2])
+            rays = S.camera_rays(w, h, eye=eye, target=(0.0, 0.0, 0.0))
+        else:
+            rays = S.sphere_rays(n, lo, hi, seed=700 + q)
+        queries.append(dict(scene=sc, rays=rays, kind=kind, coherent=coherent))
+    return scenes, queries
+
+
+def run_c3(args):
+    import torch
+    import candela_gb300 as R
+    from candela_gb300 import _lib as L
+    torch.cuda.set_device(0)
+    scenes, queries = c3_workload()
+    ctx = R.Context(0)
+    dev_scenes = []
+    for s_ in scenes:
+        sc = ctx.scene(R.STACK, s_["mesh"].vertices, s_["bvh"].tris, s_["bvh"].nodes,
+                       R.identity_entity(0, s_["bvh"].nodes.shape[0]))
+        sc.build_bvh8()
+        dev_scenes.append(sc)
+    qs = []
+    for q in queries:
+        d = torch.from_numpy(q["rays"].view(np.uint8)).cuda()
+        n = len(q["rays"])
+        out = (torch.empty((n, 8), dtype=torch.float32, device="cuda") if q["kind"] == 0
+               else torch.empty(n, dtype=torch.uint8, device="cuda"))
+        qs.append((dev_scenes[q["scene"]], d, q["kind"], out))
+    total = sum(len(q["rays"]) for q in queries)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(fn, reps):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(reps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.mean(ms)
+
+    def per_query(layout):
+        def fn():
+            for sc, d, kind, out in qs:
+                (sc.closest if kind == 0 else sc.anyhit)(d, out, layout=layout,
+                                                          block_size=128, min_blocks=1)
+        return fn
+
+    plain_ms = timed(per_query(0), args.steps)          # plain FP32 BVH2, one launch per query
+    b8_ms = timed(per_query(L.LAYOUT_BVH8Q), args.steps)  # BVH8q, one launch per query
+    plan = R.engine.BatchPlan(ctx, qs, layout=L.LAYOUT_BVH8Q)
+    tune = plan.autotune(allow_bvh8=True)
+    batched_ms = timed(plan.launch, args.steps)
+    want = [out.cpu().numpy().copy() for _, _, _, out in qs]
+    per_query(L.LAYOUT_BVH8Q if tune["family"] == 0 else 0)()
+    torch.cuda.synchronize()
+    same = all(np.array_equal(w.view(np.uint8)[:, :28] if w.ndim == 2 else w,
+                              out.cpu().numpy().view(np.uint8)[:, :28] if w.ndim == 2 else out.cpu().numpy())
+               for w, (_, _, _, out) in zip(want, qs))
+    v = total / (batched_ms / 1e3) / 1e6
+    line = {"metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(batched_ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (8 seeded scenes, 64 seeded queries)",
+            "config": {"workload": "batching: 64 queries (1k-2M rays, log-uniform; half camera, "
+                                   "half uniform-sphere rays; 50/50 closest/any) over 8 scenes "
+                                   "(10k-2M triangles); step = the whole batch",
+                       "total_rays": int(total), "scene_triangles": [s_["tris"] for s_ in scenes],
+                       "query_rays": [len(q["rays"]) for q in queries],
+                       "l2": "flushed before each timed step"},
+            "plain_fp32_bvh2_one_launch_per_query": {"mrays_s": round(total / (plain_ms / 1e3) / 1e6, 2),
+                                                     "ms": round(plain_ms, 4)},
+            "bvh8q_one_launch_per_query": {"mrays_s": round(total / (b8_ms / 1e3) / 1e6, 2),
+                                           "ms": round(b8_ms, 4)},
+            "batched_graph_autotuned": {"mrays_s": round(v, 2), "ms": round(batched_ms, 4),
+                                        "picked": tune, "hits_equal_per_query": bool(same)},
+            "speedup_batched_bvh8q_over_plain": round(plain_ms / batched_ms, 3)}
+    print(json.dumps(line), flush=True)
+
+
 def run_c5(args):
     """Differentiation workload: heightfield 512x512 (524,288 tris, vertex z = parameters), 1024x1024
     depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a second-seed
@@ -270,25 +391,49 @@ def run_c5(args):
         t.close()
         tri = sc.closest(d_rays).cpu().numpy().view(R.HIT_DTYPE)["tri"]
         im = img.cpu().numpy().astype(np.float64)
-        l = np.where(im[:, 0] > 0, (im[:, 0] - tgt[:, 0]) ** 2 + (im[:, 1] - tgt[:, 1]) ** 2, 0.0)
-        return l, tri
+        hit = im[:, 0] > 0
+        ld = np.where(hit, (im[:, 0] - tgt[:, 0]) ** 2, 0.0)
+        lr_ = np.where(hit, (im[:, 1] - tgt[:, 1]) ** 2, 0.0)
+        return ld, lr_, tri
 
+    # depth-only gradient for the depth-only FD comparison (w_radiance = 0)
+    pd = diff_params(shadow_rays=True, w_radiance=0.0)
+    _, _, tape = sc.forward(d_rays, target, pd)
+    gz_depth = tape.backward().cpu().numpy()[:, 2]
+    tape.close()
     rng = np.random.default_rng(11)
     cand = np.nonzero(np.abs(gz) > 1e-3 * np.abs(gz).max())[0]
     rng.shuffle(cand)
-    rels, tried = [], 0
+    plain, rich, depth_only, tried = [], [], [], 0
     for v in cand:
         tried += 1
-        lp, tp = render(+h, v)
-        lm, tm = render(-h, v)
-        if not np.array_equal(tp, tm):
-            continue
-        fd = (lp - lm).sum() / (2 * h)
-        rels.append(abs(fd - gz[v]) / max(abs(fd), 1e-12))
-        if len(rels) == 256 or tried > 2000:
+        r = {dz: render(dz, v) for dz in (h, -h, h / 2, -h / 2)}
+        if not all(np.array_equal(r[h][2], r[dz][2]) for dz in (-h, h / 2, -h / 2)):
+            continue  # a pixel switches triangle: not differentiable there
+        tot = {dz: (r[dz][0] + r[dz][1]).sum() for dz in r}
+        fd_h = (tot[h] - tot[-h]) / (2 * h)
+        fd_h2 = (tot[h / 2] - tot[-h / 2]) / h
+        fd_rich = (4 * fd_h2 - fd_h) / 3
+        fd_d = (r[h][0].sum() - r[-h][0].sum()) / (2 * h)
+        plain.append(abs(fd_h - gz[v]) / max(abs(fd_h), 1e-12))
+        rich.append(abs(fd_rich - gz[v]) / max(abs(fd_rich), 1e-12))
+        depth_only.append(abs(fd_d - gz_depth[v]) / max(abs(fd_d), 1e-12))
+        if len(plain) == 256 or tried > 3000:
             break
     sc.update_positions(base)
-    rels = np.array(rels)
+
+    def stats(x):
+        x = np.array(x)
+        return {"vertices": int(len(x)), "median_rel_err": float(np.median(x)) if len(x) else None,
+                "p95_rel_err": float(np.percentile(x, 95)) if len(x) else None,
+                "max_rel_err": float(x.max()) if len(x) else None,
+                "frac_within_1e-3": float((x <= 1e-3).mean()) if len(x) else None}
+
+    fd_check = {"h": h, "central": stats(plain), "richardson_h_h2": stats(rich),
+                "depth_only_central": stats(depth_only),
+                "note": "h = 1e-3 is 26% of a triangle edge on the 512x512 grid (cell 2/512), so the "
+                        "central difference of the Lambert term carries an O(h^2) truncation error of "
+                        "a few percent; Richardson extrapolation from h and h/2 removes it"}
     # 100 Adam steps on vertex z with refit
     z = base[:, 2].clone().requires_grad_(False)
     m1 = torch.zeros_like(z)
@@ -316,10 +461,7 @@ def run_c5(args):
             "config": {"workload": "differentiation: heightfield 512x512 (524,288 tris), 1024x1024 "
                                    "depth + Lambert + shadow any-hit, L2 vs second-seed image; step = "
                                    "rq_fwd + rq_bwd (primary rays counted)"},
-            "fd_check": {"vertices": int(len(rels)), "h": h,
-                         "median_rel_err": float(np.median(rels)) if len(rels) else None,
-                         "max_rel_err": float(rels.max()) if len(rels) else None,
-                         "frac_within_1e-3": float((rels <= 1e-3).mean()) if len(rels) else None},
+            "fd_check": fd_check,
             "adam": {"steps": 100, "lr": lr, "loss_first": losses[0], "loss_last": losses[-1],
                      "seconds": round(adam_s, 3)},
             "initial_loss": loss0}
@@ -340,9 +482,9 @@ def main():
         run_reference(args, wl, rank, world)
         return
 
-    if args.config == "c5":
+    if args.config in ("c3", "c5"):
         if rank == 0:
-            run_c5(args)
+            (run_c5 if args.config == "c5" else run_c3)(args)
         return
 
     import torch

@@ -68,6 +68,17 @@ class RqDiffParams(C.Structure):
                 ("shadow_offset", C.c_float), ("recompute", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
+class RqQuery(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("n", C.c_int64), ("kind", C.c_int32),
+                ("reserved", C.c_int32), ("hits", C.c_void_p), ("occluded", C.c_void_p)]
+
+
+class RqBatchTune(C.Structure):
+    _fields_ = [("family", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
+                ("n", C.c_int32), ("ms", C.c_float * 12), ("family_of", C.c_int32 * 12),
+                ("block_of", C.c_int32 * 12), ("min_blocks_of", C.c_int32 * 12)]
+
+
 class RqGiParams(C.Structure):
     _fields_ = [("spp", C.c_int32), ("seed", C.c_uint32), ("origin_offset", C.c_float),
                 ("ray_tmax", C.c_float), ("normal_mode", C.c_int32), ("query", C.c_int32),
@@ -125,6 +136,11 @@ SIGNATURES = {
     "rq_tape_free": (_S, [_P]),
     "rq_tape_bytes": (_S, [_P, C.POINTER(_I64)]),
     "rq_scene_update_positions": (_S, [_P, _P, _P]),
+    "rq_batch": (_S, [_P, C.POINTER(RqQuery), _I32, C.POINTER(RqOpts), _P]),
+    "rq_batch_plan_create": (_S, [_P, C.POINTER(RqQuery), _I32, C.POINTER(RqOpts), C.POINTER(_P)]),
+    "rq_batch_plan_launch": (_S, [_P, _P]),
+    "rq_batch_plan_autotune": (_S, [_P, _I32, C.POINTER(RqBatchTune)]),
+    "rq_batch_plan_destroy": (_S, [_P]),
     "rq_gi_frame_noalloc": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                                  _P]),
 }

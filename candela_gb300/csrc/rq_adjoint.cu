@@ -468,6 +468,7 @@ rq_status rq_scene_update_positions(rq_scene* sc, const float* xyz, void* stream
             rq::k_refit_level<<<rq::grid(e - b, 128), 128, 0, st>>>(sc->d_nodes, sc->d_tris, sc->d_verts,
                                                                     sc->d_refit + b, e - b);
     }
+    RQ_CUDA(ctx, rq::launch_tri_fast(sc->d_tris, sc->n_tris, sc->d_verts, sc->d_tri_fast, st));
     RQ_CUDA(ctx, cudaGetLastError());
     sc->bvh8 = false;          // quantised boxes are not refitted
     sc->host_stale = true;     // host copies of vertices / nodes are refreshed on demand

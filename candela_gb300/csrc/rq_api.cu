@@ -79,12 +79,11 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
     q.status = status_word(ctx);
     if (q.layout == RQ_LAYOUT_BVH8Q) {
         if (!sc->bvh8) return fail(ctx, RQ_ENOTSUP, "BVH8 not built: call rq_scene_build_bvh8");
-        if (q.mode != RQ_MODE_STRICT || !q.tie_lower)
-            return fail(ctx, RQ_ENOTSUP, "BVH8 queries use strict leaf tests and lower-index ties");
+        if (!q.tie_lower)
+            return fail(ctx, RQ_ENOTSUP, "BVH8 queries use the lower-index tie rule");
         return RQ_OK;
     }
     if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
-    if (q.mode == RQ_MODE_FAST) return fail(ctx, RQ_ENOTSUP, "fast mode not available");
     return RQ_OK;
 }
 
@@ -403,6 +402,11 @@ rq_status rq_scene_create(rq_ctx* ctx, rq_layout layout, const rq_vertex* verts,
         return fail(ctx, RQ_ENOMEM, std::string("scene device allocation: ") + cudaGetErrorString(e));
     }
     sc->bytes = static_cast<int64_t>(nb + tb + vb);
+    if ((e = cudaMalloc(&sc->d_tri_fast, 48 * n_tris)) != cudaSuccess) {
+        rq_scene_destroy(sc);
+        return fail(ctx, RQ_ENOMEM, "fast triangle records allocation failed");
+    }
+    sc->bytes += 48 * n_tris;
     if ((e = cudaMemcpy(sc->d_nodes, nodes, nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(sc->d_tris, tris, tb, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(sc->d_verts, verts, vb, cudaMemcpyHostToDevice)) != cudaSuccess) {
@@ -416,6 +420,12 @@ rq_status rq_scene_create(rq_ctx* ctx, rq_layout layout, const rq_vertex* verts,
     sc->view.verts = sc->d_verts;
     sc->view.n_verts = n_verts;
     sc->view.layout = layout;
+    sc->view.tri_fast = sc->d_tri_fast;
+    if ((e = rq::launch_tri_fast(sc->d_tris, n_tris, sc->d_verts, sc->d_tri_fast, nullptr)) != cudaSuccess ||
+        (e = cudaDeviceSynchronize()) != cudaSuccess) {
+        rq_scene_destroy(sc);
+        return cuda_fail(ctx, e, "fast triangle records");
+    }
     rq_status s = rq_scene_set_entities(sc, ents, n_ents);
     if (s != RQ_OK) {
         rq_scene_destroy(sc);
@@ -598,6 +608,7 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_b8tris) cudaFree(sc->d_b8tris);
     if (sc->d_b8roots) cudaFree(sc->d_b8roots);
     if (sc->d_refit) cudaFree(sc->d_refit);
+    if (sc->d_tri_fast) cudaFree(sc->d_tri_fast);
     if (sc->d_adj_off) cudaFree(sc->d_adj_off);
     if (sc->d_adj) cudaFree(sc->d_adj);
     delete sc;

@@ -27,6 +27,8 @@ struct SceneView {
     const uint4* b8_nodes;
     const float4* b8_tris;
     const int32_t* b8_roots;
+    // Fast-mode triangle records in reference triangle order: {v0, mesh}, {e1, 0}, {e2, 0}.
+    const float4* tri_fast;
     // Optional device-side ray count: when set, a launch over n rays processes only the first
     // min(n, *ray_count) (used for compacted secondary rays whose count is known on the device).
     const unsigned long long* ray_count;
@@ -53,6 +55,10 @@ struct LaunchVariant {
 constexpr int kNumLaunchVariants = 7;
 extern const LaunchVariant kLaunchVariants[kNumLaunchVariants];
 
+// Fast-mode triangle records from the triangle and vertex buffers (rq_kernels.cu).
+cudaError_t launch_tri_fast(const int4* tris, int64_t n_tris, const float4* verts, float4* out,
+                            cudaStream_t st);
+
 // Kernel launchers (rq_kernels.cu).  Return cudaGetLastError() after the launch.
 // `queue` (nullable) is a device ray counter for the persistent kernels; without one (or with
 // RQ_FLAG_NO_PERSISTENT) one thread runs per ray.
@@ -60,6 +66,28 @@ cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ra
                            rq_hit* hits, unsigned long long* queue, cudaStream_t st);
 cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                           uint8_t* occluded, unsigned long long* queue, cudaStream_t st);
+
+// One query of a batch (device descriptor).
+struct QueryDesc {
+    SceneView s;
+    const rq_ray* rays;
+    rq_hit* hits;
+    uint8_t* occ;
+    int64_t n;
+    int64_t base;   // first global work index of this query
+    int32_t kind;   // 0 = closest, 1 = any
+    int32_t flags;
+    int32_t tie_lower;
+    int32_t pad;
+};
+constexpr int kMaxBatchQueries = 1024;
+// Batch launch variants (block, min blocks per SM) and layout families.
+constexpr int kNumBatchVariants = 4;
+extern const LaunchVariant kBatchVariants[kNumBatchVariants];
+enum BatchFamily { kFamilyBvh8 = 0, kFamilyStrict = 1, kFamilyFast = 2 };
+// One persistent launch over every query (rq_kernels.cu).  queue is zeroed by the caller.
+cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
+                         unsigned long long* queue, unsigned* status, cudaStream_t st);
 
 // Intermediate buffers of one GI pass (n primary rays, n*spp secondary rays).
 struct GiBuffers {

@@ -8,6 +8,7 @@
 
 #include "rq_internal.h"
 #include "rq_bvh8.cuh"
+#include "rq_fast.cuh"
 #include "rq_persistent.cuh"
 #include "rq_strict.cuh"
 
@@ -119,12 +120,75 @@ __global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq
     if (counters) count_work(counters, nodes, tests);
 }
 
-// BVH8 traversal, one thread per ray, with the strict scene loop around it.
+// BVH8 traversal of one ray with the strict scene loop around it.
+template <bool kAny>
+__device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, const float4 r1, int flags,
+                                         rq_hit& hh, bool& occluded, int32_t& visits,
+                                         int32_t& tests, unsigned& status) {
+    const float rtmin = r0.w, rtmax = r1.w;
+    const strict::f3 o = strict::xyz(r0), d = strict::xyz(r1);
+    float tmax = rtmax, closest = -1.0f;
+    int32_t mesh = -1, tri = -1, ent = -1;
+    occluded = false;
+    if (rtmax > rtmin) {
+        for (int e = 0; e < s.n_ents; ++e) {
+            const rq_entity& E = s.ents[e];
+            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f)
+                continue;
+            const int32_t root = s.b8_roots[e];
+            if (root < 0) continue;
+            const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
+                                                strict::xform(E.inverse, d, 0.0f));
+            bvh8::Hit8 h{kAny ? rtmax : tmax, -1.0f, kAny ? -1 : tri, -1};
+            visits += bvh8::traverse<kAny, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests,
+                                                 status);
+            const float T = h.closest;
+            if (kAny) {
+                if (T > 0.0f) {
+                    occluded = true;
+                    break;
+                }
+            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+                tmax = T;
+                closest = T;
+                mesh = h.mesh;
+                tri = h.tri;
+                ent = e;
+            }
+        }
+    }
+    if (kAny) return;
+    hh.t = hh.u = hh.v = hh.w = -1.0f;
+    hh.tri = hh.mesh = hh.entity = -1;
+    hh.iters = visits;
+    if (closest > 0.0f) {
+        hh.tri = tri;
+        hh.mesh = mesh;
+        hh.entity = ent;
+        const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
+        if (report) {
+            const rq_entity& E = s.ents[ent];
+            const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
+            const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
+            const int4 tr = strict::ldg4i(s.tris + tri);
+            const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
+            float u, v, w;
+            strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y), strict::vpos(s, tr.z),
+                                 u, v, w);
+            hh.t = closest;
+            hh.u = u;
+            hh.v = v;
+            hh.w = w;
+        }
+    }
+}
+
+// BVH8 traversal, one thread per ray.
 template <bool kAny, int kB, int kM>
 __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
-                                              rq_hit* __restrict__ hits, uint8_t* __restrict__ occ,
-                                              int flags, unsigned* status_out,
-                                              unsigned long long* counters) {
+                                                 rq_hit* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                 int flags, unsigned* status_out,
+                                                 unsigned long long* counters) {
     if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     int32_t visits = 0, tests = 0;
@@ -132,70 +196,111 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __re
     if (i < n) {
         float4 r0, r1;
         load_ray(rays, i, r0, r1);
-        const float rtmin = r0.w, rtmax = r1.w;
-        const strict::f3 o = strict::xyz(r0), d = strict::xyz(r1);
-        float tmax = rtmax, closest = -1.0f;
-        int32_t mesh = -1, tri = -1, ent = -1;
-        bool occluded = false;
-        if (rtmax > rtmin) {
-            for (int e = 0; e < s.n_ents; ++e) {
-                const rq_entity& E = s.ents[e];
-                if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f)
-                    continue;
-                const int32_t root = s.b8_roots[e];
-                if (root < 0) continue;
-                const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
-                                                    strict::xform(E.inverse, d, 0.0f));
-                bvh8::Hit8 h{kAny ? rtmax : tmax, -1.0f, kAny ? -1 : tri, -1};
-                visits += bvh8::traverse<kAny, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h,
-                                                     tests, status);
-                const float T = h.closest;
-                if (kAny) {
-                    if (T > 0.0f) {
-                        occluded = true;
-                        break;
-                    }
-                } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
-                    tmax = T;
-                    closest = T;
-                    mesh = h.mesh;
-                    tri = h.tri;
-                    ent = e;
-                }
-            }
-        }
-        if (kAny) {
+        rq_hit hh;
+        bool occluded;
+        bvh8_ray<kAny>(s, r0, r1, flags, hh, occluded, visits, tests, status);
+        if (kAny)
             occ[i] = occluded ? 1 : 0;
-        } else {
-            rq_hit hh;
-            hh.t = hh.u = hh.v = hh.w = -1.0f;
-            hh.tri = hh.mesh = hh.entity = -1;
-            hh.iters = visits;
-            if (closest > 0.0f) {
-                hh.tri = tri;
-                hh.mesh = mesh;
-                hh.entity = ent;
-                const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
-                if (report) {
-                    const rq_entity& E = s.ents[ent];
-                    const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
-                    const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
-                    const int4 tr = strict::ldg4i(s.tris + tri);
-                    const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
-                    float u, v, w;
-                    strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y),
-                                         strict::vpos(s, tr.z), u, v, w);
-                    hh.t = closest;
-                    hh.u = u;
-                    hh.v = v;
-                    hh.w = w;
-                }
-            }
+        else
             store_hit(hits, i, hh);
-        }
     }
     if (status) atomicOr(status_out, status);
     if (counters) count_work(counters, visits, tests);
+}
+
+// Fast-mode BVH2 traversal, one thread per ray.
+template <bool kAny, bool kStackless, int kB, int kM>
+__global__ void __launch_bounds__(kB, kM) k_fast(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
+                                                 rq_hit* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                 int flags, unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    rq_hit h;
+    h.iters = 0;
+    int32_t tests = 0;
+    if (i < n) {
+        float4 r0, r1;
+        load_ray(rays, i, r0, r1);
+        bool oc;
+        fast::scene<kAny, kStackless>(s, r0, r1, flags, h, oc, tests);
+        if (kAny)
+            occ[i] = oc ? 1 : 0;
+        else
+            store_hit(hits, i, h);
+    }
+    if (counters) count_work(counters, h.iters, tests);
+}
+
+// Batched queries: one persistent launch; each warp takes 32 consecutive work items from a global
+// counter, and every item finds its query by binary search over the queries' first work index.
+template <int kB, int kM, int kFamily>
+__global__ void __launch_bounds__(kB, kM) k_batch(const QueryDesc* __restrict__ qd, int nq, int64_t total,
+                                                  unsigned long long* queue, unsigned* status_out) {
+    __shared__ int64_t base[kMaxBatchQueries + 1];
+    for (int k = threadIdx.x; k <= nq; k += blockDim.x) base[k] = k < nq ? qd[k].base : total;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
+    unsigned status = 0;
+    while (true) {
+        unsigned long long start = 0;
+        if (lane == 0) start = atomicAdd(queue, 32ull);
+        start = __shfl_sync(0xFFFFFFFFu, start, 0);
+        if (static_cast<int64_t>(start) >= total) break;
+        const int64_t idx = static_cast<int64_t>(start) + lane;
+        if (idx >= total) continue;
+        int lo = 0, hi = nq - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (base[mid] <= idx) lo = mid; else hi = mid - 1;
+        }
+        const QueryDesc& Q = qd[lo];
+        const int64_t i = idx - base[lo];
+        float4 r0, r1;
+        load_ray(Q.rays, i, r0, r1);
+        rq_hit h;
+        bool oc = false;
+        int32_t visits = 0, tests = 0;
+        if (kFamily == kFamilyBvh8) {
+            if (Q.kind) bvh8_ray<true>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
+            else bvh8_ray<false>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
+        } else if (kFamily == kFamilyFast) {
+            const bool sl = Q.s.layout == RQ_LAYOUT_BVH2_STACKLESS;
+            if (Q.kind) {
+                if (sl) fast::scene<true, true>(Q.s, r0, r1, Q.flags, h, oc, tests);
+                else fast::scene<true, false>(Q.s, r0, r1, Q.flags, h, oc, tests);
+            } else {
+                if (sl) fast::scene<false, true>(Q.s, r0, r1, Q.flags, h, oc, tests);
+                else fast::scene<false, false>(Q.s, r0, r1, Q.flags, h, oc, tests);
+            }
+        } else {
+            const bool sl = Q.s.layout == RQ_LAYOUT_BVH2_STACKLESS;
+            if (Q.kind) {
+                oc = sl ? strict::scene_any<true>(Q.s, r0, r1, visits, tests)
+                        : strict::scene_any<false>(Q.s, r0, r1, visits, tests);
+            } else if (Q.tie_lower) {
+                if (sl) strict::scene_closest<true, true>(Q.s, r0, r1, Q.flags, h, tests);
+                else strict::scene_closest<false, true>(Q.s, r0, r1, Q.flags, h, tests);
+            } else {
+                if (sl) strict::scene_closest<true, false>(Q.s, r0, r1, Q.flags, h, tests);
+                else strict::scene_closest<false, false>(Q.s, r0, r1, Q.flags, h, tests);
+            }
+        }
+        if (Q.kind) Q.occ[i] = oc ? 1 : 0;
+        else store_hit(Q.hits, i, h);
+    }
+    if (status) atomicOr(status_out, status);
+}
+
+__global__ void k_tri_fast(const int4* __restrict__ tris, int64_t n, const float4* __restrict__ verts,
+                           float4* __restrict__ out) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 tr = tris[t];
+    const float4 a = verts[2 * static_cast<int64_t>(tr.x)], b = verts[2 * static_cast<int64_t>(tr.y)];
+    const float4 c = verts[2 * static_cast<int64_t>(tr.z)];
+    out[3 * t] = make_float4(a.x, a.y, a.z, __int_as_float(tr.w));
+    out[3 * t + 1] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
+    out[3 * t + 2] = make_float4(c.x - a.x, c.y - a.y, c.z - a.z, 0.0f);
 }
 
 inline unsigned grid_for(int64_t n, int block) {
@@ -249,6 +354,10 @@ cudaError_t closest_variant(const SceneView& s, const QueryConfig& q, const rq_r
     const unsigned g = grid_for(n, kB);
     if (q.layout == RQ_LAYOUT_BVH8Q)
         k_bvh8<false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, nullptr, q.flags, q.status, cnt);
+    else if (q.mode == RQ_MODE_FAST)
+        q.layout == RQ_LAYOUT_BVH2_STACKLESS
+            ? k_fast<false, true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, nullptr, q.flags, cnt)
+            : k_fast<false, false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, nullptr, q.flags, cnt);
     else if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
         q.tie_lower ? k_closest_strict<true, true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt)
                     : k_closest_strict<true, false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, hits, q.flags, cnt);
@@ -265,6 +374,10 @@ cudaError_t anyhit_variant(const SceneView& s, const QueryConfig& q, const rq_ra
     const unsigned g = grid_for(n, kB);
     if (q.layout == RQ_LAYOUT_BVH8Q)
         k_bvh8<true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, nullptr, occ, q.flags, q.status, cnt);
+    else if (q.mode == RQ_MODE_FAST)
+        q.layout == RQ_LAYOUT_BVH2_STACKLESS
+            ? k_fast<true, true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, nullptr, occ, q.flags, cnt)
+            : k_fast<true, false, kB, kM><<<g, kB, 0, st>>>(s, rays, n, nullptr, occ, q.flags, cnt);
     else if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
         k_anyhit_strict<true, kB, kM><<<g, kB, 0, st>>>(s, rays, n, occ, cnt);
     else
@@ -281,7 +394,8 @@ cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ra
                            rq_hit* hits, unsigned long long* queue, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int v = q.variant_closest < 0 ? 0 : q.variant_closest;
-    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q)) v = 0;
+    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q || q.mode == RQ_MODE_FAST))
+        v = 0;
     switch (v) {
         case 1: return closest_variant<128, 4>(s, q, rays, n, hits, st);
         case 2: return closest_variant<128, 6>(s, q, rays, n, hits, st);
@@ -304,7 +418,8 @@ cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray
                           uint8_t* occluded, unsigned long long* queue, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int v = q.variant_any < 0 ? 0 : q.variant_any;
-    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q)) v = 0;
+    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q || q.mode == RQ_MODE_FAST))
+        v = 0;
     switch (v) {
         case 1: return anyhit_variant<128, 4>(s, q, rays, n, occluded, st);
         case 2: return anyhit_variant<128, 6>(s, q, rays, n, occluded, st);
@@ -318,6 +433,57 @@ cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray
         }
         default: return anyhit_variant<128, 1>(s, q, rays, n, occluded, st);
     }
+}
+
+const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1}, {128, 8, 1}, {64, 12, 1}, {256, 3, 1}};
+
+namespace {
+template <int kB, int kM>
+cudaError_t batch_variant(const QueryDesc* d, int nq, int64_t total, int family,
+                          unsigned long long* queue, unsigned* status, cudaStream_t st) {
+    int g = 0;
+    switch (family) {
+        case kFamilyBvh8: g = persistent_grid(k_batch<kB, kM, kFamilyBvh8>, kB); break;
+        case kFamilyFast: g = persistent_grid(k_batch<kB, kM, kFamilyFast>, kB); break;
+        default: g = persistent_grid(k_batch<kB, kM, kFamilyStrict>, kB); break;
+    }
+    const int64_t need = (total + 31) / 32 * 32 / kB + 1;
+    if (need < g) g = static_cast<int>(need);
+    if (family == kFamilyBvh8)
+        k_batch<kB, kM, kFamilyBvh8><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+    else if (family == kFamilyFast)
+        k_batch<kB, kM, kFamilyFast><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+    else
+        k_batch<kB, kM, kFamilyStrict><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
+                         unsigned long long* queue, unsigned* status, cudaStream_t st) {
+    if (total <= 0 || nq <= 0) return cudaSuccess;
+    if (!st && !queue) {  // grid-size query only (fills the occupancy cache outside stream capture)
+        switch (variant) {
+            case 1: persistent_grid(k_batch<128, 8, kFamilyBvh8>, 128); persistent_grid(k_batch<128, 8, kFamilyStrict>, 128); persistent_grid(k_batch<128, 8, kFamilyFast>, 128); break;
+            case 2: persistent_grid(k_batch<64, 12, kFamilyBvh8>, 64); persistent_grid(k_batch<64, 12, kFamilyStrict>, 64); persistent_grid(k_batch<64, 12, kFamilyFast>, 64); break;
+            case 3: persistent_grid(k_batch<256, 3, kFamilyBvh8>, 256); persistent_grid(k_batch<256, 3, kFamilyStrict>, 256); persistent_grid(k_batch<256, 3, kFamilyFast>, 256); break;
+            default: persistent_grid(k_batch<128, 1, kFamilyBvh8>, 128); persistent_grid(k_batch<128, 1, kFamilyStrict>, 128); persistent_grid(k_batch<128, 1, kFamilyFast>, 128); break;
+        }
+        return cudaGetLastError();
+    }
+    switch (variant) {
+        case 1: return batch_variant<128, 8>(d_desc, nq, total, family, queue, status, st);
+        case 2: return batch_variant<64, 12>(d_desc, nq, total, family, queue, status, st);
+        case 3: return batch_variant<256, 3>(d_desc, nq, total, family, queue, status, st);
+        default: return batch_variant<128, 1>(d_desc, nq, total, family, queue, status, st);
+    }
+}
+
+cudaError_t launch_tri_fast(const int4* tris, int64_t n_tris, const float4* verts, float4* out,
+                            cudaStream_t st) {
+    if (n_tris <= 0) return cudaSuccess;
+    k_tri_fast<<<grid_for(n_tris, 256), 256, 0, st>>>(tris, n_tris, verts, out);
+    return cudaGetLastError();
 }
 
 }  // namespace rq

@@ -44,6 +44,7 @@ struct rq_scene {
     int32_t ents_cap = 0;
     int64_t bytes = 0;
     rq::SceneView view{};
+    float4* d_tri_fast = nullptr;  // fast-mode triangle records (3 x float4 per triangle)
     float* d_albedo = nullptr;  // 3 floats per mesh id
     int32_t n_albedo = 0;
     // host copies (validation and derived layouts)

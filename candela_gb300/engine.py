@@ -392,6 +392,61 @@ Scene.forward = _scene_forward
 Scene.update_positions = _scene_update_positions
 
 
+def _queries(queries):
+    """[(scene, device rays, kind, out)] -> ctypes array of rq_query (kind 0 closest, 1 any)."""
+    arr = (L.RqQuery * len(queries))()
+    for k, (sc, rays, kind, out) in enumerate(queries):
+        n = rays.numel() * rays.element_size() // 32
+        arr[k] = L.RqQuery(sc.handle, ptr(rays), n, kind, 0, ptr(out) if kind == 0 else None,
+                           ptr(out) if kind == 1 else None)
+    return arr
+
+
+def batch(ctx: Context, queries, layout=0, mode=0, flags=0, block_size=0, min_blocks=0, stream=None):
+    """rq_batch: every query in one persistent launch."""
+    arr = _queries(queries)
+    o = _opts(layout, mode, 0, flags, block_size, min_blocks, 0)
+    st = stream
+    if st is None and queries:
+        st = _stream(queries[0][1], None)
+    check(lib().rq_batch(ctx.handle, arr, len(queries), C.byref(o), st), ctx.handle)
+
+
+class BatchPlan:
+    """rq_batch_plan: a fixed batch replayed as a captured CUDA graph."""
+
+    def __init__(self, ctx: Context, queries, layout=0, mode=0, flags=0):
+        self.ctx = ctx
+        self._keep = queries
+        arr = _queries(queries)
+        o = _opts(layout, mode, 0, flags)
+        self.handle = C.c_void_p()
+        check(lib().rq_batch_plan_create(ctx.handle, arr, len(queries), C.byref(o),
+                                         C.byref(self.handle)), ctx.handle)
+
+    def launch(self, stream=None):
+        st = stream if stream is not None else _stream(self._keep[0][1], None)
+        check(lib().rq_batch_plan_launch(self.handle, st), self.ctx.handle)
+
+    def autotune(self, allow_bvh8=True) -> dict:
+        r = L.RqBatchTune()
+        check(lib().rq_batch_plan_autotune(self.handle, int(allow_bvh8), C.byref(r)), self.ctx.handle)
+        combos = [dict(family=r.family_of[i], block=r.block_of[i], min_blocks=r.min_blocks_of[i],
+                       ms=round(r.ms[i], 4)) for i in range(r.n)]
+        return dict(family=r.family, block_size=r.block_size, min_blocks=r.min_blocks, combos=combos)
+
+    def close(self):
+        if self.handle:
+            lib().rq_batch_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class RayIntersector:
     """Mirror of Candela::RayIntersector<T> (Intersector.h:60-451) over the C ABI.
 

@@ -287,6 +287,46 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* scene, const rq_ray* rays, int64_t 
 rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
                     uint8_t* occluded, const rq_opts* opts, void* stream);
 
+/* ---- Batched queries --------------------------------------------------------------------- */
+
+/* One query of a batch: device rays in, device hits (kind 0, closest) or occlusion bytes (kind 1,
+ * any hit) out, over any scene of the context. */
+typedef struct rq_query {
+    const rq_scene* scene;
+    const rq_ray* rays;
+    int64_t n;
+    int32_t kind;  /* 0 = closest hit, 1 = any hit */
+    int32_t reserved;
+    rq_hit* hits;
+    uint8_t* occluded;
+} rq_query;
+
+/* Runs every query in ONE persistent launch (a work queue over all queries' rays; a batch of
+ * uneven sizes keeps every SM busy).  opts->layout: RQ_LAYOUT_BVH8Q (every scene needs its BVH8)
+ * or 0 = each scene's BVH2 layout; opts->mode strict or fast.  Results equal per-query
+ * rq_closest / rq_anyhit calls with the same options.  At most 1024 queries.  No counterpart in
+ * the reference (it issues one dispatch per pass). */
+rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, const rq_opts* opts,
+                   void* stream);
+
+/* A batch fixed at creation (descriptors uploaded once), replayed as a captured CUDA graph:
+ * a memset of the work counter and the persistent launch.  The query buffers must stay valid. */
+typedef struct rq_batch_plan rq_batch_plan;
+rq_status rq_batch_plan_create(rq_ctx* ctx, const rq_query* queries, int32_t n_queries,
+                               const rq_opts* opts, rq_batch_plan** out);
+rq_status rq_batch_plan_launch(rq_batch_plan* plan, void* stream);
+/* Times every batch launch variant (block size x occupancy target) for each usable layout family
+ * (BVH8Q when every scene has one, the BVH2 layouts) on the plan's own queries, keeps the fastest
+ * and re-captures the graph.  ms[i] = time of combination i, described by family_of[i] (0 =
+ * BVH8Q, 1 = BVH2 strict, 2 = BVH2 fast), block_of[i], min_blocks_of[i]; -1 = not applicable. */
+typedef struct rq_batch_tune {
+    int32_t family, block_size, min_blocks, n;
+    float ms[12];
+    int32_t family_of[12], block_of[12], min_blocks_of[12];
+} rq_batch_tune;
+rq_status rq_batch_plan_autotune(rq_batch_plan* plan, int32_t allow_bvh8, rq_batch_tune* out);
+rq_status rq_batch_plan_destroy(rq_batch_plan* plan);
+
 /* ---- Diffuse GI / RTAO ------------------------------------------------------------------ */
 
 /* Parameters of the GI / AO pass that consumes the queries (Shaders/DiffuseTrace.glsl:386-662). */
