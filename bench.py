@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
@@ -332,6 +332,85 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c4(args):
+    """Precision workload: 256 displaced subdivision-5 icospheres over [-8,8]^2 x [0,4]
+    (5,242,880 triangles: the stated 4,194,304 does not match 256 x 20,480), 2^23 rays with origins
+    uniform in the scene bounds and directions uniform on the sphere; closest hit with the BVH8q
+    and with the strict FP32 BVH2; triangle-ID agreement and t / barycentric error against the FP64
+    recomputation of each winning hit."""
+    import torch
+    import candela_gb300 as R
+    from candela_gb300 import _lib as L
+    from candela_gb300 import scenes as S
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    mesh = S.icosphere_set(n_spheres=256, subdiv=5, seed=4, lo=(-8.0, -8.0, 0.0), hi=(8.0, 8.0, 4.0),
+                           ground=None)
+    gen_s = time.perf_counter() - t0
+    bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
+    ctx = R.Context(0)
+    sc = ctx.scene(R.STACK, mesh.vertices, bvh.tris, bvh.nodes, R.identity_entity(0, bvh.nodes.shape[0]))
+    b8 = sc.build_bvh8()
+    n = 1 << 23
+    rays = S.sphere_rays(n, (-8.0, -8.0, 0.0), (8.0, 8.0, 4.0), seed=44)
+    d = torch.from_numpy(rays.view(np.uint8)).cuda()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    tune8 = sc.autotune(d, query=0, layout=L.LAYOUT_BVH8Q)
+    tune2 = sc.autotune(d, query=0, layout=R.STACK)
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        evs = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    h2 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    h8 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    ms2 = timed(lambda: sc.closest(d, h2))
+    ms8 = timed(lambda: sc.closest(d, h8, layout=L.LAYOUT_BVH8Q))
+    u2 = h2.cpu().numpy().view(np.uint32)
+    u8 = h8.cpu().numpy().view(np.uint32)
+    hit2 = h2[:, 0].cpu().numpy() > 0
+    same_id = (u2[:, 4] == u8[:, 4]) & (hit2 == (h8[:, 0].cpu().numpy() > 0))
+    same_all = (u2[:, :7] == u8[:, :7]).all(1)
+
+    def errs(h):
+        e = sc.verify(d, h).cpu().numpy()
+        te, be = e[:, 0], e[:, 1]
+        ok = np.isfinite(te)
+        return {"hits_verified": int(ok.sum()), "t_rel_err_max": float(te[ok].max()),
+                "t_rel_err_median": float(np.median(te[ok])),
+                "bary_err_max": float(be[ok].max()), "bary_err_median": float(np.median(be[ok]))}
+
+    line = {"metric": METRIC, "value": round(n / (ms8 / 1e3) / 1e6, 2), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms8, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded icospheres and rays)",
+            "config": {"workload": "precision: 256 displaced subdiv-5 icospheres over [-8,8]^2x[0,4] "
+                                   f"({mesh.n_tris} tris), {n} incoherent rays (origins uniform in the "
+                                   "bounds, directions uniform on the sphere), closest hit",
+                       "scene_gen_s": round(gen_s, 2), "bvh2_build_ms": round(bvh.build_ms, 1),
+                       "bvh8": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
+            "bvh8q": {"mrays_s": round(n / (ms8 / 1e3) / 1e6, 2), "ms": round(ms8, 4),
+                      "picked": (tune8["block_size"], tune8["min_blocks"]), "fp64": errs(h8)},
+            "bvh2_strict": {"mrays_s": round(n / (ms2 / 1e3) / 1e6, 2), "ms": round(ms2, 4),
+                            "picked": (tune2["block_size"], tune2["min_blocks"]), "fp64": errs(h2)},
+            "triangle_id_agreement": float(same_id.mean()),
+            "identical_hit_records": float(same_all.mean()),
+            "hit_rate": float(hit2.mean()), "device_status": ctx.device_status(),
+            "speedup_bvh8q_over_bvh2": round(ms2 / ms8, 3)}
+    print(json.dumps(line), flush=True)
+
+
 def run_c5(args):
     """Differentiation workload: heightfield 512x512 (524,288 tris, vertex z = parameters), 1024x1024
     depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a second-seed
@@ -482,9 +561,9 @@ def main():
         run_reference(args, wl, rank, world)
         return
 
-    if args.config in ("c3", "c5"):
+    if args.config in ("c3", "c4", "c5"):
         if rank == 0:
-            (run_c5 if args.config == "c5" else run_c3)(args)
+            {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config](args)
         return
 
     import torch

@@ -136,6 +136,7 @@ SIGNATURES = {
     "rq_tape_free": (_S, [_P]),
     "rq_tape_bytes": (_S, [_P, C.POINTER(_I64)]),
     "rq_scene_update_positions": (_S, [_P, _P, _P]),
+    "rq_verify_hits": (_S, [_P, _P, _P, _P, _I64, _P, _P]),
     "rq_batch": (_S, [_P, C.POINTER(RqQuery), _I32, C.POINTER(RqOpts), _P]),
     "rq_batch_plan_create": (_S, [_P, C.POINTER(RqQuery), _I32, C.POINTER(RqOpts), C.POINTER(_P)]),
     "rq_batch_plan_launch": (_S, [_P, _P]),

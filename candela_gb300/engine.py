@@ -191,6 +191,15 @@ class Scene:
         return dict(variant=r.variant, block_size=r.block_size, min_blocks=r.min_blocks,
                     persistent=r.persistent, variants=variants)
 
+    def verify(self, rays, hits, stream=None):
+        """rq_verify_hits: FP64 relative t error and barycentric error per hit ((n, 2), NaN = miss)."""
+        import torch
+        n = rays.numel() * rays.element_size() // 32
+        err = torch.empty((n, 2), dtype=torch.float32, device=rays.device)
+        check(lib().rq_verify_hits(self.ctx.handle, self.handle, ptr(rays), ptr(hits), n, ptr(err),
+                                   _stream(rays, stream)), self.ctx.handle)
+        return err
+
     def build_bvh8(self) -> dict:
         """rq_scene_build_bvh8: enables RQ_LAYOUT_BVH8Q queries on this scene."""
         info = L.RqBvh8Info()

@@ -287,6 +287,13 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* scene, const rq_ray* rays, int64_t 
 rq_status rq_anyhit(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
                     uint8_t* occluded, const rq_opts* opts, void* stream);
 
+/* FP64 verification of closest hits: for each hit, recomputes t and the barycentrics of the same
+ * triangle in double precision (Moller-Trumbore on the entity-transformed ray) and writes
+ * err2[2i] = |t - t64| / t64 and err2[2i+1] = max |w - w64| over the three weights (NaN for misses
+ * and for hits the FP64 test rejects).  Device buffers.  This is the only FP64 code on the GPU. */
+rq_status rq_verify_hits(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays,
+                         const rq_hit* hits, int64_t n, float* err2, void* stream);
+
 /* ---- Batched queries --------------------------------------------------------------------- */
 
 /* One query of a batch: device rays in, device hits (kind 0, closest) or occlusion bytes (kind 1,

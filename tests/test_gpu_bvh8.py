@@ -73,3 +73,33 @@ def test_bvh8_requires_build_and_strict(ctx):
     with pytest.raises(R.RqError) as e:
         sc.closest(rays, layout=L.LAYOUT_BVH8Q)
     assert e.value.status == L.RQ_ENOTSUP
+
+
+def test_fp64_verification_kernel(ctx):
+    """rq_verify_hits: FP64 recomputation of each winning hit agrees with a numpy FP64 evaluation and
+    bounds the FP32 error."""
+    bufs = single_object("ico2", R.STACK)
+    v, t, n, e = bufs
+    sc = ctx.scene(R.STACK, *bufs)
+    rays = S.sphere_rays(50_000, (-1.5, -1.5, -0.2), (1.5, 1.5, 1.0), seed=9)
+    d = rays_to_device(rays)
+    h = sc.closest(d)
+    err = sc.verify(d, h).cpu().numpy()
+    hh = hits_from_device(h)
+    hit = hh["t"] > 0
+    assert np.isnan(err[~hit]).all()
+    ok = np.isfinite(err[:, 0])
+    assert ok.sum() >= 0.99 * hit.sum()
+    assert np.median(err[ok, 0]) < 1e-6 and err[ok, 0].max() < 1e-3
+    # numpy FP64 reference on a few hits
+    P = v["pos"][:, :3].astype(np.float64)
+    for i in np.nonzero(ok)[0][:50]:
+        a, b, c = P[t[hh["tri"][i], :3]]
+        o, dd = rays["o"][i].astype(np.float64), rays["d"][i].astype(np.float64)
+        e1, e2 = b - a, c - a
+        p_ = np.cross(dd, e2)
+        det = e1 @ p_
+        tv = o - a
+        q = np.cross(tv, e1)
+        t64 = (e2 @ q) / det
+        assert abs(abs(hh["t"][i] - t64) / t64 - err[i, 0]) <= 1e-6 * max(1.0, err[i, 0])
