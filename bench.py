@@ -643,6 +643,10 @@ def main():
     total_ms, value = combine_ranks(total_ms, rays_per_step, args.steps, world, dist, dev)
     # the plain FP32 kernel (strict BVH2, default launch) on the same pass, for the ratio
     plain_ms = timed_steps(R.STACK, args.steps, 1)
+    p_sorted = p
+    p = gi_params(**wl["params"], sort_rays=False)
+    unsorted_ms = timed_steps(B8, args.steps, 1)
+    p = p_sorted
     plain_value = rays_per_step * args.steps / (plain_ms / 1e3) / 1e6
 
     # ---- e2e: host buffers through the C ABI (pinned in, pinned out), host clock
@@ -756,6 +760,9 @@ def main():
                        "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
                        "bvh_build_s": round(wl["build_s"], 3),
                        "bvh8_build": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
+            "bvh8q_pass_without_octant_binning": {
+                "value": round(rays_per_step * args.steps / (unsorted_ms / 1e3) / 1e6, 2),
+                "ms_per_step": round(unsorted_ms / args.steps, 4)},
             "plain_fp32_bvh2": {"value": round(plain_value, 2), "unit": UNIT,
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},

@@ -115,6 +115,97 @@ __global__ void k_shadow_raygen(SceneView s, const rq_ray* __restrict__ rays,
     }
 }
 
+// Secondary ray j of the GI pass (same arithmetic as k_gi_raygen); false when the primary missed.
+__device__ __forceinline__ bool gi_ray(const SceneView& s, const rq_ray* __restrict__ prim,
+                                       const rq_hit* __restrict__ hits, int64_t j, const GiArgs& a,
+                                       f3& org, f3& dir) {
+    const int64_t i = j / a.spp;
+    float4 h0;
+    int4 h1;
+    get_hit(hits, i, h0, h1);
+    if (!(h0.x > 0.0f)) return false;
+    const float4* pr = reinterpret_cast<const float4*>(prim) + 2 * i;
+    const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+    const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+    const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    const uint32_t rid = static_cast<uint32_t>(j);
+    const float u0 = gi::u01(gi::sample_key(a.seed, rid, 0u));
+    const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
+    dir = gi::cos_weighted_hemisphere(N, u0, u1);
+    org = strict::add(P, strict::muls(N, a.origin_offset));
+    return true;
+}
+
+__device__ __forceinline__ unsigned octant(const f3& d) {
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+
+// Pass 1 of the octant-binned compaction: counts active rays per direction octant.
+__global__ void __launch_bounds__(256) k_gi_octant_count(SceneView s, const rq_ray* __restrict__ prim,
+                                                         const rq_hit* __restrict__ hits, int64_t n,
+                                                         GiArgs a, unsigned long long* counts) {
+    __shared__ unsigned c[8];
+    if (threadIdx.x < 8) c[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j < n * a.spp) {
+        f3 org, dir;
+        if (gi_ray(s, prim, hits, j, a, org, dir)) atomicAdd(&c[octant(dir)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && c[threadIdx.x])
+        atomicAdd(counts + threadIdx.x, static_cast<unsigned long long>(c[threadIdx.x]));
+}
+
+// Pass 2: writes each active ray into its octant's region (regions in octant order, starting at
+// the exclusive prefix of the counts; cursors[o] advances per block), with the slot maps.
+__global__ void __launch_bounds__(256) k_gi_octant_scatter(
+    SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n, GiArgs a,
+    const unsigned long long* counts, unsigned long long* cursors, rq_ray* __restrict__ out,
+    int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of, unsigned long long* total) {
+    __shared__ unsigned c[8];
+    __shared__ unsigned long long base[8];
+    if (threadIdx.x < 8) c[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    f3 org{0.0f, 0.0f, 0.0f}, dir{0.0f, 0.0f, 1.0f};
+    bool act = false;
+    unsigned o = 0, rank = 0;
+    if (j < n * a.spp) {
+        act = gi_ray(s, prim, hits, j, a, org, dir);
+        if (act) {
+            o = octant(dir);
+            rank = atomicAdd(&c[o], 1u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        unsigned long long pre = 0;
+        for (unsigned k = 0; k < threadIdx.x; ++k) pre += counts[k];
+        base[threadIdx.x] = c[threadIdx.x]
+                                ? pre + atomicAdd(cursors + threadIdx.x, static_cast<unsigned long long>(c[threadIdx.x]))
+                                : 0ull;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int k = 0; k < 8; ++k) t += counts[k];
+            *total = t;
+        }
+    }
+    __syncthreads();
+    if (j < n * a.spp) {
+        if (act) {
+            const int64_t cidx = static_cast<int64_t>(base[o] + rank);
+            put_ray(out, cidx, org, 0.0f, dir, a.ray_tmax);
+            slot_of[cidx] = static_cast<int32_t>(j);
+            comp_of[j] = static_cast<int32_t>(cidx);
+        } else {
+            comp_of[j] = -1;
+        }
+    }
+}
+
 // Compacting variant of k_gi_raygen: active secondary rays are appended to `out` (block-aggregated
 // atomic, so only the order of blocks varies between runs), with slot_of[c] = slot j of compact
 // ray c and comp_of[j] = c (or -1 for an inactive slot).  Results are scattered back by slot, so
@@ -508,8 +599,18 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     int32_t* comp_of = static_cast<int32_t*>(d_comp);
     RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, rq::queue_counter(ctx, 0), st));
     if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
-    rq::k_gi_raygen_compact<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
-                                                              slot_of, comp_of, count);
+    if (p->sort_rays) {
+        void* d_oct = nullptr;
+        if ((s = rq::scratch(ctx, 31, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
+        unsigned long long* counts = static_cast<unsigned long long*>(d_oct);
+        RQ_CUDA(ctx, cudaMemsetAsync(counts, 0, 16 * sizeof(unsigned long long), st));
+        rq::k_gi_octant_count<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts);
+        rq::k_gi_octant_scatter<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts,
+                                                                  counts + 8, sec, slot_of, comp_of, count);
+    } else {
+        rq::k_gi_raygen_compact<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
+                                                                  slot_of, comp_of, count);
+    }
     RQ_CUDA(ctx, cudaGetLastError());
     rq::SceneView cv = sc->view;  // secondary launches cover only the compact prefix
     cv.ray_count = count;

@@ -351,7 +351,9 @@ typedef struct rq_gi_params {
     float sun_dir[3];      /* u_SunDirection: direction the light travels */
     float sun_color[3];    /* SUN_COLOR_DIFF */
     float sky_color[3];    /* radiance returned by a miss (the reference samples u_Skymap) */
-    int32_t reserved[3];
+    int32_t sort_rays;     /* rq_gi_frame: 1 = group active secondary rays by direction octant
+                              before tracing (same results, more coherent warps) */
+    int32_t reserved[2];
 } rq_gi_params;
 
 typedef struct rq_frame_stats {
