@@ -18,6 +18,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "librq.so"
+EXAMPLE_SRC = PKG / "examples" / "rq_intersector_example.cpp"
+EXAMPLE = PKG / "lib" / "rq_intersector_example"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -84,6 +86,15 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError("link of librq.so failed")
+    # C++ host example over the C ABI (the RayIntersector<T> mirror in include/rq_intersector.hpp)
+    if force or _stale(EXAMPLE, [EXAMPLE_SRC, LIB, *INCLUDE.glob("*.h*")]):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), str(EXAMPLE_SRC), "-o", str(EXAMPLE),
+               "-L", str(LIB.parent), "-lrq", f"-Wl,-rpath,{LIB.parent}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("build of the C++ example failed")
     return LIB
 
 
