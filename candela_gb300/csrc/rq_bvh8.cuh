@@ -130,9 +130,8 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
             const uint32_t fZ0 = nz ? loz0 : hiz0, fZ1 = nz ? loz1 : hiz1;
             const float onx = bx - px, ofx = bx + px, ony = by - py, ofy = by + py;
             const float onz = bz - pz, ofz = bz + pz;
-            uint32_t hits_oct = 0;  // internal children hit, bit (slot ^ oct)
-            uint32_t tmask = 0;     // triangles of leaf children hit
             const uint32_t meta0 = w1.z, meta1 = w1.w;
+            uint32_t hitmask = 0;  // bit s: child slot s entered
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 const int k = s & 3;
@@ -147,13 +146,38 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                 const float tfz = fmaf(ubyte_biased(f, k), isz, ofz);
                 const float tn = fmaxf(max3f(tnx, tny, tnz), tmin);
                 const float tf = fminf(min3f(tfx, tfy, tfz), h.tmax);
-                if (tn <= tf) {
-                    if ((imask >> s) & 1u) {
-                        hits_oct |= 1u << (s ^ r.oct);
-                    } else {
-                        const uint32_t m = ((s < 4 ? meta0 : meta1) >> (8 * k)) & 0xFFu;
-                        if (m) tmask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-                    }
+                hitmask |= (tn <= tf ? 1u : 0u) << s;
+            }
+            // internal children in octant order: bit j of hits_oct = bit (j ^ oct) of the mask
+            uint32_t hits_oct = hitmask & imask;
+            {
+                const uint32_t s1 = ((hits_oct & 0x55u) << 1) | ((hits_oct >> 1) & 0x55u);
+                hits_oct = (r.oct & 1u) ? s1 : hits_oct;
+                const uint32_t s2 = ((hits_oct & 0x33u) << 2) | ((hits_oct >> 2) & 0x33u);
+                hits_oct = (r.oct & 2u) ? s2 : hits_oct;
+                const uint32_t s4 = ((hits_oct & 0x0Fu) << 4) | ((hits_oct >> 4) & 0x0Fu);
+                hits_oct = (r.oct & 4u) ? s4 : hits_oct;
+            }
+            uint32_t tmask = 0;  // triangles of the leaf children entered
+            uint32_t lh = hitmask & ~imask;
+            while (lh) {
+                const int s = __ffs(lh) - 1;
+                lh &= lh - 1;
+                const uint32_t m = ((s < 4 ? meta0 : meta1) >> (8 * (s & 3))) & 0xFFu;
+                if (m) tmask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+            }
+            // prefetch the node visited next while this node's triangles are tested
+            if (tmask) {
+                uint32_t gh = hits_oct ? hits_oct : static_cast<uint32_t>(group >> 32) & 0xFFu;
+                if (gh) {
+                    const uint64_t grp = hits_oct ? (static_cast<uint64_t>(w1.x) | (static_cast<uint64_t>(imask) << 40))
+                                                  : group;
+                    const uint32_t slot = static_cast<uint32_t>(__ffs(gh) - 1) ^ r.oct;
+                    const uint32_t gim = static_cast<uint32_t>(grp >> 40) & 0xFFu;
+                    const uint32_t nxt = static_cast<uint32_t>(grp) + __popc(gim & ((1u << slot) - 1u));
+                    const char* pa = reinterpret_cast<const char*>(nodes + 5 * static_cast<int64_t>(nxt));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(pa));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + 79));
                 }
             }
             // leaf triangles of this node
