@@ -594,14 +594,15 @@ def main():
     B8 = L.LAYOUT_BVH8Q
 
     if args.profile:
-        # One k_bvh8 launch: the secondary closest-hit launch of the roofline below (8,294,400 ray
-        # slots of one GI pass), with the launch variant the autotuner picks on GB300 (128 threads,
-        # 8 resident blocks).  Earlier kernels: k_closest_strict (primary) and k_gi_raygen.
+        # One k_bvh8_persistent launch: the secondary closest-hit launch of the roofline below
+        # (8,294,400 ray slots of one GI pass), with the launch variant the autotuner picks on
+        # GB300 (persistent ray queue, 128 threads, 8 resident blocks).  Earlier kernels:
+        # k_closest_strict (primary) and k_gi_raygen.
         b8 = sc.build_bvh8()
         h = sc.closest(d_rays, stream=sptr)
         sec = sc.gi_raygen(d_rays, h, p, stream=sptr)
         fn = sc.anyhit if q_any else sc.closest
-        fn(sec, layout=B8, block_size=128, min_blocks=8, stream=sptr)
+        fn(sec, layout=B8, block_size=128, min_blocks=8, persistent=1, stream=sptr)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": wl["name"], "pixels": n, "bvh8_nodes": b8["nodes"]}))
         return
@@ -643,10 +644,10 @@ def main():
     total_ms, value = combine_ranks(total_ms, rays_per_step, args.steps, world, dist, dev)
     # the plain FP32 kernel (strict BVH2, default launch) on the same pass, for the ratio
     plain_ms = timed_steps(R.STACK, args.steps, 1)
-    p_sorted = p
-    p = gi_params(**wl["params"], sort_rays=False)
-    unsorted_ms = timed_steps(B8, args.steps, 1)
-    p = p_sorted
+    p_plain = p
+    p = gi_params(**wl["params"], sort_rays=True)
+    sorted_ms = timed_steps(B8, args.steps, 1)
+    p = p_plain
     plain_value = rays_per_step * args.steps / (plain_ms / 1e3) / 1e6
 
     # ---- e2e: host buffers through the C ABI (pinned in, pinned out), host clock
@@ -690,6 +691,22 @@ def main():
         ("primary_closest_bvh8q", lambda: sc.closest(d_rays, layout=B8, stream=sptr), n, {"layout": B8}),
         ("secondary_closest_bvh8q", lambda: sc.closest(d_sec, layout=B8, stream=sptr), n_sec, {"layout": B8}),
         ("secondary_anyhit_bvh8q", lambda: sc.anyhit(d_sec, layout=B8, stream=sptr), n_sec, {"layout": B8}),
+        ("primary_closest_bvh8q_128x8",
+         lambda: sc.closest(d_rays, layout=B8, stream=sptr, block_size=128, min_blocks=8), n, None),
+        ("primary_closest_bvh8q_persistent",
+         lambda: sc.closest(d_rays, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         n, None),
+        ("secondary_closest_bvh8q_128x8",
+         lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8), n_sec, None),
+        ("secondary_closest_bvh8q_persistent",
+         lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         n_sec, None),
+        ("secondary_closest_bvh8q_persistent_m1",
+         lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=1, persistent=1),
+         n_sec, None),
+        ("secondary_anyhit_bvh8q_persistent",
+         lambda: sc.anyhit(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         n_sec, None),
     ]
     sc_sl = ctx.scene(R.STACKLESS, wl["mesh"].vertices, wl["bvh_sl"].tris, wl["bvh_sl"].nodes,
                       wl["ent_sl"])
@@ -724,6 +741,7 @@ def main():
     ref = "secondary_anyhit_strict_stack" if q_any else "secondary_closest_strict_stack"
     c2 = breakdown[ref]["counts"]
     algo_bytes = 64 * c2["node_visits"] + 64 * c2["triangle_tests"]  # BVH2-equivalent work
+    dom_persistent = bool(tuning["bvh8q_anyhit" if q_any else "bvh8q_closest"]["persistent"])
     c8 = breakdown[dom]["counts"]
     fetched8 = 80 * c8["node_visits"] + 64 * c8["triangle_tests"]
     k_ms = breakdown[dom]["ms"]
@@ -738,7 +756,8 @@ def main():
                 traffic = int(f[2])
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": dom.replace("_", " ") + " (k_bvh8)", "kernel_ms": k_ms,
+                "kernel": dom.replace("_", " ") + (" (k_bvh8_persistent)" if dom_persistent else " (k_bvh8)"),
+                "kernel_ms": k_ms,
                 "algorithmic_bytes_per_launch": int(algo_bytes),
                 "algorithmic_bytes_basis": "strict BVH2 work for the same rays: 64 B per node visit "
                                            "+ 64 B per triangle test",
@@ -760,9 +779,9 @@ def main():
                        "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
                        "bvh_build_s": round(wl["build_s"], 3),
                        "bvh8_build": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
-            "bvh8q_pass_without_octant_binning": {
-                "value": round(rays_per_step * args.steps / (unsorted_ms / 1e3) / 1e6, 2),
-                "ms_per_step": round(unsorted_ms / args.steps, 4)},
+            "bvh8q_pass_with_octant_binning": {
+                "value": round(rays_per_step * args.steps / (sorted_ms / 1e3) / 1e6, 2),
+                "ms_per_step": round(sorted_ms / args.steps, 4)},
             "plain_fp32_bvh2": {"value": round(plain_value, 2), "unit": UNIT,
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},

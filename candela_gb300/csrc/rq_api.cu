@@ -69,8 +69,8 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
         q.variant_any = sc->tuned[q.layout][1];
     }
     if (o->flags & RQ_FLAG_NO_PERSISTENT) {
-        if (q.variant_closest >= 0 && kLaunchVariants[q.variant_closest].persistent) q.variant_closest = 0;
-        if (q.variant_any >= 0 && kLaunchVariants[q.variant_any].persistent) q.variant_any = 0;
+        q.variant_closest = non_persistent_variant(q.variant_closest);
+        q.variant_any = non_persistent_variant(q.variant_any);
     }
     if (o->tie != RQ_TIE_LOWER_INDEX && o->tie != RQ_TIE_FIRST_FOUND)
         return fail(ctx, RQ_EINVAL, "unknown tie rule");
@@ -550,7 +550,7 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, 
         out->min_blocks_of[v] = kLaunchVariants[v].min_blocks;
         out->persistent_of[v] = kLaunchVariants[v].persistent;
         out->ms[v] = -1.0f;
-        if (kLaunchVariants[v].persistent && q.layout == RQ_LAYOUT_BVH8Q) continue;
+        if (kLaunchVariants[v].persistent && q.mode == RQ_MODE_FAST) continue;
         q.variant_closest = q.variant_any = v;
         float vbest = 1e30f;
         for (int rep = 0; rep < 4; ++rep) {

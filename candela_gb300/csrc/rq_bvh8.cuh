@@ -80,23 +80,32 @@ struct Hit8 {
     int32_t mesh;
 };
 
-// Visits the BVH8 rooted at `root`.  Returns the node-visit count; sets *status bits on overflow.
+// Walk state of one ray through one BVH8: the node to visit next, the current group
+// (child_base | (hit bits, octant order) << 32 | imask << 40), the group stack depth and the visit
+// count.  The stack itself lives outside the struct so that the scalars stay in registers.
+struct Walk {
+    uint64_t group;
+    int32_t node, sp, visits;
+};
+
+__device__ __forceinline__ Walk walk_begin(int32_t root) { return Walk{0ull, root, 0, 0}; }
+
+// Visits node w.node (box tests of its eight children, then its leaf triangles) and selects the
+// node after it.  Returns false when the walk has ended (stack empty, any-hit found, or an
+// overflow/budget status bit set).
 template <bool kAny, bool kTieLower>
-__device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                            int32_t root, const Ray8& r, float tmin, Hit8& h, int32_t& tests,
-                            unsigned& status) {
-    uint64_t stack[kStack];
-    int sp = 0;
-    // current group: child_base | (hit bits, octant order) << 32 | imask << 40
-    uint64_t group = 0;
-    int32_t node = root;
-    int32_t visits = 0;
+__device__ __forceinline__ bool step(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                     const Ray8& r, float tmin, Hit8& h, Walk& w, uint64_t* stack,
+                                     int32_t& tests, unsigned& status) {
     const float kUlp8 = 8.0f * 5.96046448e-08f;
-    while (true) {
-        if (node >= 0) {
-            if (++visits > kMaxVisits) {
+    uint64_t group = w.group;
+    int sp = w.sp;
+    const int32_t node = w.node;
+    {
+        {
+            if (++w.visits > kMaxVisits) {
                 status |= kStatusBudget;
-                break;
+                return false;
             }
             const uint4* nd = nodes + 5 * static_cast<int64_t>(node);
             const uint4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3),
@@ -211,7 +220,7 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                 if (static_cast<uint32_t>(group >> 32) & 0xFFu) {
                     if (sp >= kStack) {
                         status |= kStatusStackOverflow;
-                        break;
+                        return false;
                     }
                     stack[sp++] = group;
                 }
@@ -219,21 +228,34 @@ __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __res
                         (static_cast<uint64_t>(imask) << 40);
             }
         }
-        // next node: lowest remaining bit of the current group, else pop
-        uint32_t gh = static_cast<uint32_t>(group >> 32) & 0xFFu;
-        if (!gh) {
-            if (sp == 0) break;
-            group = stack[--sp];
-            gh = static_cast<uint32_t>(group >> 32) & 0xFFu;
-        }
-        const int j = __ffs(gh) - 1;
-        gh &= gh - 1;
-        const uint32_t slot = static_cast<uint32_t>(j) ^ r.oct;
-        const uint32_t gim = static_cast<uint32_t>(group >> 40) & 0xFFu;
-        node = static_cast<int32_t>(static_cast<uint32_t>(group) + __popc(gim & ((1u << slot) - 1u)));
-        group = (group & ~(0xFFull << 32)) | (static_cast<uint64_t>(gh) << 32);
     }
-    return visits;
+    // next node: lowest remaining bit of the current group, else pop
+    uint32_t gh = static_cast<uint32_t>(group >> 32) & 0xFFu;
+    if (!gh) {
+        if (sp == 0) return false;
+        group = stack[--sp];
+        gh = static_cast<uint32_t>(group >> 32) & 0xFFu;
+    }
+    const int j = __ffs(gh) - 1;
+    gh &= gh - 1;
+    const uint32_t slot = static_cast<uint32_t>(j) ^ r.oct;
+    const uint32_t gim = static_cast<uint32_t>(group >> 40) & 0xFFu;
+    w.node = static_cast<int32_t>(static_cast<uint32_t>(group) + __popc(gim & ((1u << slot) - 1u)));
+    w.group = (group & ~(0xFFull << 32)) | (static_cast<uint64_t>(gh) << 32);
+    w.sp = sp;
+    return true;
+}
+
+// Visits the BVH8 rooted at `root`.  Returns the node-visit count; sets *status bits on overflow.
+template <bool kAny, bool kTieLower>
+__device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                            int32_t root, const Ray8& r, float tmin, Hit8& h, int32_t& tests,
+                            unsigned& status) {
+    uint64_t stack[kStack];
+    Walk w = walk_begin(root);
+    while (step<kAny, kTieLower>(nodes, tris, r, tmin, h, w, stack, tests, status)) {
+    }
+    return w.visits;
 }
 
 }  // namespace bvh8

@@ -597,7 +597,11 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     float4* shade = static_cast<float4*>(d_shade);
     int32_t* slot_of = static_cast<int32_t*>(d_slot);
     int32_t* comp_of = static_cast<int32_t*>(d_comp);
-    RQ_CUDA(ctx, rq::launch_closest(sc->view, q, prim, n, phit, rq::queue_counter(ctx, 0), st));
+    // Camera rays are coherent and short (a few node visits): the one-thread-per-ray form of the
+    // tuned launch shape beats the persistent ray queue there, which pays per-ray hand-over costs.
+    rq::QueryConfig qp = q;
+    qp.variant_closest = rq::non_persistent_variant(q.variant_closest);
+    RQ_CUDA(ctx, rq::launch_closest(sc->view, qp, prim, n, phit, rq::queue_counter(ctx, 0), st));
     if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
     if (p->sort_rays) {
         void* d_oct = nullptr;

@@ -52,8 +52,11 @@ struct QueryConfig {
 struct LaunchVariant {
     int32_t block, min_blocks, persistent;
 };
-constexpr int kNumLaunchVariants = 7;
+constexpr int kNumLaunchVariants = 8;
 extern const LaunchVariant kLaunchVariants[kNumLaunchVariants];
+// The one-thread-per-ray variant with the same block size and occupancy target as variant v
+// (v itself when it is not persistent).
+int non_persistent_variant(int v);
 
 // Fast-mode triangle records from the triangle and vertex buffers (rq_kernels.cu).
 cudaError_t launch_tri_fast(const int4* tris, int64_t n_tris, const float4* verts, float4* out,

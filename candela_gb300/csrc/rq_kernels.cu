@@ -74,8 +74,8 @@ __global__ void __launch_bounds__(kB, kM) k_anyhit_strict(SceneView s, const rq_
 }
 
 // Persistent strict traversal (closest or any hit): see rq_persistent.cuh.
-template <bool kAny, bool kStackless, bool kTieLower>
-__global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq_ray* __restrict__ rays,
+template <bool kAny, bool kStackless, bool kTieLower, int kM>
+__global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, const rq_ray* __restrict__ rays,
                                                            int64_t n, rq_hit* __restrict__ hits,
                                                            uint8_t* __restrict__ occ, int flags,
                                                            unsigned long long* queue,
@@ -120,6 +120,36 @@ __global__ void __launch_bounds__(128) k_persistent_strict(SceneView s, const rq
     if (counters) count_work(counters, nodes, tests);
 }
 
+// Closest-hit record of a BVH8 query: barycentrics from the hit point with the strict arithmetic
+// (TraverseBVHStack.glsl:351-363), the reference's tri-0 quirk under RQ_FLAG_REF_COMPAT.
+__device__ __forceinline__ void bvh8_finish(const SceneView& s, int flags, const strict::f3 o,
+                                            const strict::f3 d, float closest, int32_t tri,
+                                            int32_t mesh, int32_t ent, int32_t visits, rq_hit& hh) {
+    hh.t = hh.u = hh.v = hh.w = -1.0f;
+    hh.tri = hh.mesh = hh.entity = -1;
+    hh.iters = visits;
+    if (closest > 0.0f) {
+        hh.tri = tri;
+        hh.mesh = mesh;
+        hh.entity = ent;
+        const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
+        if (report) {
+            const rq_entity& E = s.ents[ent];
+            const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
+            const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
+            const int4 tr = strict::ldg4i(s.tris + tri);
+            const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
+            float u, v, w;
+            strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y), strict::vpos(s, tr.z),
+                                 u, v, w);
+            hh.t = closest;
+            hh.u = u;
+            hh.v = v;
+            hh.w = w;
+        }
+    }
+}
+
 // BVH8 traversal of one ray with the strict scene loop around it.
 template <bool kAny>
 __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, const float4 r1, int flags,
@@ -158,29 +188,7 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
         }
     }
     if (kAny) return;
-    hh.t = hh.u = hh.v = hh.w = -1.0f;
-    hh.tri = hh.mesh = hh.entity = -1;
-    hh.iters = visits;
-    if (closest > 0.0f) {
-        hh.tri = tri;
-        hh.mesh = mesh;
-        hh.entity = ent;
-        const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
-        if (report) {
-            const rq_entity& E = s.ents[ent];
-            const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
-            const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
-            const int4 tr = strict::ldg4i(s.tris + tri);
-            const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
-            float u, v, w;
-            strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y), strict::vpos(s, tr.z),
-                                 u, v, w);
-            hh.t = closest;
-            hh.u = u;
-            hh.v = v;
-            hh.w = w;
-        }
-    }
+    bvh8_finish(s, flags, o, d, closest, tri, mesh, ent, visits, hh);
 }
 
 // BVH8 traversal, one thread per ray.
@@ -206,6 +214,131 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __re
     }
     if (status) atomicOr(status_out, status);
     if (counters) count_work(counters, visits, tests);
+}
+
+// Persistent BVH8 traversal: a resident grid loops until the ray queue is empty.  Each iteration
+// visits one node per lane.  At the top of every iteration the whole warp (converged by the
+// full-mask vote) hands new rays to its idle lanes from a warp-private pool of consecutive ray
+// indices, refilled kPoolRays at a time from the global counter by one atomicAdd, so lanes stay
+// busy while the warp's longest rays finish and a warp keeps working on neighbouring rays.
+// Inactive rays are answered in the refill loop itself.  Per ray the walk, the entity loop and
+// the acceptance tests are those of k_bvh8 (same step function), so results are identical; only
+// the assignment of rays to lanes changes.  The world ray is re-read from `rays` when a later
+// entity or the final record needs it, which keeps it out of the loop's registers.
+constexpr int kPoolRays = 64;
+
+template <bool kAny, int kB, int kM>
+__global__ void __launch_bounds__(kB, kM) k_bvh8_persistent(SceneView s, const rq_ray* __restrict__ rays,
+                                                            int64_t n, rq_hit* __restrict__ hits,
+                                                            uint8_t* __restrict__ occ, int flags,
+                                                            unsigned* status_out, unsigned long long* queue,
+                                                            unsigned long long* counters) {
+    if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
+    const unsigned kFull = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    uint64_t stack[bvh8::kStack];
+    bvh8::Ray8 r;
+    bvh8::Hit8 h;
+    bvh8::Walk w;
+    float tmin = 0.0f, tmax = 0.0f, closest = -1.0f;
+    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = 0, visits = 0;
+    int64_t id = -1;
+    bool live = false, exhausted = false;
+    unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
+    int32_t tests = 0, nodes_total = 0;
+    unsigned status = 0;
+    // Starts the walk of entity `ent` or a later one that is traversed; false when none is left.
+    auto begin = [&](const float4 r0, const float4 r1) -> bool {
+        for (; ent < s.n_ents; ++ent) {
+            const rq_entity& E = s.ents[ent];
+            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f) continue;
+            const int32_t root = s.b8_roots[ent];
+            if (root < 0) continue;
+            r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
+                               strict::xform(E.inverse, strict::xyz(r1), 0.0f));
+            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : tri, -1};
+            w = bvh8::walk_begin(root);
+            return true;
+        }
+        return false;
+    };
+    auto store = [&](const float4 r0, const float4 r1, bool occluded) {
+        nodes_total += visits;
+        if (kAny) {
+            occ[id] = occluded ? 1 : 0;
+        } else {
+            rq_hit hh;
+            bvh8_finish(s, flags, strict::xyz(r0), strict::xyz(r1), closest, tri, mesh, ent_hit, visits, hh);
+            store_hit(hits, id, hh);
+        }
+    };
+    while (true) {
+        // refill idle lanes (warp-uniform loop; inactive rays are answered here)
+        while (true) {
+            const unsigned want = __ballot_sync(kFull, !live && !exhausted);
+            if (!want) break;
+            const unsigned cnt = __popc(want);
+            const unsigned rank = __popc(want & persist::lanemask_lt());
+            const unsigned long long avail = pool_end - pool_next;
+            unsigned long long mine = pool_next + rank;
+            if (avail >= cnt) {
+                pool_next += cnt;
+            } else {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
+                base = __shfl_sync(kFull, base, 0);
+                if (rank >= avail) mine = base + (rank - avail);
+                pool_next = base + (cnt - avail);
+                pool_end = base + kPoolRays;
+            }
+            if (!live && !exhausted) {
+                if (static_cast<int64_t>(mine) >= n) {
+                    exhausted = true;
+                } else {
+                    id = static_cast<int64_t>(mine);
+                    float4 r0, r1;
+                    load_ray(rays, id, r0, r1);
+                    tmin = r0.w;
+                    tmax = r1.w;
+                    closest = -1.0f;
+                    mesh = tri = ent_hit = -1;
+                    ent = 0;
+                    visits = 0;
+                    live = (r1.w > r0.w) && begin(r0, r1);
+                    if (!live) store(r0, r1, false);
+                }
+            }
+        }
+        if (!__any_sync(kFull, live)) break;
+        if (!live) continue;
+        if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
+        // the walk of entity `ent` has ended
+        visits += w.visits;
+        const float T = h.closest;
+        bool done = false;
+        if (kAny) {
+            done = T > 0.0f;
+        } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+            tmax = T;
+            closest = T;
+            mesh = h.mesh;
+            tri = h.tri;
+            ent_hit = ent;
+        }
+        float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
+        if (!done) {
+            ++ent;
+            if (ent < s.n_ents) {
+                load_ray(rays, id, r0, r1);
+                if (begin(r0, r1)) continue;
+            }
+        }
+        if (!kAny) load_ray(rays, id, r0, r1);
+        store(r0, r1, done);
+        live = false;
+    }
+    if (status) atomicOr(status_out, status);
+    if (counters) count_work(counters, nodes_total, tests);
 }
 
 // Fast-mode BVH2 traversal, one thread per ray.
@@ -330,17 +463,46 @@ int persistent_grid(K kernel, int block) {
     return g;
 }
 
-template <bool kAny, bool kStackless, bool kTieLower>
+template <bool kAny, bool kStackless, bool kTieLower, int kM>
 cudaError_t launch_persistent(const SceneView& s, const QueryConfig& q, const rq_ray* rays,
                               int64_t n, rq_hit* hits, uint8_t* occ, unsigned long long* queue,
                               cudaStream_t st) {
     const int block = 128;
-    auto k = k_persistent_strict<kAny, kStackless, kTieLower>;
+    auto k = k_persistent_strict<kAny, kStackless, kTieLower, kM>;
     const int64_t g = std::min<int64_t>(persistent_grid(k, block), (n + block - 1) / block);
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     k<<<static_cast<unsigned>(g), block, 0, st>>>(s, rays, n, hits, occ, q.flags, queue, q.counters);
     return cudaGetLastError();
+}
+
+template <bool kAny, int kM>
+cudaError_t launch_bvh8_persistent(const SceneView& s, const QueryConfig& q, const rq_ray* rays,
+                                   int64_t n, rq_hit* hits, uint8_t* occ, unsigned long long* queue,
+                                   cudaStream_t st) {
+    const int block = 128;
+    auto k = k_bvh8_persistent<kAny, 128, kM>;
+    const int64_t g = std::min<int64_t>(persistent_grid(k, block), (n + block - 1) / block);
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k<<<static_cast<unsigned>(g), block, 0, st>>>(s, rays, n, hits, occ, q.flags, q.status, queue, q.counters);
+    return cudaGetLastError();
+}
+
+// Persistent launch of variant kM (min blocks per SM) for the query's layout.
+template <bool kAny, int kM>
+cudaError_t persistent_variant(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
+                               rq_hit* hits, uint8_t* occ, unsigned long long* queue, cudaStream_t st) {
+    if (q.layout == RQ_LAYOUT_BVH8Q) return launch_bvh8_persistent<kAny, kM>(s, q, rays, n, hits, occ, queue, st);
+    const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
+    if (kAny)
+        return sl ? launch_persistent<true, true, false, kM>(s, q, rays, n, nullptr, occ, queue, st)
+                  : launch_persistent<true, false, false, kM>(s, q, rays, n, nullptr, occ, queue, st);
+    if (sl)
+        return q.tie_lower ? launch_persistent<false, true, true, kM>(s, q, rays, n, hits, nullptr, queue, st)
+                           : launch_persistent<false, true, false, kM>(s, q, rays, n, hits, nullptr, queue, st);
+    return q.tie_lower ? launch_persistent<false, false, true, kM>(s, q, rays, n, hits, nullptr, queue, st)
+                       : launch_persistent<false, false, false, kM>(s, q, rays, n, hits, nullptr, queue, st);
 }
 
 }  // namespace
@@ -388,28 +550,30 @@ cudaError_t anyhit_variant(const SceneView& s, const QueryConfig& q, const rq_ra
 }  // namespace
 
 const LaunchVariant kLaunchVariants[kNumLaunchVariants] = {
-    {128, 1, 0}, {128, 4, 0}, {128, 6, 0}, {128, 8, 0}, {256, 3, 0}, {64, 12, 0}, {128, 1, 1}};
+    {128, 1, 0}, {128, 4, 0}, {128, 6, 0}, {128, 8, 0}, {256, 3, 0}, {64, 12, 0}, {128, 1, 1}, {128, 8, 1}};
+
+int non_persistent_variant(int v) {
+    if (v < 0 || v >= kNumLaunchVariants || !kLaunchVariants[v].persistent) return v;
+    for (int k = 0; k < kNumLaunchVariants; ++k)
+        if (!kLaunchVariants[k].persistent && kLaunchVariants[k].block == kLaunchVariants[v].block &&
+            kLaunchVariants[k].min_blocks == kLaunchVariants[v].min_blocks)
+            return k;
+    return 0;
+}
 
 cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                            rq_hit* hits, unsigned long long* queue, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int v = q.variant_closest < 0 ? 0 : q.variant_closest;
-    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q || q.mode == RQ_MODE_FAST))
-        v = 0;
+    if (kLaunchVariants[v].persistent && (!queue || q.mode == RQ_MODE_FAST)) v = non_persistent_variant(v);
     switch (v) {
         case 1: return closest_variant<128, 4>(s, q, rays, n, hits, st);
         case 2: return closest_variant<128, 6>(s, q, rays, n, hits, st);
         case 3: return closest_variant<128, 8>(s, q, rays, n, hits, st);
         case 4: return closest_variant<256, 3>(s, q, rays, n, hits, st);
         case 5: return closest_variant<64, 12>(s, q, rays, n, hits, st);
-        case 6: {
-            const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
-            if (sl)
-                return q.tie_lower ? launch_persistent<false, true, true>(s, q, rays, n, hits, nullptr, queue, st)
-                                   : launch_persistent<false, true, false>(s, q, rays, n, hits, nullptr, queue, st);
-            return q.tie_lower ? launch_persistent<false, false, true>(s, q, rays, n, hits, nullptr, queue, st)
-                               : launch_persistent<false, false, false>(s, q, rays, n, hits, nullptr, queue, st);
-        }
+        case 6: return persistent_variant<false, 1>(s, q, rays, n, hits, nullptr, queue, st);
+        case 7: return persistent_variant<false, 8>(s, q, rays, n, hits, nullptr, queue, st);
         default: return closest_variant<128, 1>(s, q, rays, n, hits, st);
     }
 }
@@ -418,19 +582,15 @@ cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray
                           uint8_t* occluded, unsigned long long* queue, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int v = q.variant_any < 0 ? 0 : q.variant_any;
-    if (kLaunchVariants[v].persistent && (!queue || q.layout == RQ_LAYOUT_BVH8Q || q.mode == RQ_MODE_FAST))
-        v = 0;
+    if (kLaunchVariants[v].persistent && (!queue || q.mode == RQ_MODE_FAST)) v = non_persistent_variant(v);
     switch (v) {
         case 1: return anyhit_variant<128, 4>(s, q, rays, n, occluded, st);
         case 2: return anyhit_variant<128, 6>(s, q, rays, n, occluded, st);
         case 3: return anyhit_variant<128, 8>(s, q, rays, n, occluded, st);
         case 4: return anyhit_variant<256, 3>(s, q, rays, n, occluded, st);
         case 5: return anyhit_variant<64, 12>(s, q, rays, n, occluded, st);
-        case 6: {
-            if (q.layout == RQ_LAYOUT_BVH2_STACKLESS)
-                return launch_persistent<true, true, false>(s, q, rays, n, nullptr, occluded, queue, st);
-            return launch_persistent<true, false, false>(s, q, rays, n, nullptr, occluded, queue, st);
-        }
+        case 6: return persistent_variant<true, 1>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 7: return persistent_variant<true, 8>(s, q, rays, n, nullptr, occluded, queue, st);
         default: return anyhit_variant<128, 1>(s, q, rays, n, occluded, st);
     }
 }

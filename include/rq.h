@@ -141,7 +141,7 @@ typedef struct rq_opts {
      * query kind, else the default (128 threads, one thread per ray). */
     int32_t block_size;
     int32_t min_blocks;  /* minimum resident blocks per SM the kernel was compiled for */
-    int32_t persistent;  /* 1 = persistent ray-queue kernel (BVH2 layouts only) */
+    int32_t persistent;  /* 1 = persistent ray-queue kernel (strict mode, every layout) */
     int32_t reserved;
 } rq_opts;
 

@@ -96,3 +96,28 @@ def test_rtao_frame(ctx):
     occ = osc.anyhit(ao)
     vis = np.where(ao["tmax"] > 0, 1.0 - occ, 0.0).astype(np.float32)
     np.testing.assert_array_equal(got[:, 3], vis)
+
+
+@pytest.mark.parametrize("query", [0, 1])
+def test_gi_frame_forms_identical(ctx, query):
+    """The GI/RTAO frame gives the same pixels bit for bit on every traversal form: strict BVH2,
+    BVH8q one thread per ray, BVH8q persistent ray queue, with and without octant binning."""
+    from candela_gb300 import _lib as L
+    bufs = single_object("hf64", R.STACK)
+    rays = rays_to_device(S.camera_rays(192, 160, **S.C1_CAMERA))
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(np.array([[0.7, 0.6, 0.5]], dtype=np.float32))
+    sc.build_bvh8()
+    kw = dict(spp=3, seed=11, origin_offset=1e-3, shadow_rays=True, shadow_offset=1e-3)
+    if query == 1:
+        kw = dict(spp=2, seed=11, origin_offset=1e-3, ray_tmax=0.25, query=1)
+    want, st = sc.gi_frame(rays, gi_params(**kw), stats=True)
+    want = want.cpu().numpy()
+    assert st["secondary_rays"] > 1000
+    for sort in (False, True):
+        p = gi_params(sort_rays=sort, **kw)
+        for launch in (dict(block_size=128, min_blocks=8), dict(block_size=128, min_blocks=8, persistent=1),
+                       dict(block_size=128, min_blocks=1, persistent=1)):
+            got = sc.gi_frame(rays, p, layout=L.LAYOUT_BVH8Q, **launch).cpu().numpy()
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (sort, launch)
+    assert ctx.device_status() == 0

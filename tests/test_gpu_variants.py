@@ -11,7 +11,8 @@ from .helpers import hits_from_device, rays_to_device, single_object
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = [(128, 1, 0), (128, 4, 0), (128, 6, 0), (128, 8, 0), (256, 3, 0), (64, 12, 0), (128, 1, 1)]
+VARIANTS = [(128, 1, 0), (128, 4, 0), (128, 6, 0), (128, 8, 0), (256, 3, 0), (64, 12, 0), (128, 1, 1),
+            (128, 8, 1)]
 
 
 @pytest.mark.parametrize("layout", [R.STACK, R.STACKLESS, L.LAYOUT_BVH8Q])
@@ -24,8 +25,6 @@ def test_all_variants_identical(ctx, layout):
     ref_h = sc.closest(rays, layout=layout, block_size=128, min_blocks=1).cpu().numpy()
     ref_o = sc.anyhit(rays, layout=layout, block_size=128, min_blocks=1).cpu().numpy()
     for b, m, p in VARIANTS:
-        if p and layout == L.LAYOUT_BVH8Q:
-            continue
         h = sc.closest(rays, layout=layout, block_size=b, min_blocks=m, persistent=p).cpu().numpy()
         assert np.array_equal(h.view(np.uint32), ref_h.view(np.uint32)), (b, m, p)
         o = sc.anyhit(rays, layout=layout, block_size=b, min_blocks=m, persistent=p).cpu().numpy()
@@ -42,9 +41,9 @@ def test_autotune_records_choice(ctx):
     res = sc.autotune(rays, query=0, layout=L.LAYOUT_BVH8Q)
     assert 0 <= res["variant"] < len(VARIANTS)
     timed = [v["ms"] for v in res["variants"] if v["ms"] >= 0]
-    assert len(timed) == 6 and min(timed) > 0
+    assert len(timed) == len(VARIANTS) and min(timed) > 0
     after = sc.closest(rays, layout=L.LAYOUT_BVH8Q).cpu().numpy()   # uses the tuned variant
     assert np.array_equal(before.view(np.uint32), after.view(np.uint32))
     res2 = sc.autotune(rays, query=1, layout=R.STACK)
-    assert res2["variants"][6]["ms"] > 0  # the persistent form is timed for BVH2
+    assert res2["variants"][6]["ms"] > 0 and res2["variants"][7]["ms"] > 0  # persistent forms timed
     assert ctx.device_status() == 0
