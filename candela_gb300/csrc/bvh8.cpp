@@ -2,8 +2,12 @@
 // Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
 // HPG 2017), built from the reference's flattened BVH2 buffers.
 //
-// Collapse: each BVH8 node starts from a BVH2 internal node's two children and repeatedly opens the
-// internal child with the largest surface area until it holds 8 children or only leaves remain.
+// Collapse: the SAH-optimal assignment of that paper.  A bottom-up dynamic programme over the
+// BVH2 gives, for every node n and slot budget i = 1..8, the cheapest way to place n's subtree in
+// at most i child slots of one BVH8 node: as one leaf child (all triangles of the subtree, at most
+// kLeafMax, or a BVH2 leaf as given), as one internal child (a new BVH8 node whose 8 slots hold n's
+// subtree), or split between its two BVH2 children.  Cost = surface area x (kNodeCost for a node
+// visit, kTriCost per triangle test).  A top-down pass then emits the chosen BVH8.
 // Quantisation: per node, a grid origin p (the node's min corner) and a power-of-two step per
 // axis; child boxes are rounded outward (floor / ceil) and then checked in double precision so that
 // every decoded child box contains the child's FP32 box.
@@ -14,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <limits>
 #include <unordered_map>
 
 namespace rq {
@@ -156,6 +161,124 @@ bool recover_tree(int32_t layout, const float* nodes, int32_t off, int32_t cnt, 
     return true;
 }
 
+constexpr float kNodeCost = 1.0f;  // one BVH8 node visit (eight child box tests)
+constexpr float kTriCost = 0.3f;   // one triangle test, relative to a node visit
+constexpr int kLeafMax = 3;        // triangles merged into one leaf child
+
+// Dynamic-programme tables of one BVH2 tree (index = temp node).
+struct Collapse {
+    std::vector<float> cost;     // cost[8n + i - 1] = C(n, i)
+    std::vector<int8_t> split;   // split[8n + i - 1] = k of the best split of n into i slots
+    std::vector<uint16_t> flag;  // bit 0: C(n, 1) is a leaf child; bit i-1 (i >= 2): C(n, i) = C(n, i-1)
+    std::vector<int32_t> ntris;  // triangles below n
+};
+
+void collapse_costs(const std::vector<TNode>& T, Collapse& D) {
+    const size_t n = T.size();
+    D.cost.assign(8 * n, 0.0f);
+    D.split.assign(8 * n, 0);
+    D.flag.assign(n, 0);
+    D.ntris.assign(n, 0);
+    const float inf = std::numeric_limits<float>::infinity();
+    // children have larger temp indices than their parent (both recoveries append them later)
+    for (size_t j = n; j-- > 0;) {
+        const TNode& t = T[j];
+        const float area = std::max(half_area(t), 0.0f);
+        float* c = &D.cost[8 * j];
+        if (t.leaf) {
+            D.ntris[j] = t.tri_count;
+            for (int i = 0; i < 8; ++i) c[i] = area * kTriCost * static_cast<float>(t.tri_count);
+            D.flag[j] = 1;
+            continue;
+        }
+        D.ntris[j] = D.ntris[t.a] + D.ntris[t.b];
+        const float* ca = &D.cost[8 * static_cast<size_t>(t.a)];
+        const float* cb = &D.cost[8 * static_cast<size_t>(t.b)];
+        float dist[9];
+        for (int i = 2; i <= 8; ++i) {
+            float best = inf;
+            int bk = 1;
+            for (int k = 1; k < i; ++k) {
+                const float v = ca[k - 1] + cb[i - k - 1];
+                if (v < best) {
+                    best = v;
+                    bk = k;
+                }
+            }
+            dist[i] = best;
+            D.split[8 * j + i - 1] = static_cast<int8_t>(bk);
+        }
+        const float internal = area * kNodeCost + dist[8];
+        const float leaf = D.ntris[j] <= kLeafMax ? area * kTriCost * static_cast<float>(D.ntris[j]) : inf;
+        uint16_t f = 0;
+        if (leaf <= internal) {
+            c[0] = leaf;
+            f |= 1;
+        } else {
+            c[0] = internal;
+        }
+        for (int i = 2; i <= 8; ++i) {
+            if (c[i - 2] <= dist[i]) {
+                c[i - 1] = c[i - 2];
+                f |= static_cast<uint16_t>(1u << (i - 1));
+            } else {
+                c[i - 1] = dist[i];
+            }
+        }
+        D.flag[j] = f;
+    }
+}
+
+struct Slot {
+    int32_t tnode;
+    bool leaf;
+};
+
+// The child slots that subtree x takes with a budget of i slots.
+void collect(const std::vector<TNode>& T, const Collapse& D, int32_t x, int i, std::vector<Slot>& out) {
+    while (true) {
+        if (T[x].leaf) {
+            out.push_back({x, true});
+            return;
+        }
+        if (i == 1) {
+            out.push_back({x, (D.flag[x] & 1u) != 0});
+            return;
+        }
+        if (D.flag[x] & (1u << (i - 1))) {
+            --i;
+            continue;
+        }
+        const int k = D.split[8 * static_cast<size_t>(x) + i - 1];
+        collect(T, D, T[x].a, k, out);
+        x = T[x].b;
+        i -= k;
+    }
+}
+
+// The eight-slot children of internal node x (its BVH8 node).
+void node_slots(const std::vector<TNode>& T, const Collapse& D, int32_t x, std::vector<Slot>& out) {
+    out.clear();
+    const int k = D.split[8 * static_cast<size_t>(x) + 7];
+    collect(T, D, T[x].a, k, out);
+    collect(T, D, T[x].b, 8 - k, out);
+}
+
+// Triangles of the subtree x in BVH2 leaf order (left before right).
+void subtree_tris(const std::vector<TNode>& T, int32_t x, std::vector<int32_t>& out) {
+    std::vector<int32_t> st{x};
+    while (!st.empty()) {
+        const int32_t y = st.back();
+        st.pop_back();
+        if (T[y].leaf) {
+            for (int32_t i = 0; i < T[y].tri_count; ++i) out.push_back(T[y].tri_start + i);
+        } else {
+            st.push_back(T[y].b);
+            st.push_back(T[y].a);
+        }
+    }
+}
+
 // Greedy octant slot assignment: slot bit i set = child centroid toward +axis i.
 void assign_slots(const std::vector<TNode>& T, const std::vector<int32_t>& kids, const float* lo,
                   const float* hi, int32_t slot_of[8]) {
@@ -215,6 +338,9 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
     out = Bvh8Out{};
     std::unordered_map<int64_t, int32_t> done;
     std::vector<TNode> T;
+    Collapse D;
+    std::vector<Slot> slots;
+    std::vector<int32_t> leaf_tris;
     for (const Bvh8Range& r : ranges) {
         const int64_t key = (static_cast<int64_t>(r.node_offset) << 32) | uint32_t(r.node_count);
         auto it = done.find(key);
@@ -231,6 +357,7 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
         const int32_t root = static_cast<int32_t>(out.nodes.size() / kBvh8NodeWords);
         done[key] = root;
         out.roots.push_back(root);
+        collapse_costs(T, D);
         // BFS emission: internal children of a node get consecutive node indices.
         std::deque<std::pair<int32_t, int32_t>> q;  // (temp node, bvh8 index)
         out.nodes.resize(out.nodes.size() + kBvh8NodeWords, 0u);
@@ -238,25 +365,13 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
         while (!q.empty()) {
             const auto [tn, me] = q.front();
             q.pop_front();
-            std::vector<int32_t> kids;
             if (T[tn].leaf) {
-                kids.push_back(tn);  // single-leaf object
+                slots.assign(1, Slot{tn, true});  // single-leaf object
             } else {
-                kids = {T[tn].a, T[tn].b};
-                while (kids.size() < 8) {
-                    int best = -1;
-                    float best_area = -1.0f;
-                    for (size_t i = 0; i < kids.size(); ++i)
-                        if (!T[kids[i]].leaf && half_area(T[kids[i]]) > best_area) {
-                            best_area = half_area(T[kids[i]]);
-                            best = static_cast<int>(i);
-                        }
-                    if (best < 0) break;
-                    const int32_t x = kids[best];
-                    kids[best] = T[x].a;
-                    kids.push_back(T[x].b);
-                }
+                node_slots(T, D, tn, slots);
             }
+            std::vector<int32_t> kids;
+            for (const Slot& sl : slots) kids.push_back(sl.tnode);
             float lo[3], hi[3];
             for (int a = 0; a < 3; ++a) {
                 lo[a] = T[kids[0]].lo[a];
@@ -269,8 +384,12 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
             int32_t slot_of[8];
             assign_slots(T, kids, lo, hi, slot_of);
             int32_t child_at[8];
+            bool leaf_at[8] = {};
             for (int s = 0; s < 8; ++s) child_at[s] = -1;
-            for (size_t i = 0; i < kids.size(); ++i) child_at[slot_of[i]] = kids[i];
+            for (size_t i = 0; i < kids.size(); ++i) {
+                child_at[slot_of[i]] = kids[i];
+                leaf_at[slot_of[i]] = slots[i].leaf;
+            }
 
             uint32_t* nd = out.nodes.data() + static_cast<int64_t>(me) * kBvh8NodeWords;
             uint8_t qb[48];
@@ -323,19 +442,21 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
                     qb[24 + a * 8 + s] = static_cast<uint8_t>(qh);
                 }
                 if (c < 0) continue;
-                if (!T[c].leaf) {
+                if (!leaf_at[s]) {
                     imask |= 1u << s;
                     new_internal.push_back(c);
                     ++n_int;
                 } else {
-                    if (tri_off + T[c].tri_count > 32) {
+                    leaf_tris.clear();
+                    subtree_tris(T, c, leaf_tris);
+                    const int32_t cnt = static_cast<int32_t>(leaf_tris.size());
+                    if (tri_off + cnt > 32 || cnt > 7) {
                         why = "more than 32 triangles under one BVH8 node";
                         return false;
                     }
-                    if (T[c].tri_count > 0)
-                        meta[s] = static_cast<uint8_t>((T[c].tri_count << 5) | tri_off);
-                    for (int32_t i = 0; i < T[c].tri_count; ++i) {
-                        const int32_t t = T[c].tri_start + i;
+                    if (cnt > 0) meta[s] = static_cast<uint8_t>((cnt << 5) | tri_off);
+                    for (int32_t i = 0; i < cnt; ++i) {
+                        const int32_t t = leaf_tris[i];
                         const int32_t* tr = tris + static_cast<int64_t>(t) * 4;
                         for (int k = 0; k < 3; ++k)
                             if (tr[k] < 0 || tr[k] >= n_verts) {
@@ -356,7 +477,7 @@ bool build_bvh8(int32_t layout, const float* nodes, int64_t n_nodes, const int32
                                                nx, ny, nz, 0.0f};
                         out.tris.insert(out.tris.end(), rec, rec + 16);
                     }
-                    tri_off += T[c].tri_count;
+                    tri_off += cnt;
                 }
             }
             nd[3] = e_byte[0] | (e_byte[1] << 8) | (e_byte[2] << 16) | (imask << 24);
