@@ -617,7 +617,9 @@ def main():
             tuning[f"{lname}_{qname}"] = sc.autotune(d_sec, query=qk, layout=lay)
     _, st = sc.gi_frame(d_rays, p, out=d_pix, layout=B8, stats=True, stream=sptr)
     rays_per_step = st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
-    launches_per_step = 5 + (2 if wl["params"].get("shadow_rays") else 0)
+    # primary traversal, ray generation, secondary traversal, shading + accumulation
+    # (+ shadow ray generation and the shadow any-hit launch)
+    launches_per_step = 4 + (2 if wl["params"].get("shadow_rays") else 0)
 
     def timed_steps(layout, steps, warmup):
         for _ in range(warmup):
@@ -647,6 +649,8 @@ def main():
     p_plain = p
     p = gi_params(**wl["params"], sort_rays=True)
     sorted_ms = timed_steps(B8, args.steps, 1)
+    p = gi_params(**wl["params"], unfused=True)
+    unfused_ms = timed_steps(B8, args.steps, 1)
     p = p_plain
     plain_value = rays_per_step * args.steps / (plain_ms / 1e3) / 1e6
 
@@ -779,6 +783,9 @@ def main():
                        "parallelism": f"{world} independent replica(s)" if world > 1 else "1 GPU",
                        "bvh_build_s": round(wl["build_s"], 3),
                        "bvh8_build": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
+            "bvh8q_pass_unfused": {
+                "value": round(rays_per_step * args.steps / (unfused_ms / 1e3) / 1e6, 2),
+                "ms_per_step": round(unfused_ms / args.steps, 4)},
             "bvh8q_pass_with_octant_binning": {
                 "value": round(rays_per_step * args.steps / (sorted_ms / 1e3) / 1e6, 2),
                 "ms_per_step": round(sorted_ms / args.steps, 4)},

@@ -84,7 +84,8 @@ class RqGiParams(C.Structure):
                 ("ray_tmax", C.c_float), ("normal_mode", C.c_int32), ("query", C.c_int32),
                 ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
                 ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3),
-                ("sky_color", C.c_float * 3), ("sort_rays", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("sky_color", C.c_float * 3), ("sort_rays", C.c_int32), ("unfused", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class RqFrameStats(C.Structure):

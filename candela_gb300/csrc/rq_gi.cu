@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "rq_gi.cuh"
+#include "rq_persistent.cuh"
 #include "rq_objects.h"
 
 namespace rq {
@@ -267,6 +268,61 @@ __global__ void __launch_bounds__(256) k_gi_raygen_compact(
     }
 }
 
+// Per-pixel form of k_gi_raygen_compact: one thread per primary ray i computes the hit point and
+// faced normal once and writes the spp secondary rays of slots j = i*spp + k.  Compaction is
+// block-aggregated and pixel-major within the block, the order k_gi_raygen_compact gives, with the
+// same slot maps; every value is computed with the same functions.
+__global__ void __launch_bounds__(256) k_gi_raygen_pixel(
+    SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
+    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of,
+    unsigned long long* count) {
+    __shared__ unsigned warp_hits[8];
+    __shared__ unsigned long long block_base;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    float4 h0 = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
+    int4 h1 = make_int4(-1, -1, -1, 0);
+    if (i < n) get_hit(hits, i, h0, h1);
+    const bool hit = i < n && h0.x > 0.0f;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+    if (lane == 0) warp_hits[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (unsigned w = 0; w < blockDim.x / 32; ++w) {
+            const unsigned c = warp_hits[w];
+            warp_hits[w] = tot;
+            tot += c;
+        }
+        block_base = tot ? atomicAdd(count, static_cast<unsigned long long>(tot) * a.spp) : 0ull;
+    }
+    __syncthreads();
+    if (i >= n) return;
+    if (!hit) {
+        for (int k = 0; k < a.spp; ++k) comp_of[i * a.spp + k] = -1;
+        return;
+    }
+    const int64_t c0 = static_cast<int64_t>(block_base) +
+                       static_cast<int64_t>(warp_hits[warp] + __popc(m & persist::lanemask_lt())) * a.spp;
+    const float4* pr = reinterpret_cast<const float4*>(prim) + 2 * i;
+    const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+    const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+    const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    const f3 org = strict::add(P, strict::muls(N, a.origin_offset));
+    for (int k = 0; k < a.spp; ++k) {
+        const int64_t j = i * a.spp + k;
+        const uint32_t rid = static_cast<uint32_t>(j);
+        const float u0 = gi::u01(gi::sample_key(a.seed, rid, 0u));
+        const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
+        const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
+        put_ray(out, c0 + k, org, 0.0f, dir, a.ray_tmax);
+        slot_of[c0 + k] = static_cast<int32_t>(j);
+        comp_of[j] = static_cast<int32_t>(c0 + k);
+    }
+}
+
 // Shadow rays for the first *count compact secondary hits.
 __global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
                                   const rq_hit* __restrict__ hits, int64_t n_max, GiArgs a,
@@ -299,6 +355,26 @@ __global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
     }
 }
 
+// Radiance and AO of one secondary hit (GetDirect, DiffuseTrace.glsl:368-372; emissive :491;
+// AO :494): h0 = (t, u, v, w), h1 = (tri, mesh, entity), rd the ray direction, l the sun's
+// visibility.  A miss returns the sky.
+__device__ __forceinline__ float4 shade_one(const SceneView& s, const float* __restrict__ albedo,
+                                            int32_t n_albedo, const GiArgs& a, const f3 rd,
+                                            const float4 h0, const int4 h1, float l) {
+    if (!(h0.x > 0.0f)) return make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    f3 alb{0.8f, 0.8f, 0.8f};
+    if (h1.y >= 0 && h1.y < n_albedo)
+        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
+    const float em = __int_as_float(s.ents[h1.z].data[0]);
+    const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
+    const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
+    const f3 rad = strict::add(direct, strict::muls(alb, em));
+    const float ao = powf(strict::gmin(strict::gmax(__fdiv_rn(h0.x, 2.4f), 0.0f), 1.0f), 1.23f);
+    return make_float4(rad.x, rad.y, rad.z, ao);
+}
+
 // Shading per slot from compact rays / hits / visibility (comp_of[j] < 0: inactive slot).
 __global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                           const int32_t* __restrict__ comp_of, int64_t m,
@@ -318,24 +394,46 @@ __global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq
     float4 h0;
     int4 h1;
     get_hit(hits, c, h0, h1);
-    if (!(h0.x > 0.0f)) {
-        out[j] = make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
-        return;
-    }
     const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * static_cast<int64_t>(c);
     const f3 rd = strict::xyz(__ldg(pr + 1));
-    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
-    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-    f3 alb{0.8f, 0.8f, 0.8f};
-    if (h1.y >= 0 && h1.y < n_albedo)
-        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
-    const float em = __int_as_float(s.ents[h1.z].data[0]);
     const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-    const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
-    const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
-    const f3 rad = strict::add(direct, strict::muls(alb, em));
-    const float ao = powf(strict::gmin(strict::gmax(__fdiv_rn(h0.x, 2.4f), 0.0f), 1.0f), 1.23f);
-    out[j] = make_float4(rad.x, rad.y, rad.z, ao);
+    out[j] = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+}
+
+// k_shade_c and k_accumulate in one pass, one thread per pixel: the spp samples are shaded with
+// shade_one and summed in sample order, so the pixel is bit-identical to the two-kernel form.
+__global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
+                                   const rq_hit* __restrict__ hits, const int32_t* __restrict__ comp_of,
+                                   int64_t n, const uint8_t* __restrict__ occl, int query,
+                                   const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                                   float4* __restrict__ pixels) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < a.spp; ++k) {
+        const int32_t c = __ldg(comp_of + i * a.spp + k);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (c >= 0) {
+            if (query == 1) {
+                v.w = occl[c] ? 0.0f : 1.0f;
+            } else {
+                float4 h0;
+                int4 h1;
+                get_hit(hits, c, h0, h1);
+                const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * static_cast<int64_t>(c);
+                const f3 rd = strict::xyz(__ldg(pr + 1));
+                const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
+                v = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+            }
+        }
+        acc.x = __fadd_rn(acc.x, v.x);
+        acc.y = __fadd_rn(acc.y, v.y);
+        acc.z = __fadd_rn(acc.z, v.z);
+        acc.w = __fadd_rn(acc.w, v.w);
+    }
+    const float inv = __fdiv_rn(1.0f, static_cast<float>(a.spp));
+    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                            __fmul_rn(acc.w, inv));
 }
 
 __global__ void k_count_hits_c(const rq_hit* __restrict__ hits, int64_t n_max,
@@ -372,24 +470,9 @@ __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_h
     float4 h0;
     int4 h1;
     get_hit(hits, j, h0, h1);
-    if (!(h0.x > 0.0f)) {
-        out[j] = make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
-        return;
-    }
-    const f3 rd = strict::xyz(r1);
-    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
-    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-    f3 alb{0.8f, 0.8f, 0.8f};
-    if (h1.y >= 0 && h1.y < n_albedo)
-        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
-    const float em = __int_as_float(s.ents[h1.z].data[0]);
     // lit[j] = 1 means the sun is visible; an occlusion buffer (1 = blocked) is read inverted.
     const float l = lit ? ((lit[j] != 0) != (lit_is_occlusion != 0) ? 1.0f : 0.0f) : 1.0f;
-    const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
-    const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
-    const f3 rad = strict::add(direct, strict::muls(alb, em));
-    const float ao = powf(strict::gmin(strict::gmax(__fdiv_rn(h0.x, 2.4f), 0.0f), 1.0f), 1.23f);
-    out[j] = make_float4(rad.x, rad.y, rad.z, ao);
+    out[j] = shade_one(s, albedo, n_albedo, a, strict::xyz(r1), h0, h1, l);
 }
 
 // AO query: visibility 1 - occluded for active rays, 0 for inactive ones.
@@ -428,12 +511,6 @@ __global__ void k_count_hits(const rq_hit* __restrict__ hits, int64_t n, unsigne
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
 }
 
-__global__ void k_count_bytes(const uint8_t* __restrict__ b, int64_t n, unsigned long long* cnt) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const bool h = i < n && b[i] != 0;
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
-    if ((threadIdx.x & 31) == 0 && m) atomicAdd(cnt, static_cast<unsigned long long>(__popc(m)));
-}
 
 inline unsigned grid(int64_t n, int b) { return static_cast<unsigned>((n + b - 1) / b); }
 
@@ -571,7 +648,6 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
         (s = rq::scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
         (s = rq::scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
         (s = rq::scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
-        (s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK ||
         (s = rq::scratch(ctx, 10, 4 * m, &d_slot)) != RQ_OK ||
         (s = rq::scratch(ctx, 11, 4 * m, &d_comp)) != RQ_OK)
         return s;
@@ -594,7 +670,6 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     rq_ray* sec = static_cast<rq_ray*>(d_sec);
     rq_hit* shit = static_cast<rq_hit*>(d_shit);
     uint8_t* occ = static_cast<uint8_t*>(d_occ);
-    float4* shade = static_cast<float4*>(d_shade);
     int32_t* slot_of = static_cast<int32_t*>(d_slot);
     int32_t* comp_of = static_cast<int32_t*>(d_comp);
     // Camera rays are coherent and short (a few node visits): the one-thread-per-ray form of the
@@ -611,9 +686,12 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
         rq::k_gi_octant_count<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts);
         rq::k_gi_octant_scatter<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts,
                                                                   counts + 8, sec, slot_of, comp_of, count);
-    } else {
+    } else if (p->unfused) {
         rq::k_gi_raygen_compact<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
                                                                   slot_of, comp_of, count);
+    } else {
+        rq::k_gi_raygen_pixel<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
+                                                                slot_of, comp_of, count);
     }
     RQ_CUDA(ctx, cudaGetLastError());
     rq::SceneView cv = sc->view;  // secondary launches cover only the compact prefix
@@ -637,9 +715,17 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
             vis = occ;
         }
     }
-    rq::k_shade_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p->query,
-                                                    sc->d_albedo, sc->n_albedo, a, shade);
-    rq::k_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(shade, n, p->spp, static_cast<float4*>(d_pix));
+    if (p->unfused) {  // per-sample shading into a scratch buffer, then the per-pixel mean
+        if ((s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
+        float4* shade = static_cast<float4*>(d_shade);
+        rq::k_shade_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p->query,
+                                                        sc->d_albedo, sc->n_albedo, a, shade);
+        rq::k_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(shade, n, p->spp, static_cast<float4*>(d_pix));
+    } else {
+        rq::k_shade_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, n, vis, p->query,
+                                                                 sc->d_albedo, sc->n_albedo, a,
+                                                                 static_cast<float4*>(d_pix));
+    }
     RQ_CUDA(ctx, cudaGetLastError());
     if (host) {
         RQ_CUDA(ctx, cudaMemcpyAsync(pixels4, d_pix, 16 * n, cudaMemcpyDeviceToHost, st));

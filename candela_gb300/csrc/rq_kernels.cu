@@ -8,25 +8,13 @@
 
 #include "rq_internal.h"
 #include "rq_bvh8.cuh"
+#include "rq_bvh8_walk.cuh"
 #include "rq_fast.cuh"
 #include "rq_persistent.cuh"
 #include "rq_strict.cuh"
 
 namespace rq {
 namespace {
-
-__device__ __forceinline__ void load_ray(const rq_ray* rays, int64_t i, float4& r0, float4& r1) {
-    const float4* p = reinterpret_cast<const float4*>(rays) + 2 * i;
-    r0 = __ldg(p);
-    r1 = __ldg(p + 1);
-}
-
-__device__ __forceinline__ void store_hit(rq_hit* hits, int64_t i, const rq_hit& h) {
-    float4* p = reinterpret_cast<float4*>(hits) + 2 * i;
-    p[0] = make_float4(h.t, h.u, h.v, h.w);
-    p[1] = make_float4(__int_as_float(h.tri), __int_as_float(h.mesh), __int_as_float(h.entity),
-                       __int_as_float(h.iters));
-}
 
 // Warp-aggregated work counters: counters[0] += node visits, counters[1] += triangle tests.
 __device__ __forceinline__ void count_work(unsigned long long* counters, int32_t nodes,
@@ -120,77 +108,6 @@ __global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, cons
     if (counters) count_work(counters, nodes, tests);
 }
 
-// Closest-hit record of a BVH8 query: barycentrics from the hit point with the strict arithmetic
-// (TraverseBVHStack.glsl:351-363), the reference's tri-0 quirk under RQ_FLAG_REF_COMPAT.
-__device__ __forceinline__ void bvh8_finish(const SceneView& s, int flags, const strict::f3 o,
-                                            const strict::f3 d, float closest, int32_t tri,
-                                            int32_t mesh, int32_t ent, int32_t visits, rq_hit& hh) {
-    hh.t = hh.u = hh.v = hh.w = -1.0f;
-    hh.tri = hh.mesh = hh.entity = -1;
-    hh.iters = visits;
-    if (closest > 0.0f) {
-        hh.tri = tri;
-        hh.mesh = mesh;
-        hh.entity = ent;
-        const bool report = (flags & RQ_FLAG_REF_COMPAT) ? tri > 0 : tri >= 0;
-        if (report) {
-            const rq_entity& E = s.ents[ent];
-            const strict::f3 ro = strict::xform(E.inverse, o, 1.0f);
-            const strict::f3 rd = strict::xform(E.inverse, d, 0.0f);
-            const int4 tr = strict::ldg4i(s.tris + tri);
-            const strict::f3 p = strict::add(ro, strict::muls(rd, closest));
-            float u, v, w;
-            strict::barycentrics(p, strict::vpos(s, tr.x), strict::vpos(s, tr.y), strict::vpos(s, tr.z),
-                                 u, v, w);
-            hh.t = closest;
-            hh.u = u;
-            hh.v = v;
-            hh.w = w;
-        }
-    }
-}
-
-// BVH8 traversal of one ray with the strict scene loop around it.
-template <bool kAny>
-__device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, const float4 r1, int flags,
-                                         rq_hit& hh, bool& occluded, int32_t& visits,
-                                         int32_t& tests, unsigned& status) {
-    const float rtmin = r0.w, rtmax = r1.w;
-    const strict::f3 o = strict::xyz(r0), d = strict::xyz(r1);
-    float tmax = rtmax, closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent = -1;
-    occluded = false;
-    if (rtmax > rtmin) {
-        for (int e = 0; e < s.n_ents; ++e) {
-            const rq_entity& E = s.ents[e];
-            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f)
-                continue;
-            const int32_t root = s.b8_roots[e];
-            if (root < 0) continue;
-            const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
-                                                strict::xform(E.inverse, d, 0.0f));
-            bvh8::Hit8 h{kAny ? rtmax : tmax, -1.0f, kAny ? -1 : tri, -1};
-            visits += bvh8::traverse<kAny, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests,
-                                                 status);
-            const float T = h.closest;
-            if (kAny) {
-                if (T > 0.0f) {
-                    occluded = true;
-                    break;
-                }
-            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
-                tmax = T;
-                closest = T;
-                mesh = h.mesh;
-                tri = h.tri;
-                ent = e;
-            }
-        }
-    }
-    if (kAny) return;
-    bvh8_finish(s, flags, o, d, closest, tri, mesh, ent, visits, hh);
-}
-
 // BVH8 traversal, one thread per ray.
 template <bool kAny, int kB, int kM>
 __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
@@ -216,17 +133,8 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __re
     if (counters) count_work(counters, visits, tests);
 }
 
-// Persistent BVH8 traversal: a resident grid loops until the ray queue is empty.  Each iteration
-// visits one node per lane.  At the top of every iteration the whole warp (converged by the
-// full-mask vote) hands new rays to its idle lanes from a warp-private pool of consecutive ray
-// indices, refilled kPoolRays at a time from the global counter by one atomicAdd, so lanes stay
-// busy while the warp's longest rays finish and a warp keeps working on neighbouring rays.
-// Inactive rays are answered in the refill loop itself.  Per ray the walk, the entity loop and
-// the acceptance tests are those of k_bvh8 (same step function), so results are identical; only
-// the assignment of rays to lanes changes.  The world ray is re-read from `rays` when a later
-// entity or the final record needs it, which keeps it out of the loop's registers.
-constexpr int kPoolRays = 64;
-
+// Persistent BVH8 traversal (bvh8_persistent_loop in rq_bvh8_walk.cuh), results as hit records
+// or occlusion bytes.
 template <bool kAny, int kB, int kM>
 __global__ void __launch_bounds__(kB, kM) k_bvh8_persistent(SceneView s, const rq_ray* __restrict__ rays,
                                                             int64_t n, rq_hit* __restrict__ hits,
@@ -234,109 +142,10 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8_persistent(SceneView s, const r
                                                             unsigned* status_out, unsigned long long* queue,
                                                             unsigned long long* counters) {
     if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
-    const unsigned kFull = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    uint64_t stack[bvh8::kStack];
-    bvh8::Ray8 r;
-    bvh8::Hit8 h;
-    bvh8::Walk w;
-    float tmin = 0.0f, tmax = 0.0f, closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = 0, visits = 0;
-    int64_t id = -1;
-    bool live = false, exhausted = false;
-    unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
     int32_t tests = 0, nodes_total = 0;
     unsigned status = 0;
-    // Starts the walk of entity `ent` or a later one that is traversed; false when none is left.
-    auto begin = [&](const float4 r0, const float4 r1) -> bool {
-        for (; ent < s.n_ents; ++ent) {
-            const rq_entity& E = s.ents[ent];
-            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f) continue;
-            const int32_t root = s.b8_roots[ent];
-            if (root < 0) continue;
-            r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
-                               strict::xform(E.inverse, strict::xyz(r1), 0.0f));
-            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : tri, -1};
-            w = bvh8::walk_begin(root);
-            return true;
-        }
-        return false;
-    };
-    auto store = [&](const float4 r0, const float4 r1, bool occluded) {
-        nodes_total += visits;
-        if (kAny) {
-            occ[id] = occluded ? 1 : 0;
-        } else {
-            rq_hit hh;
-            bvh8_finish(s, flags, strict::xyz(r0), strict::xyz(r1), closest, tri, mesh, ent_hit, visits, hh);
-            store_hit(hits, id, hh);
-        }
-    };
-    while (true) {
-        // refill idle lanes (warp-uniform loop; inactive rays are answered here)
-        while (true) {
-            const unsigned want = __ballot_sync(kFull, !live && !exhausted);
-            if (!want) break;
-            const unsigned cnt = __popc(want);
-            const unsigned rank = __popc(want & persist::lanemask_lt());
-            const unsigned long long avail = pool_end - pool_next;
-            unsigned long long mine = pool_next + rank;
-            if (avail >= cnt) {
-                pool_next += cnt;
-            } else {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
-                base = __shfl_sync(kFull, base, 0);
-                if (rank >= avail) mine = base + (rank - avail);
-                pool_next = base + (cnt - avail);
-                pool_end = base + kPoolRays;
-            }
-            if (!live && !exhausted) {
-                if (static_cast<int64_t>(mine) >= n) {
-                    exhausted = true;
-                } else {
-                    id = static_cast<int64_t>(mine);
-                    float4 r0, r1;
-                    load_ray(rays, id, r0, r1);
-                    tmin = r0.w;
-                    tmax = r1.w;
-                    closest = -1.0f;
-                    mesh = tri = ent_hit = -1;
-                    ent = 0;
-                    visits = 0;
-                    live = (r1.w > r0.w) && begin(r0, r1);
-                    if (!live) store(r0, r1, false);
-                }
-            }
-        }
-        if (!__any_sync(kFull, live)) break;
-        if (!live) continue;
-        if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
-        // the walk of entity `ent` has ended
-        visits += w.visits;
-        const float T = h.closest;
-        bool done = false;
-        if (kAny) {
-            done = T > 0.0f;
-        } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
-            tmax = T;
-            closest = T;
-            mesh = h.mesh;
-            tri = h.tri;
-            ent_hit = ent;
-        }
-        float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
-        if (!done) {
-            ++ent;
-            if (ent < s.n_ents) {
-                load_ray(rays, id, r0, r1);
-                if (begin(r0, r1)) continue;
-            }
-        }
-        if (!kAny) load_ray(rays, id, r0, r1);
-        store(r0, r1, done);
-        live = false;
-    }
+    const QuerySink sink{s, flags, hits, occ};
+    bvh8_persistent_loop<kAny>(s, rays, n, flags, queue, sink, tests, nodes_total, status);
     if (status) atomicOr(status_out, status);
     if (counters) count_work(counters, nodes_total, tests);
 }

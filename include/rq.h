@@ -353,7 +353,9 @@ typedef struct rq_gi_params {
     float sky_color[3];    /* radiance returned by a miss (the reference samples u_Skymap) */
     int32_t sort_rays;     /* rq_gi_frame: 1 = group active secondary rays by direction octant
                               before tracing (same results, more coherent warps) */
-    int32_t reserved[2];
+    int32_t unfused;       /* rq_gi_frame: 0 = ray generation and shading + accumulation one
+                              thread per pixel; 1 = one thread per sample (same pixels) */
+    int32_t reserved;
 } rq_gi_params;
 
 typedef struct rq_frame_stats {

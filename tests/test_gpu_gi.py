@@ -101,7 +101,8 @@ def test_rtao_frame(ctx):
 @pytest.mark.parametrize("query", [0, 1])
 def test_gi_frame_forms_identical(ctx, query):
     """The GI/RTAO frame gives the same pixels bit for bit on every traversal form: strict BVH2,
-    BVH8q one thread per ray, BVH8q persistent ray queue, with and without octant binning."""
+    BVH8q one thread per ray, BVH8q persistent ray queue, with and without octant binning, with
+    per-pixel or per-sample ray generation and shading."""
     from candela_gb300 import _lib as L
     bufs = single_object("hf64", R.STACK)
     rays = rays_to_device(S.camera_rays(192, 160, **S.C1_CAMERA))
@@ -115,9 +116,42 @@ def test_gi_frame_forms_identical(ctx, query):
     want = want.cpu().numpy()
     assert st["secondary_rays"] > 1000
     for sort in (False, True):
-        p = gi_params(sort_rays=sort, **kw)
-        for launch in (dict(block_size=128, min_blocks=8), dict(block_size=128, min_blocks=8, persistent=1),
-                       dict(block_size=128, min_blocks=1, persistent=1)):
-            got = sc.gi_frame(rays, p, layout=L.LAYOUT_BVH8Q, **launch).cpu().numpy()
-            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (sort, launch)
+        for unfused in (False, True):
+            p = gi_params(sort_rays=sort, unfused=unfused, **kw)
+            for launch in (dict(block_size=128, min_blocks=8), dict(block_size=128, min_blocks=8, persistent=1),
+                           dict(block_size=128, min_blocks=1, persistent=1)):
+                got, st2 = sc.gi_frame(rays, p, layout=L.LAYOUT_BVH8Q, stats=True, **launch)
+                got = got.cpu().numpy()
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (sort, unfused, launch)
+                assert st2 == st, (sort, unfused, launch)
+    assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("query", [0, 1])
+def test_gi_frame_per_pixel_host_buffers_and_ref_compat(ctx, query):
+    """The per-pixel ray generation and shading kernels, through host buffers and with
+    RQ_FLAG_REF_COMPAT (a hit on triangle 0 shades as a miss), equal the per-sample kernels, and
+    the ray counts equal the oracle pipeline's."""
+    from candela_gb300 import _lib as L
+    bufs = single_object("ico2", R.STACK)
+    osc = oracle_scene(bufs, R.STACK)
+    rays = S.camera_rays(160, 128, eye=(0.0, -4.0, 2.0), target=(0.0, 0.0, 0.3))
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(np.random.default_rng(1).uniform(0.2, 0.9, (7, 3)).astype(np.float32))
+    sc.build_bvh8()
+    kw = dict(spp=2, seed=3, origin_offset=0.05)
+    if query == 1:
+        kw.update(ray_tmax=0.5, query=1)
+    for flags in (0, L.FLAG_REF_COMPAT):
+        want, st = sc.gi_frame(rays_to_device(rays), gi_params(unfused=True, **kw), layout=L.LAYOUT_BVH8Q,
+                               flags=flags, stats=True)
+        got_host = sc.gi_frame(rays, gi_params(**kw), layout=L.LAYOUT_BVH8Q, flags=flags)
+        np.testing.assert_array_equal(got_host.view(np.uint32), want.cpu().numpy().view(np.uint32))
+    ph = osc.closest(rays)
+    sec = osc.gi_raygen(rays, ph, kw["spp"], kw["seed"], kw["origin_offset"], kw.get("ray_tmax", 1e6))
+    _, st = sc.gi_frame(rays_to_device(rays), gi_params(**kw), layout=L.LAYOUT_BVH8Q, stats=True)
+    assert st["primary_hits"] == (ph["t"] > 0).sum()
+    assert st["secondary_rays"] == (sec["tmax"] > 0).sum()
+    want_sec = (osc.anyhit(sec) != 0).sum() if query == 1 else (osc.closest(sec)["t"] > 0).sum()
+    assert st["secondary_hits"] == want_sec
     assert ctx.device_status() == 0
