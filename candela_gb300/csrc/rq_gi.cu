@@ -161,11 +161,11 @@ __global__ void __launch_bounds__(256) k_gi_octant_count(SceneView s, const rq_r
 }
 
 // Pass 2: writes each active ray into its octant's region (regions in octant order, starting at
-// the exclusive prefix of the counts; cursors[o] advances per block), with the slot maps.
+// the exclusive prefix of the counts; cursors[o] advances per block), with the slot map comp_of.
 __global__ void __launch_bounds__(256) k_gi_octant_scatter(
     SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n, GiArgs a,
     const unsigned long long* counts, unsigned long long* cursors, rq_ray* __restrict__ out,
-    int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of, unsigned long long* total) {
+    int32_t* __restrict__ comp_of, unsigned long long* total) {
     __shared__ unsigned c[8];
     __shared__ unsigned long long base[8];
     if (threadIdx.x < 8) c[threadIdx.x] = 0;
@@ -199,7 +199,6 @@ __global__ void __launch_bounds__(256) k_gi_octant_scatter(
         if (act) {
             const int64_t cidx = static_cast<int64_t>(base[o] + rank);
             put_ray(out, cidx, org, 0.0f, dir, a.ray_tmax);
-            slot_of[cidx] = static_cast<int32_t>(j);
             comp_of[j] = static_cast<int32_t>(cidx);
         } else {
             comp_of[j] = -1;
@@ -208,13 +207,12 @@ __global__ void __launch_bounds__(256) k_gi_octant_scatter(
 }
 
 // Compacting variant of k_gi_raygen: active secondary rays are appended to `out` (block-aggregated
-// atomic, so only the order of blocks varies between runs), with slot_of[c] = slot j of compact
-// ray c and comp_of[j] = c (or -1 for an inactive slot).  Results are scattered back by slot, so
+// atomic, so only the order of blocks varies between runs), with comp_of[j] = the compact index
+// of slot j's ray (or -1 for an inactive slot).  Results are scattered back by slot, so
 // per-pixel sums keep their sample order; only the assignment of rays to threads changes.
 __global__ void __launch_bounds__(256) k_gi_raygen_compact(
     SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
-    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of,
-    unsigned long long* count) {
+    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ comp_of, unsigned long long* count) {
     __shared__ unsigned warp_count[8];
     __shared__ unsigned long long block_base;
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -260,7 +258,6 @@ __global__ void __launch_bounds__(256) k_gi_raygen_compact(
             const int64_t c = static_cast<int64_t>(block_base) + warp_count[warp] +
                               __popc(m & ((1u << lane) - 1u));
             put_ray(out, c, org, 0.0f, dir, a.ray_tmax);
-            slot_of[c] = static_cast<int32_t>(j);
             comp_of[j] = static_cast<int32_t>(c);
         } else {
             comp_of[j] = -1;
@@ -271,11 +268,10 @@ __global__ void __launch_bounds__(256) k_gi_raygen_compact(
 // Per-pixel form of k_gi_raygen_compact: one thread per primary ray i computes the hit point and
 // faced normal once and writes the spp secondary rays of slots j = i*spp + k.  Compaction is
 // block-aggregated and pixel-major within the block, the order k_gi_raygen_compact gives, with the
-// same slot maps; every value is computed with the same functions.
+// same slot map; every value is computed with the same functions.
 __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
     SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
-    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ slot_of, int32_t* __restrict__ comp_of,
-    unsigned long long* count) {
+    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ comp_of, unsigned long long* count) {
     __shared__ unsigned warp_hits[8];
     __shared__ unsigned long long block_base;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -318,7 +314,6 @@ __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
         const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
         const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
         put_ray(out, c0 + k, org, 0.0f, dir, a.ray_tmax);
-        slot_of[c0 + k] = static_cast<int32_t>(j);
         comp_of[j] = static_cast<int32_t>(c0 + k);
     }
 }
@@ -524,6 +519,118 @@ rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
 
 }  // namespace
 
+// Adds the compact ray count of a pass to the frame statistics.
+__global__ void k_add_count(unsigned long long* dst, const unsigned long long* src) { *dst += *src; }
+
+// One GI pass over n primary rays on stream st, in three phases: (1) primary closest hits and
+// secondary ray generation, (2) one secondary traversal over all compact rays (+ shadow rays),
+// (3) shading and the per-pixel mean.  Device buffers: prim and pixels4.  With host buffers
+// (h_prim / h_pix non-null, prim / pixels4 then device staging of n rays / pixels), the rays are
+// copied in first, and phase 3 runs in chunks of kGiHostChunk pixels whose pixels are copied out
+// on pipe[1] while the next chunk is shaded.  (Copying the rays in chunks overlapped with phase 1
+// was measured slower on GB300: the primary traversal slowed several-fold while the host-to-device
+// copies ran.)  With `stats`, the ray counts are added to the context's frame counters (cleared by
+// the caller).
+rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const rq_gi_params& p,
+                  const rq_ray* prim, int64_t n, float4* pixels4, cudaStream_t st, bool stats,
+                  const rq_ray* h_prim, float* h_pix) {
+    rq_status s;
+    const int64_t m = n * p.spp;
+    void *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr, *d_shade = nullptr,
+         *d_shadow = nullptr, *d_comp = nullptr;
+    if ((s = scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
+        (s = scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
+        (s = scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
+        (s = scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
+        (s = scratch(ctx, 11, 4 * m, &d_comp)) != RQ_OK)
+        return s;
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
+    unsigned long long* count = frame_counter(ctx);  // compact (active) secondary rays
+    RQ_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
+    const GiArgs a = to_args(p);
+    rq_hit* phit = static_cast<rq_hit*>(d_phit);
+    rq_ray* sec = static_cast<rq_ray*>(d_sec);
+    rq_hit* shit = static_cast<rq_hit*>(d_shit);
+    uint8_t* occ = static_cast<uint8_t*>(d_occ);
+    int32_t* comp_of = static_cast<int32_t*>(d_comp);
+    const int64_t chunk = h_pix ? kGiHostChunk : n;
+    // Camera rays are coherent and short (a few node visits): the one-thread-per-ray form of the
+    // tuned launch shape beats the persistent ray queue there, which pays per-ray hand-over costs.
+    QueryConfig qp = q;
+    qp.variant_closest = non_persistent_variant(q.variant_closest);
+    // phase 1
+    if (h_prim)
+        RQ_CUDA(ctx, cudaMemcpyAsync(const_cast<rq_ray*>(prim), h_prim, sizeof(rq_ray) * n,
+                                     cudaMemcpyHostToDevice, st));
+    RQ_CUDA(ctx, launch_closest(sc->view, qp, prim, n, phit, queue_counter(ctx, 0), st));
+    if (stats) k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
+    if (!p.sort_rays && !p.unfused) {
+        k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count);
+    } else if (p.sort_rays) {
+        void* d_oct = nullptr;
+        if ((s = scratch(ctx, 31, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
+        unsigned long long* counts = static_cast<unsigned long long*>(d_oct);
+        RQ_CUDA(ctx, cudaMemsetAsync(counts, 0, 16 * sizeof(unsigned long long), st));
+        k_gi_octant_count<<<grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts);
+        k_gi_octant_scatter<<<grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts, counts + 8, sec,
+                                                          comp_of, count);
+    } else if (p.unfused) {
+        k_gi_raygen_compact<<<grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count);
+    }
+    RQ_CUDA(ctx, cudaGetLastError());
+    if (stats) k_add_count<<<1, 1, 0, st>>>(cnt + 5, count);
+    // phase 2
+    SceneView cv = sc->view;  // secondary launches cover only the compact prefix
+    cv.ray_count = count;
+    const uint8_t* vis = nullptr;
+    if (p.query == 1) {
+        RQ_CUDA(ctx, launch_anyhit(cv, q, sec, m, occ, queue_counter(ctx, 1), st));
+        if (stats) k_count_bytes_c<<<grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 2);
+        vis = occ;
+    } else {
+        RQ_CUDA(ctx, launch_closest(cv, q, sec, m, shit, queue_counter(ctx, 1), st));
+        if (stats) k_count_hits_c<<<grid(m, 256), 256, 0, st>>>(shit, m, count, cnt + 2);
+        if (p.shadow_rays) {
+            if ((s = scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
+            rq_ray* sh = static_cast<rq_ray*>(d_shadow);
+            k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count,
+                                                            stats ? cnt + 3 : nullptr);
+            RQ_CUDA(ctx, cudaGetLastError());
+            RQ_CUDA(ctx, launch_anyhit(cv, q, sh, m, occ, queue_counter(ctx, 2), st));
+            if (stats) k_count_bytes_c<<<grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 4);
+            vis = occ;
+        }
+    }
+    // phase 3
+    float4* shade = nullptr;
+    if (p.unfused) {  // per-sample shading into a scratch buffer, then the per-pixel mean
+        if ((s = scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
+        shade = static_cast<float4*>(d_shade);
+        k_shade_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p.query, sc->d_albedo,
+                                                sc->n_albedo, a, shade);
+    }
+    for (int64_t off = 0; off < n; off += chunk) {
+        const int64_t c = std::min(chunk, n - off);
+        if (p.unfused)
+            k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, pixels4 + off);
+        else
+            k_shade_accumulate<<<grid(c, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of + off * p.spp, c, vis,
+                                                             p.query, sc->d_albedo, sc->n_albedo, a, pixels4 + off);
+        RQ_CUDA(ctx, cudaGetLastError());
+        if (h_pix) {
+            RQ_CUDA(ctx, cudaEventRecord(ctx->ev, st));
+            RQ_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[1], ctx->ev, 0));
+            RQ_CUDA(ctx, cudaMemcpyAsync(h_pix + 4 * off, pixels4 + off, 16 * c, cudaMemcpyDeviceToHost,
+                                         ctx->pipe[1]));
+        }
+    }
+    if (h_pix) {
+        RQ_CUDA(ctx, cudaEventRecord(ctx->ev, ctx->pipe[1]));
+        RQ_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev, 0));
+    }
+    return RQ_OK;
+}
+
 // The GI pass over caller-provided intermediate buffers: the kernel sequence of rq_gi_frame
 // without its ray-count statistics.  Used by the no-allocation entry point (rq_noalloc.cu).
 cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
@@ -640,105 +747,29 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
     const bool host = (q.flags & RQ_FLAG_HOST_BUFFERS) != 0;
     q.flags &= ~RQ_FLAG_HOST_BUFFERS;
-    const int64_t m = n * p->spp;
-    void *d_prim = nullptr, *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr,
-         *d_shade = nullptr, *d_pix = nullptr, *d_shadow = nullptr, *d_slot = nullptr,
-         *d_comp = nullptr;
-    if ((s = rq::scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
-        (s = rq::scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
-        (s = rq::scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
-        (s = rq::scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
-        (s = rq::scratch(ctx, 10, 4 * m, &d_slot)) != RQ_OK ||
-        (s = rq::scratch(ctx, 11, 4 * m, &d_comp)) != RQ_OK)
-        return s;
-    if (host) {
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
+    if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
+    if (!host) {
+        if ((s = rq::gi_pass(ctx, sc, q, *p, primary, n, reinterpret_cast<float4*>(pixels4), st,
+                             stats != nullptr, nullptr, nullptr)) != RQ_OK)
+            return s;
+    } else {
+        void *d_prim = nullptr, *d_pix = nullptr;
         if ((s = rq::scratch(ctx, 0, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
             (s = rq::scratch(ctx, 6, 16 * n, &d_pix)) != RQ_OK)
             return s;
-        RQ_CUDA(ctx, cudaMemcpyAsync(d_prim, primary, sizeof(rq_ray) * n, cudaMemcpyHostToDevice, st));
-    } else {
-        d_prim = const_cast<rq_ray*>(primary);
-        d_pix = pixels4;
-    }
-    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
-    unsigned long long* count = rq::frame_counter(ctx);  // active (compact) secondary rays
-    RQ_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
-    if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
-    const rq::GiArgs a = rq::to_args(*p);
-    const rq_ray* prim = static_cast<const rq_ray*>(d_prim);
-    rq_hit* phit = static_cast<rq_hit*>(d_phit);
-    rq_ray* sec = static_cast<rq_ray*>(d_sec);
-    rq_hit* shit = static_cast<rq_hit*>(d_shit);
-    uint8_t* occ = static_cast<uint8_t*>(d_occ);
-    int32_t* slot_of = static_cast<int32_t*>(d_slot);
-    int32_t* comp_of = static_cast<int32_t*>(d_comp);
-    // Camera rays are coherent and short (a few node visits): the one-thread-per-ray form of the
-    // tuned launch shape beats the persistent ray queue there, which pays per-ray hand-over costs.
-    rq::QueryConfig qp = q;
-    qp.variant_closest = rq::non_persistent_variant(q.variant_closest);
-    RQ_CUDA(ctx, rq::launch_closest(sc->view, qp, prim, n, phit, rq::queue_counter(ctx, 0), st));
-    if (stats) rq::k_count_hits<<<rq::grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
-    if (p->sort_rays) {
-        void* d_oct = nullptr;
-        if ((s = rq::scratch(ctx, 31, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
-        unsigned long long* counts = static_cast<unsigned long long*>(d_oct);
-        RQ_CUDA(ctx, cudaMemsetAsync(counts, 0, 16 * sizeof(unsigned long long), st));
-        rq::k_gi_octant_count<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts);
-        rq::k_gi_octant_scatter<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts,
-                                                                  counts + 8, sec, slot_of, comp_of, count);
-    } else if (p->unfused) {
-        rq::k_gi_raygen_compact<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
-                                                                  slot_of, comp_of, count);
-    } else {
-        rq::k_gi_raygen_pixel<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec,
-                                                                slot_of, comp_of, count);
-    }
-    RQ_CUDA(ctx, cudaGetLastError());
-    rq::SceneView cv = sc->view;  // secondary launches cover only the compact prefix
-    cv.ray_count = count;
-    const uint8_t* vis = nullptr;
-    if (p->query == 1) {
-        RQ_CUDA(ctx, rq::launch_anyhit(cv, q, sec, m, occ, rq::queue_counter(ctx, 1), st));
-        if (stats) rq::k_count_bytes_c<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 2);
-        vis = occ;
-    } else {
-        RQ_CUDA(ctx, rq::launch_closest(cv, q, sec, m, shit, rq::queue_counter(ctx, 1), st));
-        if (stats) rq::k_count_hits_c<<<rq::grid(m, 256), 256, 0, st>>>(shit, m, count, cnt + 2);
-        if (p->shadow_rays) {
-            if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
-            rq_ray* sh = static_cast<rq_ray*>(d_shadow);
-            rq::k_shadow_raygen_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count,
-                                                                    stats ? cnt + 3 : nullptr);
-            RQ_CUDA(ctx, cudaGetLastError());
-            RQ_CUDA(ctx, rq::launch_anyhit(cv, q, sh, m, occ, rq::queue_counter(ctx, 2), st));
-            if (stats) rq::k_count_bytes_c<<<rq::grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 4);
-            vis = occ;
-        }
-    }
-    if (p->unfused) {  // per-sample shading into a scratch buffer, then the per-pixel mean
-        if ((s = rq::scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
-        float4* shade = static_cast<float4*>(d_shade);
-        rq::k_shade_c<<<rq::grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p->query,
-                                                        sc->d_albedo, sc->n_albedo, a, shade);
-        rq::k_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(shade, n, p->spp, static_cast<float4*>(d_pix));
-    } else {
-        rq::k_shade_accumulate<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, n, vis, p->query,
-                                                                 sc->d_albedo, sc->n_albedo, a,
-                                                                 static_cast<float4*>(d_pix));
-    }
-    RQ_CUDA(ctx, cudaGetLastError());
-    if (host) {
-        RQ_CUDA(ctx, cudaMemcpyAsync(pixels4, d_pix, 16 * n, cudaMemcpyDeviceToHost, st));
+        if ((s = rq::gi_pass(ctx, sc, q, *p, static_cast<const rq_ray*>(d_prim), n,
+                             static_cast<float4*>(d_pix), st, stats != nullptr, primary, pixels4)) != RQ_OK)
+            return s;
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
     }
     if (stats) {
-        unsigned long long c[8], act = 0;
+        unsigned long long c[8];
         RQ_CUDA(ctx, cudaMemcpyAsync(c, cnt, sizeof(c), cudaMemcpyDeviceToHost, st));
-        RQ_CUDA(ctx, cudaMemcpyAsync(&act, count, sizeof(act), cudaMemcpyDeviceToHost, st));
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
         stats->primary_rays = n;
         stats->primary_hits = static_cast<int64_t>(c[0]);
-        stats->secondary_rays = static_cast<int64_t>(act);
+        stats->secondary_rays = static_cast<int64_t>(c[5]);
         stats->secondary_hits = static_cast<int64_t>(c[2]);
         stats->shadow_rays = static_cast<int64_t>(c[3]);
         stats->shadow_occluded = static_cast<int64_t>(c[4]);

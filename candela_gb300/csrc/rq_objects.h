@@ -83,6 +83,9 @@ inline unsigned long long* work_counters(rq_ctx* ctx) {
 inline unsigned long long* frame_counter(rq_ctx* ctx) {
     return reinterpret_cast<unsigned long long*>(ctx->counters) + 12;
 }
+// Pixels per chunk of the shading phase of a GI frame on host buffers (each chunk's pixels are
+// copied out while the next chunk is shaded).
+constexpr int64_t kGiHostChunk = int64_t(1) << 18;
 // Device status bits of the kernels (atomicOr), read by rq_device_status.
 inline unsigned* status_word(rq_ctx* ctx) { return reinterpret_cast<unsigned*>(ctx->counters) + 30; }
 // Ray-queue counter k (0..15) of the persistent kernels, inside the context's counter block.

@@ -155,3 +155,26 @@ def test_gi_frame_per_pixel_host_buffers_and_ref_compat(ctx, query):
     want_sec = (osc.anyhit(sec) != 0).sum() if query == 1 else (osc.closest(sec)["t"] > 0).sum()
     assert st["secondary_hits"] == want_sec
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("query", [0, 1])
+def test_gi_frame_host_chunks_equal_device_pass(ctx, query):
+    """A host-buffer frame of several shading chunks (pixels copied out chunk by chunk while the
+    next chunk is shaded) gives the pixels and ray counts of the device-buffer pass, bit for bit."""
+    from candela_gb300 import _lib as L
+    bufs = single_object("hf64", R.STACK)
+    rays = S.camera_rays(1280, 1024, **S.C1_CAMERA)
+    assert len(rays) > 4 * (1 << 18)
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(np.array([[0.7, 0.6, 0.5]], dtype=np.float32))
+    sc.build_bvh8()
+    kw = dict(spp=2, seed=21, origin_offset=1e-3)
+    if query == 1:
+        kw.update(ray_tmax=0.25, query=1)
+    p = gi_params(**kw)
+    for layout in (R.STACK, L.LAYOUT_BVH8Q):
+        want, st = sc.gi_frame(rays_to_device(rays), p, layout=layout, stats=True)
+        got, st_h = sc.gi_frame(rays, p, layout=layout, stats=True)
+        np.testing.assert_array_equal(got.view(np.uint32), want.cpu().numpy().view(np.uint32))
+        assert st_h == st
+    assert ctx.device_status() == 0
