@@ -107,6 +107,7 @@ SIGNATURES = {
     "rq_destroy": (_S, [_P]),
     "rq_last_error": (C.c_char_p, [_P]),
     "rq_build_bvh": (_S, [_P, _I64, _P, _I64, _P, _I32, _S, C.POINTER(RqBuildOpts), C.POINTER(_P)]),
+    "rq_build_bvh_gpu": (_S, [_P, _P, _I64, _P, _I64, _P, _I32, _S, C.POINTER(RqBuildOpts), C.POINTER(_P)]),
     "rq_bvh_info_get": (_S, [_P, C.POINTER(RqBvhInfo)]),
     "rq_bvh_nodes": (_S, [_P, C.POINTER(_P), C.POINTER(_I64)]),
     "rq_bvh_triangles": (_S, [_P, C.POINTER(_P), C.POINTER(_I64)]),

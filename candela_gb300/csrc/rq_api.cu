@@ -280,6 +280,49 @@ rq_status rq_build_bvh(const rq_vertex* verts, int64_t n_verts, const uint32_t* 
     return RQ_OK;
 }
 
+rq_status rq_build_bvh_gpu(rq_ctx* ctx, const rq_vertex* verts, int64_t n_verts, const uint32_t* indices,
+                           int64_t n_indices, const int32_t* mesh_ids, int32_t tri_offset, rq_layout layout,
+                           const rq_build_opts* opts, rq_bvh** out) {
+    if (!out) return fail(ctx, RQ_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (!ctx) return fail(nullptr, RQ_EINVAL, "NULL context");
+    if (!verts || !indices || n_verts <= 0 || n_indices <= 0 || n_indices % 3 != 0)
+        return fail(ctx, RQ_EINVAL, "vertex/index arrays empty or not a multiple of 3");
+    if (layout != RQ_LAYOUT_BVH2_STACK && layout != RQ_LAYOUT_BVH2_STACKLESS)
+        return fail(ctx, RQ_EINVAL, "layout must be BVH2_STACK or BVH2_STACKLESS");
+    if (tri_offset < 0) return fail(ctx, RQ_EINVAL, "tri_offset < 0");
+    rq_build_opts d{};
+    if (!opts) opts = &d;
+    rq::BuildInput in{};
+    in.vert_records = reinterpret_cast<const float*>(verts);
+    in.n_verts = n_verts;
+    in.indices = indices;
+    in.n_tris = n_indices / 3;
+    in.mesh_ids = mesh_ids;
+    in.tri_offset = tri_offset;
+    in.leaf_size = opts->leaf_size == 0 ? 2 : opts->leaf_size;
+    in.layout = layout == RQ_LAYOUT_BVH2_STACK ? 0 : 1;
+    in.swap_children = opts->swap_children;
+    in.swap_seed = opts->swap_seed;
+    auto* b = new (std::nothrow) rq_bvh;
+    if (!b) return fail(ctx, RQ_ENOMEM, "bvh allocation failed");
+    b->layout = layout;
+    std::string why;
+    rq_status s;
+    try {
+        s = rq::build_bvh_gpu(ctx->device, in, b->out, why);
+    } catch (const std::bad_alloc&) {
+        delete b;
+        return fail(ctx, RQ_ENOMEM, "host allocation failed during GPU BVH build");
+    }
+    if (s != RQ_OK) {
+        delete b;
+        return fail(ctx, s, why.c_str());
+    }
+    *out = b;
+    return RQ_OK;
+}
+
 rq_status rq_bvh_info_get(const rq_bvh* b, rq_bvh_info* info) {
     if (!b || !info) return fail(nullptr, RQ_EINVAL, "NULL argument");
     info->n_nodes = b->out.n_nodes;

@@ -35,15 +35,20 @@ class BVH:
 
 def build_bvh(vertices: np.ndarray, indices: np.ndarray, mesh_ids=None, tri_offset: int = 0,
               layout: int = STACK, leaf_size: int = 2, swap_children: bool = False,
-              swap_seed: int = 0, n_threads: int = 0) -> BVH:
-    """BVH::BuildBVH for one object (BVHConstructor.cpp:951-1108) via rq_build_bvh."""
+              swap_seed: int = 0, n_threads: int = 0, ctx=None) -> BVH:
+    """BVH::BuildBVH for one object (BVHConstructor.cpp:951-1108) via rq_build_bvh, or via
+    rq_build_bvh_gpu on the context's GPU when `ctx` is given (same buffers)."""
     v = np.ascontiguousarray(vertices, dtype=VERTEX_DTYPE)
     idx = np.ascontiguousarray(indices, dtype=np.uint32).ravel()
     mid = None if mesh_ids is None else np.ascontiguousarray(mesh_ids, dtype=np.int32)
     opts = L.RqBuildOpts(leaf_size, int(swap_children), swap_seed & 0xFFFFFFFF, n_threads)
     h = C.c_void_p()
-    check(lib().rq_build_bvh(ptr(v), v.shape[0], ptr(idx), idx.size, ptr(mid), tri_offset, layout,
-                             C.byref(opts), C.byref(h)))
+    if ctx is None:
+        check(lib().rq_build_bvh(ptr(v), v.shape[0], ptr(idx), idx.size, ptr(mid), tri_offset, layout,
+                                 C.byref(opts), C.byref(h)))
+    else:
+        check(lib().rq_build_bvh_gpu(ctx.handle, ptr(v), v.shape[0], ptr(idx), idx.size, ptr(mid), tri_offset,
+                                     layout, C.byref(opts), C.byref(h)), ctx.handle)
     try:
         info = L.RqBvhInfo()
         check(lib().rq_bvh_info_get(h, C.byref(info)))

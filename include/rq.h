@@ -203,6 +203,12 @@ typedef struct rq_bvh_info {
 rq_status rq_build_bvh(const rq_vertex* verts, int64_t n_verts, const uint32_t* indices,
                        int64_t n_indices, const int32_t* mesh_ids, int32_t tri_offset,
                        rq_layout layout, const rq_build_opts* opts, rq_bvh** out);
+/* The same build on the GPU of `ctx` (no counterpart in the reference, whose constructor runs
+ * on the host only): the buffers rq_build_bvh returns, byte for byte, from the same host arrays;
+ * opts->n_threads is ignored.  The result is an ordinary rq_bvh (host buffers). */
+rq_status rq_build_bvh_gpu(rq_ctx* ctx, const rq_vertex* verts, int64_t n_verts, const uint32_t* indices,
+                           int64_t n_indices, const int32_t* mesh_ids, int32_t tri_offset,
+                           rq_layout layout, const rq_build_opts* opts, rq_bvh** out);
 rq_status rq_bvh_info_get(const rq_bvh* bvh, rq_bvh_info* info);
 /* Borrowed pointers, valid until rq_bvh_free. */
 rq_status rq_bvh_nodes(const rq_bvh* bvh, const void** nodes, int64_t* n_nodes);
