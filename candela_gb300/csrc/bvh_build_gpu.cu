@@ -8,8 +8,8 @@
 //     binning into per-node bins (shared-memory partial bins merged with atomics), the split
 //     search of SearchSAHPlaneBinned (:276-363) with the host's rounding order, the Lomuto
 //     partition (:532-550) in parallel (below), child bounds by position-keyed reductions;
-//   * a node of at most kSmall triangles is finished by one thread, which builds its whole
-//     subtree sequentially with the host's code path (in place on its own triangle range);
+//   * a node of at most kSmall triangles is finished by one warp, which builds its whole subtree
+//     in shared memory (in place on its own triangle range);
 //   * flattening on the GPU: leaf order, stackless DFS with escape links and swaps, stack BFS.
 //
 // Order-dependent details, reproduced exactly:
@@ -548,119 +548,330 @@ __global__ void k_child_decode(Tri T, Nodes N, int32_t base, int32_t count, cons
     }
 }
 
-// ---- small subtrees: one thread, the host builder's sequential code ---------------------------
+// ---- small subtrees: one warp builds the subtree of a node of at most kSmall triangles --------
+//
+// Per node: bins in shared memory (shared atomics; bin boxes only feed the areas), the sweep of
+// SearchSAHPlaneBinned as warp prefix / suffix scans over the 64 bins (min / max / sum are exact
+// and associative, so each prefix equals the sequential running box), the first strictly
+// smallest cost by a warp reduction over (cost, split index), the parallel Lomuto partition in
+// shared memory, and the child bounds by position-keyed warp reductions.
+constexpr int kSmallWarps = 4;
+constexpr int kStackCap = kSmall + 4;
 
-struct Bins {
-    int32_t count[3][kBins];
-    Box3 box[3][kBins];
+struct WarpSmem {
+    unsigned cnt[3 * kBins];
+    unsigned kmin[3 * kBins * 3];
+    unsigned kmax[3 * kBins * 3];
+    int32_t ref[kSmall];
+    int32_t out[kSmall];
+    int32_t ptr[kSmall];
+    int32_t ptr2[kSmall];
+    int32_t jj[kSmall];
+    int32_t stack[kStackCap];
 };
 
-__device__ void small_subtree(Tri T, Nodes N, int32_t root, int32_t* refs, int32_t leaf_size,
-                              int32_t* node_counter, int32_t* fails, int32_t* overflow) {
-    int32_t stack[2 * kSmall + 2];
-    int sp = 0;
-    stack[sp++] = root;
-    Bins bins;
-    while (sp > 0) {
-        const int32_t id = stack[--sp];
-        const int32_t s = N.start[id], len = N.len[id];
-        if (len <= leaf_size || len <= 1) {
-            N.left[id] = N.right[id] = -1;
-            continue;
+__device__ __forceinline__ void box_union(float* mn, float* mx, const float* bmn, const float* bmx) {
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = gmin(mn[k], bmn[k]);
+        mx[k] = gmax(mx[k], bmx[k]);
+    }
+}
+__device__ __forceinline__ float box_area(const float* mn, const float* mx) {  // Bounds::GetArea
+    const float ex = __fsub_rn(mx[0], mn[0]), ey = __fsub_rn(mx[1], mn[1]), ez = __fsub_rn(mx[2], mn[2]);
+    float a = __fmul_rn(ex, ey);
+    a = __fadd_rn(a, __fmul_rn(ey, ez));
+    a = __fadd_rn(a, __fmul_rn(ez, ex));
+    return a;
+}
+
+// Sweep of one axis by the whole warp: returns the key (cost, split) of the first strictly
+// smallest cost below INF_COST, or ~0 when there is none.
+__device__ unsigned long long warp_sweep(const WarpSmem& W, int a, unsigned lane) {
+    float bmn[2][3], bmx[2][3];
+    int c[2];
+    for (int h = 0; h < 2; ++h) {
+        const int b = a * kBins + 2 * static_cast<int>(lane) + h;
+        c[h] = static_cast<int>(W.cnt[b]);
+        for (int k = 0; k < 3; ++k) {
+            bmn[h][k] = c[h] ? okey_value(W.kmin[b * 3 + k]) : kArbMax;
+            bmx[h][k] = c[h] ? okey_value(W.kmax[b * 3 + k]) : kArbMin;
         }
+    }
+    // lane totals
+    float tmn[3], tmx[3];
+    for (int k = 0; k < 3; ++k) {
+        tmn[k] = gmin(bmn[0][k], bmn[1][k]);
+        tmx[k] = gmax(bmx[0][k], bmx[1][k]);
+    }
+    const int tc = c[0] + c[1];
+    // exclusive prefix over lanes < lane (E) and exclusive suffix over lanes > lane (Q)
+    float emn[3] = {kArbMax, kArbMax, kArbMax}, emx[3] = {kArbMin, kArbMin, kArbMin};
+    float qmn[3] = {kArbMax, kArbMax, kArbMax}, qmx[3] = {kArbMin, kArbMin, kArbMin};
+    int ec = 0, qc = 0;
+    {
+        float imn[3], imx[3];
+        int ic = tc;
+        for (int k = 0; k < 3; ++k) {
+            imn[k] = tmn[k];
+            imx[k] = tmx[k];
+        }
+        for (int o = 1; o < 32; o <<= 1) {  // inclusive prefix
+            float umn[3], umx[3];
+            for (int k = 0; k < 3; ++k) {
+                umn[k] = __shfl_up_sync(0xFFFFFFFFu, imn[k], o);
+                umx[k] = __shfl_up_sync(0xFFFFFFFFu, imx[k], o);
+            }
+            const int uc = __shfl_up_sync(0xFFFFFFFFu, ic, o);
+            if (lane >= static_cast<unsigned>(o)) {
+                box_union(imn, imx, umn, umx);
+                ic += uc;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            emn[k] = __shfl_up_sync(0xFFFFFFFFu, imn[k], 1);
+            emx[k] = __shfl_up_sync(0xFFFFFFFFu, imx[k], 1);
+        }
+        ec = __shfl_up_sync(0xFFFFFFFFu, ic, 1);
+        if (lane == 0) {
+            for (int k = 0; k < 3; ++k) {
+                emn[k] = kArbMax;
+                emx[k] = kArbMin;
+            }
+            ec = 0;
+        }
+        for (int k = 0; k < 3; ++k) {
+            imn[k] = tmn[k];
+            imx[k] = tmx[k];
+        }
+        ic = tc;
+        for (int o = 1; o < 32; o <<= 1) {  // inclusive suffix
+            float umn[3], umx[3];
+            for (int k = 0; k < 3; ++k) {
+                umn[k] = __shfl_down_sync(0xFFFFFFFFu, imn[k], o);
+                umx[k] = __shfl_down_sync(0xFFFFFFFFu, imx[k], o);
+            }
+            const int uc = __shfl_down_sync(0xFFFFFFFFu, ic, o);
+            if (lane + o < 32u) {
+                box_union(imn, imx, umn, umx);
+                ic += uc;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            qmn[k] = __shfl_down_sync(0xFFFFFFFFu, imn[k], 1);
+            qmx[k] = __shfl_down_sync(0xFFFFFFFFu, imx[k], 1);
+        }
+        qc = __shfl_down_sync(0xFFFFFFFFu, ic, 1);
+        if (lane == 31) {
+            for (int k = 0; k < 3; ++k) {
+                qmn[k] = kArbMax;
+                qmx[k] = kArbMin;
+            }
+            qc = 0;
+        }
+    }
+    unsigned long long best = ~0ull;
+    // split i = 2*lane: left = E + bin0, right = Q + bin1
+    {
+        float lmn[3], lmx[3], rmn[3], rmx[3];
+        for (int k = 0; k < 3; ++k) {
+            lmn[k] = emn[k];
+            lmx[k] = emx[k];
+            rmn[k] = qmn[k];
+            rmx[k] = qmx[k];
+        }
+        box_union(lmn, lmx, bmn[0], bmx[0]);
+        box_union(rmn, rmx, bmn[1], bmx[1]);
+        float cst = __fmul_rn(__int2float_rn(ec + c[0]), box_area(lmn, lmx));
+        cst = __fadd_rn(cst, __fmul_rn(__int2float_rn(qc + c[1]), box_area(rmn, rmx)));
+        if (cst < kInfCost)
+            best = (static_cast<unsigned long long>(okey(cst)) << 32) | (2u * lane);
+    }
+    // split i = 2*lane + 1 (i <= 62): left = E + bin0 + bin1, right = Q
+    if (lane < 31) {
+        float lmn[3], lmx[3];
+        for (int k = 0; k < 3; ++k) {
+            lmn[k] = emn[k];
+            lmx[k] = emx[k];
+        }
+        box_union(lmn, lmx, tmn, tmx);
+        float cst = __fmul_rn(__int2float_rn(ec + tc), box_area(lmn, lmx));
+        cst = __fadd_rn(cst, __fmul_rn(__int2float_rn(qc), box_area(qmn, qmx)));
+        if (cst < kInfCost) {
+            const unsigned long long key = (static_cast<unsigned long long>(okey(cst)) << 32) | (2u * lane + 1u);
+            best = key < best ? key : best;
+        }
+    }
+    best = warp_min64(best);
+    return __shfl_sync(0xFFFFFFFFu, best, 0);
+}
+
+__device__ __forceinline__ unsigned lane_lt_mask() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__global__ void __launch_bounds__(32 * kSmallWarps) k_small(Tri T, Nodes N, const int32_t* __restrict__ list,
+                                                            int32_t count, int32_t* refs, int32_t leaf_size,
+                                                            int32_t* node_counter, int32_t* fails, int32_t* overflow) {
+    __shared__ WarpSmem smem[kSmallWarps];
+    const unsigned lane = threadIdx.x & 31u;
+    const int w = threadIdx.x >> 5;
+    const int32_t item = blockIdx.x * kSmallWarps + w;
+    if (item >= count) return;  // whole warp
+    WarpSmem& W = smem[w];
+    int sp = 0;
+    if (lane == 0) W.stack[0] = list[item];
+    sp = 1;
+    __syncwarp();
+    for (int guard = 0; sp > 0 && guard < 4 * kSmall + 8; ++guard) {
+        const int32_t id = W.stack[--sp];
+        __syncwarp();
+        const int32_t s = N.start[id], len = N.len[id];
+        if (len <= leaf_size || len <= 1) continue;  // leaf: left/right stay -1
         float mn[3], ext[3], scale[3];
         bool active[3];
         node_frame(N, id, mn, ext, scale, active);
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < kBins; ++b) {
-                bins.count[a][b] = 0;
-                bins.box[a][b].reset();
+        for (int i = lane; i < 3 * kBins; i += 32) W.cnt[i] = 0u;
+        for (int i = lane; i < 3 * kBins * 3; i += 32) {
+            W.kmin[i] = 0xFFFFFFFFu;
+            W.kmax[i] = 0u;
+        }
+        for (int i = lane; i < len; i += 32) W.ref[i] = refs[s + i];
+        __syncwarp();
+        for (int i = lane; i < len; i += 32) {
+            const int32_t r = W.ref[i];
+            uint32_t km[3], kx[3];
+            for (int k = 0; k < 3; ++k) {
+                km[k] = okey(T.mn(k, r));
+                kx[k] = okey(T.mx(k, r));
             }
-        for (int32_t i = s; i < s + len; ++i) {
-            const int32_t r = refs[i];
-            const float bmn[3] = {T.mn(0, r), T.mn(1, r), T.mn(2, r)};
-            const float bmx[3] = {T.mx(0, r), T.mx(1, r), T.mx(2, r)};
             for (int a = 0; a < 3; ++a) {
                 if (!active[a]) continue;
-                const int bi = bin_of(T.cen(a, r), mn[a], scale[a]);
-                ++bins.count[a][bi];
-                bins.box[a][bi].grow_acc_first(bmn, bmx);
-            }
-        }
-        float best = kInfCost;
-        int axis = 0;
-        float border = mn[0];
-        for (int a = 0; a < 3; ++a) {
-            if (!active[a]) continue;
-            unsigned cnt[kBins];
-            float bmn[3 * kBins], bmx[3 * kBins];
-            for (int b = 0; b < kBins; ++b) {
-                cnt[b] = static_cast<unsigned>(bins.count[a][b]);
+                const int b = a * kBins + bin_of(T.cen(a, r), mn[a], scale[a]);
+                atomicAdd(&W.cnt[b], 1u);
                 for (int k = 0; k < 3; ++k) {
-                    bmn[3 * b + k] = bins.box[a][b].mn[k];
-                    bmx[3 * b + k] = bins.box[a][b].mx[k];
+                    atomicMin(&W.kmin[b * 3 + k], km[k]);
+                    atomicMax(&W.kmax[b * 3 + k], kx[k]);
                 }
             }
-            int bi;
-            const float c = sweep_axis(cnt, bmn, bmx, bi);
-            if (bi >= 0 && c < best) {
-                best = c;
-                axis = a;
-                const float step = __fdiv_rn(ext[a], static_cast<float>(kBins));
-                border = __fadd_rn(mn[a], __fmul_rn(step, static_cast<float>(bi + 1)));
+        }
+        __syncwarp();
+        // split: axes in order, first strictly smaller cost (SearchSAHPlaneBinned)
+        int axis = 0;
+        float border = mn[0];
+        {
+            unsigned long long bkey = ~0ull;
+            for (int a = 0; a < 3; ++a) {
+                if (!active[a]) continue;
+                const unsigned long long key = warp_sweep(W, a, lane);
+                if (key == ~0ull) continue;
+                if ((key >> 32) < (bkey >> 32)) {  // strictly smaller cost (okey order)
+                    bkey = key;
+                    axis = a;
+                }
+            }
+            if (bkey != ~0ull) {
+                const int bi = static_cast<int>(bkey & 0xFFFFFFFFull);
+                const float step = __fdiv_rn(ext[axis], static_cast<float>(kBins));
+                border = __fadd_rn(mn[axis], __fmul_rn(step, static_cast<float>(bi + 1)));
             }
         }
-        int32_t mid = s;
-        for (int32_t i = s; i < s + len; ++i) {  // Lomuto partition (:532-550)
-            if (T.cen(axis, refs[i]) < border) {
-                const int32_t t = refs[i];
-                refs[i] = refs[mid];
-                refs[mid] = t;
-                ++mid;
+        // parallel Lomuto partition in shared memory (see the file header)
+        int32_t k_below = 0;
+        for (int i0 = 0; i0 < len; i0 += 32) {
+            const int i = i0 + static_cast<int>(lane);
+            const bool p = i < len && T.cen(axis, W.ref[i]) < border;
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, p);
+            if (i < len) {
+                const int32_t j = k_below + __popc(bal & lane_lt_mask());
+                W.jj[i] = j;
+                W.ptr[i] = p ? j : i;
             }
+            k_below += __popc(bal);
         }
-        if (mid == s || mid == s + len) {
-            mid = s + len / 2;
-            atomicAdd(fails, 1);
+        __syncwarp();
+        const bool fb = k_below == 0 || k_below == len;
+        int32_t mid = fb ? len / 2 : k_below;
+        if (fb) {
+            if (lane == 0) atomicAdd(fails, 1);
+        } else {
+            int32_t* pa = W.ptr;
+            int32_t* pb = W.ptr2;
+            for (int r = 0; r < 9; ++r) {  // 2^8 = kSmall: chains are shorter than len <= kSmall
+                for (int i = lane; i < len; i += 32) pb[i] = pa[pa[i]];
+                __syncwarp();
+                int32_t* t = pa;
+                pa = pb;
+                pb = t;
+            }
+            for (int i = lane; i < len; i += 32) {
+                const int32_t r = W.ref[i];
+                if (T.cen(axis, r) < border) W.out[W.jj[i]] = r;
+                if (i >= k_below) W.out[i] = W.ref[pa[i]];
+            }
+            __syncwarp();
+            for (int i = lane; i < len; i += 32) {
+                refs[s + i] = W.out[i];
+                W.ref[i] = W.out[i];
+            }
+            __syncwarp();
         }
-        const int32_t L = atomicAdd(node_counter, 2), R = L + 1;
-        if (L + 1 >= N.cap || sp + 2 > 2 * kSmall + 2) {
-            atomicOr(overflow, 1);
+        // children
+        int32_t L = 0;
+        if (lane == 0) L = atomicAdd(node_counter, 2);
+        L = __shfl_sync(0xFFFFFFFFu, L, 0);
+        if (L + 1 >= N.cap || sp + 2 > kStackCap) {
+            if (lane == 0) atomicOr(overflow, 1);
             return;
         }
-        N.left[id] = L;
-        N.right[id] = R;
-        const int32_t cb[2] = {s, mid}, cl[2] = {mid - s, s + len - mid}, kid[2] = {L, R};
+        const int32_t R = L + 1;
+        const int32_t cb[2] = {0, mid}, cl[2] = {mid, len - mid}, kid[2] = {L, R};
         for (int j = 0; j < 2; ++j) {
-            const int32_t c = kid[j];
-            N.start[c] = cb[j];
-            N.len[c] = cl[j];
-            N.parent[c] = id;
-            N.left[c] = N.right[c] = -1;
-            float bmn[3] = {kArbMax, kArbMax, kArbMax}, bmx[3] = {kArbMin, kArbMin, kArbMin};
-            for (int32_t i = cb[j]; i < cb[j] + cl[j]; ++i) {
-                const int32_t r = refs[i];
-                for (int k = 0; k < 3; ++k) {  // glm::min(x, acc): child bounds (:573-597)
-                    bmn[k] = gmin(T.mn(k, r), bmn[k]);
-                    bmx[k] = gmax(T.mx(k, r), bmx[k]);
+            unsigned long long kmn[3], kmx[3];
+            for (int k = 0; k < 3; ++k) {
+                kmn[k] = ~0ull;
+                kmx[k] = 0ull;
+            }
+            for (int i = cb[j] + static_cast<int>(lane); i < cb[j] + cl[j]; i += 32) {
+                const int32_t r = W.ref[i];
+                for (int k = 0; k < 3; ++k) {
+                    const unsigned long long a =
+                        (static_cast<unsigned long long>(okey(T.mn(k, r))) << 32) | static_cast<uint32_t>(i);
+                    const unsigned long long b = (static_cast<unsigned long long>(okey(T.mx(k, r))) << 32) |
+                                                 (0xFFFFFFFFu - static_cast<uint32_t>(i));
+                    kmn[k] = a < kmn[k] ? a : kmn[k];
+                    kmx[k] = b > kmx[k] ? b : kmx[k];
                 }
             }
             for (int k = 0; k < 3; ++k) {
-                N.box[k * N.cap + c] = bmn[k];
-                N.box[(3 + k) * N.cap + c] = bmx[k];
+                kmn[k] = warp_min64(kmn[k]);
+                kmx[k] = warp_max64(kmx[k]);
+            }
+            if (lane == 0) {
+                const int32_t c = kid[j];
+                N.start[c] = s + cb[j];
+                N.len[c] = cl[j];
+                N.parent[c] = id;
+                N.left[c] = N.right[c] = -1;
+                for (int k = 0; k < 3; ++k) {  // glm::min(x, acc): the first of equal values
+                    const int32_t pmn = static_cast<int32_t>(static_cast<uint32_t>(kmn[k]));
+                    const int32_t pmx = static_cast<int32_t>(0xFFFFFFFFu - static_cast<uint32_t>(kmx[k]));
+                    const float vmn = T.mn(k, W.ref[pmn]), vmx = T.mx(k, W.ref[pmx]);
+                    N.box[k * N.cap + c] = vmn < kArbMax ? vmn : kArbMax;
+                    N.box[(3 + k) * N.cap + c] = vmx > kArbMin ? vmx : kArbMin;
+                }
             }
         }
-        stack[sp++] = R;
-        stack[sp++] = L;
+        if (lane == 0) {
+            N.left[id] = L;
+            N.right[id] = R;
+            W.stack[sp] = R;
+            W.stack[sp + 1] = L;
+        }
+        sp += 2;
+        __syncwarp();
     }
-}
-
-__global__ void __launch_bounds__(64) k_small(Tri T, Nodes N, const int32_t* __restrict__ list, int32_t count,
-                                              int32_t* refs, int32_t leaf_size, int32_t* node_counter,
-                                              int32_t* fails, int32_t* overflow) {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    small_subtree(T, N, list[i], refs, leaf_size, node_counter, fails, overflow);
 }
 
 // ---- flattening --------------------------------------------------------------------------------
@@ -818,22 +1029,106 @@ __global__ void k_stack_out(Nodes N, int32_t total, int32_t n, int32_t tri_offse
 
 inline unsigned blocks(int64_t n, int b) { return static_cast<unsigned>((n + b - 1) / b); }
 
-// Device allocations of one build, freed on scope exit.
+// Sub-allocator over one device buffer: measure mode (base == nullptr) only adds up the aligned
+// sizes, so the same carve sequence first sizes and then fills the context's build buffer.
 struct Arena {
-    std::vector<void*> ptrs;
-    cudaError_t err = cudaSuccess;
+    char* base = nullptr;
+    size_t used = 0, cap = 0;
+    bool over = false;
     template <class T>
     T* get(int64_t count) {
-        void* p = nullptr;
-        if (err == cudaSuccess) err = cudaMalloc(&p, static_cast<size_t>(std::max<int64_t>(count, 1)) * sizeof(T));
-        if (err != cudaSuccess) return nullptr;
-        ptrs.push_back(p);
-        return static_cast<T*>(p);
-    }
-    ~Arena() {
-        for (void* p : ptrs) cudaFree(p);
+        const size_t bytes = (static_cast<size_t>(std::max<int64_t>(count, 1)) * sizeof(T) + 255) & ~size_t(255);
+        T* p = base ? reinterpret_cast<T*>(base + used) : nullptr;
+        used += bytes;
+        if (base && used > cap) over = true;
+        return p;
     }
 };
+
+// Every device buffer of one build (tree-sized ones at the node capacity 2n + 1).
+struct Buffers {
+    float* verts;
+    uint32_t* idx;
+    int32_t* mesh;
+    float* tb;
+    int32_t *refs, *refs2;
+    uint32_t *pred, *P, *sums;
+    int32_t *ptr, *ptr2;
+    int32_t *nstart, *nlen, *nleft, *nright, *nparent;
+    float* nbox;
+    unsigned long long* ckeys;
+    int32_t *cnt, *large, *next, *small;
+    unsigned *bin_cnt, *bin_kmin, *bin_kmax;
+    int32_t* axis;
+    float* border;
+    int32_t *k_below, *mid, *fallback, *slot_info;
+    Chunk* chunks;
+    unsigned long long* rootkeys;
+    // flattening
+    int32_t *sorted, *size, *arrive, *anc, *anc2;
+    int4* tris;
+    int64_t *val, *val2, *walk;
+    float* F;
+    int32_t *draws, *first, *bfs, *lvl, *lvl2;
+    uint32_t* flag;
+};
+
+void carve(Arena& a, Buffers& b, int64_t n, int64_t n_verts, bool mesh, int layout) {
+    const int64_t cap = 2 * n + 1;
+    const int64_t max_slots = n / (kSmall + 1) + 2;
+    b.verts = a.get<float>(n_verts * 8);
+    b.idx = a.get<uint32_t>(n * 3);
+    b.mesh = mesh ? a.get<int32_t>(n) : nullptr;
+    b.tb = a.get<float>(9 * n);
+    b.refs = a.get<int32_t>(n);
+    b.refs2 = a.get<int32_t>(n);
+    b.pred = a.get<uint32_t>(n);
+    b.P = a.get<uint32_t>(cap + 1);
+    b.sums = a.get<uint32_t>(cap / kScanBlock + 2);
+    b.ptr = a.get<int32_t>(n);
+    b.ptr2 = a.get<int32_t>(n);
+    b.nstart = a.get<int32_t>(cap);
+    b.nlen = a.get<int32_t>(cap);
+    b.nleft = a.get<int32_t>(cap);
+    b.nright = a.get<int32_t>(cap);
+    b.nparent = a.get<int32_t>(cap);
+    b.nbox = a.get<float>(6 * cap);
+    b.ckeys = a.get<unsigned long long>(6 * cap);
+    b.cnt = a.get<int32_t>(16);
+    b.large = a.get<int32_t>(max_slots);
+    b.next = a.get<int32_t>(max_slots);
+    b.small = a.get<int32_t>(n + 1);
+    b.bin_cnt = a.get<unsigned>(max_slots * 3 * kBins);
+    b.bin_kmin = a.get<unsigned>(max_slots * 3 * kBins * 3);
+    b.bin_kmax = a.get<unsigned>(max_slots * 3 * kBins * 3);
+    b.axis = a.get<int32_t>(max_slots);
+    b.border = a.get<float>(max_slots);
+    b.k_below = a.get<int32_t>(max_slots);
+    b.mid = a.get<int32_t>(max_slots);
+    b.fallback = a.get<int32_t>(max_slots);
+    b.slot_info = a.get<int32_t>(2 * max_slots);
+    b.chunks = a.get<Chunk>(n / kChunk + max_slots + 2);
+    b.rootkeys = a.get<unsigned long long>(6);
+    b.sorted = a.get<int32_t>(n);
+    b.tris = a.get<int4>(n);
+    b.size = a.get<int32_t>(cap);
+    b.arrive = a.get<int32_t>(cap);
+    b.val = a.get<int64_t>(cap);
+    b.val2 = a.get<int64_t>(cap);
+    b.anc = a.get<int32_t>(cap);
+    b.anc2 = a.get<int32_t>(cap);
+    b.F = a.get<float>(cap * (layout == 1 ? 8 : 16));
+    if (layout == 1) {
+        b.draws = a.get<int32_t>(cap / 2 + 1);
+        b.first = a.get<int32_t>(cap);
+        b.walk = a.get<int64_t>(cap);
+    } else {
+        b.bfs = a.get<int32_t>(cap);
+        b.lvl = a.get<int32_t>(cap + 1);
+        b.lvl2 = a.get<int32_t>(cap + 1);
+        b.flag = a.get<uint32_t>(cap + 1);
+    }
+}
 
 }  // namespace
 
@@ -847,8 +1142,9 @@ static cudaError_t scan_u32(const uint32_t* in, int64_t n, uint32_t* out, uint32
 }
 
 // GPU build of one object.  Returns RQ_OK and fills `out` like build_bvh, else a status with
-// `why`.  Inputs are host arrays (the rq_build_bvh interface).
-rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std::string& why) {
+// `why`.  Inputs are host arrays (the rq_build_bvh interface).  Device buffers come from one
+// grow-only scratch buffer of the context, so repeated builds allocate nothing.
+rq_status build_bvh_gpu(rq_ctx* ctx, const BuildInput& in, BuildOutput& out, std::string& why) {
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t n = in.n_tris;
     if (!in.vert_records || !in.indices || n <= 0 || in.n_verts <= 0 || in.leaf_size < 1 || in.leaf_size > 15 ||
@@ -863,57 +1159,63 @@ rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std:
             why = "vertex index out of range";
             return RQ_EINVAL;
         }
-    cudaError_t e = cudaSetDevice(device);
+    cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) {
         why = cudaGetErrorString(e);
         return RQ_ECUDA;
     }
-    cudaStream_t st = nullptr;
-    if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) {
-        why = cudaGetErrorString(e);
-        return RQ_ECUDA;
-    }
-    struct StreamGuard {
-        cudaStream_t s;
-        ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
+    cudaStream_t st = ctx->stream;
     const int64_t cap = 2 * n + 1;
-    Arena A;
-    float* d_verts = A.get<float>(in.n_verts * 8);
-    uint32_t* d_idx = A.get<uint32_t>(n * 3);
-    int32_t* d_mesh = in.mesh_ids ? A.get<int32_t>(n) : nullptr;
-    float* d_tb = A.get<float>(9 * n);
-    int32_t* d_refs = A.get<int32_t>(n);
-    int32_t* d_refs2 = A.get<int32_t>(n);
-    uint32_t* d_pred = A.get<uint32_t>(n);
-    uint32_t* d_P = A.get<uint32_t>(std::max<int64_t>(n, cap) + 1);
-    uint32_t* d_sums = A.get<uint32_t>(std::max<int64_t>(n, cap) / kScanBlock + 2);
-    int32_t* d_ptr = A.get<int32_t>(n);
-    int32_t* d_ptr2 = A.get<int32_t>(n);
-    Nodes N{A.get<int32_t>(cap), A.get<int32_t>(cap), A.get<int32_t>(cap), A.get<int32_t>(cap),
-            A.get<int32_t>(cap), A.get<float>(6 * cap), cap};
-    unsigned long long* d_ckeys = A.get<unsigned long long>(6 * cap);
-    int32_t* d_cnt = A.get<int32_t>(16);  // [0] nodes, [1] fails, [2] overflow, [3] next large, [4] small, [5] leaves
-    int32_t* d_large = A.get<int32_t>(n / (kSmall + 1) + 2);
-    int32_t* d_next = A.get<int32_t>(n / (kSmall + 1) + 2);
-    int32_t* d_small = A.get<int32_t>(n + 1);
     const int64_t max_slots = n / (kSmall + 1) + 2;
-    Level L{};
-    L.bin_cnt = A.get<unsigned>(max_slots * 3 * kBins);
-    L.bin_kmin = A.get<unsigned>(max_slots * 3 * kBins * 3);
-    L.bin_kmax = A.get<unsigned>(max_slots * 3 * kBins * 3);
-    L.axis = A.get<int32_t>(max_slots);
-    L.border = A.get<float>(max_slots);
-    L.k_below = A.get<int32_t>(max_slots);
-    L.mid = A.get<int32_t>(max_slots);
-    L.fallback = A.get<int32_t>(max_slots);
-    int32_t* d_slot_info = A.get<int32_t>(2 * max_slots);  // start, len per slot (for the host)
-    Chunk* d_chunks = A.get<Chunk>(n / kChunk + max_slots + 2);
-    unsigned long long* d_rootkeys = A.get<unsigned long long>(6);
-    if (A.err != cudaSuccess) {
-        why = "device allocation failed during GPU BVH build";
-        return RQ_ENOMEM;
+    Buffers B{};
+    {
+        Arena m;
+        carve(m, B, n, in.n_verts, in.mesh_ids != nullptr, in.layout);
+        void* base = nullptr;
+        rq_status s = scratch(ctx, kBuildScratchSlot, m.used, &base);
+        if (s != RQ_OK) {
+            why = "device allocation failed during GPU BVH build";
+            return RQ_ENOMEM;
+        }
+        Arena a;
+        a.base = static_cast<char*>(base);
+        a.cap = m.used;
+        carve(a, B, n, in.n_verts, in.mesh_ids != nullptr, in.layout);
+        if (a.over) {
+            why = "GPU BVH build: buffer layout mismatch";
+            return RQ_EINVAL;
+        }
     }
+    float* d_verts = B.verts;
+    uint32_t* d_idx = B.idx;
+    int32_t* d_mesh = B.mesh;
+    float* d_tb = B.tb;
+    int32_t* d_refs = B.refs;
+    int32_t* d_refs2 = B.refs2;
+    uint32_t* d_pred = B.pred;
+    uint32_t* d_P = B.P;
+    uint32_t* d_sums = B.sums;
+    int32_t* d_ptr = B.ptr;
+    int32_t* d_ptr2 = B.ptr2;
+    Nodes N{B.nstart, B.nlen, B.nleft, B.nright, B.nparent, B.nbox, cap};
+    unsigned long long* d_ckeys = B.ckeys;
+    int32_t* d_cnt = B.cnt;  // [0] nodes, [1] fails, [2] overflow, [3] next large, [4] small, [5] leaves
+    int32_t* d_large = B.large;
+    int32_t* d_next = B.next;
+    int32_t* d_small = B.small;
+    Level L{};
+    L.bin_cnt = B.bin_cnt;
+    L.bin_kmin = B.bin_kmin;
+    L.bin_kmax = B.bin_kmax;
+    L.axis = B.axis;
+    L.border = B.border;
+    L.k_below = B.k_below;
+    L.mid = B.mid;
+    L.fallback = B.fallback;
+    int32_t* d_slot_info = B.slot_info;  // start, len per slot (for the host)
+    Chunk* d_chunks = B.chunks;
+    unsigned long long* d_rootkeys = B.rootkeys;
+    (void)max_slots;
     auto fail_cuda = [&](cudaError_t err, const char* what) {
         why = std::string(what) + ": " + cudaGetErrorString(err);
         return RQ_ECUDA;
@@ -1025,7 +1327,8 @@ rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std:
     }
     GB_CHECK(cudaMemcpyAsync(d_cnt, &node_count, sizeof(int32_t), cudaMemcpyHostToDevice, st));
     if (n_small > 0)
-        k_small<<<blocks(n_small, 64), 64, 0, st>>>(T, N, d_small, n_small, d_refs, in.leaf_size, d_cnt, d_cnt + 1,
+        k_small<<<blocks(n_small, kSmallWarps), 32 * kSmallWarps, 0, st>>>(T, N, d_small, n_small, d_refs,
+                                                                        in.leaf_size, d_cnt, d_cnt + 1,
                                                     d_cnt + 2);
     GB_CHECK(cudaGetLastError());
     int32_t cnt_h[3] = {0, 0, 0};
@@ -1039,19 +1342,15 @@ rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std:
     out.split_fails = cnt_h[1];
 
     // ---- flatten
-    int32_t* d_sorted = A.get<int32_t>(n);
-    int4* d_tris = A.get<int4>(n);
-    int32_t* d_size = A.get<int32_t>(total);
-    int32_t* d_arrive = A.get<int32_t>(total);
-    int64_t* d_val = A.get<int64_t>(total);
-    int64_t* d_val2 = A.get<int64_t>(total);
-    int32_t* d_anc = A.get<int32_t>(total);
-    int32_t* d_anc2 = A.get<int32_t>(total);
-    float* d_F = A.get<float>(static_cast<int64_t>(total) * (in.layout == 1 ? 8 : 16));
-    if (A.err != cudaSuccess) {
-        why = "device allocation failed during GPU BVH flattening";
-        return RQ_ENOMEM;
-    }
+    int32_t* d_sorted = B.sorted;
+    int4* d_tris = B.tris;
+    int32_t* d_size = B.size;
+    int32_t* d_arrive = B.arrive;
+    int64_t* d_val = B.val;
+    int64_t* d_val2 = B.val2;
+    int32_t* d_anc = B.anc;
+    int32_t* d_anc2 = B.anc2;
+    float* d_F = B.F;
     GB_CHECK(cudaMemsetAsync(d_cnt + 5, 0, sizeof(int32_t), st));
     k_leaves<<<blocks(total, 256), 256, 0, st>>>(N, total, static_cast<int32_t>(n), d_refs, d_sorted, d_cnt + 5);
     k_tris_out<<<blocks(n, 256), 256, 0, st>>>(d_idx, d_mesh, n, d_sorted, d_tris);
@@ -1078,13 +1377,9 @@ rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std:
             std::uniform_int_distribution<std::mt19937::result_type> dist(1, 4);
             for (int32_t i = 0; i < n_internal; ++i) draws[i] = static_cast<int32_t>(dist(rng));
         }
-        int32_t* d_draws = A.get<int32_t>(draws.size());
-        int32_t* d_first = A.get<int32_t>(total);
-        int64_t* d_walk = A.get<int64_t>(total);
-        if (A.err != cudaSuccess) {
-            why = "device allocation failed during GPU BVH flattening";
-            return RQ_ENOMEM;
-        }
+        int32_t* d_draws = B.draws;
+        int32_t* d_first = B.first;
+        int64_t* d_walk = B.walk;
         GB_CHECK(cudaMemcpyAsync(d_draws, draws.data(), sizeof(int32_t) * draws.size(), cudaMemcpyHostToDevice, st));
         int64_t* val = d_val;
         int32_t* anc = d_anc;
@@ -1101,14 +1396,10 @@ rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std:
         out.nodes.resize(static_cast<size_t>(total) * 8);
     } else {
         GB_CHECK(cudaMemsetAsync(d_F, 0, sizeof(float) * 16 * static_cast<int64_t>(total), st));
-        int32_t* d_bfs = A.get<int32_t>(total);
-        int32_t* d_lvl = A.get<int32_t>(total + 1);
-        int32_t* d_lvl2 = A.get<int32_t>(total + 1);
-        uint32_t* d_flag = A.get<uint32_t>(total + 1);
-        if (A.err != cudaSuccess) {
-            why = "device allocation failed during GPU BVH flattening";
-            return RQ_ENOMEM;
-        }
+        int32_t* d_bfs = B.bfs;
+        int32_t* d_lvl = B.lvl;
+        int32_t* d_lvl2 = B.lvl2;
+        uint32_t* d_flag = B.flag;
         const int32_t zero = 0;
         GB_CHECK(cudaMemcpyAsync(d_lvl, &zero, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         int32_t count = 1, bfs_base = 0;

@@ -310,7 +310,7 @@ rq_status rq_build_bvh_gpu(rq_ctx* ctx, const rq_vertex* verts, int64_t n_verts,
     std::string why;
     rq_status s;
     try {
-        s = rq::build_bvh_gpu(ctx->device, in, b->out, why);
+        s = rq::build_bvh_gpu(ctx, in, b->out, why);
     } catch (const std::bad_alloc&) {
         delete b;
         return fail(ctx, RQ_ENOMEM, "host allocation failed during GPU BVH build");

@@ -93,8 +93,10 @@ inline unsigned long long* queue_counter(rq_ctx* ctx, int k) {
     return reinterpret_cast<unsigned long long*>(ctx->counters) + 16 + k;
 }
 // GPU build of one object's BVH2 (bvh_build_gpu.cu): the buffers build_bvh produces, from host
-// input arrays, on `device`.  RQ_OK, or a status with `why` set.
-rq_status build_bvh_gpu(int device, const BuildInput& in, BuildOutput& out, std::string& why);
+// input arrays, on the context's device.  RQ_OK, or a status with `why` set.
+rq_status build_bvh_gpu(rq_ctx* ctx, const BuildInput& in, BuildOutput& out, std::string& why);
+// Scratch slot holding the GPU BVH build's buffers.
+constexpr int kBuildScratchSlot = 12;
 // Grow-only device scratch buffer of the context (slot < kScratchSlots).
 rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out);
 
