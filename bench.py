@@ -607,6 +607,15 @@ def main():
         print(json.dumps({"profile_case": wl["name"], "pixels": n, "bvh8_nodes": b8["nodes"]}))
         return
 
+    # the same BVH built on the GPU (rq_build_bvh_gpu): time and byte identity with the host build
+    gpu_builds = [R.build_bvh(wl["mesh"].vertices, wl["mesh"].indices, wl["mesh"].mesh_ids, 0, layout=R.STACK,
+                              ctx=ctx) for _ in range(3)]
+    bvh_build = {"host_ms": round(wl["build_s"] * 1e3, 1), "host_threads": os.cpu_count() or 1,
+                 "gpu_ms": round(min(b.build_ms for b in gpu_builds[1:]), 2),
+                 "gpu_identical_bytes": bool(np.array_equal(gpu_builds[-1].nodes.view(np.uint32),
+                                                            wl["bvh"].nodes.view(np.uint32))
+                                             and np.array_equal(gpu_builds[-1].tris, wl["bvh"].tris))}
+    del gpu_builds
     # ---- set-up (untimed): BVH8, secondary rays of one pass, autotuning, ray counts
     b8 = sc.build_bvh8()
     d_hits = sc.closest(d_rays, stream=sptr)
@@ -793,6 +802,7 @@ def main():
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},
             "e2e": e2e, "roofline": roofline, "breakdown": breakdown, "bvh8q_vs_strict": agreement,
+            "bvh_build": bvh_build,
             "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
                              "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}
