@@ -160,6 +160,34 @@ def make_workload(config: str):
                 params=params, name=name, albedo=albedo, build_s=build_s)
 
 
+def collide_boxes(wl, n: int = 1 << 20) -> np.ndarray:
+    """Collision query boxes for the scene: centred within 0.05 of a random vertex, half-extents
+    0.002-0.03 (the reference's player query is a box of half-extent 0.1)."""
+    from candela_gb300 import scenes as S
+    pos = wl["mesh"].positions()
+    pick = (S.uniform(3, 7, n) * pos.shape[0]).astype(np.int64)
+    boxes = S.query_boxes(n, (-0.05,) * 3, (0.05,) * 3, 0.002, 0.03, seed=4)
+    boxes[:, 0:3] += pos[pick]
+    boxes[:, 4:7] += pos[pick]
+    return boxes
+
+
+def cpu_collide(wl):
+    """The CPU restatement of the collision queries on all host cores: the same 1M boxes as the
+    GPU leg, once per layout."""
+    from oracle import oracle as O
+    nthreads = os.cpu_count() or 1
+    boxes = collide_boxes(wl)
+    out = {"boxes": len(boxes), "cores": nthreads, "kind": "port"}
+    for name, lay, bvh, ent in (("stack", O.ORC_STACK, wl["bvh"], wl["ent"]),
+                                ("stackless", O.ORC_STACKLESS, wl["bvh_sl"], wl["ent_sl"])):
+        osc = O.OracleScene(lay, wl["mesh"].vertices, bvh.tris, bvh.nodes, ent)
+        t0 = time.perf_counter()
+        osc.collide(boxes, nthreads=nthreads)
+        out[f"{name}_mboxes_s"] = round(len(boxes) / (time.perf_counter() - t0) / 1e6, 2)
+    return out
+
+
 def cpu_baseline(wl, seconds: float):
     """The CPU restatement of the reference path on all host cores, on a bounded sample:
     repeated whole-pass runs over a prefix of the primary rays until `seconds` elapse."""
@@ -749,6 +777,22 @@ def main():
                  "anyhit_identical": float((o_strict == o_b8).mean()),
                  "rays": n_sec_slots, "device_status": ctx.device_status()}
 
+    # ---- AABB collision queries (rq_collide) over the same scene: 1M boxes near the surface
+    boxes = collide_boxes(wl)
+    n_box = len(boxes)
+    d_boxes = torch.from_numpy(boxes).to(dev)
+    d_coll = torch.empty((n_box, 4), dtype=torch.int32, device=dev)
+    coll_ms = timed(lambda: sc.collide(d_boxes, out=d_coll, stream=sptr))
+    coll_sl_ms = timed(lambda: sc_sl.collide(d_boxes, out=d_coll, stream=sptr))
+    collided = float(sc.collide(d_boxes, out=d_coll, stream=sptr)[:, 0].float().mean().item())
+    collide = {"boxes": n_box, "collided_frac": round(collided, 4),
+               "stack_mboxes_s": round(n_box / (coll_ms / 1e3) / 1e6, 1), "stack_ms": round(coll_ms, 4),
+               "stackless_mboxes_s": round(n_box / (coll_sl_ms / 1e3) / 1e6, 1),
+               "stackless_ms": round(coll_sl_ms, 4),
+               "boxes_desc": "centred within 0.05 of a random vertex, half-extents 0.002-0.03"}
+    if rank == 0:
+        collide["cpu_baseline"] = cpu_collide(wl)
+
     # ---- roofline of the dominant kernel (secondary closest / AO any-hit on BVH8q)
     dom = "secondary_anyhit_bvh8q" if q_any else "secondary_closest_bvh8q"
     ref = "secondary_anyhit_strict_stack" if q_any else "secondary_closest_strict_stack"
@@ -802,7 +846,7 @@ def main():
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},
             "e2e": e2e, "roofline": roofline, "breakdown": breakdown, "bvh8q_vs_strict": agreement,
-            "bvh_build": bvh_build,
+            "bvh_build": bvh_build, "collide": collide,
             "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
                              "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}

@@ -146,6 +146,7 @@ SIGNATURES = {
     "rq_batch_plan_destroy": (_S, [_P]),
     "rq_gi_frame_noalloc": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                                  _P]),
+    "rq_collide": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
 }
 
 NOALLOC_MAX_RAYS = 65536

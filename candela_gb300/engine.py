@@ -262,6 +262,42 @@ class Scene:
                               _stream(rays, stream)), self.ctx.handle)
         return out
 
+    def collide(self, boxes, out=None, *, flags=0, stream=None):
+        """First (entity, mesh, triangle) each box overlaps (rq_collide; CollideScene of
+        Collide.comp).  `boxes` is a float32 (n, 8) array {min.xyzw, max.xyzw} on the host
+        (copies inside the call) or a CUDA tensor; returns int32 (n, 4) rows
+        {collided, entity, mesh, tri}, {0, -1, -1, -1} for a box that overlaps nothing."""
+        host = isinstance(boxes, np.ndarray)
+        if host:
+            boxes = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 8)
+            n = boxes.shape[0]
+        else:
+            n = boxes.numel() * boxes.element_size() // 32
+        if out is None:
+            if host:
+                out = np.empty((n, 4), dtype=np.int32)
+            else:
+                import torch
+                out = torch.empty((n, 4), dtype=torch.int32, device=boxes.device)
+        o = _opts(flags=flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        check(lib().rq_collide(self.ctx.handle, self.handle, ptr(boxes), n, ptr(out), C.byref(o),
+                               _stream(boxes, stream)), self.ctx.handle)
+        return out
+
+    def collide_box(self, bmin, bmax, **kw) -> bool:
+        """Physics::CollideBox (Physics.cpp:203-228): does the world-space box touch the scene."""
+        b = np.array([[*bmin, 0.0, *bmax, 0.0]], dtype=np.float32)
+        return bool(self.collide(b, **kw)[0, 0])
+
+    def collide_points(self, points, half=0.01, **kw):
+        """Physics::CollidePoint (Physics.cpp:176-201) for many points: each point is the box
+        point -/+ half (0.01 in the reference); returns the rq_collide rows."""
+        p = np.asarray(points, dtype=np.float32).reshape(-1, 3)
+        b = np.zeros((p.shape[0], 8), dtype=np.float32)
+        b[:, 0:3] = p - np.float32(half)
+        b[:, 4:7] = p + np.float32(half)
+        return self.collide(b, **kw)
+
 
 def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode=0, query=0,
               shadow_rays=False, shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866),

@@ -2,13 +2,15 @@
 //
 // Reads objects (raw vertex / index files), adds them with AddObject, pushes translated entities,
 // and writes the global buffers the reference would upload to its SSBOs.  With --gpu it uploads the
-// scene (BufferData) and writes the closest-hit and any-hit results for a ray file.
+// scene (BufferData) and writes the closest-hit and any-hit results for a ray file, and the
+// collision records for a box file when one is present.
 //
 //   rq_intersector_example <stack|stackless> <input dir> <output dir> [--gpu]
 //
 // Input dir: objects.txt ("<count>" then per object "<id> <mesh number>"), verts_<k>.bin
 // (32-byte rq_vertex records), idx_<k>.bin (uint32, 3 per triangle), entities.txt (per line
-// "<object id> <tx> <ty> <tz> <translucency>"), rays.bin (32-byte rq_ray records, --gpu only).
+// "<object id> <tx> <ty> <tz> <translucency>"), rays.bin (32-byte rq_ray records, --gpu only),
+// boxes.bin (optional, 32-byte rq_box records, --gpu only).
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -77,6 +79,8 @@ int run(const std::string& in, const std::string& out, bool gpu) {
         const std::vector<rq_ray> rays = read_raw<rq_ray>(in + "/rays.bin");
         write_raw(out + "/hits.bin", ri.Intersect(rays));
         write_raw(out + "/occ.bin", ri.Occluded(rays));
+        if (std::ifstream(in + "/boxes.bin").good())
+            write_raw(out + "/coll.bin", ri.Collide(read_raw<rq_box>(in + "/boxes.bin")));
     }
     std::cout << "objects " << count << " nodes " << ri.m_BVHNodes.size() << " triangles "
               << ri.m_BVHTriangles.size() << " entities " << ri.m_BVHEntities.size() << "\n";

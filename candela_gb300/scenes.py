@@ -324,6 +324,20 @@ def sphere_rays(n: int, lo, hi, seed: int = 4, tmax: float = 1000000.0) -> np.nd
     return r
 
 
+def query_boxes(n: int, lo, hi, half_lo: float, half_hi: float, seed: int = 6) -> np.ndarray:
+    """Collision query boxes ((n, 8) float32 {min.xyz, 1, max.xyz, 1}): centres uniform in
+    [lo, hi], half-extents per axis uniform in [half_lo, half_hi]."""
+    u = uniform(seed, 404, n * 6).reshape(n, 6)
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    c = lo + (hi - lo) * u[:, :3]
+    h = half_lo + (half_hi - half_lo) * u[:, 3:]
+    b = np.ones((n, 8), dtype=np.float32)
+    b[:, 0:3] = (c - h).astype(np.float32)
+    b[:, 4:7] = (c + h).astype(np.float32)
+    return b
+
+
 # ---------------------------------------------------------------------------------------------
 # Named workloads
 

@@ -340,6 +340,35 @@ typedef struct rq_batch_tune {
 rq_status rq_batch_plan_autotune(rq_batch_plan* plan, int32_t allow_bvh8, rq_batch_tune* out);
 rq_status rq_batch_plan_destroy(rq_batch_plan* plan);
 
+/* ---- AABB collision queries ---------------------------------------------------------------- */
+
+/* A world-space query box (xyz used; w ignored), the AABB that Collide.comp reads per entity. */
+typedef struct rq_box {
+    float min[4];
+    float max[4];
+} rq_box;
+/* First overlap found for a query box: collided = 1, the entity index, the triangle's mesh id and
+ * the triangle index; {0, -1, -1, -1} when the box overlaps nothing. */
+typedef struct rq_collision {
+    int32_t collided, entity, mesh, tri;
+} rq_collision;
+
+/* Box/triangle collision queries over the scene's BVH2.  Replaces CollideScene (Shaders/
+ * Intersectors/Include/CollideBVHStack.glsl:301-323, CollideBVHStackless.glsl:225-247) as
+ * dispatched by Collide.comp:34, and Physics::CollideBox / CollidePoint (Physics.cpp:176-228,
+ * a point is the box point -/+ 0.01).  Each box is moved into every entity's object space by its
+ * inverse matrix (the two corners, as the reference does) and the entity's BVH is walked: the
+ * stack layout descends the overlapping children nearest-centre first (AABBAABBOverlapF), the
+ * stackless layout follows the skip links; leaf triangles take the separating-axis test over the
+ * nine edge axes.  Entities are tried in order and the first triangle found wins.  Default: the
+ * nine distinct axes and the global triangle index.  RQ_FLAG_REF_COMPAT reproduces the
+ * reference: axis 5 repeats cross(u2, f2) (the reference writes AxisUxFx[5] = cross(u2, f2) where
+ * cross(u1, f2) belongs) and the stack walk reports the index within the leaf.
+ * RQ_FLAG_HOST_BUFFERS: boxes/out are host memory.  Strict FP32 arithmetic; RQ_ENOTSUP for a
+ * layout other than the scene's BVH2. */
+rq_status rq_collide(rq_ctx* ctx, const rq_scene* scene, const rq_box* boxes, int64_t n,
+                     rq_collision* out, const rq_opts* opts, void* stream);
+
 /* ---- Diffuse GI / RTAO ------------------------------------------------------------------ */
 
 /* Parameters of the GI / AO pass that consumes the queries (Shaders/DiffuseTrace.glsl:386-662). */

@@ -238,6 +238,29 @@ class RayIntersector {
         return occ;
     }
 
+    // Collision queries (Collide.comp): the first {collided, entity, mesh, triangle} per box.
+    std::vector<rq_collision> Collide(const std::vector<rq_box>& boxes, rq_opts opts = rq_opts{}) const {
+        std::vector<rq_collision> out(boxes.size());
+        opts.flags |= RQ_FLAG_HOST_BUFFERS;
+        check(rq_collide(ctx_, need_scene(), boxes.data(), static_cast<int64_t>(boxes.size()), out.data(), &opts,
+                         nullptr),
+              ctx_);
+        return out;
+    }
+
+    // Physics::CollideBox (Physics.cpp:203-228).
+    bool CollideBox(const float min[3], const float max[3]) const {
+        rq_box b = {{min[0], min[1], min[2], 1.0f}, {max[0], max[1], max[2], 1.0f}};
+        return Collide({b})[0].collided != 0;
+    }
+
+    // Physics::CollidePoint (Physics.cpp:176-201): the box point -/+ 0.01.
+    bool CollidePoint(const float p[3]) const {
+        const float lo[3] = {p[0] - 0.01f, p[1] - 0.01f, p[2] - 0.01f};
+        const float hi[3] = {p[0] + 0.01f, p[1] + 0.01f, p[2] + 0.01f};
+        return CollideBox(lo, hi);
+    }
+
     rq_scene* scene() const { return scene_; }
     const std::unordered_map<int32_t, ObjectData>& objects() const { return m_ObjectData; }
 

@@ -69,6 +69,7 @@ def orc() -> C.CDLL:
                                     C.c_int, P]
         L.orc_shade.argtypes = [sp, P, P, I64, P, P, I32, P, P, P, I32, C.c_int, P]
         L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
+        L.orc_collide.argtypes = [sp, P, I64, P, C.c_int, C.c_int]
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
         L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -117,6 +118,15 @@ class OracleScene:
         orc().orc_gi_raygen(C.byref(self.s), _p(primary), _p(hits), primary.shape[0], spp,
                             seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode,
                             nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def collide(self, boxes, flags=0, nthreads=None):
+        """Collide.comp for n query boxes ((n, 8) float32: min xyzw, max xyzw): (n, 4) int32
+        {collided, entity, mesh, tri}."""
+        boxes = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 8)
+        out = np.empty((boxes.shape[0], 4), dtype=np.int32)
+        orc().orc_collide(C.byref(self.s), _p(boxes), boxes.shape[0], _p(out), flags,
+                          nthreads or os.cpu_count() or 1)
         return out
 
     def shadow_raygen(self, rays, hits, sun_dir, origin_offset, normal_mode=0, nthreads=None):

@@ -443,6 +443,163 @@ void parallel_for(int64_t n, int nthreads, F f) {
     for (auto& x : th) x.join();
 }
 
+// ---- AABB collision queries -------------------------------------------------------------------
+// Collide.comp with Include/CollideBVHStack.glsl (stack layout) and
+// Include/CollideBVHStackless.glsl (stackless layout; the same walk as Physics.cpp:79-174).
+
+// BoxTriangleOverlap, CollideBVHStack.glsl:104-152 / Physics.cpp:29-77: separating-axis test on the
+// nine edge cross products, with the full box extent as e.  The reference fills AxisUxFx[5] with
+// cross(u2, f2) (a repeat of [8]) where cross(u1, f2) belongs; ref_axis keeps that.
+bool box_triangle_overlap(V3 v0, V3 v1, V3 v2, V3 bmin, V3 bmax, bool ref_axis) {
+    const V3 c = {(bmin.x + bmax.x) / 2.0f, (bmin.y + bmax.y) / 2.0f, (bmin.z + bmax.z) / 2.0f};
+    const V3 e = sub(bmax, bmin);
+    v0 = sub(v0, c);
+    v1 = sub(v1, c);
+    v2 = sub(v2, c);
+    const V3 f0 = sub(v1, v0), f1 = sub(v2, v1), f2 = sub(v0, v2);
+    const V3 u0 = {1.0f, 0.0f, 0.0f}, u1 = {0.0f, 1.0f, 0.0f}, u2 = {0.0f, 0.0f, 1.0f};
+    V3 ax[9];
+    ax[0] = cross(u0, f0);
+    ax[1] = cross(u0, f1);
+    ax[2] = cross(u0, f2);
+    ax[3] = cross(u1, f0);
+    ax[4] = cross(u1, f1);
+    ax[5] = ref_axis ? cross(u2, f2) : cross(u1, f2);
+    ax[6] = cross(u2, f0);
+    ax[7] = cross(u2, f1);
+    ax[8] = cross(u2, f2);
+    for (int i = 0; i < 9; ++i) {
+        const V3 a = ax[i];
+        const float p0 = dot(v0, a), p1 = dot(v1, a), p2 = dot(v2, a);
+        float r = e.x * std::fabs(dot(u0, a));
+        r = r + e.y * std::fabs(dot(u1, a));
+        r = r + e.z * std::fabs(dot(u2, a));
+        if (gmax(-gmax(gmax(p0, p1), p2), gmin(gmin(p0, p1), p2)) > r) return false;
+    }
+    return true;
+}
+
+// AABBAABBOverlap and AABBAABBOverlapF (squared centre distance, -1 when apart),
+// CollideBVHStack.glsl:90-102 (Physics.cpp:23-27).
+inline bool aabb_overlap(V3 amin, V3 amax, V3 bmin, V3 bmax) {
+    return (amin.x <= bmax.x && amax.x >= bmin.x) && (amin.y <= bmax.y && amax.y >= bmin.y) &&
+           (amin.z <= bmax.z && amax.z >= bmin.z);
+}
+inline float aabb_overlap_f(V3 amin, V3 amax, V3 bmin, V3 bmax) {
+    const bool hit = aabb_overlap(amin, amax, bmin, bmax);
+    const V3 ca = {(amin.x + amax.x) / 2.0f, (amin.y + amax.y) / 2.0f, (amin.z + amax.z) / 2.0f};
+    const V3 cb = {(bmin.x + bmax.x) / 2.0f, (bmin.y + bmax.y) / 2.0f, (bmin.z + bmax.z) / 2.0f};
+    const V3 d = sub(cb, ca);
+    const float dist = dot(d, d);
+    return hit ? dist : -1.0f;
+}
+
+// One leaf's triangles against the box; tri = the reported index (the reference's stack walk
+// reports the index inside the leaf, ref_tri).
+inline bool collide_leaf(const Scene& s, int32_t packed, V3 bmin, V3 bmax, bool ref_axis, bool leaf_index,
+                         int32_t& mesh, int32_t& tri) {
+    const int32_t st = packed >> 4, len = packed & 0xF;
+    for (int32_t i = 0; i < len; ++i) {
+        const int32_t* t = s.tris + (int64_t)(st + i) * 4;
+        if (box_triangle_overlap(vpos(s, t[0]), vpos(s, t[1]), vpos(s, t[2]), bmin, bmax, ref_axis)) {
+            mesh = t[3];
+            tri = leaf_index ? i : st + i;
+            return true;
+        }
+    }
+    return false;
+}
+
+// CollideBVH, CollideBVHStack.glsl:154-299.
+bool collide_bvh_stack(const Scene& s, V3 bmin, V3 bmax, int32_t start, int32_t count, bool ref, int32_t& mesh,
+                       int32_t& tri) {
+    int32_t stack[64];
+    int32_t sp = 0, iters = 0, cur = start;
+    while (iters < 1024) {
+        if (sp >= 64 || sp < 0 || cur < start || cur > start + count || cur < 0 || cur >= s.n_nodes) break;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)cur * 16;
+        const V3 lmin = ld3(nd), lmax = ld3(nd + 4), rmin = ld3(nd + 8), rmax = ld3(nd + 12);
+        const int32_t lw = f2i(nd[3]), rw = f2i(nd[11]);
+        const bool ll = lw != -1, rl = rw != -1;
+        const float lt = ll ? -1.0f : aabb_overlap_f(lmin, lmax, bmin, bmax);
+        const float rt = rl ? -1.0f : aabb_overlap_f(rmin, rmax, bmin, bmax);
+        if (ll && collide_leaf(s, lw, bmin, bmax, ref, ref, mesh, tri)) return true;
+        if (rl && collide_leaf(s, rw, bmin, bmax, ref, ref, mesh, tri)) return true;
+        if (lt > 0.0f && rt > 0.0f) {
+            int32_t a = f2i(nd[7]) + start, b = f2i(nd[15]) + start;
+            if (rt < lt) {
+                const int32_t x = a;
+                a = b;
+                b = x;
+            }
+            cur = a;
+            if (sp >= 63) break;
+            stack[sp++] = b;
+            continue;
+        } else if (lt > 0.0f) {
+            cur = f2i(nd[7]) + start;
+            continue;
+        } else if (rt > 0.0f) {
+            cur = f2i(nd[15]) + start;
+            continue;
+        }
+        if (sp <= 0) break;
+        cur = stack[--sp];
+    }
+    return false;
+}
+
+// CollideBVH, CollideBVHStackless.glsl:131-223 (Physics.cpp:79-174).
+bool collide_bvh_stackless(const Scene& s, V3 bmin, V3 bmax, int32_t start, int32_t count, bool ref,
+                           int32_t& mesh, int32_t& tri) {
+    int32_t iters = 0, ptr = start;
+    while (ptr >= 0 && iters < 1024) {
+        if (ptr < start || ptr > start + count || ptr < 0 || ptr >= s.n_nodes) break;
+        ++iters;
+        const float* nd = s.nodes + (int64_t)ptr * 8;
+        if (aabb_overlap(ld3(nd), ld3(nd + 4), bmin, bmax)) {
+            const int32_t packed = f2i(nd[3]);
+            if (packed != -1) {
+                if (collide_leaf(s, packed, bmin, bmax, ref, false, mesh, tri)) return true;
+                const int32_t nx = f2i(nd[7]);
+                if (nx < 0) break;
+                ptr = nx + start;
+                continue;
+            }
+            ++ptr;
+            continue;
+        }
+        const int32_t nx = f2i(nd[7]);
+        if (nx < 0) break;
+        ptr = nx + start;
+    }
+    return false;
+}
+
+// CollideScene, CollideBVHStack.glsl:301-323 (CollideBVHStackless.glsl:225-247): entities in order, the first collision wins; the box
+// corners are moved by the entity's inverse matrix (two corners, as the reference does).
+void collide_scene(const Scene& s, const float box[8], bool ref, int32_t out[4]) {
+    out[0] = 0;
+    out[1] = out[2] = out[3] = -1;
+    const V3 wmin = ld3(box), wmax = ld3(box + 4);
+    for (int i = 0; i < s.n_ents; ++i) {
+        const orc_entity& e = s.ents[i];
+        const V3 bmin = xform(e.inverse, wmin, 1.0f), bmax = xform(e.inverse, wmax, 1.0f);
+        int32_t mesh = -1, tri = -1;
+        const bool hit = s.layout == ORC_STACKLESS
+                             ? collide_bvh_stackless(s, bmin, bmax, e.node_offset, e.node_count, ref, mesh, tri)
+                             : collide_bvh_stack(s, bmin, bmax, e.node_offset, e.node_count, ref, mesh, tri);
+        if (hit) {
+            out[0] = 1;
+            out[1] = i;
+            out[2] = mesh;
+            out[3] = tri;
+            return;
+        }
+    }
+}
+
 // ---- GI ray generation and shading ---------------------------------------------------------
 
 // Exact binary16 -> binary32 conversion (GLSL unpackHalf2x16 component).
@@ -699,6 +856,14 @@ void orc_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, in
             o[0] = rad.x; o[1] = rad.y; o[2] = rad.z;
             o[3] = std::pow(clamp01(h.t / 2.4f), 1.23f);  // DiffuseTrace.glsl:494
         }
+    });
+}
+
+void orc_collide(const orc_scene* sc, const float* boxes, int64_t n, int32_t* out, int flags, int nthreads) {
+    const Scene s = make_scene(sc);
+    const bool ref = (flags & ORC_FLAG_REF_COMPAT) != 0;
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) collide_scene(s, boxes + i * 8, ref, out + i * 4);
     });
 }
 

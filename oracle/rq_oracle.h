@@ -90,6 +90,11 @@ void orc_shadow_raygen(const orc_scene* s, const orc_ray* rays, const orc_hit* h
 
 // Counter-based hash (Jarzynski & Olano 2020, "pcg_hash") and the turn-based sine/cosine used
 // by the GI ray generator, exposed for tests.
+// AABB collision queries (Collide.comp): boxes = n x {min[4], max[4]} (w unused), out = n x
+// {collided, entity, mesh, tri} (-1 fields when nothing collides).  ORC_FLAG_REF_COMPAT keeps the
+// reference's repeated separating axis and, for the stack layout, the within-leaf triangle index.
+void orc_collide(const orc_scene* s, const float* boxes, int64_t n, int32_t* out, int flags, int nthreads);
+
 uint32_t orc_pcg_hash(uint32_t x);
 void orc_sincos_turns(float x, float* s, float* c);
 

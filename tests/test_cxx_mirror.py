@@ -73,6 +73,8 @@ def test_cxx_mirror_rejects_unknown_object(tmp_path):
 def test_cxx_mirror_queries_on_gpu(ctx, tmp_path, name):
     rays = S.sphere_rays(50_000, (-1.5, -1.5, -0.5), (1.5, 1.5, 1.5), seed=31)
     objs = _write_inputs(tmp_path, rays)
+    boxes = S.query_boxes(20_000, (-1.2, -1.2, -0.4), (1.2, 1.2, 1.2), 0.005, 0.1, seed=32)
+    boxes.tofile(tmp_path / "boxes.bin")
     r = subprocess.run([str(_build.EXAMPLE), name, str(tmp_path), str(tmp_path), "--gpu"],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -82,3 +84,7 @@ def test_cxx_mirror_queries_on_gpu(ctx, tmp_path, name):
     assert_hits_identical(hits, osc.closest(rays), "C++ mirror")
     occ = np.fromfile(tmp_path / "occ.bin", dtype=np.uint8)
     np.testing.assert_array_equal(occ, osc.anyhit(rays))
+    coll = np.fromfile(tmp_path / "coll.bin", dtype=np.int32).reshape(-1, 4)
+    want = osc.collide(boxes)
+    np.testing.assert_array_equal(coll, want)
+    assert 0 < want[:, 0].sum() < len(boxes)
