@@ -20,6 +20,7 @@ MODE_STRICT, MODE_FAST = 0, 1
 TIE_LOWER_INDEX, TIE_FIRST_FOUND = 0, 1
 FLAG_REF_COMPAT, FLAG_IGNORE_TRANSPARENT, FLAG_HOST_BUFFERS, FLAG_NO_PERSISTENT = 1, 2, 4, 8
 FLAG_COUNT = 16
+FLAG_ENTITY_LOOP = 32
 
 VERTEX_DTYPE = np.dtype([("pos", "<f4", (4,)), ("packed", "<u4", (4,))])
 TRI_DTYPE = np.dtype(("<i4", (4,)))
@@ -147,6 +148,7 @@ SIGNATURES = {
     "rq_gi_frame_noalloc": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P,
                                  _P]),
     "rq_collide": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
+    "rq_scene_tlas_info": (_S, [_P, C.POINTER(C.c_int64 * 3)]),
 }
 
 NOALLOC_MAX_RAYS = 65536

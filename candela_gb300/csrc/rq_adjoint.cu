@@ -471,6 +471,8 @@ rq_status rq_scene_update_positions(rq_scene* sc, const float* xyz, void* stream
     RQ_CUDA(ctx, rq::launch_tri_fast(sc->d_tris, sc->n_tris, sc->d_verts, sc->d_tri_fast, st));
     RQ_CUDA(ctx, cudaGetLastError());
     sc->bvh8 = false;          // quantised boxes are not refitted
+    sc->view.tlas = nullptr;   // nor are the top-level boxes: every entity is walked until the
+                               // entities or the BVH8 are set again
     sc->host_stale = true;     // host copies of vertices / nodes are refreshed on demand
     return RQ_OK;
 }

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -12,6 +13,7 @@
 #include "bvh8.h"
 #include "bvh_build.h"
 #include "rq_internal.h"
+#include "tlas.h"
 #include "rq_objects.h"
 #include "rq_validate.h"
 
@@ -84,6 +86,87 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
         return RQ_OK;
     }
     if (q.layout != sc->layout) return fail(ctx, RQ_ENOTSUP, "layout not built for this scene");
+    return RQ_OK;
+}
+
+rq_status refresh_host(rq_scene* sc) {
+    if (!sc->host_stale) return RQ_OK;
+    rq_ctx* ctx = sc->ctx;
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    RQ_CUDA(ctx, cudaDeviceSynchronize());
+    RQ_CUDA(ctx, cudaMemcpy(sc->h_nodes.data(), sc->d_nodes, sc->h_nodes.size() * 4, cudaMemcpyDeviceToHost));
+    RQ_CUDA(ctx, cudaMemcpy(sc->h_verts.data(), sc->d_verts, sc->h_verts.size() * 4, cudaMemcpyDeviceToHost));
+    sc->host_stale = false;
+    return RQ_OK;
+}
+
+rq_status rebuild_tlas(rq_scene* sc) {
+    rq_ctx* ctx = sc->ctx;
+    sc->view.tlas = nullptr;
+    sc->view.tlas_pre = nullptr;
+    sc->tlas_nodes = sc->tlas_cullable = 0;
+    if (sc->d_tlas) cudaFree(sc->d_tlas);
+    if (sc->d_tlas_pre) cudaFree(sc->d_tlas_pre);
+    sc->d_tlas = nullptr;
+    sc->d_tlas_pre = nullptr;
+    sc->tlas_bytes = 0;
+    const int32_t n = sc->n_ents;
+    if (n < kTlasMinEntities) return RQ_OK;
+    rq_status s = refresh_host(sc);
+    if (s != RQ_OK) return s;
+    std::vector<TlasEntity> te(n);
+    const bool stack = sc->layout == RQ_LAYOUT_BVH2_STACK;
+    for (int32_t i = 0; i < n; ++i) {
+        const rq_entity& e = sc->h_ents[i];
+        TlasEntity& t = te[i];
+        std::memcpy(t.inverse, e.inverse, sizeof(t.inverse));
+        float alpha;
+        std::memcpy(&alpha, &e.data[1], 4);
+        t.opaque = !(alpha < 0.99f);  // IntersectSceneIgnoreTransparent skips alpha < 0.99
+        t.b8 = sc->bvh8 && static_cast<size_t>(i) < sc->h_b8roots.size() && sc->h_b8roots[i] >= 0;
+        t.cullable = false;
+        const int64_t off = e.node_offset;
+        if (off < 0 || off >= sc->n_nodes || e.node_count < 0) continue;
+        const float* nd = sc->h_nodes.data() + off * (stack ? 16 : 8);
+        int32_t w0, w1;
+        if (stack) {  // both root children must be internal: leaf children are tested box-free
+            std::memcpy(&w0, &nd[3], 4);
+            std::memcpy(&w1, &nd[11], 4);
+            if (w0 != -1 || w1 != -1) continue;
+            for (int a = 0; a < 3; ++a) {
+                t.lo[a] = std::min(nd[a], nd[8 + a]);
+                t.hi[a] = std::max(nd[4 + a], nd[12 + a]);
+            }
+        } else {  // the root's box is tested first; its skip link must end the walk
+            std::memcpy(&w1, &nd[7], 4);
+            if (w1 != -1) continue;
+            for (int a = 0; a < 3; ++a) {
+                t.lo[a] = nd[a];
+                t.hi[a] = nd[4 + a];
+            }
+        }
+        if (t.b8 && sc->b8_bounds[6 * i] <= sc->b8_bounds[6 * i + 3])
+            for (int a = 0; a < 3; ++a) {
+                t.lo[a] = std::min(t.lo[a], sc->b8_bounds[6 * i + a]);
+                t.hi[a] = std::max(t.hi[a], sc->b8_bounds[6 * i + 3 + a]);
+            }
+        t.cullable = true;
+    }
+    TlasOut out;
+    std::string why;
+    if (!build_tlas(te, out, why)) return fail(ctx, RQ_EINVAL, "top-level build: " + why);
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t nb = out.nodes.size() * 4, pb = out.prefix.size() * 4;
+    if (cudaMalloc(&sc->d_tlas, nb) != cudaSuccess || cudaMalloc(&sc->d_tlas_pre, pb) != cudaSuccess)
+        return fail(ctx, RQ_ENOMEM, "top-level allocation failed");
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_tlas, out.nodes.data(), nb, cudaMemcpyHostToDevice));
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_tlas_pre, out.prefix.data(), pb, cudaMemcpyHostToDevice));
+    sc->tlas_bytes = static_cast<int64_t>(nb + pb);
+    sc->tlas_nodes = out.n_nodes;
+    sc->tlas_cullable = out.n_cullable;
+    sc->view.tlas = sc->d_tlas;
+    sc->view.tlas_pre = sc->d_tlas_pre;
+    sc->view.tlas_margin = out.ray_margin;
     return RQ_OK;
 }
 
@@ -502,20 +585,15 @@ rq_status rq_scene_set_entities(rq_scene* sc, const rq_entity* ents, int32_t n_e
     for (int i = 0; i < n_ents; ++i) ident = ident && is_identity(ents[i].inverse);
     sc->view.all_identity = ident ? 1 : 0;
     sc->h_ents.assign(ents, ents + n_ents);
-    if (sc->bvh8) return rq_scene_build_bvh8(sc, nullptr);
-    return RQ_OK;
+    if (sc->bvh8) return rq_scene_build_bvh8(sc, nullptr);  // rebuilds the top level too
+    return rq::rebuild_tlas(sc);
 }
 
 rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
     if (!sc) return fail(nullptr, RQ_EINVAL, "NULL scene");
     rq_ctx* ctx = sc->ctx;
-    if (sc->host_stale) {  // positions were updated on the device: refresh the host copies
-        RQ_CUDA(ctx, cudaSetDevice(ctx->device));
-        RQ_CUDA(ctx, cudaDeviceSynchronize());
-        RQ_CUDA(ctx, cudaMemcpy(sc->h_nodes.data(), sc->d_nodes, sc->h_nodes.size() * 4, cudaMemcpyDeviceToHost));
-        RQ_CUDA(ctx, cudaMemcpy(sc->h_verts.data(), sc->d_verts, sc->h_verts.size() * 4, cudaMemcpyDeviceToHost));
-        sc->host_stale = false;
-    }
+    rq_status st0 = rq::refresh_host(sc);  // positions may have been updated on the device
+    if (st0 != RQ_OK) return st0;
     std::vector<rq::Bvh8Range> ranges;
     for (const rq_entity& e : sc->h_ents) ranges.push_back({e.node_offset, e.node_count});
     rq::Bvh8Out b;
@@ -558,6 +636,28 @@ rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
     sc->view.b8_tris = sc->d_b8tris;
     sc->view.b8_roots = sc->d_b8roots;
     sc->bvh8 = true;
+    // object-space bounds of each entity's BVH8 root children, one grid step wider (the kernel
+    // pads its slab test by half a step plus rounding)
+    sc->h_b8roots = b.roots;
+    sc->b8_bounds.assign(6 * sc->h_ents.size(), 0.0);
+    for (size_t i = 0; i < sc->h_ents.size() && i < b.roots.size(); ++i) {
+        double* bb = &sc->b8_bounds[6 * i];
+        bb[0] = bb[1] = bb[2] = 1e300;
+        bb[3] = bb[4] = bb[5] = -1e300;
+        if (b.roots[i] < 0) continue;
+        const uint32_t* nd = b.nodes.data() + static_cast<size_t>(b.roots[i]) * rq::kBvh8NodeWords;
+        for (int c = 0; c < 8; ++c) {
+            float lo[3], hi[3];
+            rq::bvh8_decode_child(nd, c, lo, hi);
+            if (!(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2])) continue;  // empty slot
+            for (int a = 0; a < 3; ++a) {
+                const double step = std::ldexp(1.0, static_cast<int>((nd[3] >> (8 * a)) & 0xFFu) - 127);
+                bb[a] = std::min(bb[a], double(lo[a]) - step);
+                bb[3 + a] = std::max(bb[3 + a], double(hi[a]) + step);
+            }
+        }
+    }
+    if ((st0 = rq::rebuild_tlas(sc)) != RQ_OK) return st0;
     if (info) {
         info->nodes = b.n_nodes;
         info->triangles = b.n_tris;
@@ -635,7 +735,17 @@ rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset) {
 
 rq_status rq_scene_bytes(const rq_scene* sc, int64_t* bytes) {
     if (!sc || !bytes) return fail(nullptr, RQ_EINVAL, "NULL argument");
-    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap + sc->b8_bytes;
+    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap + sc->b8_bytes + sc->tlas_bytes;
+    return RQ_OK;
+}
+
+rq_status rq_scene_tlas_info(const rq_scene* sc, rq_tlas_info* info) {
+    if (!sc || !info) return fail(nullptr, RQ_EINVAL, "NULL argument");
+    info->nodes = sc->view.tlas ? sc->tlas_nodes : 0;
+    info->entities = sc->n_ents;
+    info->cullable = sc->view.tlas ? sc->tlas_cullable : 0;
+    info->reserved = 0;
+    info->bytes = sc->view.tlas ? sc->tlas_bytes : 0;
     return RQ_OK;
 }
 
@@ -654,6 +764,8 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_tri_fast) cudaFree(sc->d_tri_fast);
     if (sc->d_adj_off) cudaFree(sc->d_adj_off);
     if (sc->d_adj) cudaFree(sc->d_adj);
+    if (sc->d_tlas) cudaFree(sc->d_tlas);
+    if (sc->d_tlas_pre) cudaFree(sc->d_tlas_pre);
     delete sc;
     return RQ_OK;
 }

@@ -39,7 +39,7 @@ rq_status describe(rq_ctx* ctx, const rq_query* q, int32_t nq, const rq_opts* o,
         if (family == kFamilyBvh8 && !x.scene->bvh8)
             return fail(ctx, RQ_ENOTSUP, "query " + std::to_string(k) + ": scene has no BVH8");
         QueryDesc& d = out[k];
-        d.s = x.scene->view;
+        d.s = entity_view(x.scene->view, o ? o->flags : 0);
         d.rays = x.rays;
         d.hits = x.hits;
         d.occ = x.occluded;

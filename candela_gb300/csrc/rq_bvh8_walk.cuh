@@ -65,10 +65,13 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
     int32_t mesh = -1, tri = -1, ent = -1;
     occluded = false;
     if (rtmax > rtmin) {
-        for (int e = 0; e < s.n_ents; ++e) {
+        const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
+        int32_t cur = tlas::begin(s, wo, wd);
+        for (int e = -1; (e = tlas::next(s, cur, e, wo, wd, kAny ? rtmax : tmax,
+                                    skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0;) {
             const rq_entity& E = s.ents[e];
-            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f)
-                continue;
+            if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
             const int32_t root = s.b8_roots[e];
             if (root < 0) continue;
             const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
@@ -119,15 +122,19 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
     bvh8::Hit8 h;
     bvh8::Walk w;
     float tmin = 0.0f, tmax = 0.0f, closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = 0, visits = 0;
+    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = -1, visits = 0;
+    int32_t ents = tlas::kPlain;  // entity cursor (rq_tlas.cuh); `ent` is the last entity it gave
     int64_t id = -1;
     bool live = false, exhausted = false;
     unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
     // Starts the walk of entity `ent` or a later one that is traversed; false when none is left.
     auto begin = [&](const float4 r0, const float4 r1) -> bool {
-        for (; ent < s.n_ents; ++ent) {
+        const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const float3 wo = make_float3(r0.x, r0.y, r0.z), wd = make_float3(r1.x, r1.y, r1.z);
+        while ((ent = tlas::next(s, ents, ent, wo, wd, kAny ? r1.w : tmax,
+                                 skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0) {
             const rq_entity& E = s.ents[ent];
-            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(E) < 0.99f) continue;
+            if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
             const int32_t root = s.b8_roots[ent];
             if (root < 0) continue;
             r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
@@ -172,8 +179,9 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                     tmax = r1.w;
                     closest = -1.0f;
                     mesh = tri = ent_hit = -1;
-                    ent = 0;
                     visits = 0;
+                    ent = -1;
+                    ents = tlas::begin(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
                     live = (r1.w > r0.w) && begin(r0, r1);
                     if (!live) store(r0, r1, false);
                 }
@@ -197,11 +205,8 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
         }
         float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
         if (!done) {
-            ++ent;
-            if (ent < s.n_ents) {
-                load_ray(rays, id, r0, r1);
-                if (begin(r0, r1)) continue;
-            }
+            load_ray(rays, id, r0, r1);
+            if (begin(r0, r1)) continue;
         }
         if (!kAny) load_ray(rays, id, r0, r1);
         store(r0, r1, done);

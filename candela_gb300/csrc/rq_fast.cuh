@@ -179,9 +179,13 @@ __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int 
     const f3 o = strict::xyz(r0), d = strict::xyz(r1);
     Best best{rtmax, -1.0f, 0.0f, 0.0f, -1, -1};
     int32_t ent = -1;
-    for (int i = 0; i < s.n_ents; ++i) {
+    const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+    const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
+    int32_t cur = tlas::begin(s, wo, wd);
+    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, kAny ? rtmax : best.tmax,
+                                skip_transparent ? tlas::kOpaque : tlas::kAll, h.iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
-        if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(e) < 0.99f) continue;
+        if (skip_transparent && strict::ent_alpha(e) < 0.99f) continue;
         const Ray r = make_ray(strict::xform(e.inverse, o, 1.0f), strict::xform(e.inverse, d, 0.0f));
         Best bb = best;
         bb.closest = -1.0f;

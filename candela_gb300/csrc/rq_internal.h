@@ -32,7 +32,20 @@ struct SceneView {
     // Optional device-side ray count: when set, a launch over n rays processes only the first
     // min(n, *ray_count) (used for compacted secondary rays whose count is known on the device).
     const unsigned long long* ray_count;
+    // Top level over the entities (tlas.h; NULL = walk every entity): pre-order nodes (2 x float4),
+    // per-entity prefix counts (int4), per-ray margin factor.
+    const float4* tlas;
+    const int4* tlas_pre;
+    float tlas_margin;
+    int32_t tlas_pad;
 };
+
+// The view a query runs on: RQ_FLAG_ENTITY_LOOP walks every entity in turn.
+inline SceneView entity_view(const SceneView& s, int flags) {
+    SceneView v = s;
+    if (flags & RQ_FLAG_ENTITY_LOOP) v.tlas = nullptr;
+    return v;
+}
 
 // Query configuration resolved by the host API.
 struct QueryConfig {

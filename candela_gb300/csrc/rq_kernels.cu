@@ -375,15 +375,16 @@ cudaError_t launch_closest(const SceneView& s, const QueryConfig& q, const rq_ra
     if (n <= 0) return cudaSuccess;
     int v = q.variant_closest < 0 ? 0 : q.variant_closest;
     if (kLaunchVariants[v].persistent && (!queue || q.mode == RQ_MODE_FAST)) v = non_persistent_variant(v);
+    const SceneView sv = entity_view(s, q.flags);
     switch (v) {
-        case 1: return closest_variant<128, 4>(s, q, rays, n, hits, st);
-        case 2: return closest_variant<128, 6>(s, q, rays, n, hits, st);
-        case 3: return closest_variant<128, 8>(s, q, rays, n, hits, st);
-        case 4: return closest_variant<256, 3>(s, q, rays, n, hits, st);
-        case 5: return closest_variant<64, 12>(s, q, rays, n, hits, st);
-        case 6: return persistent_variant<false, 1>(s, q, rays, n, hits, nullptr, queue, st);
-        case 7: return persistent_variant<false, 8>(s, q, rays, n, hits, nullptr, queue, st);
-        default: return closest_variant<128, 1>(s, q, rays, n, hits, st);
+        case 1: return closest_variant<128, 4>(sv, q, rays, n, hits, st);
+        case 2: return closest_variant<128, 6>(sv, q, rays, n, hits, st);
+        case 3: return closest_variant<128, 8>(sv, q, rays, n, hits, st);
+        case 4: return closest_variant<256, 3>(sv, q, rays, n, hits, st);
+        case 5: return closest_variant<64, 12>(sv, q, rays, n, hits, st);
+        case 6: return persistent_variant<false, 1>(sv, q, rays, n, hits, nullptr, queue, st);
+        case 7: return persistent_variant<false, 8>(sv, q, rays, n, hits, nullptr, queue, st);
+        default: return closest_variant<128, 1>(sv, q, rays, n, hits, st);
     }
 }
 
@@ -392,15 +393,16 @@ cudaError_t launch_anyhit(const SceneView& s, const QueryConfig& q, const rq_ray
     if (n <= 0) return cudaSuccess;
     int v = q.variant_any < 0 ? 0 : q.variant_any;
     if (kLaunchVariants[v].persistent && (!queue || q.mode == RQ_MODE_FAST)) v = non_persistent_variant(v);
+    const SceneView sv = entity_view(s, q.flags);
     switch (v) {
-        case 1: return anyhit_variant<128, 4>(s, q, rays, n, occluded, st);
-        case 2: return anyhit_variant<128, 6>(s, q, rays, n, occluded, st);
-        case 3: return anyhit_variant<128, 8>(s, q, rays, n, occluded, st);
-        case 4: return anyhit_variant<256, 3>(s, q, rays, n, occluded, st);
-        case 5: return anyhit_variant<64, 12>(s, q, rays, n, occluded, st);
-        case 6: return persistent_variant<true, 1>(s, q, rays, n, nullptr, occluded, queue, st);
-        case 7: return persistent_variant<true, 8>(s, q, rays, n, nullptr, occluded, queue, st);
-        default: return anyhit_variant<128, 1>(s, q, rays, n, occluded, st);
+        case 1: return anyhit_variant<128, 4>(sv, q, rays, n, occluded, st);
+        case 2: return anyhit_variant<128, 6>(sv, q, rays, n, occluded, st);
+        case 3: return anyhit_variant<128, 8>(sv, q, rays, n, occluded, st);
+        case 4: return anyhit_variant<256, 3>(sv, q, rays, n, occluded, st);
+        case 5: return anyhit_variant<64, 12>(sv, q, rays, n, occluded, st);
+        case 6: return persistent_variant<true, 1>(sv, q, rays, n, nullptr, occluded, queue, st);
+        case 7: return persistent_variant<true, 8>(sv, q, rays, n, nullptr, occluded, queue, st);
+        default: return anyhit_variant<128, 1>(sv, q, rays, n, occluded, st);
     }
 }
 

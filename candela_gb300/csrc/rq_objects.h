@@ -59,6 +59,13 @@ struct rq_scene {
     int32_t b8roots_cap = 0;
     int64_t b8_nodes = 0, b8_tris = 0, b8_bytes = 0;
     double b8_build_ms = 0.0;
+    std::vector<int32_t> h_b8roots;  // per entity: BVH8 root (-1: none)
+    std::vector<double> b8_bounds;   // per entity: object-space bounds its BVH8 root can box-test
+    // top level over the entities (tlas.h); rebuilt with the entities and the BVH8
+    float4* d_tlas = nullptr;
+    int4* d_tlas_pre = nullptr;
+    int64_t tlas_bytes = 0;
+    int32_t tlas_nodes = 0, tlas_cullable = 0;
     // refit plan (node, object offset) bottom-up by level, and vertex -> (triangle, corner) lists
     bool refit_ready = false, adj_ready = false, host_stale = false;
     std::vector<int64_t> refit_level_off;
@@ -72,6 +79,10 @@ struct rq_scene {
 namespace rq {
 
 rq_status fail(rq_ctx* ctx, rq_status s, const std::string& msg);
+// Rebuilds the top level over the scene's entities (none below kTlasMinEntities entities).
+rq_status rebuild_tlas(rq_scene* sc);
+// Copies device-updated node and vertex buffers back to the host copies.
+rq_status refresh_host(rq_scene* sc);
 rq_status cuda_fail(rq_ctx* ctx, cudaError_t e, const char* what);
 // Resolves rq_opts (NULL = defaults) against the scene into a kernel configuration.
 rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, QueryConfig& q);

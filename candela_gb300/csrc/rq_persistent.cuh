@@ -28,18 +28,19 @@ struct StrictRay {
     int32_t mesh, tri, ent_hit, iters_total;
     // current entity traversal (IntersectBVHStack / IntersectBVHStackless)
     int32_t ent, start, count, cur, sp, iters;
+    int32_t ents;  // entity cursor (rq_tlas.cuh); `ent` is the last entity it gave
     f3 ro, rd, inv;
     strict::Best bb;
     bool occluded;
 
     // Skips to the next entity that is traversed (ignore-transparent filter); false when done.
     __device__ __forceinline__ bool begin_entity(const SceneView& s, int flags) {
-        while (ent < s.n_ents) {
+        const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
+        while ((ent = tlas::next(s, ents, ent, wo, wd, kAny ? rtmax : tmax,
+                                 skip_transparent ? tlas::kOpaque : tlas::kAll, iters_total)) >= 0) {
             const rq_entity& e = s.ents[ent];
-            if (!kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT) && strict::ent_alpha(e) < 0.99f) {
-                ++ent;
-                continue;
-            }
+            if (skip_transparent && strict::ent_alpha(e) < 0.99f) continue;
             ro = strict::xform(e.inverse, o, 1.0f);
             rd = strict::xform(e.inverse, d, 0.0f);
             inv = strict::rcp3(rd);
@@ -64,8 +65,9 @@ struct StrictRay {
         mesh = tri = ent_hit = -1;
         iters_total = 0;
         occluded = false;
-        ent = 0;
+        ent = -1;
         if (!(rtmax > rtmin)) return false;  // inactive ray
+        ents = tlas::begin(s, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z));
         return begin_entity(s, flags);
     }
 
@@ -85,7 +87,6 @@ struct StrictRay {
             tri = bb.tri;
             ent_hit = ent;
         }
-        ++ent;
         return begin_entity(s, flags);
     }
 

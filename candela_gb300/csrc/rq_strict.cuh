@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "rq_internal.h"
+#include "rq_tlas.cuh"
 
 namespace rq {
 namespace strict {
@@ -255,7 +256,10 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
     float tmax = rtmax;
     float closest = -1.0f;
     int32_t mesh = -1, tri = -1, ent = -1;
-    for (int i = 0; i < s.n_ents; ++i) {
+    const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
+    int32_t cur = tlas::begin(s, wo, wd);
+    const int counted = (flags & RQ_FLAG_IGNORE_TRANSPARENT) ? tlas::kOpaque : tlas::kAll;
+    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, tmax, counted, h.iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
         if ((flags & RQ_FLAG_IGNORE_TRANSPARENT) && ent_alpha(e) < 0.99f) continue;
         const f3 ro = xform(e.inverse, o, 1.0f);
@@ -302,7 +306,9 @@ __device__ bool scene_any(const SceneView& s, const float4 r0, const float4 r1, 
     const float rtmin = r0.w, rtmax = r1.w;
     if (!(rtmax > rtmin)) return false;
     const f3 o = xyz(r0), d = xyz(r1);
-    for (int i = 0; i < s.n_ents; ++i) {
+    const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
+    int32_t cur = tlas::begin(s, wo, wd);
+    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, rtmax, tlas::kAll, iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
         const f3 ro = xform(e.inverse, o, 1.0f);
         const f3 rd = xform(e.inverse, d, 0.0f);

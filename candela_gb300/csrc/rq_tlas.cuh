@@ -1,0 +1,75 @@
+// Entity cursor over the top-level BVH (tlas.h): the entities a ray can touch, in ascending index
+// order, so the scene loops keep the reference's order, TMax and tie handling.  A scene without a
+// top level, or a ray with a non-finite origin or direction, walks every entity.
+//
+// The cursor state is one int: the next top-level node (>= 0), kEnd once the walk has run past
+// the last node, kDone once the remaining entities have been counted, or kPlain for the plain
+// loop.  The caller keeps the last entity it was given (`prev`, -1 before the first).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rq_internal.h"
+
+namespace rq {
+namespace tlas {
+
+// Which entities the caller's loop would have walked (each skipped one adds one iteration).
+enum Count : int { kAll = -1, kOpaque = 0, kBvh8 = 1, kBvh8Opaque = 2 };
+
+constexpr int32_t kEnd = -1, kDone = -2, kPlain = -3;
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+    return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+__device__ __forceinline__ int32_t begin(const SceneView& s, float3 o, float3 d) {
+    return s.tlas != nullptr && finite3(o.x, o.y, o.z) && finite3(d.x, d.y, d.z) ? 0 : kPlain;
+}
+
+// Entities in [lo, hi) that the caller's loop would have walked.
+__device__ __forceinline__ int32_t walked(const SceneView& s, int32_t lo, int32_t hi, int count) {
+    if (hi <= lo) return 0;
+    if (count == kAll) return hi - lo;
+    const int* p = reinterpret_cast<const int*>(s.tlas_pre);
+    return __ldg(p + 4 * hi + count) - __ldg(p + 4 * lo + count);
+}
+
+// Next entity after `prev` to walk, or -1 when none is left.  `tmax` is the loop's running TMax:
+// subtrees whose widened boxes start beyond it are skipped (the walk of such an entity would
+// stop at its root as well).  `skipped` receives the iterations of the entities passed over.
+__device__ __forceinline__ int32_t next(const SceneView& s, int32_t& c, int32_t prev, float3 o, float3 d,
+                                        float tmax, int count, int32_t& skipped) {
+    if (c == kPlain) return prev + 1 < s.n_ents ? prev + 1 : -1;
+    if (c == kDone) return -1;
+    const float m = s.tlas_margin * fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    const float ix = __frcp_rn(d.x), iy = __frcp_rn(d.y), iz = __frcp_rn(d.z);
+    const float tlim = tmax * (1.0f + 1.0f / 65536.0f);
+    while (c >= 0) {
+        const float4 a = __ldg(s.tlas + 2 * c), b = __ldg(s.tlas + 2 * c + 1);
+        // slab test on the widened box; fminf / fmaxf drop the NaN of a zero direction component
+        // whose origin lies on a widened face (outside the entity's own box by the margin)
+        const float x0 = (a.x - m - o.x) * ix, x1 = (b.x + m - o.x) * ix;
+        const float y0 = (a.y - m - o.y) * iy, y1 = (b.y + m - o.y) * iy;
+        const float z0 = (a.z - m - o.z) * iz, z1 = (b.z + m - o.z) * iz;
+        const float tn = fmaxf(fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1)), 0.0f);
+        const float tf = fminf(fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1)), tlim);
+        const int32_t link = __float_as_int(b.w);
+        if (tn <= tf) {
+            const int32_t e = __float_as_int(a.w);
+            if (e >= 0) {
+                skipped += walked(s, prev + 1, e, count);
+                c = link;
+                return e;
+            }
+            ++c;
+        } else {
+            c = link;
+        }
+    }
+    skipped += walked(s, prev + 1, s.n_ents, count);
+    c = kDone;
+    return -1;
+}
+
+}  // namespace tlas
+}  // namespace rq

@@ -262,6 +262,13 @@ class Scene:
                               _stream(rays, stream)), self.ctx.handle)
         return out
 
+    def tlas_info(self) -> dict:
+        """rq_scene_tlas_info: the top level over the entities (nodes 0 = every entity walked)."""
+        buf = (C.c_int64 * 3)()
+        check(lib().rq_scene_tlas_info(self.handle, C.byref(buf)), self.ctx.handle)
+        w = np.frombuffer(bytes(buf), dtype=np.int32)
+        return {"nodes": int(w[0]), "entities": int(w[1]), "cullable": int(w[2]), "bytes": int(buf[2])}
+
     def collide(self, boxes, out=None, *, flags=0, stream=None):
         """First (entity, mesh, triangle) each box overlaps (rq_collide; CollideScene of
         Collide.comp).  `boxes` is a float32 (n, 8) array {min.xyzw, max.xyzw} on the host

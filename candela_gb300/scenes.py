@@ -324,6 +324,30 @@ def sphere_rays(n: int, lo, hi, seed: int = 4, tmax: float = 1000000.0) -> np.nd
     return r
 
 
+def instance_transforms(n: int, lo, hi, scale_lo: float, scale_hi: float, seed: int = 8,
+                        anisotropic: float = 0.1, tilt: float = 0.08) -> np.ndarray:
+    """n model matrices ((n, 4, 4) float32, row-major): translation uniform in [lo, hi], a turn
+    about z, a tilt about x of up to `tilt` turns, a uniform scale in [scale_lo, scale_hi]; a
+    fraction `anisotropic` of them is scaled (1, 0.5, 1.5) on top."""
+    u = uniform(seed, 505, n * 8).reshape(n, 8)
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    t = lo + (hi - lo) * u[:, :3]
+    cz, sz = cos_turns(u[:, 3]), sin_turns(u[:, 3])
+    ax = tilt * (2.0 * u[:, 4] - 1.0)
+    cx, sx = cos_turns(ax), sin_turns(ax)
+    s = scale_lo + (scale_hi - scale_lo) * u[:, 5]
+    m = np.zeros((n, 4, 4))
+    for i in range(n):
+        rz = np.array([[cz[i], -sz[i], 0.0], [sz[i], cz[i], 0.0], [0.0, 0.0, 1.0]])
+        rx = np.array([[1.0, 0.0, 0.0], [0.0, cx[i], -sx[i]], [0.0, sx[i], cx[i]]])
+        sc = np.array([1.0, 0.5, 1.5]) if u[i, 6] < anisotropic else np.ones(3)
+        m[i, :3, :3] = rz @ rx @ np.diag(s[i] * sc)
+        m[i, :3, 3] = t[i]
+        m[i, 3, 3] = 1.0
+    return m.astype(np.float32)
+
+
 def query_boxes(n: int, lo, hi, half_lo: float, half_hi: float, seed: int = 6) -> np.ndarray:
     """Collision query boxes ((n, 8) float32 {min.xyz, 1, max.xyz, 1}): centres uniform in
     [lo, hi], half-extents per axis uniform in [half_lo, half_hi]."""

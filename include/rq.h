@@ -127,8 +127,11 @@ enum {
                                         alpha < 0.99 (TraverseBVHStack.glsl:368-413) */
     RQ_FLAG_HOST_BUFFERS = 4,        /* ray/hit pointers are host memory */
     RQ_FLAG_NO_PERSISTENT = 8,       /* one thread per ray instead of the persistent kernel */
-    RQ_FLAG_COUNT = 16               /* accumulate node visits and triangle tests into the
+    RQ_FLAG_COUNT = 16,              /* accumulate node visits and triangle tests into the
                                         context's work counters (rq_counters_read) */
+    RQ_FLAG_ENTITY_LOOP = 32         /* walk every entity in turn (the reference's loop) instead
+                                        of skipping the ones the top-level BVH rules out; same
+                                        results either way */
 };
 
 typedef struct rq_opts {
@@ -263,6 +266,25 @@ typedef struct rq_bvh8_info {
 rq_status rq_scene_build_bvh8(rq_scene* scene, rq_bvh8_info* info);
 /* Device bytes held by the scene (all layouts built so far). */
 rq_status rq_scene_bytes(const rq_scene* scene, int64_t* bytes);
+/* Top level over the entities, built with the entities (and rebuilt with the BVH8) when a scene
+ * has at least 4 of them.  It replaces nothing in the reference's results: IntersectScene walks
+ * every entity in turn (TraverseBVHStack.glsl:337-349); queries here walk, in the same order and
+ * with the same running TMax, only the entities whose world box (the entity's BVH root mapped by
+ * the inverse of its inverse matrix, widened by a margin that covers float rounding) the ray
+ * meets before TMax, and count one iteration for each entity passed over (the root visit the
+ * loop would have made).  Hits, ties and iteration counts therefore equal the loop's
+ * (RQ_FLAG_ENTITY_LOOP runs the loop itself).  Entities whose walk tests triangles without a box
+ * test first (a stack-layout root with a leaf child) or whose transform is singular are never
+ * passed over.  Not maintained by rq_scene_update_positions: after it every entity is walked
+ * until the entities or the BVH8 are set again. */
+typedef struct rq_tlas_info {
+    int32_t nodes;     /* 0: no top level (every entity is walked) */
+    int32_t entities;
+    int32_t cullable;  /* entities that can be passed over */
+    int32_t reserved;
+    int64_t bytes;
+} rq_tlas_info;
+rq_status rq_scene_tlas_info(const rq_scene* scene, rq_tlas_info* info);
 rq_status rq_scene_destroy(rq_scene* scene);
 
 /* ---- Queries ---------------------------------------------------------------------------- */
