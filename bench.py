@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "c6"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
@@ -439,6 +439,118 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def c6_scene():
+    """Instanced scene: 4096 entities of three objects (heightfield 64x64 tile, 8,192 tris;
+    displaced subdiv-4 icosphere, 5,120 tris; displaced subdiv-3 icosphere, 1,280 tris) with a turn
+    about z, a small tilt and scales 0.5-1.5 (10 % anisotropic), translations over
+    [-32,32]^2 x [0,0.5], pushed in Morton order of their translation."""
+    import candela_gb300 as R
+    from candela_gb300 import scenes as S
+    objs = [S.heightfield(64, seed=21),
+            S.icosphere_set(n_spheres=1, subdiv=4, seed=22, lo=(0.0, 0.0, 0.5), hi=(0.0, 0.0, 0.5),
+                            radius=(0.8, 0.8), ground=None),
+            S.icosphere_set(n_spheres=1, subdiv=3, seed=23, lo=(0.0, 0.0, 0.4), hi=(0.0, 0.0, 0.4),
+                            radius=(0.5, 0.5), ground=None)]
+    n_ent = 4096
+    M = S.instance_transforms(n_ent, (-32.0, -32.0, 0.0), (32.0, 32.0, 0.5), 0.5, 1.5, seed=6, tilt=0.02)
+    q = np.clip(((M[:, :2, 3] + 32.0) / 64.0 * 1023.0).astype(np.int64), 0, 1023)
+
+    def spread(x):
+        r = np.zeros_like(x)
+        for b in range(10):
+            r |= ((x >> b) & 1) << (2 * b)
+        return r
+    order = np.argsort(spread(q[:, 0]) | (spread(q[:, 1]) << 1), kind="stable")
+    ri = R.RayIntersector(R.STACK)
+    for k, m in enumerate(objs):
+        ri.add_object(k + 1, [m])
+    pick = (S.uniform(6, 9, n_ent) * 3).astype(np.int64)
+    for i in order:
+        ri.push_entity(int(pick[i]) + 1, model=M[i].astype(np.float64))
+    ri.buffer_entities()
+    return ri, int(sum(m.n_tris for m in objs)), n_ent
+
+
+def run_c6(args):
+    """Instancing workload (the top level over entities): 1920x1080 primary closest-hit rays plus one
+    cosine GI closest-hit ray per hit over the 4096-entity scene of c6_scene; the GI pass with the
+    top level against the reference's entity loop (RQ_FLAG_ENTITY_LOOP), same pixels."""
+    import torch
+    import candela_gb300 as R
+    from candela_gb300 import _lib as L
+    from candela_gb300 import scenes as S
+    from candela_gb300.engine import gi_params
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    ri, n_obj_tris, n_ent = c6_scene()
+    build_s = time.perf_counter() - t0
+    ctx = R.Context(0)
+    sc = ri.buffer_data(ctx)
+    tl = sc.tlas_info()
+    b8 = sc.build_bvh8()
+    rays = S.camera_rays(1920, 1080, eye=(0.0, -46.0, 30.0), target=(0.0, 0.0, 0.0))
+    n = len(rays)
+    d = torch.from_numpy(rays.view(np.uint8)).cuda()
+    pix = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    p = gi_params(spp=1, seed=1, origin_offset=1e-3, ray_tmax=1000000.0, query=0)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        evs = []
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr)[1]
+    rays_per_step = int(st["primary_rays"]) + int(st["secondary_rays"])
+    res = {}
+    for name, layout in (("bvh8q", L.LAYOUT_BVH8Q), ("strict_bvh2", R.STACK)):
+        ms_t = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, stream=sptr), args.steps, args.warmup)
+        a = pix.cpu().numpy().copy()
+        ms_l = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, flags=L.FLAG_ENTITY_LOOP, stream=sptr),
+                     1, 1)
+        b = pix.cpu().numpy().copy()
+        res[name] = {"top_level_mrays_s": round(rays_per_step / (ms_t / 1e3) / 1e6, 1),
+                     "top_level_ms": round(ms_t, 4),
+                     "entity_loop_mrays_s": round(rays_per_step / (ms_l / 1e3) / 1e6, 2),
+                     "entity_loop_ms": round(ms_l, 3), "speedup": round(ms_l / ms_t, 1),
+                     "pixels_identical": bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))}
+    # CPU restatement (walks every entity) on a bounded sample of the primary rays
+    from oracle import oracle as O
+    v, t, nn, e = ri.global_buffers()
+    osc = O.OracleScene(O.ORC_STACK, v, t, nn, e)
+    sample = rays[:: max(1, n // 4096)][:4096]
+    c0 = time.perf_counter()
+    osc.closest(sample, nthreads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - c0
+    line = {"metric": METRIC, "value": res["bvh8q"]["top_level_mrays_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["bvh8q"]["top_level_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded instanced scene and camera rays)",
+            "config": {"workload": f"instancing: {n_ent} entities of 3 objects ({n_obj_tris} object tris), "
+                                   "1920x1080 primary closest-hit + 1 cosine GI closest-hit ray per hit, "
+                                   "Lambert shading, stack BVH leaf 2, strict",
+                       "rays_per_step": rays_per_step, "scene_build_s": round(build_s, 2),
+                       "top_level": tl, "bvh8_nodes": b8["nodes"],
+                       "l2": "flushed between timed steps (512 MB write)"},
+            "gi_pass": res,
+            "cpu_baseline": {"value": round(len(sample) / cpu_s / 1e6, 4), "unit": UNIT,
+                             "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"{len(sample)} primary rays, entity loop, {cpu_s:.2f} s"},
+            "device_status": ctx.device_status()}
+    print(json.dumps(line), flush=True)
+
+
 def run_c5(args):
     """Differentiation workload: heightfield 512x512 (524,288 tris, vertex z = parameters), 1024x1024
     depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a second-seed
@@ -589,9 +701,9 @@ def main():
         run_reference(args, wl, rank, world)
         return
 
-    if args.config in ("c3", "c4", "c5"):
+    if args.config in ("c3", "c4", "c5", "c6"):
         if rank == 0:
-            {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config](args)
+            {"c3": run_c3, "c4": run_c4, "c5": run_c5, "c6": run_c6}[args.config](args)
         return
 
     import torch

@@ -55,7 +55,7 @@ __device__ __forceinline__ void bvh8_finish(const SceneView& s, int flags, const
 }
 
 // BVH8 traversal of one ray with the strict scene loop around it.
-template <bool kAny>
+template <bool kAny, bool kTlas = true>
 __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, const float4 r1, int flags,
                                          rq_hit& hh, bool& occluded, int32_t& visits,
                                          int32_t& tests, unsigned& status) {
@@ -67,8 +67,8 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
     if (rtmax > rtmin) {
         const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
         const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
-        int32_t cur = tlas::begin(s, wo, wd);
-        for (int e = -1; (e = tlas::next(s, cur, e, wo, wd, kAny ? rtmax : tmax,
+        int32_t cur = tlas::begin<kTlas>(s, wo, wd);
+        for (int e = -1; (e = tlas::next<kTlas>(s, cur, e, wo, wd, kAny ? rtmax : tmax,
                                     skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0;) {
             const rq_entity& E = s.ents[e];
             if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
@@ -110,7 +110,7 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
 // entity or the final record needs it, which keeps it out of the loop's registers.
 constexpr int kPoolRays = 64;
 
-template <bool kAny, class Sink>
+template <bool kAny, class Sink, bool kTlas = true>
 __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const rq_ray* __restrict__ rays,
                                                      int64_t n, int flags, unsigned long long* queue,
                                                      const Sink& sink, int32_t& tests,
@@ -131,7 +131,7 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
     auto begin = [&](const float4 r0, const float4 r1) -> bool {
         const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
         const float3 wo = make_float3(r0.x, r0.y, r0.z), wd = make_float3(r1.x, r1.y, r1.z);
-        while ((ent = tlas::next(s, ents, ent, wo, wd, kAny ? r1.w : tmax,
+        while ((ent = tlas::next<kTlas>(s, ents, ent, wo, wd, kAny ? r1.w : tmax,
                                  skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0) {
             const rq_entity& E = s.ents[ent];
             if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
@@ -181,7 +181,7 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                     mesh = tri = ent_hit = -1;
                     visits = 0;
                     ent = -1;
-                    ents = tlas::begin(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
+                    ents = tlas::begin<kTlas>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
                     live = (r1.w > r0.w) && begin(r0, r1);
                     if (!live) store(r0, r1, false);
                 }

@@ -167,7 +167,7 @@ __device__ int32_t bvh_stackless(const SceneView& s, const Ray& r, int32_t start
 }
 
 // Scene loop (IntersectScene structure), closest or any hit.
-template <bool kAny, bool kStackless>
+template <bool kAny, bool kStackless, bool kTlas = true>
 __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int flags, rq_hit& h,
                       bool& occluded, int32_t& tests) {
     h.t = h.u = h.v = h.w = -1.0f;
@@ -181,8 +181,8 @@ __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int 
     int32_t ent = -1;
     const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
     const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
-    int32_t cur = tlas::begin(s, wo, wd);
-    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, kAny ? rtmax : best.tmax,
+    int32_t cur = tlas::begin<kTlas>(s, wo, wd);
+    for (int i = -1; (i = tlas::next<kTlas>(s, cur, i, wo, wd, kAny ? rtmax : best.tmax,
                                 skip_transparent ? tlas::kOpaque : tlas::kAll, h.iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
         if (skip_transparent && strict::ent_alpha(e) < 0.99f) continue;

@@ -18,7 +18,7 @@ namespace persist {
 using strict::f3;
 
 // Traversal of one ray through the scene's entities, one node per step().
-template <bool kAny, bool kStackless, bool kTieLower>
+template <bool kAny, bool kStackless, bool kTieLower, bool kTlas = true>
 struct StrictRay {
     // world ray
     f3 o, d;
@@ -37,7 +37,7 @@ struct StrictRay {
     __device__ __forceinline__ bool begin_entity(const SceneView& s, int flags) {
         const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
         const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
-        while ((ent = tlas::next(s, ents, ent, wo, wd, kAny ? rtmax : tmax,
+        while ((ent = tlas::next<kTlas>(s, ents, ent, wo, wd, kAny ? rtmax : tmax,
                                  skip_transparent ? tlas::kOpaque : tlas::kAll, iters_total)) >= 0) {
             const rq_entity& e = s.ents[ent];
             if (skip_transparent && strict::ent_alpha(e) < 0.99f) continue;
@@ -67,7 +67,7 @@ struct StrictRay {
         occluded = false;
         ent = -1;
         if (!(rtmax > rtmin)) return false;  // inactive ray
-        ents = tlas::begin(s, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z));
+        ents = tlas::begin<kTlas>(s, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z));
         return begin_entity(s, flags);
     }
 

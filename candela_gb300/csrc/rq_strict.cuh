@@ -244,7 +244,7 @@ __device__ int32_t bvh_stackless(const SceneView& s, f3 ro, f3 rd, int32_t start
 __device__ __forceinline__ float ent_alpha(const rq_entity& e) { return __int_as_float(e.data[1]); }
 
 // IntersectScene / IntersectSceneIgnoreTransparent (:327-413; stackless :280-366).
-template <bool kStackless, bool kTieLower>
+template <bool kStackless, bool kTieLower, bool kTlas = true>
 __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 r1, int flags,
                               rq_hit& h, int32_t& tests) {
     h.t = h.u = h.v = h.w = -1.0f;
@@ -257,9 +257,9 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
     float closest = -1.0f;
     int32_t mesh = -1, tri = -1, ent = -1;
     const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
-    int32_t cur = tlas::begin(s, wo, wd);
+    int32_t cur = tlas::begin<kTlas>(s, wo, wd);
     const int counted = (flags & RQ_FLAG_IGNORE_TRANSPARENT) ? tlas::kOpaque : tlas::kAll;
-    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, tmax, counted, h.iters)) >= 0;) {
+    for (int i = -1; (i = tlas::next<kTlas>(s, cur, i, wo, wd, tmax, counted, h.iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
         if ((flags & RQ_FLAG_IGNORE_TRANSPARENT) && ent_alpha(e) < 0.99f) continue;
         const f3 ro = xform(e.inverse, o, 1.0f);
@@ -300,15 +300,15 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
 }
 
 // IntersectSceneOcclusion (:659-676; stackless :558-575) with the per-ray TMax.
-template <bool kStackless>
+template <bool kStackless, bool kTlas = true>
 __device__ bool scene_any(const SceneView& s, const float4 r0, const float4 r1, int32_t& iters,
                           int32_t& tests) {
     const float rtmin = r0.w, rtmax = r1.w;
     if (!(rtmax > rtmin)) return false;
     const f3 o = xyz(r0), d = xyz(r1);
     const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
-    int32_t cur = tlas::begin(s, wo, wd);
-    for (int i = -1; (i = tlas::next(s, cur, i, wo, wd, rtmax, tlas::kAll, iters)) >= 0;) {
+    int32_t cur = tlas::begin<kTlas>(s, wo, wd);
+    for (int i = -1; (i = tlas::next<kTlas>(s, cur, i, wo, wd, rtmax, tlas::kAll, iters)) >= 0;) {
         const rq_entity& e = s.ents[i];
         const f3 ro = xform(e.inverse, o, 1.0f);
         const f3 rd = xform(e.inverse, d, 0.0f);

@@ -22,7 +22,10 @@ __device__ __forceinline__ bool finite3(float x, float y, float z) {
     return isfinite(x) && isfinite(y) && isfinite(z);
 }
 
+// kTlas = false: the kernel was launched for a scene without a top level (plain loop only).
+template <bool kTlas>
 __device__ __forceinline__ int32_t begin(const SceneView& s, float3 o, float3 d) {
+    if (!kTlas) return kPlain;
     return s.tlas != nullptr && finite3(o.x, o.y, o.z) && finite3(d.x, d.y, d.z) ? 0 : kPlain;
 }
 
@@ -37,9 +40,10 @@ __device__ __forceinline__ int32_t walked(const SceneView& s, int32_t lo, int32_
 // Next entity after `prev` to walk, or -1 when none is left.  `tmax` is the loop's running TMax:
 // subtrees whose widened boxes start beyond it are skipped (the walk of such an entity would
 // stop at its root as well).  `skipped` receives the iterations of the entities passed over.
+template <bool kTlas>
 __device__ __forceinline__ int32_t next(const SceneView& s, int32_t& c, int32_t prev, float3 o, float3 d,
                                         float tmax, int count, int32_t& skipped) {
-    if (c == kPlain) return prev + 1 < s.n_ents ? prev + 1 : -1;
+    if (!kTlas || c == kPlain) return prev + 1 < s.n_ents ? prev + 1 : -1;
     if (c == kDone) return -1;
     const float m = s.tlas_margin * fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
     const float ix = __frcp_rn(d.x), iy = __frcp_rn(d.y), iz = __frcp_rn(d.z);
