@@ -800,6 +800,11 @@ def main():
     sorted_ms = timed_steps(B8, args.steps, 1)
     p = gi_params(**wl["params"], unfused=True)
     unfused_ms = timed_steps(B8, args.steps, 1)
+    # the RT second-bounce loop: two further bounces per GI hit (rays counted from the pass stats)
+    p = gi_params(**wl["params"], bounces=2)
+    st_b = sc.gi_frame(d_rays, p, out=d_pix, layout=B8, stats=True, stream=sptr)[1]
+    rays_bounce = rays_per_step + int(st_b["bounce_rays"])
+    bounce_ms = timed_steps(B8, args.steps, 1)
     p = p_plain
     plain_value = rays_per_step * args.steps / (plain_ms / 1e3) / 1e6
 
@@ -951,6 +956,10 @@ def main():
             "bvh8q_pass_unfused": {
                 "value": round(rays_per_step * args.steps / (unfused_ms / 1e3) / 1e6, 2),
                 "ms_per_step": round(unfused_ms / args.steps, 4)},
+            "bvh8q_pass_with_2_bounces": {
+                "value": round(rays_per_step and rays_bounce * args.steps / (bounce_ms / 1e3) / 1e6, 2),
+                "ms_per_step": round(bounce_ms / args.steps, 4), "rays_per_step": rays_bounce,
+                "bounce_rays": int(st_b["bounce_rays"]), "bounce_hits": int(st_b["bounce_hits"])},
             "bvh8q_pass_with_octant_binning": {
                 "value": round(rays_per_step * args.steps / (sorted_ms / 1e3) / 1e6, 2),
                 "ms_per_step": round(sorted_ms / args.steps, 4)},

@@ -86,13 +86,14 @@ class RqGiParams(C.Structure):
                 ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
                 ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3),
                 ("sky_color", C.c_float * 3), ("sort_rays", C.c_int32), ("unfused", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("bounces", C.c_int32)]
 
 
 class RqFrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("secondary_rays", C.c_int64), ("secondary_hits", C.c_int64),
-                ("shadow_rays", C.c_int64), ("shadow_occluded", C.c_int64)]
+                ("shadow_rays", C.c_int64), ("shadow_occluded", C.c_int64),
+                ("bounce_rays", C.c_int64), ("bounce_hits", C.c_int64)]
 
 
 _P = C.c_void_p

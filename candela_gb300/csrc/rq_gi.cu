@@ -22,7 +22,14 @@ struct GiArgs {
     int32_t normal_mode;
     float shadow_offset;
     f3 sun_dir, sun_color, sky;
+    int32_t bounces;
 };
+
+// Origin offset of the bounce rays (HitPosition + iNormal * 0.02, DiffuseTrace.glsl:518).
+constexpr float kBounceOffset = 0.02f;
+// A bounce that misses sees 2.2 x the skymap (DiffuseTrace.glsl:523), the first bounce 2.0 x
+// (:490); the sky parameter holds the first bounce's radiance.
+constexpr float kBounceSky = 1.1f;
 
 GiArgs to_args(const rq_gi_params& p) {
     GiArgs a;
@@ -35,6 +42,7 @@ GiArgs to_args(const rq_gi_params& p) {
     a.sun_dir = {p.sun_dir[0], p.sun_dir[1], p.sun_dir[2]};
     a.sun_color = {p.sun_color[0], p.sun_color[1], p.sun_color[2]};
     a.sky = {p.sky_color[0], p.sky_color[1], p.sky_color[2]};
+    a.bounces = p.bounces;
     return a;
 }
 
@@ -271,7 +279,8 @@ __global__ void __launch_bounds__(256) k_gi_raygen_compact(
 // same slot map; every value is computed with the same functions.
 __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
     SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
-    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ comp_of, unsigned long long* count) {
+    GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ comp_of, unsigned long long* count,
+    int32_t* __restrict__ samp_of) {
     __shared__ unsigned warp_hits[8];
     __shared__ unsigned long long block_base;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -315,6 +324,7 @@ __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
         const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
         put_ray(out, c0 + k, org, 0.0f, dir, a.ray_tmax);
         comp_of[j] = static_cast<int32_t>(c0 + k);
+        if (samp_of) samp_of[c0 + k] = static_cast<int32_t>(j);
     }
 }
 
@@ -350,6 +360,13 @@ __global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
     }
 }
 
+// ModelColor of a mesh (GetData, TraverseBVHStack.glsl:440-451); 0.8 grey without an entry.
+__device__ __forceinline__ f3 mesh_albedo(const float* __restrict__ albedo, int32_t n_albedo, int32_t mesh) {
+    if (mesh >= 0 && mesh < n_albedo)
+        return {__ldg(albedo + 3 * mesh), __ldg(albedo + 3 * mesh + 1), __ldg(albedo + 3 * mesh + 2)};
+    return {0.8f, 0.8f, 0.8f};
+}
+
 // Radiance and AO of one secondary hit (GetDirect, DiffuseTrace.glsl:368-372; emissive :491;
 // AO :494): h0 = (t, u, v, w), h1 = (tri, mesh, entity), rd the ray direction, l the sun's
 // visibility.  A miss returns the sky.
@@ -359,9 +376,7 @@ __device__ __forceinline__ float4 shade_one(const SceneView& s, const float* __r
     if (!(h0.x > 0.0f)) return make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
     f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
     if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-    f3 alb{0.8f, 0.8f, 0.8f};
-    if (h1.y >= 0 && h1.y < n_albedo)
-        alb = {__ldg(albedo + 3 * h1.y), __ldg(albedo + 3 * h1.y + 1), __ldg(albedo + 3 * h1.y + 2)};
+    const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
     const float em = __int_as_float(s.ents[h1.z].data[0]);
     const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
     const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
@@ -427,6 +442,132 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
         acc.w = __fadd_rn(acc.w, v.w);
     }
     const float inv = __fdiv_rn(1.0f, static_cast<float>(a.spp));
+    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                            __fmul_rn(acc.w, inv));
+}
+
+// ---- RT second-bounce loop (DiffuseTrace.glsl:502-536), per compact GI slot c ----------------
+// rad[c]: the slot's radiance (rgb) and AO (w); thr[c]: the path throughput (rgb), w = 1 while
+// the path continues.
+
+// First bounce: the GI hit's shading, and its albedo as the throughput (Throughput = Albedo.xyz).
+__global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
+                              const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
+                              const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                              float4* __restrict__ rad, float4* __restrict__ thr) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    float4 h0;
+    int4 h1;
+    get_hit(hits, c, h0, h1);
+    const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * c + 1));
+    const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
+    rad[c] = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+    if (h0.x > 0.0f) {
+        const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
+        thr[c] = make_float4(alb.x, alb.y, alb.z, 1.0f);
+    } else {
+        thr[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+// Bounce b's rays from the previous segment's hits: origin P + N * 0.02, a cosine direction about
+// N from sample samp_of[c], dimensions 2 + 2b and 3 + 2b.  prev_rays may alias out (each slot
+// reads its own ray before writing it).
+__global__ void k_bounce_raygen(SceneView s, const rq_ray* prev_rays, const rq_hit* __restrict__ prev_hits,
+                                const float4* __restrict__ thr, const int32_t* __restrict__ samp_of,
+                                const unsigned long long* count, int64_t n_max, GiArgs a, int bounce,
+                                rq_ray* out, unsigned long long* active) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool act = false;
+    if (c < n) {
+        if (thr[c].w > 0.0f) {
+            float4 h0;
+            int4 h1;
+            get_hit(prev_hits, c, h0, h1);
+            const float4* pr = reinterpret_cast<const float4*>(prev_rays) + 2 * c;
+            const float4 r0 = pr[0], r1 = pr[1];
+            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+            const uint32_t rid = static_cast<uint32_t>(samp_of[c]);
+            const float u0 = gi::u01(gi::sample_key(a.seed, rid, 2u + 2u * bounce));
+            const float u1 = gi::u01(gi::sample_key(a.seed, rid, 3u + 2u * bounce));
+            const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
+            put_ray(out, c, strict::add(P, strict::muls(N, kBounceOffset)), 0.0f, dir, a.ray_tmax);
+            act = true;
+        } else {
+            put_ray(out, c, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
+        }
+    }
+    if (active) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
+    }
+}
+
+// Bounce shading: rad += (GetDirect + emissive) * throughput, throughput *= albedo; a miss adds
+// 1.1 x sky x throughput (nothing under ref_miss, as the reference) and ends the path.
+__global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
+                               const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
+                               const float* __restrict__ albedo, int32_t n_albedo, GiArgs a, int ref_miss,
+                               float4* __restrict__ rad, float4* __restrict__ thr, unsigned long long* hit_count) {
+    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool hit = false;
+    if (c < n) {
+        float4 T = thr[c];
+        if (T.w > 0.0f) {
+            float4 h0;
+            int4 h1;
+            get_hit(hits, c, h0, h1);
+            float4 R = rad[c];
+            if (h0.x > 0.0f) {
+                const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * c + 1));
+                const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
+                const float4 v = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+                R.x = __fadd_rn(R.x, __fmul_rn(v.x, T.x));
+                R.y = __fadd_rn(R.y, __fmul_rn(v.y, T.y));
+                R.z = __fadd_rn(R.z, __fmul_rn(v.z, T.z));
+                const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
+                T = make_float4(__fmul_rn(T.x, alb.x), __fmul_rn(T.y, alb.y), __fmul_rn(T.z, alb.z), 1.0f);
+                hit = true;
+            } else {
+                if (!ref_miss) {
+                    R.x = __fadd_rn(R.x, __fmul_rn(__fmul_rn(a.sky.x, kBounceSky), T.x));
+                    R.y = __fadd_rn(R.y, __fmul_rn(__fmul_rn(a.sky.y, kBounceSky), T.y));
+                    R.z = __fadd_rn(R.z, __fmul_rn(__fmul_rn(a.sky.z, kBounceSky), T.z));
+                }
+                T.w = 0.0f;
+            }
+            rad[c] = R;
+            thr[c] = T;
+        }
+    }
+    if (hit_count) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(hit_count, static_cast<unsigned long long>(__popc(m)));
+    }
+}
+
+// Per-pixel mean of the slots' radiance (summed in sample order; inactive samples add 0).
+__global__ void k_gather_accumulate(const float4* __restrict__ rad, const int32_t* __restrict__ comp_of,
+                                    int64_t n, int32_t spp, float4* __restrict__ pixels) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < spp; ++k) {
+        const int32_t c = __ldg(comp_of + i * spp + k);
+        const float4 v = c >= 0 ? __ldg(rad + c) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        acc.x = __fadd_rn(acc.x, v.x);
+        acc.y = __fadd_rn(acc.y, v.y);
+        acc.z = __fadd_rn(acc.z, v.z);
+        acc.w = __fadd_rn(acc.w, v.w);
+    }
+    const float inv = __fdiv_rn(1.0f, static_cast<float>(spp));
     pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
                             __fmul_rn(acc.w, inv));
 }
@@ -514,6 +655,7 @@ rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
     if (p->spp < 1 || p->spp > 1024) return fail(ctx, RQ_EINVAL, "spp must be 1..1024");
     if (p->normal_mode != 0 && p->normal_mode != 1) return fail(ctx, RQ_EINVAL, "bad normal_mode");
     if (p->query != 0 && p->query != 1) return fail(ctx, RQ_EINVAL, "bad query kind");
+    if (p->bounces < 0 || p->bounces > 8) return fail(ctx, RQ_EINVAL, "bounces must be 0..8");
     return RQ_OK;
 }
 
@@ -558,14 +700,28 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     // tuned launch shape beats the persistent ray queue there, which pays per-ray hand-over costs.
     QueryConfig qp = q;
     qp.variant_closest = non_persistent_variant(q.variant_closest);
+    // RT second-bounce loop: per compact slot its sample index, radiance and path throughput
+    const bool bounce = p.query == 0 && p.bounces > 0;
+    int32_t* samp_of = nullptr;
+    float4 *rad = nullptr, *thr = nullptr;
+    if (bounce) {
+        void *d_samp = nullptr, *d_rad = nullptr, *d_thr = nullptr;
+        if ((s = scratch(ctx, 8, 4 * m, &d_samp)) != RQ_OK || (s = scratch(ctx, 10, 16 * m, &d_rad)) != RQ_OK ||
+            (s = scratch(ctx, 15, 16 * m, &d_thr)) != RQ_OK)
+            return s;
+        samp_of = static_cast<int32_t*>(d_samp);
+        rad = static_cast<float4*>(d_rad);
+        thr = static_cast<float4*>(d_thr);
+    }
     // phase 1
     if (h_prim)
         RQ_CUDA(ctx, cudaMemcpyAsync(const_cast<rq_ray*>(prim), h_prim, sizeof(rq_ray) * n,
                                      cudaMemcpyHostToDevice, st));
     RQ_CUDA(ctx, launch_closest(sc->view, qp, prim, n, phit, queue_counter(ctx, 0), st));
     if (stats) k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
-    if (!p.sort_rays && !p.unfused) {
-        k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count);
+    if ((!p.sort_rays && !p.unfused) || bounce) {
+        k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count,
+                                                        samp_of);
     } else if (p.sort_rays) {
         void* d_oct = nullptr;
         if ((s = scratch(ctx, 31, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
@@ -601,9 +757,36 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
             vis = occ;
         }
     }
+    if (bounce) {
+        // the bounces reuse the secondary ray / hit buffers in place (slot c only reads its own)
+        k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, sc->d_albedo,
+                                                    sc->n_albedo, a, rad, thr);
+        RQ_CUDA(ctx, cudaGetLastError());
+        QueryConfig qb = q;  // bounces use IntersectRay, not the ignore-transparent variant
+        qb.flags &= ~RQ_FLAG_IGNORE_TRANSPARENT;
+        for (int b = 0; b < p.bounces; ++b) {
+            k_bounce_raygen<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, thr, samp_of, count, m, a, b, sec,
+                                                          stats ? cnt + 6 : nullptr);
+            RQ_CUDA(ctx, cudaGetLastError());
+            RQ_CUDA(ctx, launch_closest(cv, qb, sec, m, shit, queue_counter(ctx, 1), st));
+            const uint8_t* bvis = nullptr;
+            if (p.shadow_rays) {
+                if ((s = scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
+                rq_ray* sh = static_cast<rq_ray*>(d_shadow);
+                k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count, nullptr);
+                RQ_CUDA(ctx, cudaGetLastError());
+                RQ_CUDA(ctx, launch_anyhit(cv, qb, sh, m, occ, queue_counter(ctx, 2), st));
+                bvis = occ;
+            }
+            k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, bvis, count, m, sc->d_albedo,
+                                                         sc->n_albedo, a, (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0,
+                                                         rad, thr, stats ? cnt + 7 : nullptr);
+            RQ_CUDA(ctx, cudaGetLastError());
+        }
+    }
     // phase 3
     float4* shade = nullptr;
-    if (p.unfused) {  // per-sample shading into a scratch buffer, then the per-pixel mean
+    if (p.unfused && !bounce) {  // per-sample shading into a scratch buffer, then the per-pixel mean
         if ((s = scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
         shade = static_cast<float4*>(d_shade);
         k_shade_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p.query, sc->d_albedo,
@@ -611,7 +794,9 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     }
     for (int64_t off = 0; off < n; off += chunk) {
         const int64_t c = std::min(chunk, n - off);
-        if (p.unfused)
+        if (bounce)
+            k_gather_accumulate<<<grid(c, 256), 256, 0, st>>>(rad, comp_of + off * p.spp, c, p.spp, pixels4 + off);
+        else if (p.unfused)
             k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, pixels4 + off);
         else
             k_shade_accumulate<<<grid(c, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of + off * p.spp, c, vis,
@@ -773,6 +958,8 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
         stats->secondary_hits = static_cast<int64_t>(c[2]);
         stats->shadow_rays = static_cast<int64_t>(c[3]);
         stats->shadow_occluded = static_cast<int64_t>(c[4]);
+        stats->bounce_rays = static_cast<int64_t>(c[6]);
+        stats->bounce_hits = static_cast<int64_t>(c[7]);
     }
     return RQ_OK;
 }

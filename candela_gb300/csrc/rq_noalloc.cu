@@ -70,6 +70,7 @@ rq_status rq_gi_frame_noalloc(rq_ctx* ctx, const rq_scene* sc, const rq_ray* pri
     if (p->spp < 1 || p->spp > 1024 || (p->query != 0 && p->query != 1) ||
         (p->normal_mode != 0 && p->normal_mode != 1))
         return rq::fail(ctx, RQ_EINVAL, "bad gi params");
+    if (p->bounces != 0) return rq::fail(ctx, RQ_EINVAL, "the no-alloc GI pass has no further bounces");
     if (n > kMaxRays || n * p->spp > kMaxRays) {
         char msg[160];
         std::snprintf(msg, sizeof(msg),

@@ -309,14 +309,15 @@ class Scene:
 def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode=0, query=0,
               shadow_rays=False, shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866),
               sun_color=(4.0, 3.8, 3.5), sky_color=(0.5, 0.7, 1.0), sort_rays=False,
-              unfused=False) -> L.RqGiParams:
-    """rq_gi_params for the diffuse-GI (query=0) or RTAO (query=1) pass."""
+              unfused=False, bounces=0) -> L.RqGiParams:
+    """rq_gi_params for the diffuse-GI (query=0) or RTAO (query=1) pass; `bounces` further
+    bounces per GI hit (the RT second-bounce loop)."""
     sd = np.asarray(sun_dir, dtype=np.float64)
     sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
     f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
     return L.RqGiParams(spp, seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode, query,
                         int(shadow_rays), shadow_offset, f3(sd), f3(sun_color), f3(sky_color),
-                        int(sort_rays), int(unfused), 0)
+                        int(sort_rays), int(unfused), int(bounces))
 
 
 def _empty_like_dev(ref, shape, dtype):

@@ -412,13 +412,20 @@ typedef struct rq_gi_params {
                               before tracing (same results, more coherent warps) */
     int32_t unfused;       /* rq_gi_frame: 0 = ray generation and shading + accumulation one
                               thread per pixel; 1 = one thread per sample (same pixels) */
-    int32_t reserved;
+    int32_t bounces;       /* GI only: further bounces after each GI hit (u_SecondaryBounces of the
+                              RT second-bounce loop, DiffuseTrace.glsl:502-536), 0..8; each adds
+                              (GetDirect + emissive) x throughput (the product of the albedos on
+                              the path), a miss adds 1.1 x sky x throughput (the loop's 2.2 x
+                              skymap against the first bounce's 2.0) and ends the path.  With
+                              RQ_FLAG_REF_COMPAT a bounce miss adds nothing, as the reference's
+                              loop does (it tests the first bounce's t for the sky) */
 } rq_gi_params;
 
 typedef struct rq_frame_stats {
     int64_t primary_rays, primary_hits;
     int64_t secondary_rays, secondary_hits;  /* active secondary rays and their hits (or occluded) */
     int64_t shadow_rays, shadow_occluded;
+    int64_t bounce_rays, bounce_hits;        /* rays traced by rq_gi_params.bounces, their hits */
 } rq_frame_stats;
 
 /* Per-mesh albedo (rgb floats, indexed by the triangle's mesh id), the ModelColor of the

@@ -69,6 +69,8 @@ def orc() -> C.CDLL:
                                     C.c_int, P]
         L.orc_shade.argtypes = [sp, P, P, I64, P, P, I32, P, P, P, I32, C.c_int, P]
         L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
+        L.orc_bounce_raygen.argtypes = [sp, P, P, P, P, I64, C.c_uint32, I32, C.c_float, C.c_float, I32,
+                                        C.c_int, P]
         L.orc_collide.argtypes = [sp, P, I64, P, C.c_int, C.c_int]
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
@@ -137,6 +139,19 @@ class OracleScene:
         orc().orc_shadow_raygen(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(sd),
                                 origin_offset, normal_mode, nthreads or os.cpu_count() or 1,
                                 _p(out))
+        return out
+
+    def bounce_raygen(self, rays, hits, alive, sample_id, seed, bounce, offset=0.02,
+                      ray_tmax=1000000.0, normal_mode=0, nthreads=None):
+        """Rays of one RT second bounce from the hits of `rays` (DiffuseTrace.glsl:502-536)."""
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        alive = np.ascontiguousarray(alive, dtype=np.uint8)
+        sid = np.ascontiguousarray(sample_id, dtype=np.uint32)
+        out = np.empty(rays.shape[0], dtype=RAY_DTYPE)
+        orc().orc_bounce_raygen(C.byref(self.s), _p(rays), _p(hits), _p(alive), _p(sid), rays.shape[0],
+                                seed & 0xFFFFFFFF, bounce, offset, ray_tmax, normal_mode,
+                                nthreads or os.cpu_count() or 1, _p(out))
         return out
 
     def shade(self, rays, hits, shadow_lit, albedo, sun_dir, sun_color, sky_color,

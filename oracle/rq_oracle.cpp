@@ -821,6 +821,38 @@ void orc_shadow_raygen(const orc_scene* sc, const orc_ray* rays, const orc_hit* 
     });
 }
 
+// Rays of bounce `bounce` of the RT second-bounce loop (DiffuseTrace.glsl:502-536): from hit i of
+// `rays` (alive[i] != 0), origin P + N * offset (0.02 in the reference, :518) and a cosine
+// direction about the facing normal (:519) from sample sample_id[i], dimensions 2 + 2*bounce and
+// 3 + 2*bounce of the counter-based hash that draws the first GI ray (dimensions 0 and 1).
+void orc_bounce_raygen(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, const uint8_t* alive,
+                       const uint32_t* sample_id, int64_t n, uint32_t seed, int32_t bounce, float offset,
+                       float ray_tmax, int32_t normal_mode, int nthreads, orc_ray* out) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const orc_hit& h = hits[i];
+            orc_ray& o = out[i];
+            if (!alive[i] || !(h.t > 0.0f)) {
+                o = orc_ray{{0, 0, 0}, 0.0f, {0, 0, 1}, -1.0f};
+                continue;
+            }
+            const V3 ro = ld3(rays[i].o), rd = ld3(rays[i].d);
+            const V3 P = add(ro, muls(rd, h.t));
+            V3 N = hit_normal(s, h, normal_mode);
+            if (dot(N, rd) > 0.0001f) N = neg(N);
+            const float r0 = u01(sample_key(seed, sample_id[i], 2u + 2u * uint32_t(bounce)));
+            const float r1 = u01(sample_key(seed, sample_id[i], 3u + 2u * uint32_t(bounce)));
+            const V3 dir = cos_weighted_hemisphere(N, r0, r1);
+            const V3 org = add(P, muls(N, offset));
+            o.o[0] = org.x; o.o[1] = org.y; o.o[2] = org.z;
+            o.d[0] = dir.x; o.d[1] = dir.y; o.d[2] = dir.z;
+            o.tmin = 0.0f;
+            o.tmax = ray_tmax;
+        }
+    });
+}
+
 void orc_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n,
                const uint8_t* shadow_lit, const float* albedo, int32_t n_albedo,
                const float sun_dir[3], const float sun_color[3], const float sky_color[3],

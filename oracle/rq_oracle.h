@@ -87,6 +87,9 @@ void orc_shade(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int
 void orc_shadow_raygen(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int64_t n,
                        const float sun_dir[3], float origin_offset, int32_t normal_mode,
                        int nthreads, orc_ray* out);
+void orc_bounce_raygen(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, const uint8_t* alive,
+                       const uint32_t* sample_id, int64_t n, uint32_t seed, int32_t bounce, float offset,
+                       float ray_tmax, int32_t normal_mode, int nthreads, orc_ray* out);
 
 // Counter-based hash (Jarzynski & Olano 2020, "pcg_hash") and the turn-based sine/cosine used
 // by the GI ray generator, exposed for tests.

@@ -178,3 +178,72 @@ def test_gi_frame_host_chunks_equal_device_pass(ctx, query):
         np.testing.assert_array_equal(got.view(np.uint32), want.cpu().numpy().view(np.uint32))
         assert st_h == st
     assert ctx.device_status() == 0
+
+
+def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0):
+    """The GI pass with the RT second-bounce loop, composed from the oracle's pieces in the
+    kernels' operation order (float32 numpy arithmetic, one rounding per operation)."""
+    f = np.float32
+    spp, seed = p.spp, p.seed
+    sd, sc_, sky = np.array(p.sun_dir), np.array(p.sun_color), np.array(p.sky_color, np.float32)
+    ph = osc.closest(rays, flags=flags)
+    sec = osc.gi_raygen(rays, ph, spp, seed, p.origin_offset)
+    sh = osc.closest(sec, flags=flags)
+    lit = 1 - osc.anyhit(osc.shadow_raygen(sec, sh, sd, p.shadow_offset)) if p.shadow_rays else None
+    rad = osc.shade(sec, sh, lit, albedo, sd, sc_, sky).astype(np.float32)
+    alb_of = lambda mesh: np.where((mesh >= 0)[:, None] & (mesh < len(albedo))[:, None],  # noqa: E731
+                                   albedo[np.clip(mesh, 0, len(albedo) - 1)], f(0.8)).astype(np.float32)
+    alive = sh["t"] > 0
+    thr = np.where(alive[:, None], alb_of(sh["mesh"]), f(0)).astype(np.float32)
+    prev_r, prev_h = sec, sh
+    sid = np.arange(len(sec), dtype=np.uint32)
+    bflags = flags & ~R.engine.L.FLAG_IGNORE_TRANSPARENT
+    n_rays = n_hits = 0
+    for b in range(bounces):
+        br = osc.bounce_raygen(prev_r, prev_h, alive, sid, seed, b, 0.02, p.ray_tmax)
+        bh = osc.closest(br, flags=bflags)
+        blit = 1 - osc.anyhit(osc.shadow_raygen(br, bh, sd, p.shadow_offset)) if p.shadow_rays else None
+        v = osc.shade(br, bh, blit, albedo, sd, sc_, sky).astype(np.float32)
+        hit = alive & (bh["t"] > 0)
+        miss = alive & ~(bh["t"] > 0)
+        n_rays += int(alive.sum())
+        n_hits += int(hit.sum())
+        rad[hit, :3] = rad[hit, :3] + v[hit, :3] * thr[hit]
+        if not ref_miss:
+            rad[miss, :3] = rad[miss, :3] + (sky * f(1.1)) * thr[miss]
+        thr[hit] = thr[hit] * alb_of(bh["mesh"][hit])
+        alive = hit
+        prev_r, prev_h = br, bh
+    rad = np.where((sec["tmax"] > sec["tmin"])[:, None], rad, f(0))
+    acc = np.zeros((len(rays), 4), np.float32)
+    r3 = rad.reshape(len(rays), spp, 4)
+    for k in range(spp):
+        acc = acc + r3[:, k]
+    return acc * (f(1) / f(spp)), n_rays, n_hits
+
+
+@pytest.mark.parametrize("bounces,shadow,ref", [(1, False, False), (3, True, False), (2, True, True)])
+def test_gi_frame_bounces_match_oracle_pipeline(ctx, bounces, shadow, ref):
+    """The RT second-bounce loop: bounce rays, hits and shadow rays bit-exact through the oracle's
+    pieces; radiance within the shading tolerance (the AO pow); ray counts equal."""
+    from candela_gb300 import _lib as L
+    bufs = single_object("ico2", R.STACK)
+    osc = oracle_scene(bufs, R.STACK)
+    rays = S.camera_rays(160, 120, eye=(0.0, -4.0, 2.5), target=(0.0, 0.0, 0.4))
+    albedo = np.array([[0.7, 0.6, 0.5], [0.9, 0.3, 0.3], [0.3, 0.9, 0.3], [0.5, 0.5, 0.9]], dtype=np.float32)
+    p = gi_params(spp=2, seed=7, origin_offset=1e-3, shadow_rays=shadow, bounces=bounces)
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(albedo)
+    flags = L.FLAG_REF_COMPAT if ref else 0
+    want, n_rays, n_hits = _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref, flags)
+    got_dev, st = sc.gi_frame(rays_to_device(rays), p, flags=flags, stats=True)
+    got = got_dev.cpu().numpy()
+    np.testing.assert_allclose(got, want, rtol=SHADE_RTOL * 8, atol=1e-6)
+    assert st["bounce_rays"] == n_rays and st["bounce_hits"] == n_hits and n_hits > 0
+    # the bounces add light: compared with the same pass without them
+    p0 = gi_params(spp=2, seed=7, origin_offset=1e-3, shadow_rays=shadow)
+    base = sc.gi_frame(rays_to_device(rays), p0, flags=flags).cpu().numpy()
+    assert (got[:, :3] >= base[:, :3] - 1e-6).all() and got[:, :3].sum() > base[:, :3].sum()
+    np.testing.assert_array_equal(got[:, 3], base[:, 3])  # AO is the first bounce's
+    # host buffers give the same pixels
+    np.testing.assert_array_equal(sc.gi_frame(rays, p, flags=flags), got)
