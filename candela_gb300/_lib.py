@@ -89,6 +89,11 @@ class RqGiParams(C.Structure):
                 ("bounces", C.c_int32)]
 
 
+class RqTexture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("srgb", C.c_int32), ("wrap", C.c_int32),
+                ("rgba8", C.c_void_p)]
+
+
 class RqFrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("secondary_rays", C.c_int64), ("secondary_hits", C.c_int64),
@@ -150,6 +155,7 @@ SIGNATURES = {
                                  _P]),
     "rq_collide": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_scene_tlas_info": (_S, [_P, C.POINTER(C.c_int64 * 3)]),
+    "rq_scene_set_textures": (_S, [_P, _P, _I32, _P, _I32]),
 }
 
 NOALLOC_MAX_RAYS = 65536

@@ -735,7 +735,8 @@ rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset) {
 
 rq_status rq_scene_bytes(const rq_scene* sc, int64_t* bytes) {
     if (!sc || !bytes) return fail(nullptr, RQ_EINVAL, "NULL argument");
-    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap + sc->b8_bytes + sc->tlas_bytes;
+    *bytes = sc->bytes + static_cast<int64_t>(sizeof(rq_entity)) * sc->ents_cap + sc->b8_bytes + sc->tlas_bytes +
+             sc->tex_bytes;
     return RQ_OK;
 }
 
@@ -757,6 +758,10 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_verts) cudaFree(sc->d_verts);
     if (sc->d_ents) cudaFree(sc->d_ents);
     if (sc->d_albedo) cudaFree(sc->d_albedo);
+    if (sc->d_mesh_tex) cudaFree(sc->d_mesh_tex);
+    if (sc->d_tex) cudaFree(sc->d_tex);
+    if (sc->d_texels) cudaFree(sc->d_texels);
+    if (sc->d_srgb) cudaFree(sc->d_srgb);
     if (sc->d_b8nodes) cudaFree(sc->d_b8nodes);
     if (sc->d_b8tris) cudaFree(sc->d_b8tris);
     if (sc->d_b8roots) cudaFree(sc->d_b8roots);

@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "rq_gi.cuh"
 #include "rq_persistent.cuh"
@@ -361,22 +364,84 @@ __global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
 }
 
 // ModelColor of a mesh (GetData, TraverseBVHStack.glsl:440-451); 0.8 grey without an entry.
-__device__ __forceinline__ f3 mesh_albedo(const float* __restrict__ albedo, int32_t n_albedo, int32_t mesh) {
-    if (mesh >= 0 && mesh < n_albedo)
-        return {__ldg(albedo + 3 * mesh), __ldg(albedo + 3 * mesh + 1), __ldg(albedo + 3 * mesh + 2)};
+__device__ __forceinline__ f3 mesh_albedo(const Materials& mat, int32_t mesh) {
+    if (mesh >= 0 && mesh < mat.n_albedo)
+        return {__ldg(mat.albedo + 3 * mesh), __ldg(mat.albedo + 3 * mesh + 1), __ldg(mat.albedo + 3 * mesh + 2)};
     return {0.8f, 0.8f, 0.8f};
+}
+
+// The colour channels of texel (i, j): byte / 255, or the sRGB table for an sRGB texture.
+__device__ __forceinline__ f3 texel(const Materials& mat, int32_t first, int32_t w, int32_t i, int32_t j, bool srgb) {
+    const uint32_t t = __ldg(mat.texels + first + static_cast<int64_t>(j) * w + i);
+    const uint32_t r = t & 0xFFu, g = (t >> 8) & 0xFFu, b = (t >> 16) & 0xFFu;
+    if (srgb) return {__ldg(mat.srgb + r), __ldg(mat.srgb + g), __ldg(mat.srgb + b)};
+    return {__fdiv_rn(static_cast<float>(r), 255.0f), __fdiv_rn(static_cast<float>(g), 255.0f),
+            __fdiv_rn(static_cast<float>(b), 255.0f)};
+}
+
+// Texel index along one axis: GL_REPEAT (positive modulo) or GL_CLAMP_TO_EDGE.
+__device__ __forceinline__ int32_t wrap_texel(int32_t i, int32_t n, bool clamp) {
+    if (clamp) return i < 0 ? 0 : (i >= n ? n - 1 : i);
+    const int32_t r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+// texture(Textures[Ref], uv).xyz in a compute shader: level 0 (no derivatives), bilinear (the
+// GL_LINEAR magnification filter), texel centres at half-integers: x = u * width - 0.5,
+// i0 = floor(x), a = x - i0, and the four texels weighted (1-a)(1-b), a(1-b), (1-a)b, ab, summed
+// in that order.  sRGB channels are decoded before filtering.  Coordinates beyond +-2^30 texels
+// are clamped there (the float has no fraction left at that size).
+__device__ f3 sample_texture(const Materials& mat, int32_t t, float u, float v) {
+    const int4 d = __ldg(mat.tex + t);
+    const bool srgb = d.w & 1, clamp = d.w & 2;
+    const float x = __fsub_rn(__fmul_rn(u, static_cast<float>(d.y)), 0.5f);
+    const float y = __fsub_rn(__fmul_rn(v, static_cast<float>(d.z)), 0.5f);
+    const float fx = fminf(fmaxf(floorf(x), -1073741824.0f), 1073741824.0f);
+    const float fy = fminf(fmaxf(floorf(y), -1073741824.0f), 1073741824.0f);
+    const float a = fminf(fmaxf(__fsub_rn(x, fx), 0.0f), 1.0f), b = fminf(fmaxf(__fsub_rn(y, fy), 0.0f), 1.0f);
+    const int32_t ix = static_cast<int32_t>(fx), iy = static_cast<int32_t>(fy);
+    const int32_t i0 = wrap_texel(ix, d.y, clamp), i1 = wrap_texel(ix + 1, d.y, clamp);
+    const int32_t j0 = wrap_texel(iy, d.z, clamp), j1 = wrap_texel(iy + 1, d.z, clamp);
+    const float na = __fsub_rn(1.0f, a), nb = __fsub_rn(1.0f, b);
+    const float w00 = __fmul_rn(na, nb), w10 = __fmul_rn(a, nb), w01 = __fmul_rn(na, b), w11 = __fmul_rn(a, b);
+    const f3 t00 = texel(mat, d.x, d.y, i0, j0, srgb), t10 = texel(mat, d.x, d.y, i1, j0, srgb);
+    const f3 t01 = texel(mat, d.x, d.y, i0, j1, srgb), t11 = texel(mat, d.x, d.y, i1, j1, srgb);
+    return strict::add(strict::add(strict::add(strict::muls(t00, w00), strict::muls(t10, w10)), strict::muls(t01, w01)),
+                       strict::muls(t11, w11));
+}
+
+// Albedo of a hit (GetData, TraverseBVHStack.glsl:422-455): the mesh's texture at the hit's UV
+// (texture coordinates half-packed in Vertex.PackedData.w, weighted by the barycentrics u, v, w)
+// when it has one, else its ModelColor.
+__device__ __forceinline__ f3 hit_albedo(const SceneView& s, const Materials& mat, const float4 h0, const int4 h1) {
+    const int32_t mesh = h1.y;
+    if (mesh >= 0 && mesh < mat.n_mesh_tex && h0.x > 0.0f) {
+        const int32_t t = __ldg(mat.mesh_tex + mesh);
+        if (t >= 0) {
+            const int4 tr = __ldg(s.tris + h1.x);
+            const uint32_t ta = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.x) + 1).w);
+            const uint32_t tb = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.y) + 1).w);
+            const uint32_t tc = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.z) + 1).w);
+            const float u = __fadd_rn(__fadd_rn(__fmul_rn(gi::half_bits(ta), h0.y), __fmul_rn(gi::half_bits(tb), h0.z)),
+                                      __fmul_rn(gi::half_bits(tc), h0.w));
+            const float v = __fadd_rn(__fadd_rn(__fmul_rn(gi::half_bits(ta >> 16), h0.y),
+                                                __fmul_rn(gi::half_bits(tb >> 16), h0.z)),
+                                      __fmul_rn(gi::half_bits(tc >> 16), h0.w));
+            return sample_texture(mat, t, u, v);
+        }
+    }
+    return mesh_albedo(mat, mesh);
 }
 
 // Radiance and AO of one secondary hit (GetDirect, DiffuseTrace.glsl:368-372; emissive :491;
 // AO :494): h0 = (t, u, v, w), h1 = (tri, mesh, entity), rd the ray direction, l the sun's
 // visibility.  A miss returns the sky.
-__device__ __forceinline__ float4 shade_one(const SceneView& s, const float* __restrict__ albedo,
-                                            int32_t n_albedo, const GiArgs& a, const f3 rd,
+__device__ __forceinline__ float4 shade_one(const SceneView& s, const Materials& mat, const GiArgs& a, const f3 rd,
                                             const float4 h0, const int4 h1, float l) {
     if (!(h0.x > 0.0f)) return make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
     f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
     if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-    const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
+    const f3 alb = hit_albedo(s, mat, h0, h1);
     const float em = __int_as_float(s.ents[h1.z].data[0]);
     const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
     const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
@@ -388,8 +453,8 @@ __device__ __forceinline__ float4 shade_one(const SceneView& s, const float* __r
 // Shading per slot from compact rays / hits / visibility (comp_of[j] < 0: inactive slot).
 __global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                           const int32_t* __restrict__ comp_of, int64_t m,
-                          const uint8_t* __restrict__ occl, int query, const float* __restrict__ albedo,
-                          int32_t n_albedo, GiArgs a, float4* __restrict__ out) {
+                          const uint8_t* __restrict__ occl, int query, const Materials mat, GiArgs a,
+                          float4* __restrict__ out) {
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= m) return;
     const int32_t c = comp_of[j];
@@ -407,7 +472,7 @@ __global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq
     const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * static_cast<int64_t>(c);
     const f3 rd = strict::xyz(__ldg(pr + 1));
     const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-    out[j] = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+    out[j] = shade_one(s, mat, a, rd, h0, h1, l);
 }
 
 // k_shade_c and k_accumulate in one pass, one thread per pixel: the spp samples are shaded with
@@ -415,7 +480,7 @@ __global__ void k_shade_c(SceneView s, const rq_ray* __restrict__ rays, const rq
 __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
                                    const rq_hit* __restrict__ hits, const int32_t* __restrict__ comp_of,
                                    int64_t n, const uint8_t* __restrict__ occl, int query,
-                                   const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                                   const Materials mat, GiArgs a,
                                    float4* __restrict__ pixels) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -433,7 +498,7 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
                 const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * static_cast<int64_t>(c);
                 const f3 rd = strict::xyz(__ldg(pr + 1));
                 const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-                v = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+                v = shade_one(s, mat, a, rd, h0, h1, l);
             }
         }
         acc.x = __fadd_rn(acc.x, v.x);
@@ -453,7 +518,7 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
 // First bounce: the GI hit's shading, and its albedo as the throughput (Throughput = Albedo.xyz).
 __global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                               const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
-                              const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                              const Materials mat, GiArgs a,
                               float4* __restrict__ rad, float4* __restrict__ thr) {
     const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -463,9 +528,9 @@ __global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, cons
     get_hit(hits, c, h0, h1);
     const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * c + 1));
     const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-    rad[c] = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+    rad[c] = shade_one(s, mat, a, rd, h0, h1, l);
     if (h0.x > 0.0f) {
-        const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
+        const f3 alb = hit_albedo(s, mat, h0, h1);
         thr[c] = make_float4(alb.x, alb.y, alb.z, 1.0f);
     } else {
         thr[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -513,7 +578,7 @@ __global__ void k_bounce_raygen(SceneView s, const rq_ray* prev_rays, const rq_h
 // 1.1 x sky x throughput (nothing under ref_miss, as the reference) and ends the path.
 __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                                const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
-                               const float* __restrict__ albedo, int32_t n_albedo, GiArgs a, int ref_miss,
+                               const Materials mat, GiArgs a, int ref_miss,
                                float4* __restrict__ rad, float4* __restrict__ thr, unsigned long long* hit_count) {
     const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -528,11 +593,11 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
             if (h0.x > 0.0f) {
                 const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * c + 1));
                 const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-                const float4 v = shade_one(s, albedo, n_albedo, a, rd, h0, h1, l);
+                const float4 v = shade_one(s, mat, a, rd, h0, h1, l);
                 R.x = __fadd_rn(R.x, __fmul_rn(v.x, T.x));
                 R.y = __fadd_rn(R.y, __fmul_rn(v.y, T.y));
                 R.z = __fadd_rn(R.z, __fmul_rn(v.z, T.z));
-                const f3 alb = mesh_albedo(albedo, n_albedo, h1.y);
+                const f3 alb = hit_albedo(s, mat, h0, h1);
                 T = make_float4(__fmul_rn(T.x, alb.x), __fmul_rn(T.y, alb.y), __fmul_rn(T.z, alb.z), 1.0f);
                 hit = true;
             } else {
@@ -593,7 +658,7 @@ __global__ void k_count_bytes_c(const uint8_t* __restrict__ b, int64_t n_max,
 // GetDirect (DiffuseTrace.glsl:368-372) + emissive (:491) + AO (:494).
 __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                         int64_t n, const uint8_t* __restrict__ lit, int lit_is_occlusion,
-                        const float* __restrict__ albedo, int32_t n_albedo, GiArgs a,
+                        const Materials mat, GiArgs a,
                         float4* __restrict__ out) {
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -608,7 +673,7 @@ __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_h
     get_hit(hits, j, h0, h1);
     // lit[j] = 1 means the sun is visible; an occlusion buffer (1 = blocked) is read inverted.
     const float l = lit ? ((lit[j] != 0) != (lit_is_occlusion != 0) ? 1.0f : 0.0f) : 1.0f;
-    out[j] = shade_one(s, albedo, n_albedo, a, strict::xyz(r1), h0, h1, l);
+    out[j] = shade_one(s, mat, a, strict::xyz(r1), h0, h1, l);
 }
 
 // AO query: visibility 1 - occluded for active rays, 0 for inactive ones.
@@ -759,8 +824,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     }
     if (bounce) {
         // the bounces reuse the secondary ray / hit buffers in place (slot c only reads its own)
-        k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, sc->d_albedo,
-                                                    sc->n_albedo, a, rad, thr);
+        k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, materials_of(sc), a, rad, thr);
         RQ_CUDA(ctx, cudaGetLastError());
         QueryConfig qb = q;  // bounces use IntersectRay, not the ignore-transparent variant
         qb.flags &= ~RQ_FLAG_IGNORE_TRANSPARENT;
@@ -778,8 +842,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
                 RQ_CUDA(ctx, launch_anyhit(cv, qb, sh, m, occ, queue_counter(ctx, 2), st));
                 bvis = occ;
             }
-            k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, bvis, count, m, sc->d_albedo,
-                                                         sc->n_albedo, a, (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0,
+            k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, bvis, count, m, materials_of(sc), a, (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0,
                                                          rad, thr, stats ? cnt + 7 : nullptr);
             RQ_CUDA(ctx, cudaGetLastError());
         }
@@ -789,8 +852,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     if (p.unfused && !bounce) {  // per-sample shading into a scratch buffer, then the per-pixel mean
         if ((s = scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
         shade = static_cast<float4*>(d_shade);
-        k_shade_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p.query, sc->d_albedo,
-                                                sc->n_albedo, a, shade);
+        k_shade_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p.query, materials_of(sc), a, shade);
     }
     for (int64_t off = 0; off < n; off += chunk) {
         const int64_t c = std::min(chunk, n - off);
@@ -800,7 +862,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
             k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, pixels4 + off);
         else
             k_shade_accumulate<<<grid(c, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of + off * p.spp, c, vis,
-                                                             p.query, sc->d_albedo, sc->n_albedo, a, pixels4 + off);
+                                                             p.query, materials_of(sc), a, pixels4 + off);
         RQ_CUDA(ctx, cudaGetLastError());
         if (h_pix) {
             RQ_CUDA(ctx, cudaEventRecord(ctx->ev, st));
@@ -819,7 +881,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
 // The GI pass over caller-provided intermediate buffers: the kernel sequence of rq_gi_frame
 // without its ray-count statistics.  Used by the no-allocation entry point (rq_noalloc.cu).
 cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
-                               const float* albedo, int32_t n_albedo, const rq_ray* prim,
+                               const Materials& mat, const rq_ray* prim,
                                int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st) {
     const GiArgs a = to_args(p);
     const int64_t m = n * p.spp;
@@ -843,7 +905,7 @@ cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const r
             lit = b.occluded;
         }
         k_shade<<<grid(m, 256), 256, 0, st>>>(s, b.secondary, b.secondary_hits, m, lit, lit ? 1 : 0,
-                                              albedo, n_albedo, a, b.shaded);
+                                              mat, a, b.shaded);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_accumulate<<<grid(n, 256), 256, 0, st>>>(b.shaded, n, p.spp, reinterpret_cast<float4*>(pixels4));
@@ -870,6 +932,65 @@ rq_status rq_scene_set_materials(rq_scene* sc, const float* albedo_rgb, int32_t 
     RQ_CUDA(ctx, cudaMemcpy(sc->d_albedo, albedo_rgb, sizeof(float) * 3 * n_meshes,
                             cudaMemcpyHostToDevice));
     sc->n_albedo = n_meshes;
+    return RQ_OK;
+}
+
+rq_status rq_scene_set_textures(rq_scene* sc, const rq_texture* textures, int32_t n_textures,
+                                const int32_t* mesh_texture, int32_t n_meshes) {
+    if (!sc || n_textures < 0 || n_meshes < 0 || (n_textures > 0 && !textures) || (n_meshes > 0 && !mesh_texture))
+        return fail(sc ? sc->ctx : nullptr, RQ_EINVAL, "bad texture arguments");
+    rq_ctx* ctx = sc->ctx;
+    std::vector<int4> desc(n_textures);
+    int64_t total = 0;
+    for (int32_t t = 0; t < n_textures; ++t) {
+        const rq_texture& x = textures[t];
+        if (x.width < 1 || x.height < 1 || x.width > 65536 || x.height > 65536 || !x.rgba8 ||
+            (x.srgb != 0 && x.srgb != 1) || (x.wrap != 0 && x.wrap != 1))
+            return fail(ctx, RQ_EINVAL, "texture " + std::to_string(t) + ": bad size, data, srgb or wrap");
+        desc[t] = make_int4(static_cast<int32_t>(total), x.width, x.height, x.srgb | (x.wrap << 1));
+        total += static_cast<int64_t>(x.width) * x.height;
+        if (total >= (int64_t(1) << 31)) return fail(ctx, RQ_EINVAL, "more than 2^31 texels");
+    }
+    for (int32_t m = 0; m < n_meshes; ++m)
+        if (mesh_texture[m] < -1 || mesh_texture[m] >= n_textures)
+            return fail(ctx, RQ_EINVAL, "mesh " + std::to_string(m) + ": texture index out of range");
+    std::vector<uint32_t> texels(static_cast<size_t>(total));
+    for (int32_t t = 0; t < n_textures; ++t) {
+        const uint8_t* p = textures[t].rgba8;
+        const int64_t nt = static_cast<int64_t>(textures[t].width) * textures[t].height;
+        for (int64_t k = 0; k < nt; ++k)
+            texels[desc[t].x + k] = uint32_t(p[4 * k]) | (uint32_t(p[4 * k + 1]) << 8) |
+                                    (uint32_t(p[4 * k + 2]) << 16) | (uint32_t(p[4 * k + 3]) << 24);
+    }
+    float lut[256];  // IEC 61966-2-1 decoding of byte / 255, in double, rounded once
+    for (int c = 0; c < 256; ++c) {
+        const double x = c / 255.0;
+        lut[c] = static_cast<float>(x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4));
+    }
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    RQ_CUDA(ctx, cudaDeviceSynchronize());  // no kernel may still read the old arrays
+    for (void* q : {static_cast<void*>(sc->d_mesh_tex), static_cast<void*>(sc->d_tex),
+                    static_cast<void*>(sc->d_texels), static_cast<void*>(sc->d_srgb)})
+        if (q) cudaFree(q);
+    sc->d_mesh_tex = nullptr;
+    sc->d_tex = nullptr;
+    sc->d_texels = nullptr;
+    sc->d_srgb = nullptr;
+    sc->n_mesh_tex = 0;
+    sc->tex_bytes = 0;
+    if (n_meshes == 0) return RQ_OK;
+    const size_t mb = 4 * static_cast<size_t>(n_meshes), db = 16 * std::max<size_t>(1, desc.size()),
+                 tb = 4 * std::max<size_t>(1, texels.size());
+    if (cudaMalloc(&sc->d_mesh_tex, mb) != cudaSuccess || cudaMalloc(&sc->d_tex, db) != cudaSuccess ||
+        cudaMalloc(&sc->d_texels, tb) != cudaSuccess || cudaMalloc(&sc->d_srgb, sizeof(lut)) != cudaSuccess)
+        return fail(ctx, RQ_ENOMEM, "texture allocation failed");
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_mesh_tex, mesh_texture, mb, cudaMemcpyHostToDevice));
+    if (!desc.empty()) RQ_CUDA(ctx, cudaMemcpy(sc->d_tex, desc.data(), 16 * desc.size(), cudaMemcpyHostToDevice));
+    if (!texels.empty())
+        RQ_CUDA(ctx, cudaMemcpy(sc->d_texels, texels.data(), 4 * texels.size(), cudaMemcpyHostToDevice));
+    RQ_CUDA(ctx, cudaMemcpy(sc->d_srgb, lut, sizeof(lut), cudaMemcpyHostToDevice));
+    sc->n_mesh_tex = n_meshes;
+    sc->tex_bytes = static_cast<int64_t>(mb + db + tb + sizeof(lut));
     return RQ_OK;
 }
 
@@ -910,8 +1031,8 @@ rq_status rq_shade(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, const rq
     if (s != RQ_OK || n == 0) return s;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = the default stream
-    rq::k_shade<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, rays, hits, n, lit, 0, sc->d_albedo,
-                                                  sc->n_albedo, rq::to_args(*p),
+    rq::k_shade<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, rays, hits, n, lit, 0, rq::materials_of(sc),
+                                                  rq::to_args(*p),
                                                   reinterpret_cast<float4*>(out4));
     RQ_CUDA(ctx, cudaGetLastError());
     return RQ_OK;

@@ -40,6 +40,20 @@ struct SceneView {
     int32_t tlas_pad;
 };
 
+// Per-mesh surface data of the shading kernels: ModelColor per mesh id, and optional albedo
+// textures (rq_scene_set_textures): per mesh a texture index (-1: ModelColor), per texture
+// {first texel, width, height, flags (1 = sRGB colour channels, 2 = clamp to edge)}, RGBA8 texels,
+// and the sRGB decoding table of the 256 byte values.
+struct Materials {
+    const float* albedo;
+    int32_t n_albedo;
+    int32_t n_mesh_tex;
+    const int32_t* mesh_tex;
+    const int4* tex;
+    const uint32_t* texels;
+    const float* srgb;
+};
+
 // The view a query runs on: RQ_FLAG_ENTITY_LOOP walks every entity in turn.
 inline SceneView entity_view(const SceneView& s, int flags) {
     SceneView v = s;
@@ -117,7 +131,7 @@ struct GiBuffers {
 
 // The GI pass over caller-provided intermediate buffers (rq_gi.cu).
 cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
-                               const float* albedo, int32_t n_albedo, const rq_ray* prim,
+                               const Materials& mat, const rq_ray* prim,
                                int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st);
 
 }  // namespace rq

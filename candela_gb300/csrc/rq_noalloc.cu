@@ -96,7 +96,7 @@ rq_status rq_gi_frame_noalloc(rq_ctx* ctx, const rq_scene* sc, const rq_ray* pri
     b.shadow = reinterpret_cast<rq_ray*>(base + kShadowOff);
     b.shaded = reinterpret_cast<float4*>(base + kShadedOff);
     b.occluded = base + kOccOff;
-    RQ_CUDA(ctx, rq::gi_pass_on_buffers(sc->view, q, *p, sc->d_albedo, sc->n_albedo, primary, n, b,
+    RQ_CUDA(ctx, rq::gi_pass_on_buffers(sc->view, q, *p, rq::materials_of(sc), primary, n, b,
                                         pixels4, static_cast<cudaStream_t>(stream)));
     return RQ_OK;
 }

@@ -47,6 +47,13 @@ struct rq_scene {
     float4* d_tri_fast = nullptr;  // fast-mode triangle records (3 x float4 per triangle)
     float* d_albedo = nullptr;  // 3 floats per mesh id
     int32_t n_albedo = 0;
+    // albedo textures (rq_scene_set_textures)
+    int32_t* d_mesh_tex = nullptr;
+    int32_t n_mesh_tex = 0;
+    int4* d_tex = nullptr;
+    uint32_t* d_texels = nullptr;
+    float* d_srgb = nullptr;
+    int64_t tex_bytes = 0;
     // host copies (validation and derived layouts)
     std::vector<int32_t> h_tris;
     std::vector<float> h_verts;
@@ -77,6 +84,11 @@ struct rq_scene {
 };
 
 namespace rq {
+
+inline Materials materials_of(const rq_scene* sc) {
+    return Materials{sc->d_albedo, sc->n_albedo, sc->n_mesh_tex, sc->d_mesh_tex, sc->d_tex, sc->d_texels,
+                     sc->d_srgb};
+}
 
 rq_status fail(rq_ctx* ctx, rq_status s, const std::string& msg);
 // Rebuilds the top level over the scene's entities (none below kTlasMinEntities entities).

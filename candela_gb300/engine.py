@@ -330,6 +330,17 @@ class _GiMixin:
         a = np.ascontiguousarray(albedo_rgb, dtype=np.float32).reshape(-1, 3)
         check(lib().rq_scene_set_materials(self.handle, ptr(a), a.shape[0]), self.ctx.handle)
 
+    def set_textures(self, textures, mesh_texture):
+        """rq_scene_set_textures.  textures: list of (rgba8 uint8 array (H, W, 4), srgb, wrap);
+        mesh_texture: texture index per mesh id (-1: ModelColor)."""
+        keep = [np.ascontiguousarray(t[0], dtype=np.uint8) for t in textures]
+        arr = (L.RqTexture * max(1, len(keep)))()
+        for k, (img, (_, srgb, wrap)) in enumerate(zip(keep, textures)):
+            arr[k] = L.RqTexture(img.shape[1], img.shape[0], int(srgb), int(wrap), img.ctypes.data)
+        mt = np.ascontiguousarray(mesh_texture, dtype=np.int32)
+        check(lib().rq_scene_set_textures(self.handle, C.cast(arr, C.c_void_p), len(keep), ptr(mt), mt.size),
+              self.ctx.handle)
+
     def gi_raygen(self, primary, hits, params, out=None, stream=None):
         """Device tensors: primary (n*32 bytes), hits (n, 8) -> secondary rays (n*spp*32 bytes)."""
         import torch

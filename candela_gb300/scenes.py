@@ -117,6 +117,26 @@ def make_vertices(pos: np.ndarray, normals: np.ndarray) -> np.ndarray:
     return v
 
 
+def with_texcoords(vertices: np.ndarray, uv: np.ndarray) -> np.ndarray:
+    """A copy of VERTEX_DTYPE records with texture coordinates (n, 2) half-packed into the last
+    word (Vertex.PackedData.w: u in the low half, v in the high half, as packHalf2x16)."""
+    v = np.array(vertices, copy=True)
+    h = float_to_half_bits(np.asarray(uv, dtype=np.float32))
+    v["packed"][:, 3] = (h[:, 0] | (h[:, 1] << np.uint32(16))).astype(np.uint32)
+    return v
+
+
+def noise_texture(size: int, seed: int) -> np.ndarray:
+    """A (size, size, 4) uint8 RGBA texture: seeded value noise per channel plus a checker."""
+    u = uniform(seed, 606, size * size * 3).reshape(size, size, 3)
+    yy, xx = np.mgrid[0:size, 0:size]
+    checker = ((xx // max(1, size // 8) + yy // max(1, size // 8)) % 2)[..., None]
+    img = np.zeros((size, size, 4), np.uint8)
+    img[..., :3] = np.clip(40 + 150 * u + 60 * checker, 0, 255).astype(np.uint8)
+    img[..., 3] = 255
+    return img
+
+
 # ---------------------------------------------------------------------------------------------
 # Meshes
 

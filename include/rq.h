@@ -433,6 +433,24 @@ typedef struct rq_frame_stats {
  * an entry shade with albedo 0.8. */
 rq_status rq_scene_set_materials(rq_scene* scene, const float* albedo_rgb, int32_t n_meshes);
 
+/* An albedo texture (GLClasses/Texture.cpp): width x height RGBA8 texels, rows from v = 0 up,
+ * 4 bytes per texel (alpha unused).  srgb = 1 decodes the colour channels from sRGB before
+ * filtering (the GL_SRGB_ALPHA internal format), wrap 0 = GL_REPEAT, 1 = GL_CLAMP_TO_EDGE. */
+typedef struct rq_texture {
+    int32_t width, height;
+    int32_t srgb, wrap;
+    const uint8_t* rgba8;
+} rq_texture;
+
+/* Albedo textures per mesh (BVHTextureReferences[mesh].Albedo, Intersector.h:373-418): a mesh m
+ * with mesh_texture[m] >= 0 shades with that texture at the hit's UV (GetData,
+ * TraverseBVHStack.glsl:436-447: the vertices' half-packed texture coordinates weighted by the
+ * barycentrics), sampled bilinearly at level 0 as texture() does in a compute shader; other meshes
+ * keep their ModelColor.  The data are copied; n_meshes = 0 removes the textures.  The filter
+ * weights are exact binary32 products here, where GL hardware rounds them to 8 fractional bits. */
+rq_status rq_scene_set_textures(rq_scene* scene, const rq_texture* textures, int32_t n_textures,
+                                const int32_t* mesh_texture, int32_t n_meshes);
+
 /* Cosine-weighted secondary rays from primary hits: for primary ray i with a hit and k < spp,
  * out[i*spp + k] = {P + N*offset, 0, CosWeightedHemisphere(N, hash(seed, i*spp + k)), ray_tmax}
  * with N faced toward the incoming ray (DiffuseTrace.glsl:439-446, 486-488; Sampling.glsl:1-12);

@@ -46,6 +46,33 @@ class OrcScene(C.Structure):
                 ("layout", C.c_int32)]
 
 
+class OrcMaterials(C.Structure):
+    _fields_ = [("albedo", C.c_void_p), ("n_albedo", C.c_int32), ("n_mesh_tex", C.c_int32),
+                ("mesh_tex", C.c_void_p), ("tex", C.c_void_p), ("texels", C.c_void_p)]
+
+
+def materials(albedo, textures=None, mesh_texture=None):
+    """orc_materials for ModelColors (n, 3) and optional textures (list of (rgba8 (H, W, 4), srgb,
+    wrap)) with a texture index per mesh.  Returns (struct, arrays to keep alive)."""
+    alb = np.ascontiguousarray(albedo, dtype=np.float32).reshape(-1, 3)
+    keep = [alb]
+    m = OrcMaterials(alb.ctypes.data, alb.shape[0], 0, None, None, None)
+    if textures:
+        desc, texels, off = [], [], 0
+        for img, srgb, wrap in textures:
+            img = np.ascontiguousarray(img, dtype=np.uint8)
+            h, w = img.shape[:2]
+            desc.append([off, w, h, int(srgb) | (int(wrap) << 1)])
+            texels.append(img.reshape(-1, 4).copy().view(np.uint32).ravel())
+            off += w * h
+        d = np.ascontiguousarray(desc, dtype=np.int32)
+        tx = np.ascontiguousarray(np.concatenate(texels), dtype=np.uint32)
+        mt = np.ascontiguousarray(mesh_texture, dtype=np.int32)
+        keep += [d, tx, mt]
+        m.n_mesh_tex, m.mesh_tex, m.tex, m.texels = mt.size, mt.ctypes.data, d.ctypes.data, tx.ctypes.data
+    return m, keep
+
+
 _orc = None
 
 
@@ -67,7 +94,8 @@ def orc() -> C.CDLL:
         L.orc_barycentrics.argtypes = [P] * 5
         L.orc_gi_raygen.argtypes = [sp, P, P, I64, I32, C.c_uint32, C.c_float, C.c_float, I32,
                                     C.c_int, P]
-        L.orc_shade.argtypes = [sp, P, P, I64, P, P, I32, P, P, P, I32, C.c_int, P]
+        L.orc_shade.argtypes = [sp, P, P, I64, P, C.POINTER(OrcMaterials), P, P, P, I32, C.c_int, P]
+        L.orc_hit_albedo.argtypes = [sp, P, I64, C.POINTER(OrcMaterials), C.c_int, P]
         L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
         L.orc_bounce_raygen.argtypes = [sp, P, P, P, P, I64, C.c_uint32, I32, C.c_float, C.c_float, I32,
                                         C.c_int, P]
@@ -155,17 +183,25 @@ class OracleScene:
         return out
 
     def shade(self, rays, hits, shadow_lit, albedo, sun_dir, sun_color, sky_color,
-              normal_mode=0, nthreads=None):
+              normal_mode=0, nthreads=None, textures=None, mesh_texture=None):
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
-        alb = np.ascontiguousarray(albedo, dtype=np.float32).reshape(-1, 3)
+        mat, keep = materials(albedo, textures, mesh_texture)
         lit = None if shadow_lit is None else np.ascontiguousarray(shadow_lit, dtype=np.uint8)
         out = np.empty((rays.shape[0], 4), dtype=np.float32)
         f3 = lambda x: np.asarray(x, dtype=np.float32)  # noqa: E731
         sd, sc, sk = f3(sun_dir), f3(sun_color), f3(sky_color)
-        orc().orc_shade(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(lit), _p(alb),
-                        alb.shape[0], _p(sd), _p(sc), _p(sk), normal_mode,
-                        nthreads or os.cpu_count() or 1, _p(out))
+        orc().orc_shade(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(lit), C.byref(mat),
+                        _p(sd), _p(sc), _p(sk), normal_mode, nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def hit_albedo(self, hits, albedo, textures=None, mesh_texture=None, nthreads=None):
+        """GetData's albedo per hit ((n, 3) float32): texture at the hit's UV or ModelColor."""
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        mat, keep = materials(albedo, textures, mesh_texture)
+        out = np.empty((hits.shape[0], 3), dtype=np.float32)
+        orc().orc_hit_albedo(C.byref(self.s), _p(hits), hits.shape[0], C.byref(mat),
+                             nthreads or os.cpu_count() or 1, _p(out))
         return out
 
 

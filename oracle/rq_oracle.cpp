@@ -14,6 +14,7 @@
 //  * 1.0/x and a/b are IEEE divisions; normalize(v) = v / sqrt(dot(v,v)).
 #include "rq_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -648,6 +649,69 @@ V3 hit_normal(const Scene& s, const orc_hit& h, int mode) {
     return normalize(cross(sub(B, A), sub(C, A)));
 }
 
+// ---- GetData's albedo (Include/TraverseBVHStack.glsl:422-455) ------------------------------
+// ModelColor of the mesh, or its texture at the hit's UV: the three vertices' half-packed
+// texture coordinates (Vertex.PackedData.w) weighted by the barycentrics (u, v, w), then
+// texture() of a compute shader: level 0, GL_LINEAR (bilinear, texel centres at half integers),
+// GL_REPEAT or GL_CLAMP_TO_EDGE, sRGB channels decoded (IEC 61966-2-1) before filtering.
+
+float srgb_decode(uint32_t c) {
+    static const std::vector<float> lut = [] {
+        std::vector<float> t(256);
+        for (int k = 0; k < 256; ++k) {
+            const double x = k / 255.0;
+            t[k] = float(x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4));
+        }
+        return t;
+    }();
+    return lut[c & 0xFFu];
+}
+
+V3 texel_rgb(const orc_materials& m, int32_t first, int32_t w, int32_t i, int32_t j, bool srgb) {
+    const uint32_t t = m.texels[first + int64_t(j) * w + i];
+    const uint32_t r = t & 0xFFu, g = (t >> 8) & 0xFFu, b = (t >> 16) & 0xFFu;
+    if (srgb) return {srgb_decode(r), srgb_decode(g), srgb_decode(b)};
+    return {float(r) / 255.0f, float(g) / 255.0f, float(b) / 255.0f};
+}
+
+int32_t wrap_index(int32_t i, int32_t n, bool clamp) {
+    if (clamp) return std::min(std::max(i, 0), n - 1);
+    const int32_t r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+V3 sample_bilinear(const orc_materials& m, int32_t t, float u, float v) {
+    const int32_t* d = m.tex + 4 * t;
+    const bool srgb = d[3] & 1, clamp = d[3] & 2;
+    const float x = u * float(d[1]) - 0.5f, y = v * float(d[2]) - 0.5f;
+    const float lim = 1073741824.0f;
+    const float fx = std::min(std::max(std::floor(x), -lim), lim), fy = std::min(std::max(std::floor(y), -lim), lim);
+    const float a = std::min(std::max(x - fx, 0.0f), 1.0f), b = std::min(std::max(y - fy, 0.0f), 1.0f);
+    const int32_t ix = int32_t(fx), iy = int32_t(fy);
+    const int32_t i0 = wrap_index(ix, d[1], clamp), i1 = wrap_index(ix + 1, d[1], clamp);
+    const int32_t j0 = wrap_index(iy, d[2], clamp), j1 = wrap_index(iy + 1, d[2], clamp);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    const V3 t00 = texel_rgb(m, d[0], d[1], i0, j0, srgb), t10 = texel_rgb(m, d[0], d[1], i1, j0, srgb);
+    const V3 t01 = texel_rgb(m, d[0], d[1], i0, j1, srgb), t11 = texel_rgb(m, d[0], d[1], i1, j1, srgb);
+    return add(add(add(muls(t00, w00), muls(t10, w10)), muls(t01, w01)), muls(t11, w11));
+}
+
+V3 hit_albedo(const Scene& s, const orc_materials& m, const orc_hit& h) {
+    if (h.mesh >= 0 && h.mesh < m.n_mesh_tex && h.t > 0.0f && m.mesh_tex[h.mesh] >= 0) {
+        const int32_t* tr = s.tris + int64_t(h.tri) * 4;
+        const uint32_t* va = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[0]) * 8);
+        const uint32_t* vb = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[1]) * 8);
+        const uint32_t* vc = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[2]) * 8);
+        const float u = (half_to_float(va[7] & 0xFFFFu) * h.u + half_to_float(vb[7] & 0xFFFFu) * h.v) +
+                        half_to_float(vc[7] & 0xFFFFu) * h.w;
+        const float v = (half_to_float(va[7] >> 16) * h.u + half_to_float(vb[7] >> 16) * h.v) +
+                        half_to_float(vc[7] >> 16) * h.w;
+        return sample_bilinear(m, m.mesh_tex[h.mesh], u, v);
+    }
+    if (h.mesh >= 0 && h.mesh < m.n_albedo) return ld3(m.albedo + 3 * h.mesh);
+    return {0.8f, 0.8f, 0.8f};
+}
+
 float u01(uint32_t h) { return float(h >> 8) * (1.0f / 16777216.0f); }
 
 uint32_t pcg_hash(uint32_t x) {
@@ -853,8 +917,21 @@ void orc_bounce_raygen(const orc_scene* sc, const orc_ray* rays, const orc_hit* 
     });
 }
 
+void orc_hit_albedo(const orc_scene* sc, const orc_hit* hits, int64_t n, const orc_materials* mat,
+                    int nthreads, float* out3) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const V3 a = hit_albedo(s, *mat, hits[i]);
+            out3[3 * i] = a.x;
+            out3[3 * i + 1] = a.y;
+            out3[3 * i + 2] = a.z;
+        }
+    });
+}
+
 void orc_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n,
-               const uint8_t* shadow_lit, const float* albedo, int32_t n_albedo,
+               const uint8_t* shadow_lit, const orc_materials* mat,
                const float sun_dir[3], const float sun_color[3], const float sky_color[3],
                int32_t normal_mode, int nthreads, float* out4) {
     const Scene s = make_scene(sc);
@@ -876,8 +953,7 @@ void orc_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, in
             const V3 rd = ld3(rays[i].d);
             V3 N = hit_normal(s, h, normal_mode);
             if (dot(N, rd) > 0.0001f) N = neg(N);
-            V3 alb = (h.mesh >= 0 && h.mesh < n_albedo) ? ld3(albedo + 3 * h.mesh)
-                                                        : V3{0.8f, 0.8f, 0.8f};
+            const V3 alb = hit_albedo(s, *mat, h);
             float em;
             std::memcpy(&em, &s.ents[h.entity].data[0], 4);
             const float lit = shadow_lit ? (shadow_lit[i] ? 1.0f : 0.0f) : 1.0f;

@@ -78,8 +78,22 @@ void orc_gi_raygen(const orc_scene* s, const orc_ray* primary, const orc_hit* hi
 // Lambert + AO shading of secondary hits (DiffuseTrace.glsl:368-372, 486-494).
 // Per secondary ray j: rgb radiance and AO term written to out4[j*4 .. j*4+3].  Shadow
 // visibility (nullable) is 1 = lit.  albedo: 3 floats per mesh id.
+// Surface data of the shading: ModelColor per mesh id and optional albedo textures (per mesh a
+// texture index or -1; per texture first texel, width, height, flags 1 = sRGB, 2 = clamp; RGBA8
+// texels as little-endian words).
+typedef struct {
+    const float* albedo;
+    int32_t n_albedo;
+    int32_t n_mesh_tex;
+    const int32_t* mesh_tex;
+    const int32_t* tex;
+    const uint32_t* texels;
+} orc_materials;
+
+void orc_hit_albedo(const orc_scene* s, const orc_hit* hits, int64_t n, const orc_materials* mat,
+                    int nthreads, float* out3);
 void orc_shade(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int64_t n,
-               const uint8_t* shadow_lit, const float* albedo, int32_t n_albedo,
+               const uint8_t* shadow_lit, const orc_materials* mat,
                const float sun_dir[3], const float sun_color[3], const float sky_color[3],
                int32_t normal_mode, int nthreads, float* out4);
 

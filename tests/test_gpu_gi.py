@@ -180,7 +180,8 @@ def test_gi_frame_host_chunks_equal_device_pass(ctx, query):
     assert ctx.device_status() == 0
 
 
-def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0):
+def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0, textures=None,
+                        mesh_texture=None, albedo_of=None):
     """The GI pass with the RT second-bounce loop, composed from the oracle's pieces in the
     kernels' operation order (float32 numpy arithmetic, one rounding per operation)."""
     f = np.float32
@@ -190,11 +191,11 @@ def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0):
     sec = osc.gi_raygen(rays, ph, spp, seed, p.origin_offset)
     sh = osc.closest(sec, flags=flags)
     lit = 1 - osc.anyhit(osc.shadow_raygen(sec, sh, sd, p.shadow_offset)) if p.shadow_rays else None
-    rad = osc.shade(sec, sh, lit, albedo, sd, sc_, sky).astype(np.float32)
-    alb_of = lambda mesh: np.where((mesh >= 0)[:, None] & (mesh < len(albedo))[:, None],  # noqa: E731
-                                   albedo[np.clip(mesh, 0, len(albedo) - 1)], f(0.8)).astype(np.float32)
+    tex = dict(textures=textures, mesh_texture=mesh_texture)
+    rad = osc.shade(sec, sh, lit, albedo, sd, sc_, sky, **tex).astype(np.float32)
+    alb_of = albedo_of or (lambda hits: osc.hit_albedo(hits, albedo))  # noqa: E731
     alive = sh["t"] > 0
-    thr = np.where(alive[:, None], alb_of(sh["mesh"]), f(0)).astype(np.float32)
+    thr = np.where(alive[:, None], alb_of(sh), f(0)).astype(np.float32)
     prev_r, prev_h = sec, sh
     sid = np.arange(len(sec), dtype=np.uint32)
     bflags = flags & ~R.engine.L.FLAG_IGNORE_TRANSPARENT
@@ -203,7 +204,7 @@ def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0):
         br = osc.bounce_raygen(prev_r, prev_h, alive, sid, seed, b, 0.02, p.ray_tmax)
         bh = osc.closest(br, flags=bflags)
         blit = 1 - osc.anyhit(osc.shadow_raygen(br, bh, sd, p.shadow_offset)) if p.shadow_rays else None
-        v = osc.shade(br, bh, blit, albedo, sd, sc_, sky).astype(np.float32)
+        v = osc.shade(br, bh, blit, albedo, sd, sc_, sky, **tex).astype(np.float32)
         hit = alive & (bh["t"] > 0)
         miss = alive & ~(bh["t"] > 0)
         n_rays += int(alive.sum())
@@ -211,7 +212,7 @@ def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0):
         rad[hit, :3] = rad[hit, :3] + v[hit, :3] * thr[hit]
         if not ref_miss:
             rad[miss, :3] = rad[miss, :3] + (sky * f(1.1)) * thr[miss]
-        thr[hit] = thr[hit] * alb_of(bh["mesh"][hit])
+        thr[hit] = thr[hit] * alb_of(bh[hit])
         alive = hit
         prev_r, prev_h = br, bh
     rad = np.where((sec["tmax"] > sec["tmin"])[:, None], rad, f(0))
@@ -247,3 +248,47 @@ def test_gi_frame_bounces_match_oracle_pipeline(ctx, bounces, shadow, ref):
     np.testing.assert_array_equal(got[:, 3], base[:, 3])  # AO is the first bounce's
     # host buffers give the same pixels
     np.testing.assert_array_equal(sc.gi_frame(rays, p, flags=flags), got)
+
+
+@pytest.mark.parametrize("srgb,wrap", [(0, 0), (1, 0), (1, 1)])
+def test_textured_shading_matches_oracle(ctx, srgb, wrap):
+    """GetData's albedo texture: UV from the half-packed texture coordinates, bilinear level-0
+    sample; the shaded colour equals the oracle's bit for bit (AO within the pow tolerance),
+    also through the bounce loop's throughput."""
+    m = S.heightfield(32, seed=5)
+    pos = m.positions().astype(np.float64)
+    uv = np.stack([(pos[:, 0] + 1.0) * 1.5 - 0.25, (pos[:, 1] + 1.0) * 1.5 + 0.1], 1)  # outside [0, 1] too
+    verts = S.with_texcoords(m.vertices, uv)
+    mids = (np.arange(m.n_tris) % 3).astype(np.int32)       # three meshes, two textured
+    b = R.build_bvh(verts, m.indices, mids, 0, layout=R.STACK)
+    bufs = (verts, b.tris, b.nodes, R.identity_entity(0, b.nodes.shape[0]))
+    osc = oracle_scene(bufs, R.STACK)
+    sc = ctx.scene(R.STACK, *bufs)
+    albedo = np.float32([[0.7, 0.6, 0.5], [0.2, 0.8, 0.4], [0.9, 0.9, 0.2]])
+    textures = [(S.noise_texture(64, 3), srgb, wrap), (S.noise_texture(17, 4), srgb, wrap)]
+    mesh_tex = [1, -1, 0]
+    sc.set_materials(albedo)
+    sc.set_textures(textures, mesh_tex)
+    rays = S.camera_rays(128, 96, **S.C1_CAMERA)
+    p = gi_params(spp=2, seed=3, origin_offset=1e-3, shadow_rays=True)
+    ph = osc.closest(rays)
+    sec = osc.gi_raygen(rays, ph, 2, 3, 1e-3)
+    sh = osc.closest(sec)
+    lit = 1 - osc.anyhit(osc.shadow_raygen(sec, sh, np.array(p.sun_dir), p.shadow_offset))
+    want = osc.shade(sec, sh, lit, albedo, np.array(p.sun_dir), np.array(p.sun_color),
+                     np.array(p.sky_color), textures=textures, mesh_texture=mesh_tex)
+    d_sec, d_sh = rays_to_device(sec), rays_to_device(sh)
+    got = sc.shade(d_sec, d_sh, p, lit=rays_to_device(lit.astype(np.uint8))).cpu().numpy()
+    np.testing.assert_array_equal(got[:, :3], want[:, :3])
+    np.testing.assert_allclose(got[:, 3], want[:, 3], rtol=SHADE_RTOL)
+    textured = (sh["t"] > 0) & np.isin(sh["mesh"], [0, 2])
+    assert textured.sum() > 300
+    plain = osc.shade(sec, sh, lit, albedo, np.array(p.sun_dir), np.array(p.sun_color), np.array(p.sky_color))
+    assert (np.abs(plain[textured, :3] - want[textured, :3]).max(1) > 0).mean() > 0.5
+    # the bounce loop multiplies by the textured albedo: compare its pixels with the oracle pipeline
+    pb = gi_params(spp=2, seed=3, origin_offset=1e-3, shadow_rays=True, bounces=1)
+    alb_fn = lambda hits: osc.hit_albedo(hits, albedo, textures, mesh_tex)  # noqa: E731
+    want_px, _, _ = _oracle_bounce_pass(osc, rays, pb, albedo, 1, False, 0, textures=textures,
+                                        mesh_texture=mesh_tex, albedo_of=alb_fn)
+    got_px = sc.gi_frame(rays_to_device(rays), pb).cpu().numpy()
+    np.testing.assert_allclose(got_px, want_px, rtol=SHADE_RTOL * 8, atol=1e-6)

@@ -246,3 +246,49 @@ def test_push_cap_reproduced(depth, expect_hit):
     assert (h["t"][0] > 0) == expect_hit
     if not expect_hit:
         assert h["iters"][0] == 64  # 63 pushes, then the 64th node's push is refused
+
+
+# ---- GetData's albedo texture (TraverseBVHStack.glsl:436-447) --------------------------------
+
+def _textured_hit(u, v, w, uvs):
+    """A one-triangle scene whose vertices carry texture coordinates `uvs`, and a hit record with
+    barycentrics (u, v, w) on it."""
+    pos = np.float32([[0, 0, 0], [1, 0, 0], [0, 1, 0], [5, 5, 5], [6, 5, 5], [5, 6, 5]])
+    vert = S.with_texcoords(S.make_vertices(pos, np.tile([0.0, 0.0, 1.0], (6, 1))),
+                            np.concatenate([uvs, np.zeros((3, 2))]).astype(np.float32))
+    b = R.build_bvh(vert, np.arange(6, dtype=np.uint32), np.array([0, 1], np.int32), 0, layout=R.STACKLESS)
+    osc = O.OracleScene(O.ORC_STACKLESS, vert, b.tris, b.nodes, R.identity_entity(0, b.nodes.shape[0]))
+    k = int(np.nonzero(b.tris[:, 3] == 0)[0][0])
+    h = np.zeros(1, dtype=R.HIT_DTYPE)
+    h["t"], h["u"], h["v"], h["w"], h["tri"], h["mesh"], h["entity"] = 1.0, u, v, w, k, 0, 0
+    return osc, h
+
+
+def test_texture_bilinear_known_answers():
+    img = np.zeros((2, 2, 4), np.uint8)
+    img[0, 0, :3], img[0, 1, :3], img[1, 0, :3], img[1, 1, :3] = 0, 255, 51, 102   # (row v, column u)
+    alb = np.float32([[0.1, 0.2, 0.3]])
+    uvs = np.float32([[0.25, 0.25], [0.75, 0.25], [0.25, 0.75]])
+    # barycentric weight 1 on vertex A: uv = (0.25, 0.25), the centre of texel (0, 0)
+    osc, h = _textured_hit(1.0, 0.0, 0.0, uvs)
+    a = osc.hit_albedo(h, alb, [(img, 0, 0)], [0])
+    np.testing.assert_array_equal(a, [[0.0, 0.0, 0.0]])
+    osc, h = _textured_hit(0.0, 1.0, 0.0, uvs)                       # texel (1, 0): 255
+    np.testing.assert_array_equal(osc.hit_albedo(h, alb, [(img, 0, 0)], [0]), [[1.0, 1.0, 1.0]])
+    # halfway between the four texel centres: the mean (0 + 255 + 51 + 102) / 4 / 255
+    osc, h = _textured_hit(0.0, 0.5, 0.5, uvs)                       # uv = (0.5, 0.5)
+    got = osc.hit_albedo(h, alb, [(img, 0, 0)], [0])
+    np.testing.assert_allclose(got, np.full((1, 3), (0 + 255 + 51 + 102) / 4 / 255), rtol=1e-6)
+    # GL_REPEAT: u = 1.25 samples the same texel as u = 0.25; clamp keeps the edge texel
+    uvs2 = np.float32([[1.25, 0.25], [0.75, 0.25], [0.25, 0.75]])
+    osc, h = _textured_hit(1.0, 0.0, 0.0, uvs2)
+    np.testing.assert_array_equal(osc.hit_albedo(h, alb, [(img, 0, 0)], [0]), [[0.0, 0.0, 0.0]])
+    np.testing.assert_array_equal(osc.hit_albedo(h, alb, [(img, 0, 1)], [0]), [[1.0, 1.0, 1.0]])
+    # sRGB: 255 -> 1, 0 -> 0, 51 -> 0.0331048 (IEC 61966-2-1)
+    osc, h = _textured_hit(0.0, 0.0, 1.0, uvs)                       # texel (0, 1): 51
+    np.testing.assert_allclose(osc.hit_albedo(h, alb, [(img, 1, 0)], [0]), [[0.0331048] * 3], rtol=1e-5)
+    # a mesh without a texture, and a miss, keep the ModelColor
+    np.testing.assert_array_equal(osc.hit_albedo(h, alb, [(img, 1, 0)], [-1]), alb)
+    h2 = h.copy()
+    h2["t"] = -1.0
+    np.testing.assert_array_equal(osc.hit_albedo(h2, alb, [(img, 1, 0)], [0]), alb)
