@@ -894,6 +894,18 @@ def main():
                  "anyhit_identical": float((o_strict == o_b8).mean()),
                  "rays": n_sec_slots, "device_status": ctx.device_status()}
 
+    # ---- specular reflection pass (rq_specular_frame) over the same camera: primary + one GGX
+    # reflection ray per pixel (roughness 0.3) + a shadow ray per reflection hit
+    from candela_gb300.engine import specular_params
+    sp = specular_params(seed=1, roughness=0.3, shadow_rays=True)
+    d_spec = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    spec_ms = timed(lambda: sc.specular_frame(d_rays, sp, out=d_spec, layout=B8, stream=sptr))
+    spec_plain_ms = timed(lambda: sc.specular_frame(d_rays, sp, out=d_spec, stream=sptr))
+    specular = {"pixels": n, "ms": round(spec_ms, 4), "strict_bvh2_ms": round(spec_plain_ms, 4),
+                "rays_upper_bound": 3 * n,
+                "mpixels_s": round(n / (spec_ms / 1e3) / 1e6, 1),
+                "desc": "1920x1080 primary + GGX reflection (roughness 0.3) + shadow ray, BVH8q"}
+
     # ---- AABB collision queries (rq_collide) over the same scene: 1M boxes near the surface
     boxes = collide_boxes(wl)
     n_box = len(boxes)
@@ -967,7 +979,7 @@ def main():
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},
             "e2e": e2e, "roofline": roofline, "breakdown": breakdown, "bvh8q_vs_strict": agreement,
-            "bvh_build": bvh_build, "collide": collide,
+            "bvh_build": bvh_build, "collide": collide, "specular": specular,
             "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
                              "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}

@@ -94,6 +94,13 @@ class RqTexture(C.Structure):
                 ("rgba8", C.c_void_p)]
 
 
+class RqSpecularParams(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("roughness", C.c_float), ("ray_tmax", C.c_float),
+                ("normal_mode", C.c_int32), ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
+                ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3), ("sky_color", C.c_float * 3),
+                ("ambient", C.c_float * 3)]
+
+
 class RqFrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("secondary_rays", C.c_int64), ("secondary_hits", C.c_int64),
@@ -156,6 +163,7 @@ SIGNATURES = {
     "rq_collide": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_scene_tlas_info": (_S, [_P, C.POINTER(C.c_int64 * 3)]),
     "rq_scene_set_textures": (_S, [_P, _P, _I32, _P, _I32]),
+    "rq_specular_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqSpecularParams), C.POINTER(RqOpts), _P, _P]),
 }
 
 NOALLOC_MAX_RAYS = 65536

@@ -363,76 +363,6 @@ __global__ void k_shadow_raygen_c(SceneView s, const rq_ray* __restrict__ rays,
     }
 }
 
-// ModelColor of a mesh (GetData, TraverseBVHStack.glsl:440-451); 0.8 grey without an entry.
-__device__ __forceinline__ f3 mesh_albedo(const Materials& mat, int32_t mesh) {
-    if (mesh >= 0 && mesh < mat.n_albedo)
-        return {__ldg(mat.albedo + 3 * mesh), __ldg(mat.albedo + 3 * mesh + 1), __ldg(mat.albedo + 3 * mesh + 2)};
-    return {0.8f, 0.8f, 0.8f};
-}
-
-// The colour channels of texel (i, j): byte / 255, or the sRGB table for an sRGB texture.
-__device__ __forceinline__ f3 texel(const Materials& mat, int32_t first, int32_t w, int32_t i, int32_t j, bool srgb) {
-    const uint32_t t = __ldg(mat.texels + first + static_cast<int64_t>(j) * w + i);
-    const uint32_t r = t & 0xFFu, g = (t >> 8) & 0xFFu, b = (t >> 16) & 0xFFu;
-    if (srgb) return {__ldg(mat.srgb + r), __ldg(mat.srgb + g), __ldg(mat.srgb + b)};
-    return {__fdiv_rn(static_cast<float>(r), 255.0f), __fdiv_rn(static_cast<float>(g), 255.0f),
-            __fdiv_rn(static_cast<float>(b), 255.0f)};
-}
-
-// Texel index along one axis: GL_REPEAT (positive modulo) or GL_CLAMP_TO_EDGE.
-__device__ __forceinline__ int32_t wrap_texel(int32_t i, int32_t n, bool clamp) {
-    if (clamp) return i < 0 ? 0 : (i >= n ? n - 1 : i);
-    const int32_t r = i % n;
-    return r < 0 ? r + n : r;
-}
-
-// texture(Textures[Ref], uv).xyz in a compute shader: level 0 (no derivatives), bilinear (the
-// GL_LINEAR magnification filter), texel centres at half-integers: x = u * width - 0.5,
-// i0 = floor(x), a = x - i0, and the four texels weighted (1-a)(1-b), a(1-b), (1-a)b, ab, summed
-// in that order.  sRGB channels are decoded before filtering.  Coordinates beyond +-2^30 texels
-// are clamped there (the float has no fraction left at that size).
-__device__ f3 sample_texture(const Materials& mat, int32_t t, float u, float v) {
-    const int4 d = __ldg(mat.tex + t);
-    const bool srgb = d.w & 1, clamp = d.w & 2;
-    const float x = __fsub_rn(__fmul_rn(u, static_cast<float>(d.y)), 0.5f);
-    const float y = __fsub_rn(__fmul_rn(v, static_cast<float>(d.z)), 0.5f);
-    const float fx = fminf(fmaxf(floorf(x), -1073741824.0f), 1073741824.0f);
-    const float fy = fminf(fmaxf(floorf(y), -1073741824.0f), 1073741824.0f);
-    const float a = fminf(fmaxf(__fsub_rn(x, fx), 0.0f), 1.0f), b = fminf(fmaxf(__fsub_rn(y, fy), 0.0f), 1.0f);
-    const int32_t ix = static_cast<int32_t>(fx), iy = static_cast<int32_t>(fy);
-    const int32_t i0 = wrap_texel(ix, d.y, clamp), i1 = wrap_texel(ix + 1, d.y, clamp);
-    const int32_t j0 = wrap_texel(iy, d.z, clamp), j1 = wrap_texel(iy + 1, d.z, clamp);
-    const float na = __fsub_rn(1.0f, a), nb = __fsub_rn(1.0f, b);
-    const float w00 = __fmul_rn(na, nb), w10 = __fmul_rn(a, nb), w01 = __fmul_rn(na, b), w11 = __fmul_rn(a, b);
-    const f3 t00 = texel(mat, d.x, d.y, i0, j0, srgb), t10 = texel(mat, d.x, d.y, i1, j0, srgb);
-    const f3 t01 = texel(mat, d.x, d.y, i0, j1, srgb), t11 = texel(mat, d.x, d.y, i1, j1, srgb);
-    return strict::add(strict::add(strict::add(strict::muls(t00, w00), strict::muls(t10, w10)), strict::muls(t01, w01)),
-                       strict::muls(t11, w11));
-}
-
-// Albedo of a hit (GetData, TraverseBVHStack.glsl:422-455): the mesh's texture at the hit's UV
-// (texture coordinates half-packed in Vertex.PackedData.w, weighted by the barycentrics u, v, w)
-// when it has one, else its ModelColor.
-__device__ __forceinline__ f3 hit_albedo(const SceneView& s, const Materials& mat, const float4 h0, const int4 h1) {
-    const int32_t mesh = h1.y;
-    if (mesh >= 0 && mesh < mat.n_mesh_tex && h0.x > 0.0f) {
-        const int32_t t = __ldg(mat.mesh_tex + mesh);
-        if (t >= 0) {
-            const int4 tr = __ldg(s.tris + h1.x);
-            const uint32_t ta = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.x) + 1).w);
-            const uint32_t tb = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.y) + 1).w);
-            const uint32_t tc = __float_as_uint(__ldg(s.verts + 2 * static_cast<int64_t>(tr.z) + 1).w);
-            const float u = __fadd_rn(__fadd_rn(__fmul_rn(gi::half_bits(ta), h0.y), __fmul_rn(gi::half_bits(tb), h0.z)),
-                                      __fmul_rn(gi::half_bits(tc), h0.w));
-            const float v = __fadd_rn(__fadd_rn(__fmul_rn(gi::half_bits(ta >> 16), h0.y),
-                                                __fmul_rn(gi::half_bits(tb >> 16), h0.z)),
-                                      __fmul_rn(gi::half_bits(tc >> 16), h0.w));
-            return sample_texture(mat, t, u, v);
-        }
-    }
-    return mesh_albedo(mat, mesh);
-}
-
 // Radiance and AO of one secondary hit (GetDirect, DiffuseTrace.glsl:368-372; emissive :491;
 // AO :494): h0 = (t, u, v, w), h1 = (tri, mesh, entity), rd the ray direction, l the sun's
 // visibility.  A miss returns the sky.
@@ -441,7 +371,7 @@ __device__ __forceinline__ float4 shade_one(const SceneView& s, const Materials&
     if (!(h0.x > 0.0f)) return make_float4(a.sky.x, a.sky.y, a.sky.z, 1.0f);
     f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
     if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-    const f3 alb = hit_albedo(s, mat, h0, h1);
+    const f3 alb = gi::hit_albedo(s, mat, h0, h1);
     const float em = __int_as_float(s.ents[h1.z].data[0]);
     const float ndl = strict::gmin(strict::gmax(strict::dot(N, strict::neg(a.sun_dir)), 0.0f), 1.0f);
     const f3 direct = strict::muls(strict::muls(strict::mul(alb, a.sun_color), l), ndl);
@@ -530,7 +460,7 @@ __global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, cons
     const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
     rad[c] = shade_one(s, mat, a, rd, h0, h1, l);
     if (h0.x > 0.0f) {
-        const f3 alb = hit_albedo(s, mat, h0, h1);
+        const f3 alb = gi::hit_albedo(s, mat, h0, h1);
         thr[c] = make_float4(alb.x, alb.y, alb.z, 1.0f);
     } else {
         thr[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -597,7 +527,7 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
                 R.x = __fadd_rn(R.x, __fmul_rn(v.x, T.x));
                 R.y = __fadd_rn(R.y, __fmul_rn(v.y, T.y));
                 R.z = __fadd_rn(R.z, __fmul_rn(v.z, T.z));
-                const f3 alb = hit_albedo(s, mat, h0, h1);
+                const f3 alb = gi::hit_albedo(s, mat, h0, h1);
                 T = make_float4(__fmul_rn(T.x, alb.x), __fmul_rn(T.y, alb.y), __fmul_rn(T.z, alb.z), 1.0f);
                 hit = true;
             } else {

@@ -320,6 +320,17 @@ def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode
                         int(sort_rays), int(unfused), int(bounces))
 
 
+def specular_params(seed=0, roughness=0.3, ray_tmax=1000000.0, normal_mode=0, shadow_rays=False,
+                    shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866), sun_color=(4.0, 3.8, 3.5),
+                    sky_color=(0.5, 0.7, 1.0), ambient=(0.1, 0.1, 0.12)) -> L.RqSpecularParams:
+    """rq_specular_params for the specular reflection pass."""
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
+    return L.RqSpecularParams(seed & 0xFFFFFFFF, roughness, ray_tmax, normal_mode, int(shadow_rays), shadow_offset,
+                              f3(sd), f3(sun_color), f3(sky_color), f3(ambient))
+
+
 def _empty_like_dev(ref, shape, dtype):
     import torch
     return torch.empty(shape, dtype=dtype, device=ref.device)
@@ -368,6 +379,18 @@ class _GiMixin:
             out = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
         check(lib().rq_shade(self.ctx.handle, self.handle, ptr(rays), ptr(hits), n, ptr(lit),
                              C.byref(params), ptr(out), _stream(rays, stream)), self.ctx.handle)
+        return out
+
+    def specular_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0, stream=None):
+        """Specular reflection pass (rq_specular_frame): (n, 4) radiance and t / 48 per pixel."""
+        host = isinstance(primary, np.ndarray)
+        n = primary.shape[0] if host else primary.numel() * primary.element_size() // 32
+        if out is None:
+            out = (np.empty((n, 4), dtype=np.float32) if host
+                   else _empty_like_dev(primary, (n, 4), __import__("torch").float32))
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        check(lib().rq_specular_frame(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params), C.byref(o),
+                                      ptr(out), _stream(primary, stream)), self.ctx.handle)
         return out
 
     def gi_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0,

@@ -477,6 +477,37 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary,
                       const rq_gi_params* params, const rq_opts* opts, float* pixels4,
                       rq_frame_stats* stats, void* stream);
 
+/* ---- Specular reflections ---------------------------------------------------------------- */
+
+/* The world-trace path of SpecularTrace.glsl (:485-596 with u_FullRT or metallic surfaces):
+ * per pixel, from the primary hit P with facing normal N and incident I = normalize(P - origin),
+ * a reflection ray from P + N * mix(0.05, 0.1, clamp(1.4 R, 0, 1)) in the direction
+ * StochasticReflectionDirection(I, N, 0.9 R) (:102-135: a mirror reflection below roughness
+ * 0.01, else the first of up to 12 GGX half-vector samples (Sampling.glsl:63-83, sample scaled by
+ * (0.8, 0.7)) above the surface reflected), traced with IntersectRay; a hit is lit by
+ * SampleLighting (:420-425): albedo x sun_color x sun visibility + albedo x 2 x ambient (the
+ * irradiance the probe volume would return) + albedo x emissive; a miss sees
+ * sky x mix(1.4, 2.65, R) (:435-437).  Non-finite radiance becomes 0 with t = -1, then radiance is
+ * clamped to [0, 6]; out4 = (radiance, t / 48) (TransformReflectionTransversal), t = -1 for a
+ * miss; pixels whose primary ray misses get 0.  Samples come from the counter-based hash of the GI
+ * pass (the reference's fract-sin hash2 depends on the driver's sin). */
+typedef struct rq_specular_params {
+    uint32_t seed;
+    float roughness;      /* PBR.x of the shaded surfaces */
+    float ray_tmax;
+    int32_t normal_mode;  /* as rq_gi_params */
+    int32_t shadow_rays;  /* 1 = sun visibility from an any-hit shadow ray (GetDirectShadow) */
+    float shadow_offset;
+    float sun_dir[3];
+    float sun_color[3];   /* SUN_COLOR_SPEC */
+    float sky_color[3];   /* u_SkyCube sample */
+    float ambient[3];     /* SampleProbes stand-in */
+} rq_specular_params;
+/* With RQ_FLAG_HOST_BUFFERS in opts, `primary` and `out4` are host memory. */
+rq_status rq_specular_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,
+                            const rq_specular_params* params, const rq_opts* opts, float* out4,
+                            void* stream);
+
 /* ---- Differentiation: depth + Lambert adjoint w.r.t. vertex positions ---------------------- */
 
 /* No counterpart in the reference (its GI is not differentiable).  Per primary ray i the forward

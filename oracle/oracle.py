@@ -96,6 +96,8 @@ def orc() -> C.CDLL:
                                     C.c_int, P]
         L.orc_shade.argtypes = [sp, P, P, I64, P, C.POINTER(OrcMaterials), P, P, P, I32, C.c_int, P]
         L.orc_hit_albedo.argtypes = [sp, P, I64, C.POINTER(OrcMaterials), C.c_int, P]
+        L.orc_spec_raygen.argtypes = [sp, P, P, I64, C.c_uint32, C.c_float, C.c_float, I32, C.c_int, P]
+        L.orc_spec_shade.argtypes = [sp, P, P, I64, P, C.POINTER(OrcMaterials), C.c_float, P, P, P, C.c_int, P]
         L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
         L.orc_bounce_raygen.argtypes = [sp, P, P, P, P, I64, C.c_uint32, I32, C.c_float, C.c_float, I32,
                                         C.c_int, P]
@@ -193,6 +195,29 @@ class OracleScene:
         sd, sc, sk = f3(sun_dir), f3(sun_color), f3(sky_color)
         orc().orc_shade(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(lit), C.byref(mat),
                         _p(sd), _p(sc), _p(sk), normal_mode, nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def spec_raygen(self, primary, hits, seed, roughness, ray_tmax=1000000.0, normal_mode=0, nthreads=None):
+        """Reflection rays of the specular pass (SpecularTrace.glsl:505-513)."""
+        primary = np.ascontiguousarray(primary, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.empty(primary.shape[0], dtype=RAY_DTYPE)
+        orc().orc_spec_raygen(C.byref(self.s), _p(primary), _p(hits), primary.shape[0], seed & 0xFFFFFFFF,
+                              roughness, ray_tmax, normal_mode, nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def spec_shade(self, rays, hits, lit, albedo, roughness, sun_color, sky_color, ambient,
+                   textures=None, mesh_texture=None, nthreads=None):
+        """(radiance, t / 48) of the specular pass (SpecularTrace.glsl:420-437, 588-596)."""
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        mat, keep = materials(albedo, textures, mesh_texture)
+        lit = None if lit is None else np.ascontiguousarray(lit, dtype=np.uint8)
+        f3 = lambda x: np.asarray(x, dtype=np.float32)  # noqa: E731
+        sc_, sk, am = f3(sun_color), f3(sky_color), f3(ambient)
+        out = np.empty((rays.shape[0], 4), dtype=np.float32)
+        orc().orc_spec_shade(C.byref(self.s), _p(rays), _p(hits), rays.shape[0], _p(lit), C.byref(mat), roughness,
+                             _p(sc_), _p(sk), _p(am), nthreads or os.cpu_count() or 1, _p(out))
         return out
 
     def hit_albedo(self, hits, albedo, textures=None, mesh_texture=None, nthreads=None):

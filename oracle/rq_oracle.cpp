@@ -917,6 +917,116 @@ void orc_bounce_raygen(const orc_scene* sc, const orc_ray* rays, const orc_hit* 
     });
 }
 
+// ---- Specular reflections (SpecularTrace.glsl:485-596, world-trace path) ----------------------
+
+namespace {
+
+// reflect(I, N) = I - 2 dot(N, I) N.
+V3 reflect_dir(V3 i, V3 n) { return sub(i, muls(n, 2.0f * dot(n, i))); }
+
+// SampleGGXVNDF, Include/Sampling.glsl:63-83, with sin / cos of 2 pi x0 from sincos_turns.
+V3 sample_ggx(V3 n, float roughness, float x0, float x1) {
+    const float alpha = roughness * roughness;
+    const float alpha2 = alpha * alpha;
+    float sp, cp;
+    sincos_turns(x0, sp, cp);
+    const float ct = std::sqrt((1.0f - x1) / (1.0f + (alpha2 - 1.0f) * x1));
+    const float st = std::sqrt(1.0f - ct * ct);
+    const V3 h = {cp * st, sp * st, ct};
+    const V3 up = std::fabs(n.z) < 0.999f ? V3{0.0f, 0.0f, 1.0f} : V3{1.0f, 0.0f, 0.0f};
+    const V3 tangent = normalize(cross(up, n));
+    const V3 bitangent = cross(n, tangent);
+    return normalize(add(add(muls(tangent, h.x), muls(bitangent, h.y)), muls(n, h.z)));
+}
+
+float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+
+}  // namespace
+
+// Reflection ray per pixel: origin P + N * mix(0.05, 0.1, clamp(1.4 R, 0, 1)) (:509), direction
+// StochasticReflectionDirection(normalize(P - origin), N, 0.9 R) (:102-135): a mirror below 0.01,
+// else the first of 12 GGX samples (hash dimensions 2k, 2k+1 scaled by 0.8, 0.7) above the surface.
+void orc_spec_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit* hits, int64_t n, uint32_t seed,
+                     float roughness, float ray_tmax, int32_t normal_mode, int nthreads, orc_ray* out) {
+    const Scene s = make_scene(sc);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const orc_hit& h = hits[i];
+            orc_ray& o = out[i];
+            if (!(h.t > 0.0f)) {
+                o = orc_ray{{0, 0, 0}, 0.0f, {0, 0, 1}, -1.0f};
+                continue;
+            }
+            const V3 ro = ld3(primary[i].o), rd = ld3(primary[i].d);
+            const V3 P = add(ro, muls(rd, h.t));
+            V3 N = hit_normal(s, h, normal_mode);
+            if (dot(N, rd) > 0.0001f) N = neg(N);
+            const V3 I = normalize(sub(P, ro));
+            const float r = roughness * 0.9f;
+            V3 dir;
+            if (r < 0.01f) {
+                dir = reflect_dir(I, N);
+            } else {
+                V3 micro = N;
+                for (uint32_t k = 0; k < 12; ++k) {
+                    const float x0 = u01(sample_key(seed, uint32_t(i), 2u * k)) * 0.8f;
+                    const float x1 = u01(sample_key(seed, uint32_t(i), 2u * k + 1u)) * 0.7f;
+                    const V3 smp = sample_ggx(N, r, x0, x1);
+                    if (dot(smp, N) > 0.001f) {
+                        micro = smp;
+                        break;
+                    }
+                }
+                dir = reflect_dir(I, micro);
+            }
+            const float off = mixf(0.05f, 0.1f, clamp01(roughness * 1.4f));
+            const V3 org = add(P, muls(N, off));
+            o.o[0] = org.x; o.o[1] = org.y; o.o[2] = org.z;
+            o.d[0] = dir.x; o.d[1] = dir.y; o.d[2] = dir.z;
+            o.tmin = 0.0f;
+            o.tmax = ray_tmax;
+        }
+    });
+}
+
+// SampleLighting (:420-425) + emissive for a hit, the sky x mix(1.4, 2.65, R) (:435-437) for a
+// miss; IsValid, clamp to [0, 6], w = t / 48 (:588-596); 0 where the primary ray missed.
+void orc_spec_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n, const uint8_t* lit,
+                    const orc_materials* mat, float roughness, const float sun_color[3], const float sky[3],
+                    const float ambient[3], int nthreads, float* out4) {
+    const Scene s = make_scene(sc);
+    const V3 sunc = ld3(sun_color), skyc = ld3(sky), amb = ld3(ambient);
+    parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            float* o = out4 + 4 * i;
+            if (!(rays[i].tmax > rays[i].tmin)) {
+                o[0] = o[1] = o[2] = o[3] = 0.0f;
+                continue;
+            }
+            const orc_hit& h = hits[i];
+            float t = h.t;
+            V3 rad;
+            if (h.t > 0.0f) {
+                const V3 alb = hit_albedo(s, *mat, h);
+                float em;
+                std::memcpy(&em, &s.ents[h.entity].data[0], 4);
+                const float l = lit ? (lit[i] ? 1.0f : 0.0f) : 1.0f;
+                rad = add(add(muls(mul(alb, sunc), l), mul(muls(alb, 2.0f), amb)), muls(alb, em));
+            } else {
+                rad = muls(skyc, mixf(1.4f, 2.65f, roughness));
+            }
+            if (!std::isfinite(rad.x) || !std::isfinite(rad.y) || !std::isfinite(rad.z)) {
+                rad = {0.0f, 0.0f, 0.0f};
+                t = -1.0f;
+            }
+            o[0] = gmin(gmax(rad.x, 0.0f), 6.0f);
+            o[1] = gmin(gmax(rad.y, 0.0f), 6.0f);
+            o[2] = gmin(gmax(rad.z, 0.0f), 6.0f);
+            o[3] = t / 48.0f;
+        }
+    });
+}
+
 void orc_hit_albedo(const orc_scene* sc, const orc_hit* hits, int64_t n, const orc_materials* mat,
                     int nthreads, float* out3) {
     const Scene s = make_scene(sc);

@@ -92,6 +92,11 @@ typedef struct {
 
 void orc_hit_albedo(const orc_scene* s, const orc_hit* hits, int64_t n, const orc_materials* mat,
                     int nthreads, float* out3);
+void orc_spec_raygen(const orc_scene* s, const orc_ray* primary, const orc_hit* hits, int64_t n, uint32_t seed,
+                     float roughness, float ray_tmax, int32_t normal_mode, int nthreads, orc_ray* out);
+void orc_spec_shade(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int64_t n, const uint8_t* lit,
+                    const orc_materials* mat, float roughness, const float sun_color[3], const float sky[3],
+                    const float ambient[3], int nthreads, float* out4);
 void orc_shade(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int64_t n,
                const uint8_t* shadow_lit, const orc_materials* mat,
                const float sun_dir[3], const float sun_color[3], const float sky_color[3],
