@@ -467,80 +467,87 @@ __global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, cons
     }
 }
 
-// Bounce b's rays from the previous segment's hits: origin P + N * 0.02, a cosine direction about
-// N from sample samp_of[c], dimensions 2 + 2b and 3 + 2b.  prev_rays may alias out (each slot
-// reads its own ray before writing it).
-__global__ void k_bounce_raygen(SceneView s, const rq_ray* prev_rays, const rq_hit* __restrict__ prev_hits,
-                                const float4* __restrict__ thr, const int32_t* __restrict__ samp_of,
-                                const unsigned long long* count, int64_t n_max, GiArgs a, int bounce,
-                                rq_ray* out, unsigned long long* active) {
-    const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
-    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    bool act = false;
-    if (c < n) {
-        if (thr[c].w > 0.0f) {
-            float4 h0;
-            int4 h1;
-            get_hit(prev_hits, c, h0, h1);
-            const float4* pr = reinterpret_cast<const float4*>(prev_rays) + 2 * c;
-            const float4 r0 = pr[0], r1 = pr[1];
-            const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
-            const f3 P = strict::add(ro, strict::muls(rd, h0.x));
-            f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
-            if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
-            const uint32_t rid = static_cast<uint32_t>(samp_of[c]);
-            const float u0 = gi::u01(gi::sample_key(a.seed, rid, 2u + 2u * bounce));
-            const float u1 = gi::u01(gi::sample_key(a.seed, rid, 3u + 2u * bounce));
-            const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
-            put_ray(out, c, strict::add(P, strict::muls(N, kBounceOffset)), 0.0f, dir, a.ray_tmax);
-            act = true;
-        } else {
-            put_ray(out, c, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
-        }
+// Bounce b's rays from the previous segment's hits, compacted: segment k of the previous bounce
+// belongs to GI slot prev_slot[k] (k itself for the GI segment); the live paths (throughput
+// w > 0) get consecutive entries of out / out_slot in warp-aggregated order.  Origin P + N * 0.02,
+// a cosine direction about N from sample samp_of[slot], dimensions 2 + 2b and 3 + 2b.
+__global__ void k_bounce_raygen(SceneView s, const rq_ray* __restrict__ prev_rays, const rq_hit* __restrict__ prev_hits,
+                                const int32_t* __restrict__ prev_slot, const unsigned long long* prev_count,
+                                int64_t n_max, const float4* __restrict__ thr, const int32_t* __restrict__ samp_of,
+                                GiArgs a, int bounce, rq_ray* __restrict__ out, int32_t* __restrict__ out_slot,
+                                unsigned long long* out_count, unsigned long long* active) {
+    const int64_t n = static_cast<int64_t>(*prev_count) < n_max ? static_cast<int64_t>(*prev_count) : n_max;
+    const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int32_t c = -1;
+    bool alive = false;
+    if (k < n) {
+        c = prev_slot ? prev_slot[k] : static_cast<int32_t>(k);
+        alive = thr[c].w > 0.0f;
     }
-    if (active) {
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
-        if ((threadIdx.x & 31) == 0 && m) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, alive);
+    unsigned long long base = 0;
+    if (lane == 0 && m) {
+        base = atomicAdd(out_count, static_cast<unsigned long long>(__popc(m)));
+        if (active) atomicAdd(active, static_cast<unsigned long long>(__popc(m)));
     }
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (!alive) return;
+    const int64_t j = static_cast<int64_t>(base) + __popc(m & persist::lanemask_lt());
+    float4 h0;
+    int4 h1;
+    get_hit(prev_hits, k, h0, h1);
+    const float4* pr = reinterpret_cast<const float4*>(prev_rays) + 2 * k;
+    const f3 ro = strict::xyz(__ldg(pr)), rd = strict::xyz(__ldg(pr + 1));
+    const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+    f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+    if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+    const uint32_t rid = static_cast<uint32_t>(samp_of[c]);
+    const float u0 = gi::u01(gi::sample_key(a.seed, rid, 2u + 2u * bounce));
+    const float u1 = gi::u01(gi::sample_key(a.seed, rid, 3u + 2u * bounce));
+    const f3 dir = gi::cos_weighted_hemisphere(N, u0, u1);
+    put_ray(out, j, strict::add(P, strict::muls(N, kBounceOffset)), 0.0f, dir, a.ray_tmax);
+    out_slot[j] = c;
 }
 
-// Bounce shading: rad += (GetDirect + emissive) * throughput, throughput *= albedo; a miss adds
-// 1.1 x sky x throughput (nothing under ref_miss, as the reference) and ends the path.
+// Bounce shading of compact segment k (GI slot slot[k]): rad += (GetDirect + emissive) *
+// throughput, throughput *= albedo; a miss adds 1.1 x sky x throughput (nothing under ref_miss, as
+// the reference) and ends the path.
 __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
-                               const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
-                               const Materials mat, GiArgs a, int ref_miss,
-                               float4* __restrict__ rad, float4* __restrict__ thr, unsigned long long* hit_count) {
+                               const uint8_t* __restrict__ occl, const int32_t* __restrict__ slot,
+                               const unsigned long long* count, int64_t n_max, const Materials mat, GiArgs a,
+                               int ref_miss, float4* __restrict__ rad, float4* __restrict__ thr,
+                               unsigned long long* hit_count) {
     const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
-    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     bool hit = false;
-    if (c < n) {
+    if (k < n) {
+        const int32_t c = slot[k];
         float4 T = thr[c];
-        if (T.w > 0.0f) {
-            float4 h0;
-            int4 h1;
-            get_hit(hits, c, h0, h1);
-            float4 R = rad[c];
-            if (h0.x > 0.0f) {
-                const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * c + 1));
-                const float l = occl ? (occl[c] ? 0.0f : 1.0f) : 1.0f;
-                const float4 v = shade_one(s, mat, a, rd, h0, h1, l);
-                R.x = __fadd_rn(R.x, __fmul_rn(v.x, T.x));
-                R.y = __fadd_rn(R.y, __fmul_rn(v.y, T.y));
-                R.z = __fadd_rn(R.z, __fmul_rn(v.z, T.z));
-                const f3 alb = gi::hit_albedo(s, mat, h0, h1);
-                T = make_float4(__fmul_rn(T.x, alb.x), __fmul_rn(T.y, alb.y), __fmul_rn(T.z, alb.z), 1.0f);
-                hit = true;
-            } else {
-                if (!ref_miss) {
-                    R.x = __fadd_rn(R.x, __fmul_rn(__fmul_rn(a.sky.x, kBounceSky), T.x));
-                    R.y = __fadd_rn(R.y, __fmul_rn(__fmul_rn(a.sky.y, kBounceSky), T.y));
-                    R.z = __fadd_rn(R.z, __fmul_rn(__fmul_rn(a.sky.z, kBounceSky), T.z));
-                }
-                T.w = 0.0f;
+        float4 h0;
+        int4 h1;
+        get_hit(hits, k, h0, h1);
+        float4 R = rad[c];
+        if (h0.x > 0.0f) {
+            const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * k + 1));
+            const float l = occl ? (occl[k] ? 0.0f : 1.0f) : 1.0f;
+            const float4 v = shade_one(s, mat, a, rd, h0, h1, l);
+            R.x = __fadd_rn(R.x, __fmul_rn(v.x, T.x));
+            R.y = __fadd_rn(R.y, __fmul_rn(v.y, T.y));
+            R.z = __fadd_rn(R.z, __fmul_rn(v.z, T.z));
+            const f3 alb = gi::hit_albedo(s, mat, h0, h1);
+            T = make_float4(__fmul_rn(T.x, alb.x), __fmul_rn(T.y, alb.y), __fmul_rn(T.z, alb.z), 1.0f);
+            hit = true;
+        } else {
+            if (!ref_miss) {
+                R.x = __fadd_rn(R.x, __fmul_rn(__fmul_rn(a.sky.x, kBounceSky), T.x));
+                R.y = __fadd_rn(R.y, __fmul_rn(__fmul_rn(a.sky.y, kBounceSky), T.y));
+                R.z = __fadd_rn(R.z, __fmul_rn(__fmul_rn(a.sky.z, kBounceSky), T.z));
             }
-            rad[c] = R;
-            thr[c] = T;
+            T.w = 0.0f;
         }
+        rad[c] = R;
+        thr[c] = T;
     }
     if (hit_count) {
         const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
@@ -753,28 +760,51 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
         }
     }
     if (bounce) {
-        // the bounces reuse the secondary ray / hit buffers in place (slot c only reads its own)
+        // Live paths are compacted every bounce: the rays ping-pong between a scratch buffer and
+        // the (no longer needed) GI rays, the hits reuse the GI hit buffer, and per segment the
+        // GI slot it belongs to is kept.
+        void *d_bray = nullptr, *d_sa = nullptr, *d_sb = nullptr, *d_bc = nullptr;
+        if ((s = scratch(ctx, 32, sizeof(rq_ray) * m, &d_bray)) != RQ_OK ||
+            (s = scratch(ctx, 33, 4 * m, &d_sa)) != RQ_OK || (s = scratch(ctx, 34, 4 * m, &d_sb)) != RQ_OK ||
+            (s = scratch(ctx, 35, 8 * sizeof(unsigned long long) + 8 * p.bounces, &d_bc)) != RQ_OK)
+            return s;
+        unsigned long long* bcount = static_cast<unsigned long long*>(d_bc);
+        RQ_CUDA(ctx, cudaMemsetAsync(bcount, 0, sizeof(unsigned long long) * p.bounces, st));
         k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, materials_of(sc), a, rad, thr);
         RQ_CUDA(ctx, cudaGetLastError());
         QueryConfig qb = q;  // bounces use IntersectRay, not the ignore-transparent variant
         qb.flags &= ~RQ_FLAG_IGNORE_TRANSPARENT;
+        rq_ray* ray_buf[2] = {static_cast<rq_ray*>(d_bray), sec};
+        int32_t* slot_buf[2] = {static_cast<int32_t*>(d_sa), static_cast<int32_t*>(d_sb)};
+        const rq_ray* prev_rays = sec;
+        const int32_t* prev_slot = nullptr;
+        const unsigned long long* prev_count = count;
         for (int b = 0; b < p.bounces; ++b) {
-            k_bounce_raygen<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, thr, samp_of, count, m, a, b, sec,
-                                                          stats ? cnt + 6 : nullptr);
+            rq_ray* brays = ray_buf[b & 1];
+            int32_t* bslot = slot_buf[b & 1];
+            unsigned long long* bc = bcount + b;
+            k_bounce_raygen<<<grid(m, 256), 256, 0, st>>>(sc->view, prev_rays, shit, prev_slot, prev_count, m, thr,
+                                                          samp_of, a, b, brays, bslot, bc, stats ? cnt + 6 : nullptr);
             RQ_CUDA(ctx, cudaGetLastError());
-            RQ_CUDA(ctx, launch_closest(cv, qb, sec, m, shit, queue_counter(ctx, 1), st));
+            SceneView bv = sc->view;
+            bv.ray_count = bc;
+            RQ_CUDA(ctx, launch_closest(bv, qb, brays, m, shit, queue_counter(ctx, 1), st));
             const uint8_t* bvis = nullptr;
             if (p.shadow_rays) {
                 if ((s = scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
                 rq_ray* sh = static_cast<rq_ray*>(d_shadow);
-                k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count, nullptr);
+                k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, brays, shit, m, a, sh, bc, nullptr);
                 RQ_CUDA(ctx, cudaGetLastError());
-                RQ_CUDA(ctx, launch_anyhit(cv, qb, sh, m, occ, queue_counter(ctx, 2), st));
+                RQ_CUDA(ctx, launch_anyhit(bv, qb, sh, m, occ, queue_counter(ctx, 2), st));
                 bvis = occ;
             }
-            k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, bvis, count, m, materials_of(sc), a, (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0,
-                                                         rad, thr, stats ? cnt + 7 : nullptr);
+            k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, brays, shit, bvis, bslot, bc, m, materials_of(sc), a,
+                                                         (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0, rad, thr,
+                                                         stats ? cnt + 7 : nullptr);
             RQ_CUDA(ctx, cudaGetLastError());
+            prev_rays = brays;
+            prev_slot = bslot;
+            prev_count = bc;
         }
     }
     // phase 3

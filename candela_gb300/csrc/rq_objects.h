@@ -9,7 +9,7 @@
 #include "bvh_build.h"
 #include "rq_internal.h"
 
-constexpr int kScratchSlots = 32;
+constexpr int kScratchSlots = 40;
 
 struct rq_ctx {
     int device = 0;
