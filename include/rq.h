@@ -345,7 +345,9 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
                    void* stream);
 
 /* A batch fixed at creation (descriptors uploaded once), replayed as a captured CUDA graph:
- * a memset of the work counter and the persistent launch.  The query buffers must stay valid. */
+ * a memset of the work counter and the persistent launch.  The query buffers must stay valid, and
+ * the scenes unchanged: setting entities, materials, the BVH8 or positions after creation leaves
+ * the plan pointing at the old device arrays (create a new plan). */
 typedef struct rq_batch_plan rq_batch_plan;
 rq_status rq_batch_plan_create(rq_ctx* ctx, const rq_query* queries, int32_t n_queries,
                                const rq_opts* opts, rq_batch_plan** out);
