@@ -19,6 +19,7 @@ HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liboracle.so"
 REF_SO = HERE / "_ref" / "librefbvh.so"
 REF_LEAF4_SO = HERE / "_ref" / "librefbvh_leaf4.so"
+REF_PHYSICS_SO = HERE / "_ref" / "librefphysics.so"
 REFERENCE_ROOT = Path(os.environ.get("RQ_REFERENCE_ROOT", "/root/reference"))
 
 RAY_DTYPE = np.dtype([("o", "<f4", (3,)), ("tmin", "<f4"), ("d", "<f4", (3,)), ("tmax", "<f4")])
@@ -271,6 +272,28 @@ def sincos_turns(x: float):
 # ---- reference BVH constructor (compiled from the mounted reference tree) -----------------
 
 _ref = {}
+
+
+def ref_physics_available() -> bool:
+    return REF_PHYSICS_SO.exists()
+
+
+def ref_collide_boxes(vertices, tris, nodes, entities, boxes) -> np.ndarray:
+    """The reference's Physics::CollideBox (Physics.cpp:203-228, compiled from its source by
+    oracle/Makefile) for each box over a stackless scene: uint8 collided flags."""
+    L = C.CDLL(str(REF_PHYSICS_SO))
+    L.ref_collide_boxes.restype = None
+    L.ref_collide_boxes.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                    C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]
+    v = np.ascontiguousarray(vertices)
+    t = np.ascontiguousarray(tris, dtype=np.int32)
+    n = np.ascontiguousarray(nodes, dtype=np.float32)
+    e = np.ascontiguousarray(entities)
+    b = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 8)
+    out = np.zeros(b.shape[0], dtype=np.uint8)
+    L.ref_collide_boxes(_p(n), n.shape[0], _p(t), t.shape[0], _p(v), v.shape[0], _p(e), e.shape[0], _p(b),
+                        b.shape[0], _p(out))
+    return out
 
 
 def ref_available(leaf4: bool = False) -> bool:

@@ -6,12 +6,14 @@
 // restates the GLSL arithmetic statement by statement in C++.  Every function cites the lines it
 // follows.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
 //
-// Parity status: parity unpinned for everything in this file (traversal, GI / specular ray
-// generation and shading, texture sampling, collision queries).  The reference holds no golden
-// vectors or CPU implementation for them and its GLSL cannot run here, so the restatement is
-// checked by analytic known-answer tests and an independent FP64 brute force (tests/test_oracle*.py),
-// not by reference outputs.  The BVH constructor is pinned: ref_bvh_harness.cpp compiles the
-// reference's own source and the builder is compared byte for byte.
+// Parity status.  Pinned: the collision walk (stackless layout, the reference's axis set) against
+// the reference's host copy of it, Physics::CollideBox, compiled from Physics.cpp by
+// ref_physics_harness.cpp; and the BVH constructor (ref_bvh_harness.cpp compiles the reference's
+// own source, the builder is compared byte for byte).  Parity unpinned for the rest of this file
+// (traversal, GI / specular ray generation and shading, texture sampling, the stack-layout
+// collision walk): the reference holds no golden vectors or CPU implementation for them and its
+// GLSL cannot run here, so the restatement is checked by analytic known-answer tests and an
+// independent FP64 brute force (tests/test_oracle*.py), not by reference outputs.
 //
 // Arithmetic conventions (the definition that the strict GPU kernels must reproduce bit for bit):
 //  * IEEE binary32, round to nearest, no contraction (built with -ffp-contract=off);

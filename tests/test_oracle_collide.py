@@ -174,3 +174,32 @@ def test_collide_ref_compat_leaf_index_and_entities():
     assert np.all(a[a[:, 0] == 1, 1] == 0) and np.all(b[b[:, 0] == 1, 1] == 1)
     np.testing.assert_array_equal(b[:, 0], c[:, 0])
     np.testing.assert_array_equal(b[:, 2:], c[:, 2:])
+
+
+@pytest.mark.skipif(not O.ref_physics_available(), reason="reference source tree not mounted")
+@pytest.mark.parametrize("name", ["hf32", "ico2"])
+def test_collide_pinned_to_reference_physics(name):
+    """The stackless restatement with the reference's axis set (RQ_FLAG_REF_COMPAT) against the
+    reference's own host walk, Physics::CollideBox (Physics.cpp), compiled from its source: the
+    same collided flag for every box, with an identity entity and two translated ones (translations
+    are exact, so glm's pairwise matrix sum and the GLSL left-to-right sum agree)."""
+    ri = R.RayIntersector(R.STACKLESS)
+    ri.add_object(1, [mesh(name)])
+    ri.push_entity(1)
+    for dx in (3.0, -5.0):
+        T = np.eye(4)
+        T[:3, 3] = [dx, 0.5, 0.25]
+        ri.push_entity(1, model=T)
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    osc = O.OracleScene(O.ORC_STACKLESS, v, t, n, e)
+    boxes = _scene_boxes(name, 4000, seed=21)
+    shifted = boxes.copy()
+    shifted[:, [0, 4]] += np.float32(3.0)
+    shifted[:, [1, 5]] += np.float32(0.5)
+    shifted[:, [2, 6]] += np.float32(0.25)
+    for bx in (boxes, shifted):
+        ref = O.ref_collide_boxes(v, t, n, e, bx)
+        ours = osc.collide(bx, flags=O.ORC_FLAG_REF_COMPAT)[:, 0]
+        np.testing.assert_array_equal(ours, ref)
+        assert 0.1 < ref.mean() < 0.95
