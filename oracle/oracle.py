@@ -20,6 +20,7 @@ ORACLE_SO = HERE / "_build" / "liboracle.so"
 REF_SO = HERE / "_ref" / "librefbvh.so"
 REF_LEAF4_SO = HERE / "_ref" / "librefbvh_leaf4.so"
 REF_PHYSICS_SO = HERE / "_ref" / "librefphysics.so"
+REF_GLSL_SO = HERE / "_ref" / "librefglsl.so"
 REFERENCE_ROOT = Path(os.environ.get("RQ_REFERENCE_ROOT", "/root/reference"))
 
 RAY_DTYPE = np.dtype([("o", "<f4", (3,)), ("tmin", "<f4"), ("d", "<f4", (3,)), ("tmax", "<f4")])
@@ -106,6 +107,7 @@ def orc() -> C.CDLL:
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
         L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_cos_hemisphere.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
         _orc = L
     return _orc
 
@@ -272,6 +274,67 @@ def sincos_turns(x: float):
 # ---- reference BVH constructor (compiled from the mounted reference tree) -----------------
 
 _ref = {}
+
+
+def ref_glsl_available() -> bool:
+    return REF_GLSL_SO.exists()
+
+
+def _ref_glsl():
+    L = C.CDLL(str(REF_GLSL_SO))
+    P = C.c_void_p
+    L.ref_glsl_closest.restype = None
+    L.ref_glsl_closest.argtypes = [C.c_int, C.c_int, P, C.c_int64, P, C.c_int64, P, C.c_int64, P, C.c_int32, P,
+                                   C.c_int64, P]
+    L.ref_glsl_occluded.restype = None
+    L.ref_glsl_occluded.argtypes = [C.c_int, P, C.c_int64, P, C.c_int64, P, C.c_int64, P, C.c_int32, P, C.c_int64, P]
+    return L
+
+
+def ref_glsl_closest(layout, vertices, tris, nodes, entities, rays, ignore_transparent=False):
+    """The reference's IntersectScene[IgnoreTransparent] (TraverseBVHStack[less].glsl compiled as
+    C++ by oracle/Makefile) per ray: HIT_DTYPE records (t, u, v, w from TUVW; tri, mesh, entity,
+    iters from its outputs, -1 where it leaves them unwritten)."""
+    v, t = np.ascontiguousarray(vertices), np.ascontiguousarray(tris, dtype=np.int32)
+    n, e = np.ascontiguousarray(nodes, dtype=np.float32), np.ascontiguousarray(entities)
+    r = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+    out = np.empty(r.shape[0], dtype=HIT_DTYPE)
+    _ref_glsl().ref_glsl_closest(int(layout == ORC_STACKLESS), int(ignore_transparent), _p(n), n.shape[0], _p(t),
+                                 t.shape[0], _p(v), v.shape[0], _p(e), e.shape[0], _p(r), r.shape[0], _p(out))
+    return out
+
+
+def ref_glsl_occluded(layout, vertices, tris, nodes, entities, rays):
+    """The reference's float IntersectRay(o, d) > 0 per ray (compiled from its shader source)."""
+    v, t = np.ascontiguousarray(vertices), np.ascontiguousarray(tris, dtype=np.int32)
+    n, e = np.ascontiguousarray(nodes, dtype=np.float32), np.ascontiguousarray(entities)
+    r = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+    out = np.empty(r.shape[0], dtype=np.uint8)
+    _ref_glsl().ref_glsl_occluded(int(layout == ORC_STACKLESS), _p(n), n.shape[0], _p(t), t.shape[0], _p(v),
+                                  v.shape[0], _p(e), e.shape[0], _p(r), r.shape[0], _p(out))
+    return out
+
+
+def cos_hemisphere(normals, r):
+    """The restatement's CosWeightedHemisphere (turn-based sine / cosine) for (n, 3) normals and
+    (n, 2) samples."""
+    nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    rr = np.ascontiguousarray(r, dtype=np.float32).reshape(-1, 2)
+    out = np.empty_like(nn)
+    orc().orc_cos_hemisphere(_p(nn), _p(rr), nn.shape[0], _p(out))
+    return out
+
+
+def ref_glsl_cos_hemisphere(normals, r):
+    """The reference's CosWeightedHemisphere (Sampling.glsl compiled as C++, C-library cos / sin)."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_cos_hemisphere.restype = None
+    L.ref_glsl_cos_hemisphere.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    rr = np.ascontiguousarray(r, dtype=np.float32).reshape(-1, 2)
+    out = np.empty_like(nn)
+    L.ref_glsl_cos_hemisphere(_p(nn), _p(rr), nn.shape[0], _p(out))
+    return out
 
 
 def ref_physics_available() -> bool:

@@ -1,0 +1,152 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// Entry points around the reference's traversal shaders compiled as C++.  The recipe in
+// oracle/Makefile builds one translation unit from ref_glsl_prologue.h, then, in namespace
+// glsl_stack, the struct declarations and traversal functions of
+// Shaders/Intersectors/Include/TraverseBVHStack.glsl (lines 14-52, 75-414, 505-683: RayTriangle,
+// RayBounds, ComputeBarycentrics, IntersectBVHStack, IntersectScene, IntersectSceneIgnoreTransparent,
+// the occlusion walk, IntersectSceneOcclusion, IntersectRay), then likewise in namespace
+// glsl_stackless for TraverseBVHStackless.glsl (lines 14-46, 67-368, 461-580),
+// CosWeightedHemisphere of Shaders/Include/Sampling.glsl (lines 1-12) in namespace glsl_sampling,
+// and finally this file.  The shader text is piped through sed (`.xyz` -> `.xyz()`, `out T` /
+// `inout T` -> `T&`) and compiled with `in` defined empty; nothing is written to disk but the library
+// (oracle/_ref/librefglsl.so).  The SSBOs and uniforms the shaders read become the namespace
+// globals below, set per call.  The tests compare the CPU restatement (rq_oracle.cpp) with it.
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// Copies the caller's buffers into arrays with one zero node of padding: the shaders guard the
+// node index with `> u_TotalNodes`, so an index equal to the node count passes the guard.
+template <class NS_Node, class NS_Tri, class NS_Vert, class NS_Ent>
+struct Buffers {
+    std::vector<NS_Node> nodes;
+    std::vector<NS_Tri> tris;
+    std::vector<NS_Vert> verts;
+    std::vector<NS_Ent> ents;
+    Buffers(const void* n, int64_t nn, const void* t, int64_t nt, const void* v, int64_t nv, const void* e,
+            int32_t ne)
+        : nodes(nn + 1), tris(nt), verts(nv), ents(ne) {
+        std::memset(static_cast<void*>(nodes.data()), 0, sizeof(NS_Node) * (nn + 1));
+        std::memcpy(static_cast<void*>(nodes.data()), n, sizeof(NS_Node) * nn);
+        std::memcpy(static_cast<void*>(tris.data()), t, sizeof(NS_Tri) * nt);
+        std::memcpy(static_cast<void*>(verts.data()), v, sizeof(NS_Vert) * nv);
+        std::memcpy(static_cast<void*>(ents.data()), e, sizeof(NS_Ent) * ne);
+    }
+};
+
+void put_hit(float* o, const glsl::vec4& tuvw, int tri, int mesh, int ent, int iters) {
+    o[0] = tuvw.x;
+    o[1] = tuvw.y;
+    o[2] = tuvw.z;
+    o[3] = tuvw.w;
+    std::memcpy(o + 4, &tri, 4);
+    std::memcpy(o + 5, &mesh, 4);
+    std::memcpy(o + 6, &ent, 4);
+    std::memcpy(o + 7, &iters, 4);
+}
+
+}  // namespace
+
+static_assert(sizeof(glsl_stack::Node) == 64 && sizeof(glsl_stackless::Node) == 32, "node layouts");
+static_assert(sizeof(glsl_stack::BVHEntity) == 192 && sizeof(glsl_stack::Vertex) == 32, "record layouts");
+
+// IntersectScene (closest hit; ignore_transparent: IntersectSceneIgnoreTransparent) per ray of
+// `rays` (8 floats: origin, tmin, direction, tmax; the shaders use tmin 0 and TMax 1e6 whatever
+// the ray says).  out: 8 words per ray, TUVW then the Triangle, Mesh, Entity and Iters outputs
+// (-1 where the shader leaves an output unwritten).  stackless selects the shader file.
+extern "C" void ref_glsl_closest(int stackless, int ignore_transparent, const void* nodes, int64_t n_nodes,
+                                 const void* tris, int64_t n_tris, const void* verts, int64_t n_verts,
+                                 const void* ents, int32_t n_ents, const float* rays, int64_t n, float* out) {
+    if (!stackless) {
+        namespace G = glsl_stack;
+        Buffers<G::Node, G::Triangle, G::Vertex, G::BVHEntity> b(nodes, n_nodes, tris, n_tris, verts, n_verts,
+                                                                  ents, n_ents);
+        G::BVHNodes = b.nodes.data();
+        G::BVHTris = b.tris.data();
+        G::BVHVertices = b.verts.data();
+        G::BVHEntities = b.ents.data();
+        G::u_EntityCount = n_ents;
+        G::u_TotalNodes = static_cast<int>(n_nodes);
+        for (int64_t i = 0; i < n; ++i) {
+            const float* r = rays + 8 * i;
+            int mesh = -1, tri = -1, ent = -1, iters = -1;
+            const glsl::vec4 h = ignore_transparent
+                                     ? G::IntersectSceneIgnoreTransparent(glsl::vec3(r[0], r[1], r[2]),
+                                                                          glsl::vec3(r[4], r[5], r[6]), mesh, tri, ent,
+                                                                          iters)
+                                     : G::IntersectScene(glsl::vec3(r[0], r[1], r[2]), glsl::vec3(r[4], r[5], r[6]),
+                                                         mesh, tri, ent, iters);
+            put_hit(out + 8 * i, h, tri, mesh, ent, iters);
+        }
+    } else {
+        namespace G = glsl_stackless;
+        Buffers<G::Node, G::Triangle, G::Vertex, G::BVHEntity> b(nodes, n_nodes, tris, n_tris, verts, n_verts,
+                                                                  ents, n_ents);
+        G::BVHNodes = b.nodes.data();
+        G::BVHTris = b.tris.data();
+        G::BVHVertices = b.verts.data();
+        G::BVHEntities = b.ents.data();
+        G::u_EntityCount = n_ents;
+        G::u_TotalNodes = static_cast<int>(n_nodes);
+        for (int64_t i = 0; i < n; ++i) {
+            const float* r = rays + 8 * i;
+            int mesh = -1, tri = -1, ent = -1, iters = -1;
+            const glsl::vec4 h = ignore_transparent
+                                     ? G::IntersectSceneIgnoreTransparent(glsl::vec3(r[0], r[1], r[2]),
+                                                                          glsl::vec3(r[4], r[5], r[6]), mesh, tri, ent,
+                                                                          iters)
+                                     : G::IntersectScene(glsl::vec3(r[0], r[1], r[2]), glsl::vec3(r[4], r[5], r[6]),
+                                                         mesh, tri, ent, iters);
+            put_hit(out + 8 * i, h, tri, mesh, ent, iters);
+        }
+    }
+}
+
+// CosWeightedHemisphere (Shaders/Include/Sampling.glsl:1-12) for n normals / sample pairs.
+extern "C" void ref_glsl_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out) {
+    for (int64_t i = 0; i < n; ++i) {
+        const glsl::vec3 d = glsl_sampling::CosWeightedHemisphere(
+            glsl::vec3(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]), glsl::vec2{r[2 * i], r[2 * i + 1]});
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
+
+// float IntersectRay(o, d) (the occlusion query): out[i] = 1 when it returns a value > 0.
+extern "C" void ref_glsl_occluded(int stackless, const void* nodes, int64_t n_nodes, const void* tris, int64_t n_tris,
+                                  const void* verts, int64_t n_verts, const void* ents, int32_t n_ents,
+                                  const float* rays, int64_t n, uint8_t* out) {
+    if (!stackless) {
+        namespace G = glsl_stack;
+        Buffers<G::Node, G::Triangle, G::Vertex, G::BVHEntity> b(nodes, n_nodes, tris, n_tris, verts, n_verts,
+                                                                  ents, n_ents);
+        G::BVHNodes = b.nodes.data();
+        G::BVHTris = b.tris.data();
+        G::BVHVertices = b.verts.data();
+        G::BVHEntities = b.ents.data();
+        G::u_EntityCount = n_ents;
+        G::u_TotalNodes = static_cast<int>(n_nodes);
+        for (int64_t i = 0; i < n; ++i) {
+            const float* r = rays + 8 * i;
+            out[i] = G::IntersectRay(glsl::vec3(r[0], r[1], r[2]), glsl::vec3(r[4], r[5], r[6])) > 0.0f ? 1 : 0;
+        }
+    } else {
+        namespace G = glsl_stackless;
+        Buffers<G::Node, G::Triangle, G::Vertex, G::BVHEntity> b(nodes, n_nodes, tris, n_tris, verts, n_verts,
+                                                                  ents, n_ents);
+        G::BVHNodes = b.nodes.data();
+        G::BVHTris = b.tris.data();
+        G::BVHVertices = b.verts.data();
+        G::BVHEntities = b.ents.data();
+        G::u_EntityCount = n_ents;
+        G::u_TotalNodes = static_cast<int>(n_nodes);
+        for (int64_t i = 0; i < n; ++i) {
+            const float* r = rays + 8 * i;
+            out[i] = G::IntersectRay(glsl::vec3(r[0], r[1], r[2]), glsl::vec3(r[4], r[5], r[6])) > 0.0f ? 1 : 0;
+        }
+    }
+}

@@ -1,0 +1,102 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// A minimal GLSL vocabulary in C++ so that the reference's traversal shaders
+// (Shaders/Intersectors/Include/TraverseBVHStack.glsl and TraverseBVHStackless.glsl) compile as C++
+// (oracle/Makefile pipes their traversal functions after this header; see ref_glsl_harness.cpp).
+// The semantics are those the GLSL 4.50 specification gives, evaluated in IEEE binary32 without
+// contraction (the recipe passes -ffp-contract=off):
+//  * vector arithmetic is component-wise, one rounding per operation;
+//  * min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x (spec 8.3), component-wise for vectors;
+//  * dot(a, b) = (a.x b.x + a.y b.y) + a.z b.z, cross as in spec 8.5;
+//  * mat4 * vec4 sums the columns left to right, ((c0 x + c1 y) + c2 z) + c3 w: the specification
+//    leaves the order to the implementation, and this is the order the engine and the CPU
+//    restatement define;
+//  * floatBitsToInt / intBitsToFloat reinterpret bits.
+// `.xyz` is rewritten to `.xyz()` by the recipe; `in` becomes empty and `out T` / `inout T`
+// become `T&`.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+namespace glsl {
+
+struct vec4;
+
+struct vec3 {
+    float x, y, z;
+    vec3() = default;
+    vec3(float s) : x(s), y(s), z(s) {}
+    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    explicit vec3(const vec4& v);
+    vec3 xyz() const { return *this; }
+};
+
+struct vec4 {
+    float x, y, z, w;
+    vec4() = default;
+    vec4(float s) : x(s), y(s), z(s), w(s) {}
+    vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+    vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    vec4(float a, const vec3& v) : x(a), y(v.x), z(v.y), w(v.z) {}
+    vec3 xyz() const { return vec3(x, y, z); }
+};
+
+inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
+
+struct vec2 {
+    float x, y;
+};
+
+struct uvec4 {
+    uint32_t x, y, z, w;
+};
+
+struct mat4 {
+    vec4 c[4];  // columns
+};
+
+inline vec3 operator+(vec3 a, vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline vec3 operator-(vec3 a, vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline vec3 operator*(vec3 a, vec3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline vec3 operator/(vec3 a, vec3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+inline vec3 operator*(vec3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline vec3 operator*(float s, vec3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline vec3 operator/(float s, vec3 a) { return {s / a.x, s / a.y, s / a.z}; }
+inline vec3 operator/(vec3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+inline vec3 operator-(vec3 a) { return {-a.x, -a.y, -a.z}; }
+
+inline vec4 operator*(const mat4& m, vec4 v) {
+    vec4 r;
+    r.x = ((m.c[0].x * v.x + m.c[1].x * v.y) + m.c[2].x * v.z) + m.c[3].x * v.w;
+    r.y = ((m.c[0].y * v.x + m.c[1].y * v.y) + m.c[2].y * v.z) + m.c[3].y * v.w;
+    r.z = ((m.c[0].z * v.x + m.c[1].z * v.y) + m.c[2].z * v.z) + m.c[3].z * v.w;
+    r.w = ((m.c[0].w * v.x + m.c[1].w * v.y) + m.c[2].w * v.z) + m.c[3].w * v.w;
+    return r;
+}
+
+inline float min(float x, float y) { return y < x ? y : x; }
+inline float max(float x, float y) { return x < y ? y : x; }
+inline vec3 min(vec3 a, vec3 b) { return {min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)}; }
+inline vec3 max(vec3 a, vec3 b) { return {max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)}; }
+inline float dot(vec3 a, vec3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline vec3 cross(vec3 a, vec3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// sqrt, cos, sin: the C library's (GLSL leaves their precision to the implementation).
+inline float sqrt(float x) { return std::sqrt(x); }
+inline float cos(float x) { return std::cos(x); }
+inline float sin(float x) { return std::sin(x); }
+inline vec3 normalize(vec3 v) { return v / sqrt(dot(v, v)); }
+inline int floatBitsToInt(float f) {
+    int i;
+    std::memcpy(&i, &f, 4);
+    return i;
+}
+inline float intBitsToFloat(int i) {
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+}  // namespace glsl

@@ -6,14 +6,20 @@
 // restates the GLSL arithmetic statement by statement in C++.  Every function cites the lines it
 // follows.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
 //
-// Parity status.  Pinned: the collision walk (stackless layout, the reference's axis set) against
-// the reference's host copy of it, Physics::CollideBox, compiled from Physics.cpp by
-// ref_physics_harness.cpp; and the BVH constructor (ref_bvh_harness.cpp compiles the reference's
-// own source, the builder is compared byte for byte).  Parity unpinned for the rest of this file
-// (traversal, GI / specular ray generation and shading, texture sampling, the stack-layout
-// collision walk): the reference holds no golden vectors or CPU implementation for them and its
-// GLSL cannot run here, so the restatement is checked by analytic known-answer tests and an
-// independent FP64 brute force (tests/test_oracle*.py), not by reference outputs.
+// Parity status.  Pinned against the reference's own sources compiled here (oracle/Makefile):
+//  * traversal (both layouts, closest and any hit, scene loop, entity transforms,
+//    ignore-transparent, the tri-0 test, iteration counts) against the traversal functions of
+//    TraverseBVHStack.glsl / TraverseBVHStackless.glsl compiled as C++ (ref_glsl_harness.cpp):
+//    bit for bit, with the dot / mat*vec summation order defined here (GLSL leaves it open);
+//  * CosWeightedHemisphere (Sampling.glsl) the same way: within a few ulps (its cos / sin are the
+//    C library's there, the turn-based polynomials here);
+//  * the collision walk (stackless layout, the reference's axis set) against Physics::CollideBox,
+//    compiled from Physics.cpp (ref_physics_harness.cpp);
+//  * the BVH constructor (ref_bvh_harness.cpp), byte for byte.
+// Parity unpinned for the rest (GI / specular shading, texture sampling, the stack-layout collision
+// walk): they depend on shader inputs that cannot be compiled apart from the renderer (shadow maps,
+// G-buffer, bindless textures), so they are checked by analytic known-answer tests and an FP64
+// brute force (tests/test_oracle*.py).
 //
 // Arithmetic conventions (the definition that the strict GPU kernels must reproduce bit for bit):
 //  * IEEE binary32, round to nearest, no contraction (built with -ffp-contract=off);
@@ -835,6 +841,14 @@ void orc_barycentrics(const float p[3], const float a[3], const float b[3], cons
 
 uint32_t orc_pcg_hash(uint32_t x) { return pcg_hash(x); }
 void orc_sincos_turns(float x, float* s, float* c) { sincos_turns(x, *s, *c); }
+void orc_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out) {
+    for (int64_t i = 0; i < n; ++i) {
+        const V3 d = cos_weighted_hemisphere(ld3(normals + 3 * i), r[2 * i], r[2 * i + 1]);
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
 
 void orc_gi_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit* hits, int64_t n,
                    int32_t spp, uint32_t seed, float origin_offset, float ray_tmax,

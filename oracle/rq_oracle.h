@@ -119,6 +119,8 @@ void orc_collide(const orc_scene* s, const float* boxes, int64_t n, int32_t* out
 
 uint32_t orc_pcg_hash(uint32_t x);
 void orc_sincos_turns(float x, float* s, float* c);
+// CosWeightedHemisphere (Sampling.glsl:1-12) with the turn-based sine / cosine, n normals.
+void orc_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out);
 
 #ifdef __cplusplus
 }

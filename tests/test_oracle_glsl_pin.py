@@ -1,0 +1,99 @@
+"""Pins the CPU restatement of the traversal to the reference's own shader source: the traversal
+functions of TraverseBVHStack.glsl and TraverseBVHStackless.glsl compiled as C++ (oracle/Makefile,
+ref_glsl_harness.cpp) give the same TUVW, triangle, mesh, entity and iteration outputs, and the same
+occlusion answers, as rq_oracle.cpp with the reference's own conventions (first-found ties, the
+`TriangleIdx > 0` test).  Runs where the reference source tree is mounted."""
+import numpy as np
+import pytest
+
+import candela_gb300 as R
+from candela_gb300 import scenes as S
+from oracle import oracle as O
+
+from .helpers import ORC_LAYOUT, mesh, oracle_scene, single_object
+
+pytestmark = pytest.mark.skipif(not O.ref_glsl_available(), reason="reference source tree not mounted")
+
+FIELDS_F = ("t", "u", "v", "w")
+FIELDS_I = ("tri", "mesh", "entity")
+
+
+def _rays(lo, hi, n, seed, camera=None):
+    parts = [S.sphere_rays(n, lo, hi, seed=seed)]
+    if camera:
+        parts.append(S.camera_rays(96, 72, **camera))
+    edge = np.zeros(5, dtype=R.RAY_DTYPE)
+    edge["o"] = [[0, 0, 5], [0, 0, 5], [0.1, 0.2, 3], [0, 0, 5], [-3, 0.1, 0.05]]
+    edge["d"] = [[np.nan, 0, -1], [0, 0, 0], [0, 0, -1], [1e-30, 0, -1], [1, 0, 0]]
+    edge["tmax"] = 1e6
+    parts.append(edge)
+    return np.concatenate(parts)
+
+
+def _compare(ref, ours, iters=True):
+    for f in FIELDS_F:
+        np.testing.assert_array_equal(ours[f].view(np.uint32), ref[f].view(np.uint32), err_msg=f)
+    hit = ref["t"] > 0
+    for f in FIELDS_I:
+        np.testing.assert_array_equal(ours[f][hit], ref[f][hit], err_msg=f)
+    if iters:
+        np.testing.assert_array_equal(ours["iters"], ref["iters"])
+    return hit
+
+
+@pytest.mark.parametrize("name", ["hf32", "ico2", "c1"])
+@pytest.mark.parametrize("layout", [R.STACK, R.STACKLESS])
+def test_single_object_matches_reference_shader(name, layout):
+    bufs = single_object(name, layout)
+    osc = oracle_scene(bufs, layout)
+    rays = _rays((-1.5, -1.5, -0.3), (1.5, 1.5, 1.2), 30_000, seed=4, camera=S.C1_CAMERA)
+    ref = O.ref_glsl_closest(ORC_LAYOUT[layout], *bufs, rays)
+    ours = osc.closest(rays, tie=O.ORC_TIE_FIRST_FOUND, flags=O.ORC_FLAG_REF_COMPAT)
+    hit = _compare(ref, ours)
+    assert 0.1 < hit.mean() < 0.95
+    np.testing.assert_array_equal(osc.anyhit(rays), O.ref_glsl_occluded(ORC_LAYOUT[layout], *bufs, rays))
+
+
+@pytest.mark.parametrize("layout", [R.STACK, R.STACKLESS])
+def test_entities_and_transparency_match_reference_shader(layout):
+    """Several entities with rotations, scales and translations, some translucent: the scene loop,
+    the entity transform and IntersectSceneIgnoreTransparent.  The shader hands the same `out int
+    Iters` to every entity's walk, so its iteration output is the last entity's count, where the
+    engine sums over entities; iterations are compared per entity through one-entity scenes."""
+    ri = R.RayIntersector(layout)
+    ri.add_object(1, [mesh("hf32")])
+    ri.add_object(2, [mesh("ico2")])
+    M = S.instance_transforms(12, (-3.0, -3.0, 0.0), (3.0, 3.0, 1.0), 0.4, 1.2, seed=5, anisotropic=0.3,
+                              tilt=0.1)
+    for i in range(12):
+        ri.push_entity(1 + (i % 2), model=M[i].astype(np.float64), translucency=0.5 if i % 4 == 1 else 0.0)
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    osc = O.OracleScene(ORC_LAYOUT[layout], v, t, n, e)
+    rays = _rays((-4.0, -4.0, -0.5), (4.0, 4.0, 2.0), 20_000, seed=8,
+                 camera=dict(eye=(0.0, -8.0, 5.0), target=(0.0, 0.0, 0.3)))
+    for ignore in (False, True):
+        ref = O.ref_glsl_closest(ORC_LAYOUT[layout], v, t, n, e, rays, ignore_transparent=ignore)
+        flags = O.ORC_FLAG_REF_COMPAT | (O.ORC_FLAG_IGNORE_TRANSPARENT if ignore else 0)
+        ours = osc.closest(rays, tie=O.ORC_TIE_FIRST_FOUND, flags=flags)
+        hit = _compare(ref, ours, iters=False)
+        assert hit.mean() > 0.1 and len(np.unique(ref["entity"][hit])) >= 6
+    np.testing.assert_array_equal(osc.anyhit(rays), O.ref_glsl_occluded(ORC_LAYOUT[layout], v, t, n, e, rays))
+    # the last entity alone: its iteration count is the shader's output
+    last = e[-1:].copy()
+    ref = O.ref_glsl_closest(ORC_LAYOUT[layout], v, t, n, last, rays)
+    ours = O.OracleScene(ORC_LAYOUT[layout], v, t, n, last).closest(rays, tie=O.ORC_TIE_FIRST_FOUND,
+                                                                    flags=O.ORC_FLAG_REF_COMPAT)
+    _compare(ref, ours)
+
+
+def test_cos_hemisphere_matches_reference_sampler():
+    """CosWeightedHemisphere (Sampling.glsl:1-12) compiled from the reference with the C library's
+    cos / sin, against the restatement's turn-based sine / cosine: within a few ulps."""
+    rng = np.random.default_rng(1)
+    n = rng.normal(size=(50_000, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    r = (rng.integers(0, 1 << 24, size=(50_000, 2)) / 2.0 ** 24).astype(np.float32)
+    ours, ref = O.cos_hemisphere(n, r), O.ref_glsl_cos_hemisphere(n, r)
+    assert np.abs(ours - ref).max() < 2e-6
+    assert (ours == ref).all(1).mean() > 0.2
