@@ -315,6 +315,22 @@ def ref_glsl_occluded(layout, vertices, tris, nodes, entities, rays):
     return out
 
 
+def ref_glsl_collide(layout, vertices, tris, nodes, entities, boxes):
+    """The reference's CollideScene (CollideBVHStack[less].glsl compiled as C++): (n, 4) int32
+    {collided, entity, mesh, tri}, -1 where the shader leaves an output unwritten."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    P = C.c_void_p
+    L.ref_glsl_collide.restype = None
+    L.ref_glsl_collide.argtypes = [C.c_int, P, C.c_int64, P, C.c_int64, P, C.c_int64, P, C.c_int32, P, C.c_int64, P]
+    v, t = np.ascontiguousarray(vertices), np.ascontiguousarray(tris, dtype=np.int32)
+    n, e = np.ascontiguousarray(nodes, dtype=np.float32), np.ascontiguousarray(entities)
+    b = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 8)
+    out = np.empty((b.shape[0], 4), dtype=np.int32)
+    L.ref_glsl_collide(int(layout == ORC_STACKLESS), _p(n), n.shape[0], _p(t), t.shape[0], _p(v), v.shape[0], _p(e),
+                       e.shape[0], _p(b), b.shape[0], _p(out))
+    return out
+
+
 def cos_hemisphere(normals, r):
     """The restatement's CosWeightedHemisphere (turn-based sine / cosine) for (n, 3) normals and
     (n, 2) samples."""

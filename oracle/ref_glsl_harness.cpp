@@ -7,8 +7,9 @@
 // RayBounds, ComputeBarycentrics, IntersectBVHStack, IntersectScene, IntersectSceneIgnoreTransparent,
 // the occlusion walk, IntersectSceneOcclusion, IntersectRay), then likewise in namespace
 // glsl_stackless for TraverseBVHStackless.glsl (lines 14-46, 67-368, 461-580),
-// CosWeightedHemisphere of Shaders/Include/Sampling.glsl (lines 1-12) in namespace glsl_sampling,
-// and finally this file.  The shader text is piped through sed (`.xyz` -> `.xyz()`, `out T` /
+// the collision shaders CollideBVHStack.glsl (14-48, 67-326) and CollideBVHStackless.glsl (11-32,
+// 51-54, 56-248) in namespaces glsl_collide_stack / glsl_collide_stackless, CosWeightedHemisphere
+// of Shaders/Include/Sampling.glsl (lines 1-12) in namespace glsl_sampling, and finally this file.  The shader text is piped through sed (`.xyz` -> `.xyz()`, `out T` /
 // `inout T` -> `T&`) and compiled with `in` defined empty; nothing is written to disk but the library
 // (oracle/_ref/librefglsl.so).  The SSBOs and uniforms the shaders read become the namespace
 // globals below, set per call.  The tests compare the CPU restatement (rq_oracle.cpp) with it.
@@ -102,6 +103,47 @@ extern "C" void ref_glsl_closest(int stackless, int ignore_transparent, const vo
                                                          mesh, tri, ent, iters);
             put_hit(out + 8 * i, h, tri, mesh, ent, iters);
         }
+    }
+}
+
+// CollideScene (Collide.comp's query; CollideBVHStack.glsl / CollideBVHStackless.glsl) per box
+// ({min.xyzw, max.xyzw}): out 4 ints {collided, entity, mesh, triangle}, -1 where unwritten.
+template <class NS_Node, class NS_Tri, class NS_Vert, class NS_Ent, class Scene>
+static void collide_all(const void* nodes, int64_t n_nodes, const void* tris, int64_t n_tris, const void* verts,
+                        int64_t n_verts, const void* ents, int32_t n_ents, const float* boxes, int64_t n,
+                        int32_t* out, NS_Node** gn, NS_Tri** gt, NS_Vert** gv, NS_Ent** ge, int* gcount, int* gtotal,
+                        Scene scene) {
+    Buffers<NS_Node, NS_Tri, NS_Vert, NS_Ent> b(nodes, n_nodes, tris, n_tris, verts, n_verts, ents, n_ents);
+    *gn = b.nodes.data();
+    *gt = b.tris.data();
+    *gv = b.verts.data();
+    *ge = b.ents.data();
+    *gcount = n_ents;
+    *gtotal = static_cast<int>(n_nodes);
+    for (int64_t i = 0; i < n; ++i) {
+        const float* x = boxes + 8 * i;
+        int mesh = -1, tri = -1, ent = -1;
+        const bool hit = scene(glsl::vec3(x[0], x[1], x[2]), glsl::vec3(x[4], x[5], x[6]), mesh, tri, ent);
+        out[4 * i] = hit ? 1 : 0;
+        out[4 * i + 1] = ent;
+        out[4 * i + 2] = mesh;
+        out[4 * i + 3] = tri;
+    }
+}
+
+extern "C" void ref_glsl_collide(int stackless, const void* nodes, int64_t n_nodes, const void* tris, int64_t n_tris,
+                                 const void* verts, int64_t n_verts, const void* ents, int32_t n_ents,
+                                 const float* boxes, int64_t n, int32_t* out) {
+    if (!stackless) {
+        namespace G = glsl_collide_stack;
+        collide_all(nodes, n_nodes, tris, n_tris, verts, n_verts, ents, n_ents, boxes, n, out, &G::BVHNodes,
+                    &G::BVHTris, &G::BVHVertices, &G::BVHEntities, &G::u_EntityCount, &G::u_TotalNodes,
+                    [](glsl::vec3 a, glsl::vec3 b, int& m, int& t, int& e) { return G::CollideScene(a, b, m, t, e); });
+    } else {
+        namespace G = glsl_collide_stackless;
+        collide_all(nodes, n_nodes, tris, n_tris, verts, n_verts, ents, n_ents, boxes, n, out, &G::BVHNodes,
+                    &G::BVHTris, &G::BVHVertices, &G::BVHEntities, &G::u_EntityCount, &G::u_TotalNodes,
+                    [](glsl::vec3 a, glsl::vec3 b, int& m, int& t, int& e) { return G::CollideScene(a, b, m, t, e); });
     }
 }
 

@@ -65,6 +65,8 @@ inline vec3 operator*(float s, vec3 a) { return {s * a.x, s * a.y, s * a.z}; }
 inline vec3 operator/(float s, vec3 a) { return {s / a.x, s / a.y, s / a.z}; }
 inline vec3 operator/(vec3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
 inline vec3 operator-(vec3 a) { return {-a.x, -a.y, -a.z}; }
+inline vec3& operator-=(vec3& a, vec3 b) { return a = a - b; }
+inline vec3& operator+=(vec3& a, vec3 b) { return a = a + b; }
 
 inline vec4 operator*(const mat4& m, vec4 v) {
     vec4 r;
@@ -75,6 +77,7 @@ inline vec4 operator*(const mat4& m, vec4 v) {
     return r;
 }
 
+inline float abs(float x) { return std::fabs(x); }
 inline float min(float x, float y) { return y < x ? y : x; }
 inline float max(float x, float y) { return x < y ? y : x; }
 inline vec3 min(vec3 a, vec3 b) { return {min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)}; }

@@ -13,11 +13,11 @@
 //    bit for bit, with the dot / mat*vec summation order defined here (GLSL leaves it open);
 //  * CosWeightedHemisphere (Sampling.glsl) the same way: within a few ulps (its cos / sin are the
 //    C library's there, the turn-based polynomials here);
-//  * the collision walk (stackless layout, the reference's axis set) against Physics::CollideBox,
-//    compiled from Physics.cpp (ref_physics_harness.cpp);
+//  * the collision walks (both layouts, the reference's axis set and leaf index) against
+//    CollideBVHStack.glsl / CollideBVHStackless.glsl compiled the same way, and the stackless one
+//    also against Physics::CollideBox, compiled from Physics.cpp (ref_physics_harness.cpp);
 //  * the BVH constructor (ref_bvh_harness.cpp), byte for byte.
-// Parity unpinned for the rest (GI / specular shading, texture sampling, the stack-layout collision
-// walk): they depend on shader inputs that cannot be compiled apart from the renderer (shadow maps,
+// Parity unpinned for the rest (GI / specular shading, texture sampling): they depend on shader inputs that cannot be compiled apart from the renderer (shadow maps,
 // G-buffer, bindless textures), so they are checked by analytic known-answer tests and an FP64
 // brute force (tests/test_oracle*.py).
 //

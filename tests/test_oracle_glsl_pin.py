@@ -97,3 +97,28 @@ def test_cos_hemisphere_matches_reference_sampler():
     ours, ref = O.cos_hemisphere(n, r), O.ref_glsl_cos_hemisphere(n, r)
     assert np.abs(ours - ref).max() < 2e-6
     assert (ours == ref).all(1).mean() > 0.2
+
+
+@pytest.mark.parametrize("layout", [R.STACK, R.STACKLESS])
+def test_collide_matches_reference_shader(layout):
+    """CollideScene of CollideBVHStack.glsl / CollideBVHStackless.glsl compiled as C++ against the
+    restatement with the reference's conventions (RQ_FLAG_REF_COMPAT: the repeated separating
+    axis, the within-leaf triangle index on the stack layout): identical records."""
+    from .test_oracle_collide import _scene_boxes
+    ri = R.RayIntersector(layout)
+    ri.add_object(1, [mesh("hf32")])
+    ri.add_object(2, [mesh("ico2")])
+    M = S.instance_transforms(6, (-2.0, -2.0, 0.0), (2.0, 2.0, 0.5), 0.6, 1.2, seed=7, tilt=0.05)
+    ri.push_entity(1)
+    for i in range(6):
+        ri.push_entity(1 + (i % 2), model=M[i].astype(np.float64))
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    osc = O.OracleScene(ORC_LAYOUT[layout], v, t, n, e)
+    boxes = np.concatenate([_scene_boxes("hf32", 4000, seed=3), _scene_boxes("ico2", 4000, seed=4)])
+    ref = O.ref_glsl_collide(ORC_LAYOUT[layout], v, t, n, e, boxes)
+    ours = osc.collide(boxes, flags=O.ORC_FLAG_REF_COMPAT)
+    np.testing.assert_array_equal(ours[:, 0], ref[:, 0])
+    hit = ref[:, 0] == 1
+    np.testing.assert_array_equal(ours[hit], ref[hit])
+    assert 0.2 < hit.mean() < 0.95 and len(np.unique(ref[hit, 1])) >= 3
