@@ -98,7 +98,10 @@ def orc() -> C.CDLL:
                                     C.c_int, P]
         L.orc_shade.argtypes = [sp, P, P, I64, P, C.POINTER(OrcMaterials), P, P, P, I32, C.c_int, P]
         L.orc_hit_albedo.argtypes = [sp, P, I64, C.POINTER(OrcMaterials), C.c_int, P]
+        L.orc_hit_normal.argtypes = [sp, P, I64, I32, P]
+        L.orc_hit_uv.argtypes = [sp, P, I64, P]
         L.orc_spec_raygen.argtypes = [sp, P, P, I64, C.c_uint32, C.c_float, C.c_float, I32, C.c_int, P]
+        L.orc_spec_direction.argtypes = [P, P, I64, C.c_float, C.c_uint32, P, P]
         L.orc_spec_shade.argtypes = [sp, P, P, I64, P, C.POINTER(OrcMaterials), C.c_float, P, P, P, C.c_int, P]
         L.orc_shadow_raygen.argtypes = [sp, P, P, I64, P, C.c_float, I32, C.c_int, P]
         L.orc_bounce_raygen.argtypes = [sp, P, P, P, P, I64, C.c_uint32, I32, C.c_float, C.c_float, I32,
@@ -223,6 +226,18 @@ class OracleScene:
                              _p(sc_), _p(sk), _p(am), nthreads or os.cpu_count() or 1, _p(out))
         return out
 
+    def hit_normal(self, hits, normal_mode=0):
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.empty((hits.shape[0], 3), dtype=np.float32)
+        orc().orc_hit_normal(C.byref(self.s), _p(hits), hits.shape[0], normal_mode, _p(out))
+        return out
+
+    def hit_uv(self, hits):
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.empty((hits.shape[0], 2), dtype=np.float32)
+        orc().orc_hit_uv(C.byref(self.s), _p(hits), hits.shape[0], _p(out))
+        return out
+
     def hit_albedo(self, hits, albedo, textures=None, mesh_texture=None, nthreads=None):
         """GetData's albedo per hit ((n, 3) float32): texture at the hit's UV or ModelColor."""
         hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
@@ -328,6 +343,51 @@ def ref_glsl_collide(layout, vertices, tris, nodes, entities, boxes):
     out = np.empty((b.shape[0], 4), dtype=np.int32)
     L.ref_glsl_collide(int(layout == ORC_STACKLESS), _p(n), n.shape[0], _p(t), t.shape[0], _p(v), v.shape[0], _p(e),
                        e.shape[0], _p(b), b.shape[0], _p(out))
+    return out
+
+
+def ref_glsl_getdata(vertices, tris, entities, model_color, albedo_ref, hits):
+    """The reference's GetData (TraverseBVHStack.glsl:422-455 compiled as C++) per hit: (n, 8)
+    floats Normal, Albedo, Emissivity, Alpha; its texture() reports (u, v, texture index)."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    P = C.c_void_p
+    L.ref_glsl_getdata.restype = None
+    L.ref_glsl_getdata.argtypes = [P, C.c_int64, P, C.c_int64, P, C.c_int32, P, C.c_int32, P, C.c_int64, P]
+    v, t, e = np.ascontiguousarray(vertices), np.ascontiguousarray(tris, dtype=np.int32), np.ascontiguousarray(entities)
+    mc = np.asarray(model_color, dtype=np.float32).reshape(-1, 3)
+    refs = np.zeros((mc.shape[0], 8), dtype=np.float32)     # vec4 ModelColor, int Albedo, Normal, Pad[2]
+    refs[:, :3] = mc
+    refs.view(np.int32)[:, 4] = np.asarray(albedo_ref, dtype=np.int32)
+    refs.view(np.int32)[:, 5] = -1
+    h = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    out = np.empty((h.shape[0], 8), dtype=np.float32)
+    L.ref_glsl_getdata(_p(t), t.shape[0], _p(v), v.shape[0], _p(e), e.shape[0], _p(refs), refs.shape[0], _p(h),
+                       h.shape[0], _p(out))
+    return out
+
+
+def spec_direction(incident, normals, roughness, seed, rid):
+    """The restatement's StochasticReflectionDirection for (n, 3) incident directions and normals."""
+    i3 = np.ascontiguousarray(incident, dtype=np.float32).reshape(-1, 3)
+    n3 = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    rr = np.ascontiguousarray(rid, dtype=np.uint32)
+    out = np.empty_like(i3)
+    orc().orc_spec_direction(_p(i3), _p(n3), i3.shape[0], roughness, seed & 0xFFFFFFFF, _p(rr), _p(out))
+    return out
+
+
+def ref_glsl_spec_direction(incident, normals, roughness, seed, rid):
+    """The reference's StochasticReflectionDirection(I, N, 0.9 R) and SampleGGXVNDF compiled as C++,
+    hash2() drawing the same counter-based samples."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_spec_direction.restype = None
+    L.ref_glsl_spec_direction.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_uint32, C.c_void_p,
+                                          C.c_void_p]
+    i3 = np.ascontiguousarray(incident, dtype=np.float32).reshape(-1, 3)
+    n3 = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    rr = np.ascontiguousarray(rid, dtype=np.uint32)
+    out = np.empty_like(i3)
+    L.ref_glsl_spec_direction(_p(i3), _p(n3), i3.shape[0], roughness, seed & 0xFFFFFFFF, _p(rr), _p(out))
     return out
 
 

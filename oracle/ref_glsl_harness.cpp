@@ -147,6 +147,86 @@ extern "C" void ref_glsl_collide(int stackless, const void* nodes, int64_t n_nod
     }
 }
 
+// GetData (TraverseBVHStack.glsl:422-455) per hit record (t, u, v, w, tri, mesh, entity, iters)
+// with the texture table `refs` (32 bytes per mesh: ModelColor, Albedo texture index, ...): out 8
+// floats per hit, Normal, Albedo, Emissivity, Alpha.  texture() is replaced by (u, v, texture
+// index), so Albedo reports the UV GetData samples at for textured meshes.
+extern "C" void ref_glsl_getdata(const void* tris, int64_t n_tris, const void* verts, int64_t n_verts,
+                                 const void* ents, int32_t n_ents, const void* refs, int32_t n_refs,
+                                 const float* hits, int64_t n, float* out) {
+    namespace G = glsl_stack;
+    std::vector<G::Triangle> t(n_tris);
+    std::vector<G::Vertex> v(n_verts);
+    std::vector<G::BVHEntity> e(n_ents);
+    std::vector<G::TextureReferences> r(n_refs);
+    std::memcpy(static_cast<void*>(t.data()), tris, sizeof(G::Triangle) * n_tris);
+    std::memcpy(static_cast<void*>(v.data()), verts, sizeof(G::Vertex) * n_verts);
+    std::memcpy(static_cast<void*>(e.data()), ents, sizeof(G::BVHEntity) * n_ents);
+    std::memcpy(static_cast<void*>(r.data()), refs, sizeof(G::TextureReferences) * n_refs);
+    G::BVHTris = t.data();
+    G::BVHVertices = v.data();
+    G::BVHEntities = e.data();
+    G::BVHTextureReferences = r.data();
+    for (int k = 0; k < 512; ++k) G::Textures[k].id = k;
+    for (int64_t i = 0; i < n; ++i) {
+        const float* h = hits + 8 * i;
+        int tri, mesh, ent;
+        std::memcpy(&tri, h + 4, 4);
+        std::memcpy(&mesh, h + 5, 4);
+        std::memcpy(&ent, h + 6, 4);
+        glsl::vec3 normal(0.0f), albedo(0.0f);
+        float em = 0.0f, alpha = 0.0f;
+        G::GetData(glsl::vec4(h[0], h[1], h[2], h[3]), mesh, tri, ent, normal, albedo, em, alpha);
+        float* o = out + 8 * i;
+        o[0] = normal.x;
+        o[1] = normal.y;
+        o[2] = normal.z;
+        o[3] = albedo.x;
+        o[4] = albedo.y;
+        o[5] = albedo.z;
+        o[6] = em;
+        o[7] = alpha;
+    }
+}
+
+// hash2() of the specular shader (SpecularTrace.glsl:71-75) is a fract(sin) sequence whose values
+// depend on the driver's sin; here it draws the engine's counter-based samples instead (pcg_hash,
+// Jarzynski & Olano 2020: key = hash(hash(hash(seed) + sample) + dimension), u = (key >> 8) / 2^24),
+// dimensions 2k and 2k+1 on the k-th call, so both sides consume the same numbers.
+namespace glsl_specular {
+uint32_t g_seed = 0, g_sample = 0, g_dim = 0;
+static uint32_t pcg(uint32_t x) {
+    const uint32_t state = x * 747796405u + 2891336453u;
+    const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+static float u01(uint32_t dim) {
+    return static_cast<float>(pcg(pcg(pcg(g_seed) + g_sample) + dim) >> 8) * (1.0f / 16777216.0f);
+}
+glsl::vec2 hash2() {
+    const glsl::vec2 r{u01(g_dim), u01(g_dim + 1)};
+    g_dim += 2;
+    return r;
+}
+}  // namespace glsl_specular
+
+// StochasticReflectionDirection(I, N, PBR.x * 0.9) as SpecularTrace.glsl:513 calls it.
+extern "C" void ref_glsl_spec_direction(const float* incident, const float* normals, int64_t n, float roughness,
+                                        uint32_t seed, const uint32_t* rid, float* out) {
+    namespace G = glsl_specular;
+    for (int64_t i = 0; i < n; ++i) {
+        G::g_seed = seed;
+        G::g_sample = rid[i];
+        G::g_dim = 0;
+        const glsl::vec3 d = G::StochasticReflectionDirection(
+            glsl::vec3(incident[3 * i], incident[3 * i + 1], incident[3 * i + 2]),
+            glsl::vec3(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]), roughness * 0.9f);
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
+
 // CosWeightedHemisphere (Shaders/Include/Sampling.glsl:1-12) for n normals / sample pairs.
 extern "C" void ref_glsl_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out) {
     for (int64_t i = 0; i < n; ++i) {

@@ -12,8 +12,8 @@
 //    leaves the order to the implementation, and this is the order the engine and the CPU
 //    restatement define;
 //  * floatBitsToInt / intBitsToFloat reinterpret bits.
-// `.xyz` is rewritten to `.xyz()` by the recipe; `in` becomes empty and `out T` / `inout T`
-// become `T&`.
+// `.xyz` / `.xy` are rewritten to `.xyz()` / `.xy()` by the recipe; `in` becomes empty and
+// `out T` / `inout T` become `T&`.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -22,12 +22,14 @@
 namespace glsl {
 
 struct vec4;
+struct vec2;
 
 struct vec3 {
     float x, y, z;
     vec3() = default;
     vec3(float s) : x(s), y(s), z(s) {}
     vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    vec3(const vec2& v, float c);
     explicit vec3(const vec4& v);
     vec3 xyz() const { return *this; }
 };
@@ -46,16 +48,27 @@ inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
 
 struct vec2 {
     float x, y;
+    vec2 xy() const { return *this; }
+};
+
+inline vec3::vec3(const vec2& v, float c) : x(v.x), y(v.y), z(c) {}
+
+struct uvec2 {
+    uint32_t x, y;
 };
 
 struct uvec4 {
     uint32_t x, y, z, w;
+    uvec2 xy() const { return {x, y}; }
 };
 
 struct mat4 {
     vec4 c[4];  // columns
 };
 
+inline vec2 operator+(vec2 a, vec2 b) { return {a.x + b.x, a.y + b.y}; }
+inline vec2 operator*(vec2 a, float s) { return {a.x * s, a.y * s}; }
+inline vec2 operator*(vec2 a, vec2 b) { return {a.x * b.x, a.y * b.y}; }
 inline vec3 operator+(vec3 a, vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 inline vec3 operator-(vec3 a, vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline vec3 operator*(vec3 a, vec3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
@@ -91,6 +104,22 @@ inline float sqrt(float x) { return std::sqrt(x); }
 inline float cos(float x) { return std::cos(x); }
 inline float sin(float x) { return std::sin(x); }
 inline vec3 normalize(vec3 v) { return v / sqrt(dot(v, v)); }
+inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }
+// unpackHalf2x16: binary16 halves (low half first) converted exactly.
+inline float half_to_float(uint32_t h) {
+    const uint32_t s = (h >> 15) & 1u, e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+    float f;
+    if (e == 0) {
+        f = std::ldexp(static_cast<float>(m), -24);
+    } else if (e == 31) {
+        uint32_t bits = 0x7F800000u | (m << 13);
+        std::memcpy(&f, &bits, 4);
+    } else {
+        f = std::ldexp(static_cast<float>(m | 0x400u), static_cast<int>(e) - 25);
+    }
+    return s ? -f : f;
+}
+inline vec2 unpackHalf2x16(uint32_t v) { return {half_to_float(v & 0xFFFFu), half_to_float(v >> 16)}; }
 inline int floatBitsToInt(float f) {
     int i;
     std::memcpy(&i, &f, 4);

@@ -11,15 +11,19 @@
 //    ignore-transparent, the tri-0 test, iteration counts) against the traversal functions of
 //    TraverseBVHStack.glsl / TraverseBVHStackless.glsl compiled as C++ (ref_glsl_harness.cpp):
 //    bit for bit, with the dot / mat*vec summation order defined here (GLSL leaves it open);
-//  * CosWeightedHemisphere (Sampling.glsl) the same way: within a few ulps (its cos / sin are the
-//    C library's there, the turn-based polynomials here);
+//  * GetData (TraverseBVHStack.glsl: interpolated normal, UV, ModelColor, emissive, alpha) the
+//    same way: bit for bit;
+//  * CosWeightedHemisphere (Sampling.glsl) and StochasticReflectionDirection / SampleGGXVNDF
+//    (SpecularTrace.glsl, Sampling.glsl) the same way, with the same samples: a mirror bit for bit,
+//    sampled directions within a few ulps (the C library's cos / sin there, turn-based polynomials
+//    here; GGX's sqrt(1 - cos^2) cancellation spreads that to 1e-4 in rare samples);
 //  * the collision walks (both layouts, the reference's axis set and leaf index) against
 //    CollideBVHStack.glsl / CollideBVHStackless.glsl compiled the same way, and the stackless one
 //    also against Physics::CollideBox, compiled from Physics.cpp (ref_physics_harness.cpp);
 //  * the BVH constructor (ref_bvh_harness.cpp), byte for byte.
-// Parity unpinned for the rest (GI / specular shading, texture sampling): they depend on shader inputs that cannot be compiled apart from the renderer (shadow maps,
-// G-buffer, bindless textures), so they are checked by analytic known-answer tests and an FP64
-// brute force (tests/test_oracle*.py).
+// Parity unpinned for the rest (the shading sums, texture filtering): their shader functions read
+// renderer state that cannot be compiled apart from the renderer (shadow maps, G-buffer, bindless
+// samplers), so they are checked by analytic known-answer tests (tests/test_oracle*.py).
 //
 // Arithmetic conventions (the definition that the strict GPU kernels must reproduce bit for bit):
 //  * IEEE binary32, round to nearest, no contraction (built with -ffp-contract=off);
@@ -711,16 +715,21 @@ V3 sample_bilinear(const orc_materials& m, int32_t t, float u, float v) {
     return add(add(add(muls(t00, w00), muls(t10, w10)), muls(t01, w01)), muls(t11, w11));
 }
 
+// The hit's texture coordinates (TraverseBVHStack.glsl:436): the vertices' half-packed UVs
+// weighted by the barycentrics u, v, w, summed left to right.
+void hit_uv(const Scene& s, const orc_hit& h, float& u, float& v) {
+    const int32_t* tr = s.tris + int64_t(h.tri) * 4;
+    const uint32_t* va = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[0]) * 8);
+    const uint32_t* vb = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[1]) * 8);
+    const uint32_t* vc = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[2]) * 8);
+    u = (half_to_float(va[7] & 0xFFFFu) * h.u + half_to_float(vb[7] & 0xFFFFu) * h.v) + half_to_float(vc[7] & 0xFFFFu) * h.w;
+    v = (half_to_float(va[7] >> 16) * h.u + half_to_float(vb[7] >> 16) * h.v) + half_to_float(vc[7] >> 16) * h.w;
+}
+
 V3 hit_albedo(const Scene& s, const orc_materials& m, const orc_hit& h) {
     if (h.mesh >= 0 && h.mesh < m.n_mesh_tex && h.t > 0.0f && m.mesh_tex[h.mesh] >= 0) {
-        const int32_t* tr = s.tris + int64_t(h.tri) * 4;
-        const uint32_t* va = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[0]) * 8);
-        const uint32_t* vb = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[1]) * 8);
-        const uint32_t* vc = reinterpret_cast<const uint32_t*>(s.verts + int64_t(tr[2]) * 8);
-        const float u = (half_to_float(va[7] & 0xFFFFu) * h.u + half_to_float(vb[7] & 0xFFFFu) * h.v) +
-                        half_to_float(vc[7] & 0xFFFFu) * h.w;
-        const float v = (half_to_float(va[7] >> 16) * h.u + half_to_float(vb[7] >> 16) * h.v) +
-                        half_to_float(vc[7] >> 16) * h.w;
+        float u, v;
+        hit_uv(s, h, u, v);
         return sample_bilinear(m, m.mesh_tex[h.mesh], u, v);
     }
     if (h.mesh >= 0 && h.mesh < m.n_albedo) return ld3(m.albedo + 3 * h.mesh);
@@ -964,6 +973,24 @@ V3 sample_ggx(V3 n, float roughness, float x0, float x1) {
 
 float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 
+// StochasticReflectionDirection(I, N, 0.9 * roughness) (SpecularTrace.glsl:102-135) with sample
+// `rid` of the counter-based hash (dimensions 2k, 2k+1 for try k).
+V3 spec_direction(V3 I, V3 N, float roughness, uint32_t seed, uint32_t rid) {
+    const float r = roughness * 0.9f;
+    if (r < 0.01f) return reflect_dir(I, N);
+    V3 micro = N;
+    for (uint32_t k = 0; k < 12; ++k) {
+        const float x0 = u01(sample_key(seed, rid, 2u * k)) * 0.8f;
+        const float x1 = u01(sample_key(seed, rid, 2u * k + 1u)) * 0.7f;
+        const V3 smp = sample_ggx(N, r, x0, x1);
+        if (dot(smp, N) > 0.001f) {
+            micro = smp;
+            break;
+        }
+    }
+    return reflect_dir(I, micro);
+}
+
 }  // namespace
 
 // Reflection ray per pixel: origin P + N * mix(0.05, 0.1, clamp(1.4 R, 0, 1)) (:509), direction
@@ -985,23 +1012,7 @@ void orc_spec_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit*
             V3 N = hit_normal(s, h, normal_mode);
             if (dot(N, rd) > 0.0001f) N = neg(N);
             const V3 I = normalize(sub(P, ro));
-            const float r = roughness * 0.9f;
-            V3 dir;
-            if (r < 0.01f) {
-                dir = reflect_dir(I, N);
-            } else {
-                V3 micro = N;
-                for (uint32_t k = 0; k < 12; ++k) {
-                    const float x0 = u01(sample_key(seed, uint32_t(i), 2u * k)) * 0.8f;
-                    const float x1 = u01(sample_key(seed, uint32_t(i), 2u * k + 1u)) * 0.7f;
-                    const V3 smp = sample_ggx(N, r, x0, x1);
-                    if (dot(smp, N) > 0.001f) {
-                        micro = smp;
-                        break;
-                    }
-                }
-                dir = reflect_dir(I, micro);
-            }
+            const V3 dir = spec_direction(I, N, roughness, seed, uint32_t(i));
             const float off = mixf(0.05f, 0.1f, clamp01(roughness * 1.4f));
             const V3 org = add(P, muls(N, off));
             o.o[0] = org.x; o.o[1] = org.y; o.o[2] = org.z;
@@ -1014,6 +1025,16 @@ void orc_spec_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit*
 
 // SampleLighting (:420-425) + emissive for a hit, the sky x mix(1.4, 2.65, R) (:435-437) for a
 // miss; IsValid, clamp to [0, 6], w = t / 48 (:588-596); 0 where the primary ray missed.
+void orc_spec_direction(const float* incident, const float* normals, int64_t n, float roughness, uint32_t seed,
+                        const uint32_t* rid, float* out) {
+    for (int64_t i = 0; i < n; ++i) {
+        const V3 d = spec_direction(ld3(incident + 3 * i), ld3(normals + 3 * i), roughness, seed, rid[i]);
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
+
 void orc_spec_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n, const uint8_t* lit,
                     const orc_materials* mat, float roughness, const float sun_color[3], const float sky[3],
                     const float ambient[3], int nthreads, float* out4) {
@@ -1048,6 +1069,21 @@ void orc_spec_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hit
             o[3] = t / 48.0f;
         }
     });
+}
+
+void orc_hit_normal(const orc_scene* sc, const orc_hit* hits, int64_t n, int32_t normal_mode, float* out3) {
+    const Scene s = make_scene(sc);
+    for (int64_t i = 0; i < n; ++i) {
+        const V3 nn = hit_normal(s, hits[i], normal_mode);
+        out3[3 * i] = nn.x;
+        out3[3 * i + 1] = nn.y;
+        out3[3 * i + 2] = nn.z;
+    }
+}
+
+void orc_hit_uv(const orc_scene* sc, const orc_hit* hits, int64_t n, float* out2) {
+    const Scene s = make_scene(sc);
+    for (int64_t i = 0; i < n; ++i) hit_uv(s, hits[i], out2[2 * i], out2[2 * i + 1]);
 }
 
 void orc_hit_albedo(const orc_scene* sc, const orc_hit* hits, int64_t n, const orc_materials* mat,

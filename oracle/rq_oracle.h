@@ -92,8 +92,14 @@ typedef struct {
 
 void orc_hit_albedo(const orc_scene* s, const orc_hit* hits, int64_t n, const orc_materials* mat,
                     int nthreads, float* out3);
+// GetData's interpolated normal (normal_mode 0) or the geometric normal, and the hit's UV.
+void orc_hit_normal(const orc_scene* s, const orc_hit* hits, int64_t n, int32_t normal_mode, float* out3);
+void orc_hit_uv(const orc_scene* s, const orc_hit* hits, int64_t n, float* out2);
 void orc_spec_raygen(const orc_scene* s, const orc_ray* primary, const orc_hit* hits, int64_t n, uint32_t seed,
                      float roughness, float ray_tmax, int32_t normal_mode, int nthreads, orc_ray* out);
+// The reflection direction of the specular pass for given incident directions and normals.
+void orc_spec_direction(const float* incident, const float* normals, int64_t n, float roughness, uint32_t seed,
+                        const uint32_t* rid, float* out);
 void orc_spec_shade(const orc_scene* s, const orc_ray* rays, const orc_hit* hits, int64_t n, const uint8_t* lit,
                     const orc_materials* mat, float roughness, const float sun_color[3], const float sky[3],
                     const float ambient[3], int nthreads, float* out4);
