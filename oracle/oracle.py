@@ -391,6 +391,42 @@ def ref_glsl_spec_direction(incident, normals, roughness, seed, rid):
     return out
 
 
+def ref_glsl_shade(specular, rays, hits, albedo, normals, lit, sun_dir, sun_color, sky, probe=(0.0, 0.0, 0.0),
+                   roughness=0.0):
+    """The reference's shading statements compiled as C++: the diffuse pass's hit shading
+    (DiffuseTrace.glsl:486-494, GetDirect :368-372) giving (FinalRadiance, AO), or the specular
+    pass's (SpecularTrace.glsl:554-563, 588-596, SampleLighting :420-425, Sky :435-437) giving the
+    stored (radiance, t / 48).  albedo: (n, 4) rgb + emissive as GetData returns them; normals:
+    (n, 3) GetData's normal; lit: what GetDirectShadow returns (0 / 1); sky: what the sky
+    textures return; probe: what SampleProbes returns."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_shade.restype = None
+    L.ref_glsl_shade.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4 + [C.c_float, C.c_void_p]
+    rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    n = rays.shape[0]
+    x = np.empty((n, 18), dtype=np.float32)
+    x[:, 0:3], x[:, 3:6] = rays["o"], rays["d"]
+    x[:, 6], x[:, 7], x[:, 8], x[:, 9] = hits["t"], hits["u"], hits["v"], hits["w"]
+    x[:, 10:14] = albedo
+    x[:, 14:17] = normals
+    x[:, 17] = np.asarray(lit, dtype=np.float32)
+    f3 = lambda v: np.ascontiguousarray(v, dtype=np.float32)  # noqa: E731
+    sd, sc, sk, pr = f3(sun_dir), f3(sun_color), f3(sky), f3(probe)
+    out = np.empty((n, 4), dtype=np.float32)
+    L.ref_glsl_shade(int(specular), _p(x), n, _p(sd), _p(sc), _p(sk), _p(pr), roughness, _p(out))
+    return out
+
+
+def ref_glsl_sun_colors():
+    """SUN_COLOR_DIFF and SUN_COLOR_SPEC (ColorConstants.h) as the reference's shaders evaluate them."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_sun_colors.restype = None
+    out = np.empty(6, dtype=np.float32)
+    L.ref_glsl_sun_colors(_p(out))
+    return out[:3].copy(), out[3:].copy()
+
+
 def cos_hemisphere(normals, r):
     """The restatement's CosWeightedHemisphere (turn-based sine / cosine) for (n, 3) normals and
     (n, 2) samples."""

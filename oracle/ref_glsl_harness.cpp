@@ -227,6 +227,57 @@ extern "C" void ref_glsl_spec_direction(const float* incident, const float* norm
     }
 }
 
+// The diffuse pass's hit shading (DiffuseTrace.glsl:486-494 with GetDirect :368-372) and the
+// specular pass's (SpecularTrace.glsl:554-563, 588-596 with SampleLighting :420-425, Sky :435-437,
+// IsValid Utility.glsl:117-125 and TransformReflectionTransversal SpatialUtility.glsl:12-14), per
+// ray.  in: 18 floats {origin, direction, TUVW, Albedo (rgb, emissive), the normal GetData returns
+// (not yet faced), sun visibility (0 or 1, what GetDirectShadow returns)}; out: 4 floats, the
+// diffuse statements' {FinalRadiance, AO} or the specular pass's stored texel.  sun_dir, sun
+// colour, sky (what the sky textures return), probe (what SampleProbes returns) and roughness
+// (PBR.x) are the renderer state the statements read.
+extern "C" void ref_glsl_shade(int specular, const float* in, int64_t n, const float* sun_dir, const float* sun,
+                               const float* sky, const float* probe, float roughness, float* out) {
+    const glsl::vec3 sd(sun_dir[0], sun_dir[1], sun_dir[2]), sc(sun[0], sun[1], sun[2]);
+    const glsl::vec3 sk(sky[0], sky[1], sky[2]), pr(probe[0], probe[1], probe[2]);
+    for (int64_t i = 0; i < n; ++i) {
+        const float* x = in + 18 * i;
+        const glsl::vec3 o(x[0], x[1], x[2]), d(x[3], x[4], x[5]), nrm(x[14], x[15], x[16]);
+        const glsl::vec4 tuvw(x[6], x[7], x[8], x[9]), alb(x[10], x[11], x[12], x[13]);
+        glsl::vec4 r;
+        if (!specular) {
+            namespace G = glsl_diffuse_shade;
+            G::g_shadow = x[17];
+            G::g_sun = sc;
+            G::u_SunDirection = sd;
+            G::g_sky = sk;
+            G::shade(o, d, tuvw, alb, nrm, r);
+        } else {
+            namespace G = glsl_specular_shade;
+            G::g_shadow = x[17];
+            G::g_sun = sc;
+            G::g_sky = sk;
+            G::g_probe = pr;
+            G::shade(o, d, tuvw, alb, nrm, glsl::vec4(roughness, 0.0f, 0.0f, 0.0f));
+            r = G::g_out;
+        }
+        out[4 * i] = r.x;
+        out[4 * i + 1] = r.y;
+        out[4 * i + 2] = r.z;
+        out[4 * i + 3] = r.w;
+    }
+}
+
+// SUN_COLOR_DIFF and SUN_COLOR_SPEC of ColorConstants.h as the shaders evaluate them.
+extern "C" void ref_glsl_sun_colors(float* out6) {
+    const glsl::vec3 a = glsl_diffuse_shade::sun_color_constant(), b = glsl_specular_shade::sun_color_constant();
+    out6[0] = a.x;
+    out6[1] = a.y;
+    out6[2] = a.z;
+    out6[3] = b.x;
+    out6[4] = b.y;
+    out6[5] = b.z;
+}
+
 // CosWeightedHemisphere (Shaders/Include/Sampling.glsl:1-12) for n normals / sample pairs.
 extern "C" void ref_glsl_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out) {
     for (int64_t i = 0; i < n; ++i) {

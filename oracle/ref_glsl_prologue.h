@@ -105,6 +105,13 @@ inline float cos(float x) { return std::cos(x); }
 inline float sin(float x) { return std::sin(x); }
 inline vec3 normalize(vec3 v) { return v / sqrt(dot(v, v)); }
 inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }
+inline float clamp(float x, float lo, float hi) { return min(max(x, lo), hi); }
+inline vec3 clamp(vec3 v, float lo, float hi) { return {clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi)}; }
+inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+inline float pow(float x, float y) { return std::pow(x, y); }
+inline vec3 pow(vec3 x, vec3 y) { return {pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z)}; }
+inline bool isnan(float x) { return std::isnan(x); }
+inline bool isinf(float x) { return std::isinf(x); }
 // unpackHalf2x16: binary16 halves (low half first) converted exactly.
 inline float half_to_float(uint32_t h) {
     const uint32_t s = (h >> 15) & 1u, e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;

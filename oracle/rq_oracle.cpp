@@ -20,10 +20,14 @@
 //  * the collision walks (both layouts, the reference's axis set and leaf index) against
 //    CollideBVHStack.glsl / CollideBVHStackless.glsl compiled the same way, and the stackless one
 //    also against Physics::CollideBox, compiled from Physics.cpp (ref_physics_harness.cpp);
+//  * the shading sums: the diffuse pass's hit shading (DiffuseTrace.glsl:486-494 with GetDirect)
+//    and the specular pass's (SpecularTrace.glsl:554-563, 588-596 with SampleLighting, Sky,
+//    IsValid, the clamp and the t / 48 store), compiled the same way with the renderer state they
+//    read (shadow-map lookup, probe volume, sky textures) given as values: bit for bit;
 //  * the BVH constructor (ref_bvh_harness.cpp), byte for byte.
-// Parity unpinned for the rest (the shading sums, texture filtering): their shader functions read
-// renderer state that cannot be compiled apart from the renderer (shadow maps, G-buffer, bindless
-// samplers), so they are checked by analytic known-answer tests (tests/test_oracle*.py).
+// Parity unpinned for the texture filter only: the reference samples through bindless GL
+// samplers, which cannot run here, so bilinear filtering, wrap modes and the sRGB decode are
+// checked by analytic known-answer tests (tests/test_oracle.py).
 //
 // Arithmetic conventions (the definition that the strict GPU kernels must reproduce bit for bit):
 //  * IEEE binary32, round to nearest, no contraction (built with -ffp-contract=off);

@@ -1,8 +1,9 @@
-"""Pins the CPU restatement of the traversal to the reference's own shader source: the traversal
-functions of TraverseBVHStack.glsl and TraverseBVHStackless.glsl compiled as C++ (oracle/Makefile,
-ref_glsl_harness.cpp) give the same TUVW, triangle, mesh, entity and iteration outputs, and the same
-occlusion answers, as rq_oracle.cpp with the reference's own conventions (first-found ties, the
-`TriangleIdx > 0` test).  Runs where the reference source tree is mounted."""
+"""Pins the CPU restatement to the reference's own shader source compiled as C++ (oracle/Makefile,
+ref_glsl_harness.cpp): the traversal functions of TraverseBVHStack.glsl and TraverseBVHStackless.glsl
+give the same TUVW, triangle, mesh, entity and iteration outputs, and the same occlusion answers, as
+rq_oracle.cpp with the reference's own conventions (first-found ties, the `TriangleIdx > 0` test);
+likewise the collision shaders, GetData, the samplers and the diffuse / specular shading
+statements.  Runs where the reference source tree is mounted."""
 import numpy as np
 import pytest
 
@@ -170,3 +171,71 @@ def test_specular_direction_matches_reference_sampler():
     for rough in (0.3, 0.8, 1.0):
         d = np.abs(O.spec_direction(i, n, rough, 7, rid) - O.ref_glsl_spec_direction(i, n, rough, 7, rid)).max(1)
         assert d.max() < 1e-3 and np.median(d) < 2e-7 and (d < 1e-5).mean() > 0.99
+
+
+def _shading_scene():
+    """Two objects, five entities: emissive 0, 0.5, 2 and +inf (the last drives the specular pass's
+    IsValid branch), one tilted; camera rays and sphere rays with misses."""
+    ri = R.RayIntersector(R.STACK)
+    ri.add_object(1, [mesh("hf32")])
+    ri.add_object(2, [mesh("ico2")])
+    M = S.instance_transforms(4, (-2.0, -2.0, 0.2), (2.0, 2.0, 0.8), 0.5, 0.9, seed=9, tilt=0.2)
+    ri.push_entity(1)
+    for i, em in enumerate((0.5, 2.0, 0.0, np.inf)):
+        ri.push_entity(2 if i % 2 == 0 else 1, model=M[i].astype(np.float64), emissive=em)
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    osc = O.OracleScene(O.ORC_STACK, v, t, n, e)
+    rays = np.concatenate([S.camera_rays(80, 60, eye=(0.0, -5.0, 3.0), target=(0.0, 0.0, 0.3)),
+                           S.sphere_rays(20_000, (-2.5, -2.5, -0.2), (2.5, 2.5, 1.5), seed=11)])
+    hits = osc.closest(rays)
+    emissive = e["data"][:, 0].view(np.float32)
+    model = np.float32([[0.7, 0.6, 0.5], [0.2, 0.8, 0.4], [0.9, 0.9, 0.2], [0.3, 0.3, 0.3]])
+    alb = np.zeros((rays.shape[0], 4), dtype=np.float32)
+    hit = hits["t"] > 0
+    alb[hit, :3] = osc.hit_albedo(hits[hit], model)
+    alb[hit, 3] = emissive[hits["entity"][hit]]
+    nrm = np.full((rays.shape[0], 3), -1.0, dtype=np.float32)
+    nrm[hit] = osc.hit_normal(hits[hit], 0)
+    lit = np.random.default_rng(2).integers(0, 2, rays.shape[0]).astype(np.uint8)
+    return osc, rays, hits, model, alb, nrm, lit
+
+
+def test_diffuse_shading_matches_reference_shader():
+    """The diffuse pass's hit shading (DiffuseTrace.glsl:486-494, GetDirect :368-372) compiled as
+    C++ with GetDirectShadow returning the shadow ray's answer and the sky texture a constant:
+    the restatement's shade() gives the same radiance and AO bit for bit (its sky_color is the
+    shader's texture value times its 2).  Run with the reference's SUN_COLOR_DIFF and with another
+    colour."""
+    osc, rays, hits, model, alb, nrm, lit = _shading_scene()
+    sun_dir, sky = np.float32([0.3, 0.4, -0.866]), np.float32([0.45, 0.6, 0.95])
+    ref_sun, _ = O.ref_glsl_sun_colors()
+    for sun in (ref_sun, np.float32([4.0, 3.8, 3.5])):
+        ref = O.ref_glsl_shade(0, rays, hits, alb, nrm, lit, sun_dir, sun, sky)
+        ours = osc.shade(rays, hits, lit, model, sun_dir, sun, sky * np.float32(2.0))
+        np.testing.assert_array_equal(ours.view(np.uint32), ref.view(np.uint32))
+    hit = hits["t"] > 0
+    assert 0.2 < hit.mean() < 0.9 and (ref[hit, :3].sum(1) > 0).mean() > 0.3
+    assert np.isinf(ref[hit & (alb[:, 3] == np.inf)]).any()
+
+
+def test_specular_shading_matches_reference_shader():
+    """The specular pass's shading and store (SpecularTrace.glsl:554-563 and 588-596: SampleLighting
+    :420-425, Sky :435-437, IsValid Utility.glsl:117-125, TransformReflectionTransversal
+    SpatialUtility.glsl:12-14) compiled as C++, SampleProbes returning the ambient term: the
+    restatement's spec_shade() stores the same texel bit for bit, including the non-finite
+    radiance the +inf emissive entity gives (zeroed, t = -1)."""
+    osc, rays, hits, model, alb, nrm, lit = _shading_scene()
+    sky, amb = np.float32([0.45, 0.6, 0.95]), np.float32([0.1, 0.1, 0.12])
+    _, ref_sun = O.ref_glsl_sun_colors()
+    clamped = 0
+    for sun in (ref_sun, np.float32([4.0, 3.8, 3.5])):
+        for rough in (0.0, 0.35, 1.0):
+            ref = O.ref_glsl_shade(1, rays, hits, alb, nrm, lit, (0.0, 0.0, -1.0), sun, sky, amb, rough)
+            ours = osc.spec_shade(rays, hits, lit, model, rough, sun, sky, amb)
+            np.testing.assert_array_equal(ours.view(np.uint32), ref.view(np.uint32))
+            clamped += int((ref[:, :3] == 6.0).sum())
+    hit = hits["t"] > 0
+    bad = hit & (alb[:, 3] == np.inf)
+    assert bad.sum() > 10 and (ref[bad, 3] == np.float32(-1.0 / 48.0)).all()
+    assert clamped > 100 and (ref[~hit, :3] > 0).all()
