@@ -188,6 +188,26 @@ def cpu_collide(wl):
     return out
 
 
+PROBE_GRID, PROBE_ORIGIN, PROBE_SIZE = (48, 48, 24), (0.0, 0.0, 1.0), (4.5, 4.5, 1.25)
+
+
+def cpu_probe(wl, albedo):
+    """The CPU restatement of one probe-update frame (rays, closest hits, shadow rays, shading,
+    SH) on all host cores, over the same 55,296-probe grid as the GPU leg."""
+    from oracle import oracle as O
+    from candela_gb300.engine import probe_params, probe_volumes
+    nthreads = os.cpu_count() or 1
+    osc = O.OracleScene(O.ORC_STACK, wl["mesh"].vertices, wl["bvh"].tris, wl["bvh"].nodes, wl["ent"])
+    pp = probe_params(grid=PROBE_GRID, origin=PROBE_ORIGIN, size=PROBE_SIZE, seed=2)
+    sh, raw, pmap = probe_volumes(pp)
+    t0 = time.perf_counter()
+    osc.probe_update(pp, albedo, sh, raw, pmap)
+    dt = time.perf_counter() - t0
+    n = O.probe_count(pp)
+    return {"probes": n, "ms": round(dt * 1e3, 2), "mprobes_s": round(n / dt / 1e6, 3), "cores": nthreads,
+            "kind": "port"}
+
+
 def cpu_baseline(wl, seconds: float):
     """The CPU restatement of the reference path on all host cores, on a bounded sample:
     repeated whole-pass runs over a prefix of the primary rays until `seconds` elapse."""
@@ -922,6 +942,25 @@ def main():
     if rank == 0:
         collide["cpu_baseline"] = cpu_collide(wl)
 
+    # ---- radiance probe volume (rq_probe_update): the reference's default probe count (48 x 24 x
+    # 48 = 55,296 probes), laid over the scene, and a 128 x 128 x 64 grid (1M probes); each frame
+    # reads the previous frame's volume (reprojection, bounce) and writes the other one
+    from candela_gb300.engine import probe_params, probe_volumes
+    probe = {"desc": "one ray per probe + a shadow ray per hit, shading, SampleProbes bounce, L1 SH "
+                     "encode, temporal blend, pack; BVH8q"}
+    for name, grid in (("default_grid", PROBE_GRID), ("grid_128x128x64", (128, 128, 64))):
+        pp = probe_params(grid=grid, origin=PROBE_ORIGIN, size=PROBE_SIZE, seed=2)
+        vols = [probe_volumes(pp, device=dev) for _ in range(2)]
+        sc.probe_update(pp, vols[0][0], vols[0][1], vols[0][2], out_sh=vols[1][0], out_raw=vols[1][1],
+                        layout=B8, stream=sptr)
+        pr_ms = timed(lambda: sc.probe_update(pp, vols[1][0], vols[1][1], vols[1][2], out_sh=vols[0][0],
+                                              out_raw=vols[0][1], layout=B8, stream=sptr))
+        n_pr = int(np.prod(grid))
+        probe[name] = {"probes": n_pr, "ms": round(pr_ms, 4), "mprobes_s": round(n_pr / (pr_ms / 1e3) / 1e6, 1)}
+        del vols
+    if rank == 0:
+        probe["cpu_baseline"] = cpu_probe(wl, wl["albedo"])
+
     # ---- roofline of the dominant kernel (secondary closest / AO any-hit on BVH8q)
     dom = "secondary_anyhit_bvh8q" if q_any else "secondary_closest_bvh8q"
     ref = "secondary_anyhit_strict_stack" if q_any else "secondary_closest_strict_stack"
@@ -979,7 +1018,7 @@ def main():
                                 "ms_per_step": round(plain_ms / args.steps, 4),
                                 "speedup_bvh8q_over_plain": round(value / world / plain_value, 3)},
             "e2e": e2e, "roofline": roofline, "breakdown": breakdown, "bvh8q_vs_strict": agreement,
-            "bvh_build": bvh_build, "collide": collide, "specular": specular,
+            "bvh_build": bvh_build, "collide": collide, "specular": specular, "probe_update": probe,
             "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
                              "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}

@@ -101,6 +101,13 @@ class RqSpecularParams(C.Structure):
                 ("ambient", C.c_float * 3)]
 
 
+class RqProbeParams(C.Structure):
+    _fields_ = [("grid", C.c_int32 * 3), ("origin", C.c_float * 3), ("prev_origin", C.c_float * 3),
+                ("size", C.c_float * 3), ("seed", C.c_uint32), ("temporal", C.c_int32), ("normal_mode", C.c_int32),
+                ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float), ("ray_tmax", C.c_float),
+                ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3), ("sky_color", C.c_float * 3)]
+
+
 class RqFrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("secondary_rays", C.c_int64), ("secondary_hits", C.c_int64),
@@ -164,6 +171,7 @@ SIGNATURES = {
     "rq_scene_tlas_info": (_S, [_P, C.POINTER(C.c_int64 * 3)]),
     "rq_scene_set_textures": (_S, [_P, _P, _I32, _P, _I32]),
     "rq_specular_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqSpecularParams), C.POINTER(RqOpts), _P, _P]),
+    "rq_probe_update": (_S, [_P, _P, C.POINTER(RqProbeParams), _P, _P, _P, _P, _P, C.POINTER(RqOpts), _P]),
 }
 
 NOALLOC_MAX_RAYS = 65536

@@ -331,6 +331,32 @@ def specular_params(seed=0, roughness=0.3, ray_tmax=1000000.0, normal_mode=0, sh
                               f3(sd), f3(sun_color), f3(sky_color), f3(ambient))
 
 
+def probe_params(grid=(128, 64, 128), origin=(0.0, 0.0, 0.0), prev_origin=None, size=(64.0, 32.0, 64.0), seed=0,
+                 temporal=True, normal_mode=0, shadow_rays=True, shadow_offset=1e-3, ray_tmax=1000000.0,
+                 sun_dir=(0.3, 0.4, -0.866), sun_color=(4.0, 3.8, 3.5), sky_color=(0.5, 0.7, 1.0)) -> L.RqProbeParams:
+    """rq_probe_params for one frame of the radiance-probe update; prev_origin defaults to origin
+    (a volume that did not move)."""
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
+    return L.RqProbeParams((C.c_int32 * 3)(*[int(g) for g in grid]), f3(origin),
+                           f3(origin if prev_origin is None else prev_origin), f3(size), seed & 0xFFFFFFFF,
+                           int(temporal), normal_mode, int(shadow_rays), shadow_offset, ray_tmax, f3(sd),
+                           f3(sun_color), f3(sky_color))
+
+
+def probe_volumes(params, device=None):
+    """Zeroed (sh (n, 8) int32 bit patterns, raw (n, 4), map (n, 128)) for a probe grid: numpy when
+    device is None, else torch tensors on that device."""
+    n = int(params.grid[0]) * int(params.grid[1]) * int(params.grid[2])
+    if device is None:
+        return (np.zeros((n, 8), dtype=np.uint32), np.zeros((n, 4), dtype=np.float32),
+                np.zeros((n, 128), dtype=np.float32))
+    import torch
+    return (torch.zeros((n, 8), dtype=torch.int32, device=device), torch.zeros((n, 4), dtype=torch.float32, device=device),
+            torch.zeros((n, 128), dtype=torch.float32, device=device))
+
+
 def _empty_like_dev(ref, shape, dtype):
     import torch
     return torch.empty(shape, dtype=dtype, device=ref.device)
@@ -392,6 +418,23 @@ class _GiMixin:
         check(lib().rq_specular_frame(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params), C.byref(o),
                                       ptr(out), _stream(primary, stream)), self.ctx.handle)
         return out
+
+    def probe_update(self, params, prev_sh, prev_raw, probe_map, out_sh=None, out_raw=None, *, layout=0, mode=0,
+                     tie=0, flags=0, stream=None):
+        """One frame of the radiance-probe update (rq_probe_update).  numpy volumes -> host path.
+        probe_map is updated in place; returns (out_sh, out_raw)."""
+        host = isinstance(prev_sh, np.ndarray)
+        n = int(params.grid[0]) * int(params.grid[1]) * int(params.grid[2])
+        if out_sh is None:
+            out_sh = np.empty((n, 8), dtype=np.uint32) if host else _empty_like_dev(prev_sh, (n, 8), prev_sh.dtype)
+        if out_raw is None:
+            out_raw = (np.empty((n, 4), dtype=np.float32) if host
+                       else _empty_like_dev(prev_raw, (n, 4), __import__("torch").float32))
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        check(lib().rq_probe_update(self.ctx.handle, self.handle, C.byref(params), ptr(prev_sh), ptr(prev_raw),
+                                    ptr(probe_map), ptr(out_sh), ptr(out_raw), C.byref(o),
+                                    _stream(prev_sh, stream)), self.ctx.handle)
+        return out_sh, out_raw
 
     def gi_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0,
                  block_size=0, min_blocks=0, persistent=0, stats=False, stream=None):

@@ -510,6 +510,55 @@ rq_status rq_specular_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* pr
                             const rq_specular_params* params, const rq_opts* opts, float* out4,
                             void* stream);
 
+/* ---- Radiance probe volume ----------------------------------------------------------------- */
+
+/* One frame of UpdateRadianceProbes.glsl (dispatched by ProbeGI::UpdateProbes, ProbeGI.cpp:
+ * 162-238) over a grid of gx x gy x gz probes, probe p = (z * gy + y) * gx + x at
+ * origin + (2 (x, y, z) / grid - 1) * size.  Per probe: one closest-hit ray in a uniformly
+ * distributed direction (LambertBRDF normalised, :351-372); a miss sees
+ * sky x 2.2 x clamp(dir.y, 0, 1), a hit max(albedo x sun_color x sun visibility x
+ * clamp(dot(N, -sun_dir), 0, 1), 0) + albedo x emissive (:140-144, :440-450) plus the previous
+ * volume's irradiance at the hit, SampleProbes(P + 0.001 N, N) x 0.999 x albedo (:190-237,
+ * :462-467: trilinear over the 8 surrounding probes of the previous volume, each weighted by
+ * clamp(dot(N, dir to probe), 0, 1)^2 and renormalised, L1 spherical harmonics evaluated at N).
+ * The radiance is encoded as L1 SH (SphericalHarmonics.glsl EncodeSH); where the probe position
+ * reprojects into the previous volume (at prev_origin), the SH, the raw radiance and this probe's
+ * depth moments are blended with the previous frame's by min(1 - 1/frames, 0.98) when temporal
+ * (:480-509), and the SH is packed (PackSH: 6 snorm16 pairs scaled by the largest coefficient;
+ * word 7 = accumulated frames).
+ *
+ * Buffers, probe-major: prev_sh / out_sh 8 uint32 per probe (the u_PrevFrameSH / o_SHOutput
+ * A.xyzw, B.xyzw texels), prev_raw / out_raw 4 floats per probe (radiance, 0: the o_CurrentRaw
+ * texel, kept in float32 where the reference stores r11g11b10), probe_map 64 x 2 floats per probe
+ * (the 8x8 octahedral depth / depth^2 map, MapData), updated in place at the pixel the ray's
+ * direction maps to.  prev_sh and out_sh, and prev_raw and out_raw, must not overlap.
+ * Differences from the shader, each deliberate: the map of probe (x, y, z) starts at p * 64 (the
+ * shader's Get1DIdx adds gx where it means x, :68, so the probes of a row race on one map); the
+ * sun visibility comes from an any-hit shadow ray (the shader reads cascaded shadow maps); the sky
+ * is a constant colour (u_Skymap); directions come from the counter-based hash of the GI pass
+ * (dimensions 0 and 1 of the probe index) with sin(acos c) = sqrt(1 - c^2) and the cube-root
+ * radius, which normalisation removes, left out; out-of-range texel reads return 0 (robust image
+ * access); packSnorm2x16 rounds half to even and packs NaN as 0 (GLSL leaves both open). */
+typedef struct rq_probe_params {
+    int32_t grid[3];       /* u_Resolution */
+    float origin[3];       /* u_BoxOrigin */
+    float prev_origin[3];  /* u_PreviousOrigin: where prev_sh / prev_raw were written */
+    float size[3];         /* u_Size (half extent) */
+    uint32_t seed;         /* per-frame seed of the direction samples */
+    int32_t temporal;      /* u_Temporal */
+    int32_t normal_mode;   /* as rq_gi_params */
+    int32_t shadow_rays;   /* 1 = any-hit shadow ray toward the sun, 0 = every hit lit */
+    float shadow_offset;   /* shadow ray origin = hit + N * shadow_offset */
+    float ray_tmax;        /* 1e6 in the shader */
+    float sun_dir[3];
+    float sun_color[3];    /* SUN_COLOR_PROBES */
+    float sky_color[3];    /* u_Skymap sample */
+} rq_probe_params;
+/* With RQ_FLAG_HOST_BUFFERS in opts, every buffer is host memory. */
+rq_status rq_probe_update(rq_ctx* ctx, const rq_scene* scene, const rq_probe_params* params,
+                          const uint32_t* prev_sh, const float* prev_raw, float* probe_map,
+                          uint32_t* out_sh, float* out_raw, const rq_opts* opts, void* stream);
+
 /* ---- Differentiation: depth + Lambert adjoint w.r.t. vertex positions ---------------------- */
 
 /* No counterpart in the reference (its GI is not differentiable).  Per primary ray i the forward

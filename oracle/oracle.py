@@ -75,6 +75,41 @@ def materials(albedo, textures=None, mesh_texture=None):
     return m, keep
 
 
+class OrcProbeParams(C.Structure):
+    """orc_probe_params (the layout of rq_probe_params)."""
+    _fields_ = [("grid", C.c_int32 * 3), ("origin", C.c_float * 3), ("prev_origin", C.c_float * 3),
+                ("size", C.c_float * 3), ("seed", C.c_uint32), ("temporal", C.c_int32), ("normal_mode", C.c_int32),
+                ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float), ("ray_tmax", C.c_float),
+                ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3), ("sky_color", C.c_float * 3)]
+
+
+def probe_params(p) -> OrcProbeParams:
+    """OrcProbeParams holding the bytes of a structure with rq_probe_params' layout."""
+    b = bytes(p)
+    assert len(b) == C.sizeof(OrcProbeParams)
+    return OrcProbeParams.from_buffer_copy(b)
+
+
+def probe_count(p) -> int:
+    return int(p.grid[0]) * int(p.grid[1]) * int(p.grid[2])
+
+
+def probe_raygen(p, nthreads=None):
+    """One ray per probe (UpdateRadianceProbes.glsl:410-427): RAY_DTYPE records, probe-major."""
+    q = probe_params(p)
+    out = np.empty(probe_count(q), dtype=RAY_DTYPE)
+    orc().orc_probe_raygen(C.byref(q), nthreads or os.cpu_count() or 1, _p(out))
+    return out
+
+
+def probe_direction(seed, ids):
+    """The probe ray direction of each probe index (normalised LambertBRDF of the hash samples)."""
+    ii = np.ascontiguousarray(ids, dtype=np.uint32)
+    out = np.empty((ii.shape[0], 3), dtype=np.float32)
+    orc().orc_probe_direction(seed & 0xFFFFFFFF, _p(ii), ii.shape[0], _p(out))
+    return out
+
+
 _orc = None
 
 
@@ -107,6 +142,10 @@ def orc() -> C.CDLL:
         L.orc_bounce_raygen.argtypes = [sp, P, P, P, P, I64, C.c_uint32, I32, C.c_float, C.c_float, I32,
                                         C.c_int, P]
         L.orc_collide.argtypes = [sp, P, I64, P, C.c_int, C.c_int]
+        pp = C.POINTER(OrcProbeParams)
+        L.orc_probe_raygen.argtypes = [pp, C.c_int, P]
+        L.orc_probe_direction.argtypes = [C.c_uint32, P, I64, P]
+        L.orc_probe_shade.argtypes = [sp, pp, P, P, P, C.POINTER(OrcMaterials), P, P, P, P, P, C.c_int]
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
         L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -226,6 +265,42 @@ class OracleScene:
                              _p(sc_), _p(sk), _p(am), nthreads or os.cpu_count() or 1, _p(out))
         return out
 
+    def probe_shade(self, p, rays, hits, lit, albedo, prev_sh, prev_raw, probe_map, textures=None,
+                    mesh_texture=None, nthreads=None):
+        """Shading, bounce, SH encoding, temporal blend and packing of the probe rays
+        (UpdateRadianceProbes.glsl:438-519).  Returns (out_sh (n, 8) uint32, out_raw (n, 4),
+        the updated probe map (n, 128))."""
+        q = probe_params(p)
+        n = probe_count(q)
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        assert rays.shape[0] == n and hits.shape[0] == n
+        mat, keep = materials(albedo, textures, mesh_texture)
+        lit = None if lit is None else np.ascontiguousarray(lit, dtype=np.uint8)
+        psh = np.ascontiguousarray(prev_sh, dtype=np.uint32).reshape(n, 8)
+        praw = np.ascontiguousarray(prev_raw, dtype=np.float32).reshape(n, 4)
+        pmap = np.array(probe_map, dtype=np.float32, copy=True).reshape(n, 128)
+        osh = np.empty((n, 8), dtype=np.uint32)
+        oraw = np.empty((n, 4), dtype=np.float32)
+        orc().orc_probe_shade(C.byref(self.s), C.byref(q), _p(rays), _p(hits), _p(lit), C.byref(mat), _p(psh),
+                              _p(praw), _p(pmap), _p(osh), _p(oraw), nthreads or os.cpu_count() or 1)
+        return osh, oraw, pmap
+
+    def probe_update(self, p, albedo, prev_sh, prev_raw, probe_map, flags=0, textures=None, mesh_texture=None):
+        """The whole probe-update frame as the engine composes it: probe rays, closest hits,
+        shadow rays toward the sun (any hit) when p.shadow_rays, then probe_shade.  Returns
+        (out_sh, out_raw, probe map, rays, hits)."""
+        rays = probe_raygen(p)
+        hits = self.closest(rays, flags=flags)
+        lit = None
+        if p.shadow_rays:
+            sr = self.shadow_raygen(rays, hits, np.array(p.sun_dir, dtype=np.float32), p.shadow_offset,
+                                    p.normal_mode)
+            lit = 1 - self.anyhit(sr)
+        osh, oraw, pmap = self.probe_shade(p, rays, hits, lit, albedo, prev_sh, prev_raw, probe_map,
+                                           textures, mesh_texture)
+        return osh, oraw, pmap, rays, hits
+
     def hit_normal(self, hits, normal_mode=0):
         hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
         out = np.empty((hits.shape[0], 3), dtype=np.float32)
@@ -278,6 +353,22 @@ def barycentrics(p, a, b, c):
 
 def pcg_hash(x: int) -> int:
     return orc().orc_pcg_hash(x & 0xFFFFFFFF)
+
+
+def pcg_hash_np(x):
+    """pcg_hash over a uint32 array (numpy arithmetic wraps like the C one)."""
+    x = np.asarray(x, dtype=np.uint32)
+    state = x * np.uint32(747796405) + np.uint32(2891336453)
+    word = ((state >> ((state >> np.uint32(28)) + np.uint32(4))) ^ state) * np.uint32(277803737)
+    return (word >> np.uint32(22)) ^ word
+
+
+def sample_u01(seed, ids, dim):
+    """The GI / probe samplers' uniform value in [0, 1) for (seed, ray or probe id, dimension)."""
+    with np.errstate(over="ignore"):
+        h = pcg_hash_np(pcg_hash_np(pcg_hash_np(np.uint32(seed & 0xFFFFFFFF)) + np.asarray(ids, dtype=np.uint32))
+                        + np.uint32(dim))
+    return (h >> np.uint32(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)
 
 
 def sincos_turns(x: float):
@@ -425,6 +516,56 @@ def ref_glsl_sun_colors():
     out = np.empty(6, dtype=np.float32)
     L.ref_glsl_sun_colors(_p(out))
     return out[:3].copy(), out[3:].copy()
+
+
+def ref_glsl_probe(p, rays, hits, albedo, normals, lit, prev_sh, prev_raw, probe_map):
+    """UpdateRadianceProbes.glsl main compiled as C++ for every probe of p's grid, fed the ray
+    directions, hits (TUVW), GetData's albedo (n, 4: rgb, emissive) and normal, and the sun
+    visibility.  Returns (out_sh (n, 8), out_raw (n, 4), the updated map (n, 128))."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_probe.restype = None
+    L.ref_glsl_probe.argtypes = [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 9
+    n = probe_count(p)
+    rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    x = np.zeros((n, 16), dtype=np.float32)
+    x[:, 0:3] = rays["d"]
+    x[:, 3], x[:, 4], x[:, 5], x[:, 6] = hits["t"], hits["u"], hits["v"], hits["w"]
+    x[:, 7:11] = albedo
+    x[:, 11:14] = normals
+    x[:, 14] = np.asarray(lit, dtype=np.float32)
+    arr = lambda v, t=np.float32: np.ascontiguousarray(np.array(v[:], dtype=t))  # noqa: E731
+    grid = arr(p.grid, np.int32)
+    org, prev, size = arr(p.origin), arr(p.prev_origin), arr(p.size)
+    sd, sc, sk = arr(p.sun_dir), arr(p.sun_color), arr(p.sky_color)
+    psh = np.ascontiguousarray(prev_sh, dtype=np.uint32).reshape(n, 8)
+    praw = np.ascontiguousarray(prev_raw, dtype=np.float32).reshape(n, 4)
+    pmap = np.array(probe_map, dtype=np.float32, copy=True).reshape(n, 128)
+    osh = np.zeros((n, 8), dtype=np.uint32)
+    oraw = np.zeros((n, 4), dtype=np.float32)
+    L.ref_glsl_probe(_p(grid), _p(org), _p(prev), _p(size), int(p.temporal), _p(sd), _p(sc), _p(sk), _p(x), _p(psh),
+                     _p(praw), _p(pmap), _p(osh), _p(oraw))
+    return osh, oraw, pmap
+
+
+def ref_glsl_lambert_direction(h):
+    """normalize(LambertBRDF(h)) (UpdateRadianceProbes.glsl:351-372) for (n, 3) hash values."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_lambert_direction.restype = None
+    L.ref_glsl_lambert_direction.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+    hh = np.ascontiguousarray(h, dtype=np.float32).reshape(-1, 3)
+    out = np.empty_like(hh)
+    L.ref_glsl_lambert_direction(_p(hh), hh.shape[0], _p(out))
+    return out
+
+
+def ref_glsl_probe_sun_color():
+    """SUN_COLOR_PROBES (ColorConstants.h) as the probe shader evaluates it."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_probe_sun_color.restype = None
+    out = np.empty(3, dtype=np.float32)
+    L.ref_glsl_probe_sun_color(_p(out))
+    return out
 
 
 def cos_hemisphere(normals, r):

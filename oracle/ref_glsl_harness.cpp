@@ -267,6 +267,69 @@ extern "C" void ref_glsl_shade(int specular, const float* in, int64_t n, const f
     }
 }
 
+// UpdateRadianceProbes.glsl main (:408-520 with the functions it calls, SphericalHarmonics.glsl
+// and Octahedral.glsl) for every probe of a gx x gy x gz grid, in probe order.  Per probe `in`
+// holds 16 floats: the ray direction ImportanceSample returns, the TUVW, Albedo (rgb, emissive) and
+// normal IntersectRay returns, and what GetDirectShadow returns.  prev_sh (8 words per probe:
+// the u_PrevFrameSH / u_PreviousSH A and B texels), prev_raw (4 floats, u_PrevRaw), map (128
+// floats, MapData, updated in place), out_sh and out_raw (o_SHOutputA/B, o_CurrentRaw).
+extern "C" void ref_glsl_probe(const int32_t* grid, const float* origin, const float* prev_origin, const float* size,
+                               int temporal, const float* sun_dir, const float* sun, const float* sky, const float* in,
+                               const uint32_t* prev_sh, const float* prev_raw, float* map, uint32_t* out_sh,
+                               float* out_raw) {
+    namespace G = glsl_probe;
+    G::u_Resolution = glsl::vec3(float(grid[0]), float(grid[1]), float(grid[2]));
+    G::u_BoxOrigin = glsl::vec3(origin[0], origin[1], origin[2]);
+    G::u_PreviousOrigin = glsl::vec3(prev_origin[0], prev_origin[1], prev_origin[2]);
+    G::u_Size = glsl::vec3(size[0], size[1], size[2]);
+    G::u_Temporal = temporal != 0;
+    G::u_SunDirection = glsl::vec3(sun_dir[0], sun_dir[1], sun_dir[2]);
+    G::g_sun = glsl::vec3(sun[0], sun[1], sun[2]);
+    G::g_sky = glsl::vec3(sky[0], sky[1], sky[2]);
+    G::u_Time = 0.0f;
+    G::u_PrevFrameSHA = G::u_PreviousSHA = G::SHImage{prev_sh, 0};
+    G::u_PrevFrameSHB = G::u_PreviousSHB = G::SHImage{prev_sh, 1};
+    G::o_SHOutputA = G::SHOut{out_sh, 0};
+    G::o_SHOutputB = G::SHOut{out_sh, 1};
+    G::u_PrevRaw = G::RawImage{prev_raw};
+    G::o_CurrentRaw = G::RawOut{out_raw};
+    G::MapData = reinterpret_cast<G::ProbeMapPixel*>(map);
+    static_assert(sizeof(G::ProbeMapPixel) == 8, "ProbeMapPixel layout");
+    int64_t i = 0;
+    for (int z = 0; z < grid[2]; ++z)
+        for (int y = 0; y < grid[1]; ++y)
+            for (int x = 0; x < grid[0]; ++x, ++i) {
+                const float* v = in + 16 * i;
+                G::gl_GlobalInvocationID = glsl::uvec3{uint32_t(x), uint32_t(y), uint32_t(z)};
+                G::g_dir = glsl::vec3(v[0], v[1], v[2]);
+                G::g_tuvw = glsl::vec4(v[3], v[4], v[5], v[6]);
+                G::g_alb = glsl::vec4(v[7], v[8], v[9], v[10]);
+                G::g_nrm = glsl::vec3(v[11], v[12], v[13]);
+                G::g_shadow = v[14];
+                G::probe_main();
+            }
+}
+
+// The unit vector LambertBRDF (UpdateRadianceProbes.glsl:351-362) gives for hash values (h.x, h.y,
+// h.z), normalised as ImportanceSample does (:370-372).
+extern "C" void ref_glsl_lambert_direction(const float* h, int64_t n, float* out) {
+    for (int64_t i = 0; i < n; ++i) {
+        const glsl::vec3 d =
+            glsl::normalize(glsl_probe::LambertBRDF(glsl::vec3(h[3 * i], h[3 * i + 1], h[3 * i + 2])));
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
+
+// SUN_COLOR_PROBES as the shader evaluates it.
+extern "C" void ref_glsl_probe_sun_color(float* out3) {
+    const glsl::vec3 c = glsl_probe::sun_color_constant();
+    out3[0] = c.x;
+    out3[1] = c.y;
+    out3[2] = c.z;
+}
+
 // SUN_COLOR_DIFF and SUN_COLOR_SPEC of ColorConstants.h as the shaders evaluate them.
 extern "C" void ref_glsl_sun_colors(float* out6) {
     const glsl::vec3 a = glsl_diffuse_shade::sun_color_constant(), b = glsl_specular_shade::sun_color_constant();

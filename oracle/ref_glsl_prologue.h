@@ -11,10 +11,12 @@
 //  * mat4 * vec4 sums the columns left to right, ((c0 x + c1 y) + c2 z) + c3 w: the specification
 //    leaves the order to the implementation, and this is the order the engine and the CPU
 //    restatement define;
-//  * floatBitsToInt / intBitsToFloat reinterpret bits.
+//  * floatBitsToInt / intBitsToFloat / floatBitsToUint / uintBitsToFloat reinterpret bits;
+//  * packSnorm2x16 rounds half to even and packs NaN as 0, pow(x, 2.0) is x * x (both left open).
 // `.xyz` / `.xy` are rewritten to `.xyz()` / `.xy()` by the recipe; `in` becomes empty and
 // `out T` / `inout T` become `T&`.
 #pragma once
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -23,6 +25,8 @@ namespace glsl {
 
 struct vec4;
 struct vec2;
+struct ivec3;
+typedef uint32_t uint;
 
 struct vec3 {
     float x, y, z;
@@ -31,7 +35,9 @@ struct vec3 {
     vec3(float a, float b, float c) : x(a), y(b), z(c) {}
     vec3(const vec2& v, float c);
     explicit vec3(const vec4& v);
+    explicit vec3(const ivec3& v);
     vec3 xyz() const { return *this; }
+    vec2 xz() const;
 };
 
 struct vec4 {
@@ -48,10 +54,35 @@ inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
 
 struct vec2 {
     float x, y;
+    vec2() = default;
+    vec2(float s) : x(s), y(s) {}
+    vec2(float a, float b) : x(a), y(b) {}
     vec2 xy() const { return *this; }
 };
 
 inline vec3::vec3(const vec2& v, float c) : x(v.x), y(v.y), z(c) {}
+inline vec2 vec3::xz() const { return {x, z}; }
+
+// int(float) truncates toward zero (GLSL 4.50 5.4.1).
+struct uvec3 {
+    uint32_t x, y, z;
+    uvec3 xyz() const { return *this; }
+};
+struct ivec3 {
+    int x, y, z;
+    ivec3() = default;
+    ivec3(int a, int b, int c) : x(a), y(b), z(c) {}
+    explicit ivec3(const vec3& v) : x(int(v.x)), y(int(v.y)), z(int(v.z)) {}
+    explicit ivec3(const uvec3& v) : x(int(v.x)), y(int(v.y)), z(int(v.z)) {}
+};
+inline vec3::vec3(const ivec3& v) : x(float(v.x)), y(float(v.y)), z(float(v.z)) {}
+struct ivec2 {
+    int x, y;
+    ivec2() = default;
+    ivec2(int s) : x(s), y(s) {}
+    ivec2(int a, int b) : x(a), y(b) {}
+    explicit ivec2(const vec2& v) : x(int(v.x)), y(int(v.y)) {}
+};
 
 struct uvec2 {
     uint32_t x, y;
@@ -80,6 +111,12 @@ inline vec3 operator/(vec3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
 inline vec3 operator-(vec3 a) { return {-a.x, -a.y, -a.z}; }
 inline vec3& operator-=(vec3& a, vec3 b) { return a = a - b; }
 inline vec3& operator+=(vec3& a, vec3 b) { return a = a + b; }
+inline vec3& operator*=(vec3& a, vec3 b) { return a = a * b; }
+inline vec3& operator/=(vec3& a, float s) { return a = a / s; }
+inline vec3 operator+(vec3 a, float s) { return {a.x + s, a.y + s, a.z + s}; }
+inline bool operator==(vec3 a, vec3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+inline vec2 operator*(float s, vec2 a) { return {s * a.x, s * a.y}; }
+inline vec2 operator+(vec2 a, float s) { return {a.x + s, a.y + s}; }
 
 inline vec4 operator*(const mat4& m, vec4 v) {
     vec4 r;
@@ -105,10 +142,21 @@ inline float cos(float x) { return std::cos(x); }
 inline float sin(float x) { return std::sin(x); }
 inline vec3 normalize(vec3 v) { return v / sqrt(dot(v, v)); }
 inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }
+inline vec3 max(vec3 a, float s) { return {max(a.x, s), max(a.y, s), max(a.z, s)}; }
+inline vec3 abs(vec3 v) { return {abs(v.x), abs(v.y), abs(v.z)}; }
+inline vec3 floor(vec3 v) { return {std::floor(v.x), std::floor(v.y), std::floor(v.z)}; }
+inline vec3 ceil(vec3 v) { return {std::ceil(v.x), std::ceil(v.y), std::ceil(v.z)}; }
+inline float length(vec3 v) { return std::sqrt(dot(v, v)); }
+inline float acos(float x) { return std::acos(x); }
 inline float clamp(float x, float lo, float hi) { return min(max(x, lo), hi); }
+inline vec2 clamp(vec2 v, float lo, float hi) { return {clamp(v.x, lo, hi), clamp(v.y, lo, hi)}; }
 inline vec3 clamp(vec3 v, float lo, float hi) { return {clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi)}; }
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
-inline float pow(float x, float y) { return std::pow(x, y); }
+inline vec2 mix(vec2 x, vec2 y, float a) { return {mix(x.x, y.x, a), mix(x.y, y.y, a)}; }
+inline vec3 mix(vec3 x, vec3 y, float a) { return {mix(x.x, y.x, a), mix(x.y, y.y, a), mix(x.z, y.z, a)}; }
+// pow: the C library's, except pow(x, 2.0) = x * x (the correctly rounded square; GLSL leaves
+// pow's precision to the implementation).
+inline float pow(float x, float y) { return y == 2.0f ? x * x : std::pow(x, y); }
 inline vec3 pow(vec3 x, vec3 y) { return {pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z)}; }
 inline bool isnan(float x) { return std::isnan(x); }
 inline bool isinf(float x) { return std::isinf(x); }
@@ -127,6 +175,26 @@ inline float half_to_float(uint32_t h) {
     return s ? -f : f;
 }
 inline vec2 unpackHalf2x16(uint32_t v) { return {half_to_float(v & 0xFFFFu), half_to_float(v >> 16)}; }
+// packSnorm2x16 / unpackSnorm2x16 (GLSL 4.50 8.4): round(clamp(c, -1, 1) * 32767) with rounding
+// half to even and NaN packed as 0 (both left open by the specification); clamp(f / 32767, -1, 1).
+inline uint32_t snorm16(float c) {
+    const float s = clamp(c, -1.0f, 1.0f) * 32767.0f;
+    if (s != s) return 0u;
+    return uint32_t(uint16_t(int16_t(std::nearbyint(s))));
+}
+inline uint32_t packSnorm2x16(vec2 v) { return snorm16(v.x) | (snorm16(v.y) << 16); }
+inline float unsnorm16(uint32_t h) { return clamp(float(int16_t(uint16_t(h & 0xFFFFu))) / 32767.0f, -1.0f, 1.0f); }
+inline vec2 unpackSnorm2x16(uint32_t p) { return {unsnorm16(p), unsnorm16(p >> 16)}; }
+inline uint32_t floatBitsToUint(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+inline float uintBitsToFloat(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
 inline int floatBitsToInt(float f) {
     int i;
     std::memcpy(&i, &f, 4);

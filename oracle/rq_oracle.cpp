@@ -1149,3 +1149,315 @@ void orc_collide(const orc_scene* sc, const float* boxes, int64_t n, int32_t* ou
 }
 
 }  // extern "C"
+
+// ---- Radiance probe volume: UpdateRadianceProbes.glsl, one frame ----------------------------
+
+namespace {
+
+// SphericalHarmonics.glsl: struct SH {L00, L11, L10, L1_1} and its first-order basis constants.
+struct SH4 {
+    V3 l00, l11, l10, l1_1;
+};
+constexpr float kY00 = 0.28209479177387814347f;
+constexpr float kY11 = -0.48860251190291992159f;
+constexpr float kY10 = 0.48860251190291992159f;
+constexpr float kY1_1 = -0.48860251190291992159f;
+
+inline V3 vdiv(V3 a, V3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+inline V3 vadds(V3 a, float s) { return {a.x + s, a.y + s, a.z + s}; }
+inline V3 vmaxs(V3 a, float s) { return {gmax(a.x, s), gmax(a.y, s), gmax(a.z, s)}; }
+inline V3 vmix(V3 x, V3 y, float a) { return {mixf(x.x, y.x, a), mixf(x.y, y.y, a), mixf(x.z, y.z, a)}; }
+inline float bits_f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+inline uint32_t f_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+struct ProbeGrid {
+    int gx, gy, gz;
+    V3 res, size, origin, prev;
+    int64_t count() const { return int64_t(gx) * gy * gz; }
+    bool inside(int x, int y, int z) const { return x >= 0 && x < gx && y >= 0 && y < gy && z >= 0 && z < gz; }
+    int64_t index(int x, int y, int z) const { return (int64_t(z) * gy + y) * gx + x; }
+};
+ProbeGrid probe_grid(const orc_probe_params& p) {
+    ProbeGrid g;
+    g.gx = p.grid[0];
+    g.gy = p.grid[1];
+    g.gz = p.grid[2];
+    g.res = {float(g.gx), float(g.gy), float(g.gz)};
+    g.size = ld3(p.size);
+    g.origin = ld3(p.origin);
+    g.prev = ld3(p.prev_origin);
+    return g;
+}
+
+// Probe (texel) position about `base`: TexCoords = vec3(Pixel) / u_Resolution,
+// Clip = TexCoords * 2 - 1, base + Clip * u_Size (:412-417; GetVisibility :178-180).
+V3 probe_position(const ProbeGrid& g, V3 base, int x, int y, int z) {
+    const V3 tc = vdiv(V3{float(x), float(y), float(z)}, g.res);
+    const V3 clip = vadds(muls(tc, 2.0f), -1.0f);
+    return add(base, mul(clip, g.size));
+}
+
+// LambertBRDF(vec3(hash2(), hash2().x)) normalised (:351-372): phi = 2 pi h.x, cos(theta) =
+// 2 h.y - 1; sin(theta) as sqrt(1 - cos^2) and the radius u^(1/3) (which the normalisation
+// removes) left out; h from dimensions 0 and 1 of the counter-based hash for the probe index.
+V3 probe_direction(uint32_t seed, uint32_t id) {
+    const float hx = u01(sample_key(seed, id, 0u)), hy = u01(sample_key(seed, id, 1u));
+    float sp, cp;
+    sincos_turns(hx, sp, cp);
+    const float c = 2.0f * hy - 1.0f;
+    const float st = std::sqrt(1.0f - c * c);
+    return normalize(V3{st * cp, st * sp, c});
+}
+
+// The 8x8 map pixel of a direction: UnitVectorToOctahedron (Octahedral.glsl) scaled by 7 and
+// truncated, Get1DIdx(ivec2, ivec2(8)) = x * 8 + y (:470-472).
+int oct_pixel(V3 d) {
+    const float s = dot(V3{std::fabs(d.x), std::fabs(d.y), std::fabs(d.z)}, V3{1.0f, 1.0f, 1.0f});
+    float x = d.x / s, z = d.z / s;
+    if (d.y < 0.0f) {
+        const float ox = x, oz = z;
+        x = (ox >= 0.0f ? 1.0f : -1.0f) * (1.0f - std::fabs(oz));
+        z = (oz >= 0.0f ? 1.0f : -1.0f) * (1.0f - std::fabs(ox));
+    }
+    const float u = clamp01(0.5f * x + 0.5f), v = clamp01(0.5f * z + 0.5f);
+    return int(u * 7.0f) * 8 + int(v * 7.0f);
+}
+
+// EncodeSH (SphericalHarmonics.glsl): each coefficient is 0 + Y * radiance * A.
+SH4 encode_sh(V3 rad, V3 dir) {
+    const float pi = 3.14159265359f, m = 2.0f;
+    const float a0 = m * pi, a1 = ((2.0f * pi) / 3.0f) * m;
+    const V3 z = {0.0f, 0.0f, 0.0f};
+    SH4 r;
+    r.l00 = add(z, muls(muls(rad, kY00), a0));
+    r.l1_1 = add(z, muls(muls(rad, kY1_1 * dir.y), a1));
+    r.l10 = add(z, muls(muls(rad, kY10 * dir.z), a1));
+    r.l11 = add(z, muls(muls(rad, kY11 * dir.x), a1));
+    return r;
+}
+
+// SampleSH(sh, direction): the four clamped lobes summed in the shader's order.
+V3 sample_sh(const SH4& sh, V3 d) {
+    V3 r = {0.0f, 0.0f, 0.0f};
+    r = add(r, vmaxs(muls(sh.l00, kY00), 0.0f));
+    r = add(r, vmaxs(muls(muls(sh.l1_1, kY1_1), d.y), 0.0f));
+    r = add(r, vmaxs(muls(muls(sh.l10, kY10), d.z), 0.0f));
+    r = add(r, vmaxs(muls(muls(sh.l11, kY11), d.x), 0.0f));
+    return r;
+}
+
+// packSnorm2x16 of one component: round(clamp(c, -1, 1) * 32767), half to even, NaN as 0.
+uint32_t snorm16(float c) {
+    const float s = gmin(gmax(c, -1.0f), 1.0f) * 32767.0f;
+    if (s != s) return 0u;
+    return uint32_t(uint16_t(int16_t(std::nearbyint(s))));
+}
+uint32_t pack_snorm2(float a, float b) { return snorm16(a) | (snorm16(b) << 16); }
+float unsnorm16(uint32_t h) { return gmin(gmax(float(int16_t(uint16_t(h & 0xFFFFu))) / 32767.0f, -1.0f), 1.0f); }
+
+inline float max3abs(V3 x) { return gmax(gmax(std::fabs(x.x), std::fabs(x.y)), std::fabs(x.z)); }
+
+// PackSH: coefficients divided by the largest magnitude (starting from -1000), six snorm pairs,
+// the scale's bits, 0.
+void pack_sh(SH4 sh, uint32_t* w) {
+    float m = -1000.0f;
+    m = gmax(m, max3abs(sh.l00));
+    m = gmax(m, max3abs(sh.l11));
+    m = gmax(m, max3abs(sh.l10));
+    m = gmax(m, max3abs(sh.l1_1));
+    const V3 a = {sh.l00.x / m, sh.l00.y / m, sh.l00.z / m}, b = {sh.l11.x / m, sh.l11.y / m, sh.l11.z / m};
+    const V3 c = {sh.l10.x / m, sh.l10.y / m, sh.l10.z / m}, d = {sh.l1_1.x / m, sh.l1_1.y / m, sh.l1_1.z / m};
+    w[0] = pack_snorm2(a.x, a.y);
+    w[1] = pack_snorm2(a.z, b.x);
+    w[2] = pack_snorm2(b.y, b.z);
+    w[3] = pack_snorm2(c.x, c.y);
+    w[4] = pack_snorm2(c.z, d.x);
+    w[5] = pack_snorm2(d.y, d.z);
+    w[6] = f_bits(m);
+    w[7] = 0u;
+}
+
+// UnpackSH: the snorm pairs times the scale stored in B.z.
+SH4 unpack_sh(const uint32_t* w) {
+    const float k = bits_f(w[6]);
+    float u[12];
+    for (int i = 0; i < 6; ++i) {
+        u[2 * i] = unsnorm16(w[i]) * k;
+        u[2 * i + 1] = unsnorm16(w[i] >> 16) * k;
+    }
+    return SH4{{u[0], u[1], u[2]}, {u[3], u[4], u[5]}, {u[6], u[7], u[8]}, {u[9], u[10], u[11]}};
+}
+
+// The previous volume's texel (x, y, z): 8 words, zeros outside the volume.
+void load_texel(const ProbeGrid& g, const uint32_t* vol, int x, int y, int z, uint32_t* w) {
+    if (!g.inside(x, y, z)) {
+        for (int k = 0; k < 8; ++k) w[k] = 0u;
+        return;
+    }
+    std::memcpy(w, vol + 8 * g.index(x, y, z), 32);
+}
+
+// GetVisibility (:176-188): clamp(dot(N, direction to the probe), 0, 1)^2, pow(x, 2) taken as x * x.
+float probe_visibility(const ProbeGrid& g, int x, int y, int z, V3 wp, V3 n) {
+    const V3 pp = probe_position(g, g.prev, x, y, z);
+    V3 v = sub(pp, wp);
+    const float len = std::sqrt(dot(v, v));
+    v = {v.x / len, v.y / len, v.z / len};
+    const float w = clamp01(dot(n, v));
+    return w * w;
+}
+
+// SampleProbes (:190-237) over the previous volume.
+V3 sample_probes(const ProbeGrid& g, const uint32_t* vol, V3 wp, V3 n) {
+    wp = add(wp, muls(n, 0.45f));
+    V3 sp = vdiv(sub(wp, g.prev), g.size);
+    sp = vadds(muls(sp, 0.5f), 0.5f);
+    if (!(sp.x == clamp01(sp.x) && sp.y == clamp01(sp.y) && sp.z == clamp01(sp.z))) return {0.0f, 0.0f, 0.0f};
+    const V3 vc = mul(sp, g.res);
+    const V3 mn = {std::floor(vc.x), std::floor(vc.y), std::floor(vc.z)};
+    const V3 mx = {std::ceil(vc.x), std::ceil(vc.y), std::ceil(vc.z)};
+    const V3 ext = sub(mx, mn);
+    const float inv = 1.0f / (ext.x * ext.y * ext.z);
+    const float ax = mx.x - vc.x, ay = mx.y - vc.y, az = mx.z - vc.z;  // Max - p
+    const float bx = vc.x - mn.x, by = vc.y - mn.y, bz = vc.z - mn.z;  // p - Min
+    float w[8] = {ax * ay * az * inv, ax * by * az * inv, bx * by * az * inv, bx * ay * az * inv,
+                  ax * ay * bz * inv, ax * by * bz * inv, bx * by * bz * inv, bx * ay * bz * inv};
+    const int x0 = int(mn.x), y0 = int(mn.y), z0 = int(mn.z), x1 = int(mx.x), y1 = int(mx.y), z1 = int(mx.z);
+    const int tx[8] = {x0, x0, x1, x1, x0, x0, x1, x1}, ty[8] = {y0, y1, y1, y0, y0, y1, y1, y0};
+    const int tz[8] = {z0, z0, z0, z0, z1, z1, z1, z1};
+    SH4 sh[8];
+    float alpha = 0.0f;
+    for (int i = 0; i < 8; ++i) {
+        uint32_t t[8];
+        load_texel(g, vol, tx[i], ty[i], tz[i], t);
+        sh[i] = unpack_sh(t);
+        const float vis = probe_visibility(g, tx[i], ty[i], tz[i], wp, n);
+        alpha = alpha + w[i] * (1.0f - vis);
+        w[i] = w[i] * vis;
+    }
+    const float ws = 1.0f - alpha;
+    SH4 f = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+    for (int i = 0; i < 8; ++i) {
+        const float k = w[i] / gmax(ws, 0.000001f);
+        f.l00 = add(f.l00, muls(sh[i].l00, k));
+        f.l1_1 = add(f.l1_1, muls(sh[i].l1_1, k));
+        f.l10 = add(f.l10, muls(sh[i].l10, k));
+        f.l11 = add(f.l11, muls(sh[i].l11, k));
+    }
+    return vmaxs(sample_sh(f, n), 0.0f);
+}
+
+// Reproject (:298-313): the previous volume's texel under the world position, or false.
+bool reproject(const ProbeGrid& g, V3 wp, int& x, int& y, int& z) {
+    V3 sp = vdiv(sub(wp, g.prev), g.size);
+    sp = vadds(muls(sp, 0.5f), 0.5f);
+    if (!(sp.x > 0.0f && sp.x < 1.0f && sp.y > 0.0f && sp.y < 1.0f && sp.z > 0.0f && sp.z < 1.0f)) return false;
+    sp = vadds(mul(sp, g.res), 0.5f);
+    x = int(sp.x);
+    y = int(sp.y);
+    z = int(sp.z);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_probe_raygen(const orc_probe_params* p, int nthreads, orc_ray* out) {
+    const ProbeGrid g = probe_grid(*p);
+    parallel_for(g.count(), nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const int x = int(i % g.gx), y = int((i / g.gx) % g.gy), z = int(i / (int64_t(g.gx) * g.gy));
+            const V3 o = probe_position(g, g.origin, x, y, z);
+            const V3 d = probe_direction(p->seed, uint32_t(i));
+            out[i] = orc_ray{{o.x, o.y, o.z}, 0.0f, {d.x, d.y, d.z}, p->ray_tmax};
+        }
+    });
+}
+
+void orc_probe_direction(uint32_t seed, const uint32_t* ids, int64_t n, float* out3) {
+    for (int64_t i = 0; i < n; ++i) {
+        const V3 d = probe_direction(seed, ids[i]);
+        out3[3 * i] = d.x;
+        out3[3 * i + 1] = d.y;
+        out3[3 * i + 2] = d.z;
+    }
+}
+
+// UpdateRadianceProbes.glsl main (:408-520) after the trace: shading, the bounce from the previous
+// volume, SH encoding, temporal blend and packing; probe_map updated in place.
+void orc_probe_shade(const orc_scene* sc, const orc_probe_params* p, const orc_ray* rays, const orc_hit* hits,
+                     const uint8_t* lit, const orc_materials* mat, const uint32_t* prev_sh, const float* prev_raw,
+                     float* probe_map, uint32_t* out_sh, float* out_raw, int nthreads) {
+    const Scene s = make_scene(sc);
+    const ProbeGrid g = probe_grid(*p);
+    const V3 sun = ld3(p->sun_color), sky = ld3(p->sky_color), sdir = ld3(p->sun_dir);
+    parallel_for(g.count(), nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const V3 o = ld3(rays[i].o), d = ld3(rays[i].d);
+            const orc_hit& h = hits[i];
+            const float t = h.t;
+            V3 N = {-1.0f, -1.0f, -1.0f}, alb = {0.0f, 0.0f, 0.0f};
+            float em = 0.0f;
+            if (t > 0.0f) {
+                N = hit_normal(s, h, p->normal_mode);
+                alb = hit_albedo(s, *mat, h);
+                std::memcpy(&em, &s.ents[h.entity].data[0], 4);
+            }
+            if (dot(N, d) > 0.0001f) N = neg(N);
+            const V3 wp = add(o, muls(d, t));
+            const float lsky = clamp01(dot(d, V3{0.0f, 1.0f, 0.0f}));
+            V3 fr;
+            if (t < 0.0f) {
+                fr = muls(muls(sky, 2.2f), lsky);
+            } else {
+                const float shadow = lit ? (lit[i] ? 1.0f : 0.0f) : 1.0f;
+                const float ndl = clamp01(dot(N, neg(sdir)));
+                fr = add(vmaxs(muls(muls(mul(alb, sun), shadow), ndl), 0.0f), muls(muls(alb, em), 1.0f));
+            }
+            if (t > 0.0f) fr = add(fr, mul(muls(sample_probes(g, prev_sh, add(wp, muls(N, 0.001f)), N), 0.999f), alb));
+            float* px = probe_map + 128 * i + 2 * oct_pixel(d);
+            const float depth = t < 0.0f ? 256.0f : t, depth2 = depth * depth;
+            SH4 sh = encode_sh(fr, d);
+            int32_t frames = 0;
+            int rx, ry, rz;
+            if (reproject(g, o, rx, ry, rz)) {
+                uint32_t w[8];
+                load_texel(g, prev_sh, rx, ry, rz, w);
+                frames = int32_t(w[7] + 1u);
+                const float ta = p->temporal ? gmin(1.0f - 1.0f / float(frames), 0.98f) : 0.0f;
+                const float m0 = px[0], m1 = px[1];
+                px[0] = mixf(depth, m0, ta);
+                px[1] = mixf(depth2, m1, ta);
+                const SH4 ps = unpack_sh(w);
+                sh.l00 = vmix(sh.l00, ps.l00, ta);
+                sh.l11 = vmix(sh.l11, ps.l11, ta);
+                sh.l10 = vmix(sh.l10, ps.l10, ta);
+                sh.l1_1 = vmix(sh.l1_1, ps.l1_1, ta);
+                const V3 pr = g.inside(rx, ry, rz) ? ld3(prev_raw + 4 * g.index(rx, ry, rz)) : V3{0.0f, 0.0f, 0.0f};
+                fr = vmix(fr, pr, ta);
+            } else {
+                px[0] = depth;
+                px[1] = depth2;
+            }
+            uint32_t* w = out_sh + 8 * i;
+            pack_sh(sh, w);
+            w[7] = uint32_t(frames);
+            float* r = out_raw + 4 * i;
+            r[0] = fr.x;
+            r[1] = fr.y;
+            r[2] = fr.z;
+            r[3] = 0.0f;
+        }
+    });
+}
+
+}  // extern "C"

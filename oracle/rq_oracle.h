@@ -123,6 +123,32 @@ void orc_bounce_raygen(const orc_scene* s, const orc_ray* rays, const orc_hit* h
 // reference's repeated separating axis and, for the stack layout, the within-leaf triangle index.
 void orc_collide(const orc_scene* s, const float* boxes, int64_t n, int32_t* out, int flags, int nthreads);
 
+// One frame of the radiance-probe update (UpdateRadianceProbes.glsl); the parameters have the
+// layout of rq_probe_params.  orc_probe_raygen writes one ray per probe (probe-major, x fastest);
+// after the caller traces them (closest hit) and the shadow rays (orc_shadow_raygen, any hit),
+// orc_probe_shade shades, encodes, blends and packs: prev_sh / out_sh 8 words per probe, prev_raw
+// / out_raw 4 floats, probe_map 128 floats (updated in place); lit (nullable) 1 = lit.
+typedef struct {
+    int32_t grid[3];
+    float origin[3];
+    float prev_origin[3];
+    float size[3];
+    uint32_t seed;
+    int32_t temporal;
+    int32_t normal_mode;
+    int32_t shadow_rays;
+    float shadow_offset;
+    float ray_tmax;
+    float sun_dir[3];
+    float sun_color[3];
+    float sky_color[3];
+} orc_probe_params;
+void orc_probe_raygen(const orc_probe_params* p, int nthreads, orc_ray* out);
+void orc_probe_direction(uint32_t seed, const uint32_t* ids, int64_t n, float* out3);
+void orc_probe_shade(const orc_scene* s, const orc_probe_params* p, const orc_ray* rays, const orc_hit* hits,
+                     const uint8_t* lit, const orc_materials* mat, const uint32_t* prev_sh, const float* prev_raw,
+                     float* probe_map, uint32_t* out_sh, float* out_raw, int nthreads);
+
 uint32_t orc_pcg_hash(uint32_t x);
 void orc_sincos_turns(float x, float* s, float* c);
 // CosWeightedHemisphere (Sampling.glsl:1-12) with the turn-based sine / cosine, n normals.

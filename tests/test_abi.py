@@ -47,6 +47,9 @@ def test_struct_sizes_match_reference_layouts():
     assert L.ENTITY_DTYPE.itemsize == 192        # BVHEntity
     assert C.sizeof(L.RqOpts) == 32
     assert C.sizeof(L.RqGiParams) == 80
+    assert C.sizeof(L.RqProbeParams) == 108     # rq_probe_params, the oracle's orc_probe_params
+    from oracle import oracle as O
+    assert C.sizeof(O.OrcProbeParams) == C.sizeof(L.RqProbeParams)
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU failure path")
