@@ -51,7 +51,8 @@ def parse():
                     help="wall-clock bound of the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
                     help="run one GI pass and exit (the case the ncu captures use: the 2nd "
-                         "traversal launch is the full-size secondary closest-hit launch)")
+                         "traversal launch is the full-size secondary closest-hit launch; with "
+                         "--config c6, two passes over the instanced scene)")
     return ap.parse_args()
 
 
@@ -531,6 +532,24 @@ def run_c6(args):
         torch.cuda.synchronize()
         return statistics.mean(a.elapsed_time(b) for a, b in evs)
 
+    # launch variants tuned on the GI rays of this scene (as for C2): the GI pass's secondary launch
+    # takes the tuned variant, its primary launch the one-thread-per-ray form of the same shape
+    if args.profile:
+        # two BVH8q GI passes with the top level and the launch variant the autotuner picks here on
+        # GB300 (persistent ray queue, 128 threads, 8 blocks per SM): the ncu captures of the
+        # instancing row; the second k_bvh8_persistent launch is the second pass's GI rays
+        launch = dict(block_size=128, min_blocks=8, persistent=1)
+        st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr, **launch)[1]
+        rays_per_step = int(st["primary_rays"]) + int(st["secondary_rays"])
+        sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stream=sptr, **launch)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "c6", "rays": rays_per_step, "device_status": ctx.device_status()}))
+        return
+    h0 = sc.closest(d, layout=L.LAYOUT_BVH8Q, stream=sptr)
+    d_gi = sc.gi_raygen(d, h0, p, stream=sptr)
+    tuning = {name: sc.autotune(d_gi, query=0, layout=lay) for name, lay in (("bvh8q", L.LAYOUT_BVH8Q),
+                                                                             ("strict_bvh2", R.STACK))}
+    del h0, d_gi
     st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr)[1]
     rays_per_step = int(st["primary_rays"]) + int(st["secondary_rays"])
     res = {}
@@ -545,6 +564,14 @@ def run_c6(args):
                      "entity_loop_mrays_s": round(rays_per_step / (ms_l / 1e3) / 1e6, 2),
                      "entity_loop_ms": round(ms_l, 3), "speedup": round(ms_l / ms_t, 1),
                      "pixels_identical": bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))}
+    # the primary (camera) launch alone: one thread per ray against the persistent ray queue
+    h_p = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    primary = {}
+    for name, kw in (("one_thread_per_ray_ms", dict(block_size=128, min_blocks=8, persistent=0)),
+                     ("persistent_ms", dict(block_size=128, min_blocks=8, persistent=1))):
+        primary[name] = round(timed(lambda: sc.closest(d, h_p, layout=L.LAYOUT_BVH8Q, stream=sptr, **kw),
+                                    args.steps, args.warmup), 4)
+    del h_p
     # CPU restatement (walks every entity) on a bounded sample of the primary rays
     from oracle import oracle as O
     v, t, nn, e = ri.global_buffers()
@@ -563,7 +590,9 @@ def run_c6(args):
                        "rays_per_step": rays_per_step, "scene_build_s": round(build_s, 2),
                        "top_level": tl, "bvh8_nodes": b8["nodes"],
                        "l2": "flushed between timed steps (512 MB write)"},
-            "gi_pass": res,
+            "gi_pass": res, "primary_launch_bvh8q": primary,
+            "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
+                             "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
             "cpu_baseline": {"value": round(len(sample) / cpu_s / 1e6, 4), "unit": UNIT,
                              "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"{len(sample)} primary rays, entity loop, {cpu_s:.2f} s"},

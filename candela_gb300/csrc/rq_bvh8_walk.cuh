@@ -149,6 +149,108 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
         nodes_total += visits;
         sink.template put<kAny>(id, r0, r1, closest, tri, mesh, ent_hit, visits, occluded);
     };
+    if constexpr (kTlas) {
+        // Scenes with a top level: a lane looking for its ray's next entity (`seek`) advances the
+        // top-level cursor by at most kSeekNodes nodes per iteration, interleaved with the node
+        // steps of the lanes that are walking an entity, so that a long top-level walk does not
+        // hold the warp.  The entities, their order and every count are those of the loop below.
+        constexpr int kSeekNodes = 4;
+        bool seek = false;
+        // One bounded seek: 1 = the walk of entity `ent` is set up, 0 = keep seeking, -1 = none left.
+        auto seek_step = [&](const float4 r0, const float4 r1) -> int {
+            const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+            const int32_t e = tlas::next_n<true>(s, ents, ent, make_float3(r0.x, r0.y, r0.z),
+                                                 make_float3(r1.x, r1.y, r1.z), kAny ? r1.w : tmax,
+                                                 skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits,
+                                                 kSeekNodes);
+            if (e == tlas::kMore) return 0;
+            if (e < 0) return -1;
+            ent = e;
+            const rq_entity& E = s.ents[ent];
+            if (skip_transparent && strict::ent_alpha(E) < 0.99f) return 0;
+            const int32_t root = s.b8_roots[ent];
+            if (root < 0) return 0;
+            r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
+                               strict::xform(E.inverse, strict::xyz(r1), 0.0f));
+            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : tri, -1};
+            w = bvh8::walk_begin(root);
+            return 1;
+        };
+        while (true) {
+            // refill idle lanes (warp-uniform loop; inactive rays are answered here)
+            while (true) {
+                const unsigned want = __ballot_sync(kFull, !live && !exhausted);
+                if (!want) break;
+                const unsigned cnt = __popc(want);
+                const unsigned rank = __popc(want & persist::lanemask_lt());
+                const unsigned long long avail = pool_end - pool_next;
+                unsigned long long mine = pool_next + rank;
+                if (avail >= cnt) {
+                    pool_next += cnt;
+                } else {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
+                    base = __shfl_sync(kFull, base, 0);
+                    if (rank >= avail) mine = base + (rank - avail);
+                    pool_next = base + (cnt - avail);
+                    pool_end = base + kPoolRays;
+                }
+                if (!live && !exhausted) {
+                    if (static_cast<int64_t>(mine) >= n) {
+                        exhausted = true;
+                    } else {
+                        id = static_cast<int64_t>(mine);
+                        float4 r0, r1;
+                        load_ray(rays, id, r0, r1);
+                        tmin = r0.w;
+                        tmax = r1.w;
+                        closest = -1.0f;
+                        mesh = tri = ent_hit = -1;
+                        visits = 0;
+                        ent = -1;
+                        ents = tlas::begin<true>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
+                        live = r1.w > r0.w;
+                        seek = live;
+                        if (!live) store(r0, r1, false);
+                    }
+                }
+            }
+            if (!__any_sync(kFull, live)) break;
+            if (!live) continue;
+            if (seek) {
+                float4 r0, r1;
+                load_ray(rays, id, r0, r1);
+                const int g = seek_step(r0, r1);
+                if (g > 0) {
+                    seek = false;
+                } else if (g < 0) {
+                    store(r0, r1, false);
+                    live = false;
+                }
+                continue;
+            }
+            if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
+            // the walk of entity `ent` has ended
+            visits += w.visits;
+            const float T = h.closest;
+            if (kAny) {
+                if (T > 0.0f) {
+                    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    store(z, z, true);
+                    live = false;
+                    continue;
+                }
+            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+                tmax = T;
+                closest = T;
+                mesh = h.mesh;
+                tri = h.tri;
+                ent_hit = ent;
+            }
+            seek = true;
+        }
+        return;
+    }
     while (true) {
         // refill idle lanes (warp-uniform loop; inactive rays are answered here)
         while (true) {

@@ -77,6 +77,57 @@ __global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, cons
     int64_t id = -1;
     bool need = true;
     int32_t tests = 0, nodes = 0;
+    auto store = [&]() {
+        nodes += R.iters_total;
+        if (kAny) {
+            occ[id] = R.occluded ? 1 : 0;
+        } else {
+            rq_hit h;
+            R.finish(s, flags, h);
+            store_hit(hits, id, h);
+        }
+    };
+    if constexpr (kTlas) {
+        // Scenes with a top level: a ray looking for its next entity advances the top-level cursor
+        // by at most 4 nodes per iteration (StrictRay::seek), interleaved with the node steps of
+        // the other lanes; the entities, their order and every count are those of the loop below.
+        bool seeking = false;
+        while (true) {
+            const int64_t nid = persist::fetch(queue, need);
+            if (need) {
+                id = nid;
+                if (id >= n) break;
+                float4 r0, r1;
+                load_ray(rays, id, r0, r1);
+                if (!R.init_ray(s, r0, r1)) {
+                    store();
+                    continue;
+                }
+                need = false;
+                seeking = true;
+            }
+            if (seeking) {
+                const int g = R.seek(s, flags, 4);
+                if (g > 0) {
+                    seeking = false;
+                } else if (g < 0) {
+                    store();
+                    need = true;
+                }
+                continue;
+            }
+            if (R.step(s, stack, tests)) {
+                if (R.accept_entity()) {
+                    seeking = true;
+                } else {
+                    store();
+                    need = true;
+                }
+            }
+        }
+        if (counters) count_work(counters, nodes, tests);
+        return;
+    }
     while (true) {
         const int64_t nid = persist::fetch(queue, need);
         if (need) {

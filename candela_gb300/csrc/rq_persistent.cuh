@@ -33,6 +33,18 @@ struct StrictRay {
     strict::Best bb;
     bool occluded;
 
+    __device__ __forceinline__ void setup_entity(const rq_entity& e) {
+        ro = strict::xform(e.inverse, o, 1.0f);
+        rd = strict::xform(e.inverse, d, 0.0f);
+        inv = strict::rcp3(rd);
+        start = e.node_offset;
+        count = e.node_count;
+        cur = start;
+        sp = 0;
+        iters = 0;
+        bb = strict::Best{kAny ? rtmax : tmax, -1.0f, (!kAny && kTieLower) ? tri : -1, -1};
+    }
+
     // Skips to the next entity that is traversed (ignore-transparent filter); false when done.
     __device__ __forceinline__ bool begin_entity(const SceneView& s, int flags) {
         const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
@@ -41,21 +53,30 @@ struct StrictRay {
                                  skip_transparent ? tlas::kOpaque : tlas::kAll, iters_total)) >= 0) {
             const rq_entity& e = s.ents[ent];
             if (skip_transparent && strict::ent_alpha(e) < 0.99f) continue;
-            ro = strict::xform(e.inverse, o, 1.0f);
-            rd = strict::xform(e.inverse, d, 0.0f);
-            inv = strict::rcp3(rd);
-            start = e.node_offset;
-            count = e.node_count;
-            cur = start;
-            sp = 0;
-            iters = 0;
-            bb = strict::Best{kAny ? rtmax : tmax, -1.0f, (!kAny && kTieLower) ? tri : -1, -1};
+            setup_entity(e);
             return true;
         }
         return false;
     }
 
-    __device__ __forceinline__ bool init(const SceneView& s, float4 r0, float4 r1, int flags) {
+    // begin_entity() in bounded steps of at most `budget` top-level nodes: 1 = the walk of entity
+    // `ent` is set up, 0 = keep seeking, -1 = no entity left.
+    __device__ __forceinline__ int seek(const SceneView& s, int flags, int budget) {
+        const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const int32_t e = tlas::next_n<kTlas>(s, ents, ent, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
+                                              kAny ? rtmax : tmax, skip_transparent ? tlas::kOpaque : tlas::kAll,
+                                              iters_total, budget);
+        if (e == tlas::kMore) return 0;
+        if (e < 0) return -1;
+        ent = e;
+        const rq_entity& E = s.ents[ent];
+        if (skip_transparent && strict::ent_alpha(E) < 0.99f) return 0;
+        setup_entity(E);
+        return 1;
+    }
+
+    // The world ray's state; false for an inactive ray.
+    __device__ __forceinline__ bool init_ray(const SceneView& s, float4 r0, float4 r1) {
         o = strict::xyz(r0);
         d = strict::xyz(r1);
         rtmin = r0.w;
@@ -68,11 +89,15 @@ struct StrictRay {
         ent = -1;
         if (!(rtmax > rtmin)) return false;  // inactive ray
         ents = tlas::begin<kTlas>(s, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z));
-        return begin_entity(s, flags);
+        return true;
     }
 
-    // Ends the current entity: scene-level acceptance, then the next entity.  false = ray done.
-    __device__ __forceinline__ bool end_entity(const SceneView& s, int flags) {
+    __device__ __forceinline__ bool init(const SceneView& s, float4 r0, float4 r1, int flags) {
+        return init_ray(s, r0, r1) && begin_entity(s, flags);
+    }
+
+    // Scene-level acceptance at the end of an entity's walk; false when the ray is done (any hit).
+    __device__ __forceinline__ bool accept_entity() {
         iters_total += iters;
         const float T = bb.closest;
         if (kAny) {
@@ -87,7 +112,12 @@ struct StrictRay {
             tri = bb.tri;
             ent_hit = ent;
         }
-        return begin_entity(s, flags);
+        return true;
+    }
+
+    // Ends the current entity: scene-level acceptance, then the next entity.  false = ray done.
+    __device__ __forceinline__ bool end_entity(const SceneView& s, int flags) {
+        return accept_entity() && begin_entity(s, flags);
     }
 
     // One node of the current entity.  Returns true when this entity's traversal has ended.

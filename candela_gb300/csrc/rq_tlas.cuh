@@ -37,21 +37,23 @@ __device__ __forceinline__ int32_t walked(const SceneView& s, int32_t lo, int32_
     return __ldg(p + 4 * hi + count) - __ldg(p + 4 * lo + count);
 }
 
-// Next entity after `prev` to walk, or -1 when none is left.  `tmax` is the loop's running TMax:
-// subtrees whose widened boxes start beyond it are skipped (the walk of such an entity would
-// stop at its root as well).  `skipped` receives the iterations of the entities passed over.
+// next() with a budget: at most `budget` top-level nodes are tested per call; kMore when the
+// budget ran out before an entity was found (the cursor keeps its place, so the next call
+// continues the same walk).  The persistent kernels interleave these bounded steps with the node
+// steps of the other lanes instead of running a whole top-level walk while the warp waits.
+constexpr int32_t kMore = -4;
+
 template <bool kTlas>
-__device__ __forceinline__ int32_t next(const SceneView& s, int32_t& c, int32_t prev, float3 o, float3 d,
-                                        float tmax, int count, int32_t& skipped) {
+__device__ __forceinline__ int32_t next_n(const SceneView& s, int32_t& c, int32_t prev, float3 o, float3 d,
+                                          float tmax, int count, int32_t& skipped, int budget) {
     if (!kTlas || c == kPlain) return prev + 1 < s.n_ents ? prev + 1 : -1;
     if (c == kDone) return -1;
     const float m = s.tlas_margin * fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
     const float ix = __frcp_rn(d.x), iy = __frcp_rn(d.y), iz = __frcp_rn(d.z);
     const float tlim = tmax * (1.0f + 1.0f / 65536.0f);
     while (c >= 0) {
+        if (budget-- <= 0) return kMore;
         const float4 a = __ldg(s.tlas + 2 * c), b = __ldg(s.tlas + 2 * c + 1);
-        // slab test on the widened box; fminf / fmaxf drop the NaN of a zero direction component
-        // whose origin lies on a widened face (outside the entity's own box by the margin)
         const float x0 = (a.x - m - o.x) * ix, x1 = (b.x + m - o.x) * ix;
         const float y0 = (a.y - m - o.y) * iy, y1 = (b.y + m - o.y) * iy;
         const float z0 = (a.z - m - o.z) * iz, z1 = (b.z + m - o.z) * iz;
@@ -73,6 +75,17 @@ __device__ __forceinline__ int32_t next(const SceneView& s, int32_t& c, int32_t 
     skipped += walked(s, prev + 1, s.n_ents, count);
     c = kDone;
     return -1;
+}
+
+// Next entity after `prev` to walk, or -1 when none is left.  `tmax` is the loop's running TMax:
+// subtrees whose widened boxes start beyond it are skipped (the walk of such an entity would
+// stop at its root as well).  `skipped` receives the iterations of the entities passed over.
+// The slab test runs on the widened box; fminf / fmaxf drop the NaN of a zero direction component
+// whose origin lies on a widened face (outside the entity's own box by the margin).
+template <bool kTlas>
+__device__ __forceinline__ int32_t next(const SceneView& s, int32_t& c, int32_t prev, float3 o, float3 d,
+                                        float tmax, int count, int32_t& skipped) {
+    return next_n<kTlas>(s, c, prev, o, d, tmax, count, skipped, 0x7FFFFFFF);
 }
 
 }  // namespace tlas
