@@ -136,26 +136,13 @@ __global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, cons
             float4 r0, r1;
             load_ray(rays, id, r0, r1);
             if (!R.init(s, r0, r1, flags)) {
-                if (kAny) {
-                    occ[id] = 0;
-                } else {
-                    rq_hit h;
-                    R.finish(s, flags, h);
-                    store_hit(hits, id, h);
-                }
+                store();
                 continue;
             }
             need = false;
         }
         if (R.step(s, stack, tests) && !R.end_entity(s, flags)) {
-            nodes += R.iters_total;
-            if (kAny) {
-                occ[id] = R.occluded ? 1 : 0;
-            } else {
-                rq_hit h;
-                R.finish(s, flags, h);
-                store_hit(hits, id, h);
-            }
+            store();
             need = true;
         }
     }

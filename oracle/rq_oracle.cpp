@@ -1027,8 +1027,7 @@ void orc_spec_raygen(const orc_scene* sc, const orc_ray* primary, const orc_hit*
     });
 }
 
-// SampleLighting (:420-425) + emissive for a hit, the sky x mix(1.4, 2.65, R) (:435-437) for a
-// miss; IsValid, clamp to [0, 6], w = t / 48 (:588-596); 0 where the primary ray missed.
+// StochasticReflectionDirection for given incident directions and normals (sample rid[i]).
 void orc_spec_direction(const float* incident, const float* normals, int64_t n, float roughness, uint32_t seed,
                         const uint32_t* rid, float* out) {
     for (int64_t i = 0; i < n; ++i) {
@@ -1039,6 +1038,8 @@ void orc_spec_direction(const float* incident, const float* normals, int64_t n, 
     }
 }
 
+// SampleLighting (:420-425) + emissive for a hit, the sky x mix(1.4, 2.65, R) (:435-437) for a
+// miss; IsValid, clamp to [0, 6], w = t / 48 (:588-596); 0 where the primary ray missed.
 void orc_spec_shade(const orc_scene* sc, const orc_ray* rays, const orc_hit* hits, int64_t n, const uint8_t* lit,
                     const orc_materials* mat, float roughness, const float sun_color[3], const float sky[3],
                     const float ambient[3], int nthreads, float* out4) {
