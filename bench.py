@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "c6"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
+    ap.add_argument("--profile-probe", action="store_true",
+                    help="run two probe-volume frames on the 128 x 128 x 64 grid over the C2 scene and "
+                         "exit (the case the ncu capture of k_probe_shade uses)")
     ap.add_argument("--profile", action="store_true",
                     help="run one GI pass and exit (the case the ncu captures use: the 2nd "
                          "traversal launch is the full-size secondary closest-hit launch; with "
@@ -781,6 +784,23 @@ def main():
     sptr = stream.cuda_stream
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     B8 = L.LAYOUT_BVH8Q
+
+    if args.profile_probe:
+        # two frames of the probe-volume update on the 128 x 128 x 64 grid (BVH8q, the tuned
+        # persistent launch): the second frame's k_probe_shade reads a filled previous volume
+        from candela_gb300.engine import probe_params, probe_volumes
+        sc.build_bvh8()
+        pp = probe_params(grid=(128, 128, 64), origin=PROBE_ORIGIN, size=PROBE_SIZE, seed=2)
+        vols = [probe_volumes(pp, device=dev) for _ in range(2)]
+        launch = dict(layout=B8, block_size=128, min_blocks=8, persistent=1)
+        sc.probe_update(pp, vols[0][0], vols[0][1], vols[0][2], out_sh=vols[1][0], out_raw=vols[1][1],
+                        stream=sptr, **launch)
+        sc.probe_update(pp, vols[1][0], vols[1][1], vols[1][2], out_sh=vols[0][0], out_raw=vols[0][1],
+                        stream=sptr, **launch)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "probe update 128x128x64 over " + wl["name"],
+                          "device_status": ctx.device_status()}))
+        return
 
     if args.profile:
         # One k_bvh8_persistent launch: the secondary closest-hit launch of the roofline below

@@ -135,9 +135,19 @@ __device__ __forceinline__ uint32_t snorm16(float c) {
     return static_cast<uint32_t>(static_cast<uint16_t>(static_cast<int16_t>(__float2int_rn(s))));
 }
 __device__ __forceinline__ uint32_t pack_snorm2(float a, float b) { return snorm16(a) | (snorm16(b) << 16); }
+// f / 32767 for an int16 f, correctly rounded, by Markstein's correction step (P. Markstein, IBM J.
+// Res. Dev. 34(1), 1990): q0 = f * y with y = RN(1/32767) = 0x1.0002p-15, r = f - q0 * 32767 (exact
+// in one FMA), q = q0 + r * y.  Equal to the IEEE quotient for every one of the 65,536 numerators
+// (checked exhaustively with exact rationals by tests/test_probe_math.py), at three instructions.
+__device__ __forceinline__ float div32767(float f) {
+    const float y = 0x1.0002p-15f;
+    const float q0 = __fmul_rn(f, y);
+    const float r = __fmaf_rn(-q0, 32767.0f, f);
+    return __fmaf_rn(r, y, q0);
+}
 __device__ __forceinline__ float unsnorm16(uint32_t h) {
     const float f = static_cast<float>(static_cast<int16_t>(static_cast<uint16_t>(h & 0xFFFFu)));
-    return strict::gmin(strict::gmax(__fdiv_rn(f, 32767.0f), -1.0f), 1.0f);
+    return strict::gmin(strict::gmax(div32767(f), -1.0f), 1.0f);
 }
 __device__ __forceinline__ float max3abs(f3 x) {
     return strict::gmax(strict::gmax(fabsf(x.x), fabsf(x.y)), fabsf(x.z));
@@ -180,9 +190,9 @@ __device__ __forceinline__ void load_texel(const ProbeArgs& a, const uint4* __re
     B = __ldg(vol + 2 * i + 1);
 }
 
-// GetVisibility (:176-188): clamp(dot(N, direction to the probe), 0, 1)^2 (pow(x, 2) as x * x).
-__device__ __forceinline__ float probe_visibility(const ProbeArgs& a, int x, int y, int z, f3 wp, f3 n) {
-    const f3 pp = probe_position(a, a.prev, x, y, z);
+// GetVisibility (:176-188) of the probe at pp: clamp(dot(N, direction to it), 0, 1)^2 (pow(x, 2)
+// as x * x).
+__device__ __forceinline__ float probe_visibility(f3 pp, f3 wp, f3 n) {
     f3 v = strict::sub(pp, wp);
     const float len = __fsqrt_rn(strict::dot(v, v));
     v = vdivs(v, len);
@@ -210,10 +220,15 @@ __device__ f3 sample_probes(const ProbeArgs& a, const uint4* __restrict__ vol, f
     const int x1 = static_cast<int>(mx.x), y1 = static_cast<int>(mx.y), z1 = static_cast<int>(mx.z);
     const int tx[8] = {x0, x0, x1, x1, x0, x0, x1, x1}, ty[8] = {y0, y1, y1, y0, y0, y1, y1, y0};
     const int tz[8] = {z0, z0, z0, z0, z1, z1, z1, z1};
+    // the corners' probe positions, one coordinate per axis and bound (each component of
+    // probe_position depends on its own axis only)
+    const f3 p0 = probe_position(a, a.prev, x0, y0, z0), p1 = probe_position(a, a.prev, x1, y1, z1);
     float alpha = 0.0f;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const float vis = probe_visibility(a, tx[i], ty[i], tz[i], wp, n);
+        const bool bx1 = i == 2 || i == 3 || i == 6 || i == 7, by1 = i == 1 || i == 2 || i == 5 || i == 6;
+        const f3 pp = {bx1 ? p1.x : p0.x, by1 ? p1.y : p0.y, i >= 4 ? p1.z : p0.z};
+        const float vis = probe_visibility(pp, wp, n);
         alpha = __fadd_rn(alpha, __fmul_rn(w[i], __fsub_rn(1.0f, vis)));
         w[i] = __fmul_rn(w[i], vis);
     }

@@ -420,7 +420,7 @@ class _GiMixin:
         return out
 
     def probe_update(self, params, prev_sh, prev_raw, probe_map, out_sh=None, out_raw=None, *, layout=0, mode=0,
-                     tie=0, flags=0, stream=None):
+                     tie=0, flags=0, block_size=0, min_blocks=0, persistent=0, stream=None):
         """One frame of the radiance-probe update (rq_probe_update).  numpy volumes -> host path.
         probe_map is updated in place; returns (out_sh, out_raw)."""
         host = isinstance(prev_sh, np.ndarray)
@@ -430,7 +430,8 @@ class _GiMixin:
         if out_raw is None:
             out_raw = (np.empty((n, 4), dtype=np.float32) if host
                        else _empty_like_dev(prev_raw, (n, 4), __import__("torch").float32))
-        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0))
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size, min_blocks,
+                  persistent)
         check(lib().rq_probe_update(self.ctx.handle, self.handle, C.byref(params), ptr(prev_sh), ptr(prev_raw),
                                     ptr(probe_map), ptr(out_sh), ptr(out_raw), C.byref(o),
                                     _stream(prev_sh, stream)), self.ctx.handle)
