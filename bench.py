@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "c6"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock bound of the CPU baseline sample")
+    ap.add_argument("--profile-primary", action="store_true",
+                    help="run the GI pass's primary (camera) launch on BVH8q twice and exit (the case the "
+                         "ncu capture of the one-thread-per-ray k_bvh8 uses)")
     ap.add_argument("--profile-probe", action="store_true",
                     help="run two probe-volume frames on the 128 x 128 x 64 grid over the C2 scene and "
                          "exit (the case the ncu capture of k_probe_shade uses)")
@@ -784,6 +787,17 @@ def main():
     sptr = stream.cuda_stream
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     B8 = L.LAYOUT_BVH8Q
+
+    if args.profile_primary:
+        # the primary launch of the GI pass: 1920x1080 camera rays, BVH8q, one thread per ray with
+        # the tuned shape (128 threads, 8 blocks per SM); the second launch sees a warm L2
+        sc.build_bvh8()
+        h = torch.empty((n, 8), dtype=torch.float32, device=dev)
+        for _ in range(2):
+            sc.closest(d_rays, h, layout=B8, block_size=128, min_blocks=8, persistent=0, stream=sptr)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "primary rays of " + wl["name"], "device_status": ctx.device_status()}))
+        return
 
     if args.profile_probe:
         # two frames of the probe-volume update on the 128 x 128 x 64 grid (BVH8q, the tuned
