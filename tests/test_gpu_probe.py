@@ -113,3 +113,39 @@ def test_probe_update_rejects_bad_arguments(ctx):
     d_sh, d_raw, d_map = _torch_volumes(sh, raw, pmap)
     with pytest.raises(R.RqError):                       # output volume aliasing the previous one
         sc.probe_update(p, d_sh, d_raw, d_map, out_sh=d_sh)
+
+
+@pytest.mark.parametrize("flags", [0, L.FLAG_REF_COMPAT])
+def test_probe_update_textures_and_ref_compat(ctx, flags):
+    """Textured albedo (a repeat and a clamped sRGB texture over a heightfield with texture
+    coordinates) and the reference's conventions (RQ_FLAG_REF_COMPAT: a hit on global triangle 0
+    reads as a miss): the volume equals the oracle's bit for bit."""
+    m = S.heightfield(48, seed=8)
+    pos = m.positions().astype(np.float64)
+    verts = S.with_texcoords(m.vertices, np.stack([pos[:, 0] * 1.5 + 0.2, pos[:, 1] * -1.3], 1))
+    mids = (np.arange(m.n_tris) % 3).astype(np.int32)
+    b = R.build_bvh(verts, m.indices, mids, 0, layout=R.STACK)
+    ents = R.identity_entity(0, b.nodes.shape[0], emissive=0.1)
+    osc = O.OracleScene(O.ORC_STACK, verts, b.tris, b.nodes, ents)
+    sc = ctx.scene(R.STACK, verts, b.tris, b.nodes, ents)
+    albedo = np.float32([[0.6, 0.5, 0.4], [0.3, 0.7, 0.3], [0.8, 0.8, 0.2]])
+    tex = [(S.noise_texture(32, 3), 0, 0), (S.noise_texture(16, 4), 1, 1)]
+    mesh_tex = [0, -1, 1]
+    sc.set_materials(albedo)
+    sc.set_textures(tex, mesh_tex)
+    sh, raw, pmap = probe_volumes(probe_params(grid=(12, 12, 6)))
+    d_sh, d_raw, d_map = _torch_volumes(sh, raw, pmap)
+    frames = [probe_params(grid=(12, 12, 6), origin=org, prev_origin=prev, size=(1.0, 1.0, 0.4), seed=3 + k,
+                           sky_color=(0.4, 0.55, 0.9))
+              for k, (org, prev) in enumerate([((0.0, 0.0, 0.3), (0.0, 0.0, 0.3)),
+                                               ((0.05, -0.04, 0.31), (0.0, 0.0, 0.3))])]
+    for k, p in enumerate(frames):
+        want_sh, want_raw, want_map, rays, hits = osc.probe_update(p, albedo, sh, raw, pmap, flags=flags,
+                                                                   textures=tex, mesh_texture=mesh_tex)
+        got_sh, got_raw = sc.probe_update(p, d_sh, d_raw, d_map, flags=flags)
+        np.testing.assert_array_equal(got_sh.cpu().numpy().view(np.uint32), want_sh, err_msg=f"frame {k} sh")
+        np.testing.assert_array_equal(got_raw.cpu().numpy().view(np.uint32), want_raw.view(np.uint32))
+        np.testing.assert_array_equal(d_map.cpu().numpy().view(np.uint32), want_map.view(np.uint32))
+        sh, raw, pmap = want_sh, want_raw, want_map
+        d_sh, d_raw = got_sh, got_raw
+        assert 0.2 < (hits["t"] > 0).mean() < 0.95
