@@ -68,6 +68,37 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
         const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
         const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
         int32_t cur = tlas::begin<kTlas>(s, wo, wd);
+        if (!kAny && kTlas && cur != tlas::kPlain) {
+            // closest hit through the top level: candidates nearest first (tlas::near_next)
+            const int count = skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8;
+            uint64_t nst[tlas::kNearStack];
+            tlas::Near nw;
+            tlas::near_begin(s, nw, nst, wo, wd, tmax, status);
+            int32_t walked = 0;
+            for (int e; (e = tlas::near_next(s, nw, nst, wo, wd, tmax, 0x7FFFFFFF, status)) >= 0;) {
+                const rq_entity& E = s.ents[e];
+                if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
+                const int32_t root = s.b8_roots[e];
+                if (root < 0) continue;
+                ++walked;
+                const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
+                                                    strict::xform(E.inverse, d, 0.0f));
+                // an equal (t, triangle) from a lower entity wins: let the walk take it
+                bvh8::Hit8 h{tmax, -1.0f, (ent >= 0 && e < ent) ? tri + 1 : tri, -1};
+                visits += bvh8::traverse<false, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests, status);
+                const float T = h.closest;
+                if (T > 0.0f && (T < tmax || (T == tmax && (h.tri < tri || (h.tri == tri && e < ent))))) {
+                    tmax = T;
+                    closest = T;
+                    mesh = h.mesh;
+                    tri = h.tri;
+                    ent = e;
+                }
+            }
+            visits += tlas::walked(s, 0, s.n_ents, count) - walked;  // one per entity not walked
+            bvh8_finish(s, flags, o, d, closest, tri, mesh, ent, visits, hh);
+            return;
+        }
         for (int e = -1; (e = tlas::next<kTlas>(s, cur, e, wo, wd, kAny ? rtmax : tmax,
                                     skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0;) {
             const rq_entity& E = s.ents[e];
@@ -156,23 +187,38 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
         // hold the warp.  The entities, their order and every count are those of the loop below.
         constexpr int kSeekNodes = 4;
         bool seek = false;
+        // closest hit through the top level: candidates nearest first (tlas::near_next, which
+        // expands two children per node, so half the node budget); any hit keeps the ascending
+        // cursor (its early exit takes the first occluder in either order)
+        bool nearest = false;
+        uint64_t nst[kAny ? 1 : tlas::kNearStack];
+        tlas::Near nw{0};
+        int32_t walked = 0;
+        const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const int count = skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8;
         // One bounded seek: 1 = the walk of entity `ent` is set up, 0 = keep seeking, -1 = none left.
         auto seek_step = [&](const float4 r0, const float4 r1) -> int {
-            const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
-            const int32_t e = tlas::next_n<true>(s, ents, ent, make_float3(r0.x, r0.y, r0.z),
-                                                 make_float3(r1.x, r1.y, r1.z), kAny ? r1.w : tmax,
-                                                 skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits,
-                                                 kSeekNodes);
+            const float3 wo = make_float3(r0.x, r0.y, r0.z), wd = make_float3(r1.x, r1.y, r1.z);
+            int32_t e;
+            if (!kAny && nearest)
+                e = tlas::near_next(s, nw, nst, wo, wd, tmax, kSeekNodes / 2, status);
+            else
+                e = tlas::next_n<true>(s, ents, ent, wo, wd, kAny ? r1.w : tmax, count, visits, kSeekNodes);
             if (e == tlas::kMore) return 0;
-            if (e < 0) return -1;
+            if (e < 0) {
+                if (!kAny && nearest) visits += tlas::walked(s, 0, s.n_ents, count) - walked;
+                return -1;
+            }
             ent = e;
             const rq_entity& E = s.ents[ent];
             if (skip_transparent && strict::ent_alpha(E) < 0.99f) return 0;
             const int32_t root = s.b8_roots[ent];
             if (root < 0) return 0;
+            ++walked;
             r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
                                strict::xform(E.inverse, strict::xyz(r1), 0.0f));
-            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : tri, -1};
+            // an equal (t, triangle) from a lower entity wins: let the walk take it
+            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : ((ent_hit >= 0 && ent < ent_hit) ? tri + 1 : tri), -1};
             w = bvh8::walk_begin(root);
             return 1;
         };
@@ -211,6 +257,11 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                         ents = tlas::begin<true>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
                         live = r1.w > r0.w;
                         seek = live;
+                        walked = 0;
+                        nearest = !kAny && ents != tlas::kPlain;
+                        if (live && nearest)
+                            tlas::near_begin(s, nw, nst, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z),
+                                             tmax, status);
                         if (!live) store(r0, r1, false);
                     }
                 }
@@ -240,7 +291,7 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                     live = false;
                     continue;
                 }
-            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+            } else if (T > 0.0f && (T < tmax || (T == tmax && (h.tri < tri || (h.tri == tri && ent < ent_hit))))) {
                 tmax = T;
                 closest = T;
                 mesh = h.mesh;
@@ -249,70 +300,70 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
             }
             seek = true;
         }
-        return;
-    }
-    while (true) {
-        // refill idle lanes (warp-uniform loop; inactive rays are answered here)
+    } else {
         while (true) {
-            const unsigned want = __ballot_sync(kFull, !live && !exhausted);
-            if (!want) break;
-            const unsigned cnt = __popc(want);
-            const unsigned rank = __popc(want & persist::lanemask_lt());
-            const unsigned long long avail = pool_end - pool_next;
-            unsigned long long mine = pool_next + rank;
-            if (avail >= cnt) {
-                pool_next += cnt;
-            } else {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
-                base = __shfl_sync(kFull, base, 0);
-                if (rank >= avail) mine = base + (rank - avail);
-                pool_next = base + (cnt - avail);
-                pool_end = base + kPoolRays;
-            }
-            if (!live && !exhausted) {
-                if (static_cast<int64_t>(mine) >= n) {
-                    exhausted = true;
+            // refill idle lanes (warp-uniform loop; inactive rays are answered here)
+            while (true) {
+                const unsigned want = __ballot_sync(kFull, !live && !exhausted);
+                if (!want) break;
+                const unsigned cnt = __popc(want);
+                const unsigned rank = __popc(want & persist::lanemask_lt());
+                const unsigned long long avail = pool_end - pool_next;
+                unsigned long long mine = pool_next + rank;
+                if (avail >= cnt) {
+                    pool_next += cnt;
                 } else {
-                    id = static_cast<int64_t>(mine);
-                    float4 r0, r1;
-                    load_ray(rays, id, r0, r1);
-                    tmin = r0.w;
-                    tmax = r1.w;
-                    closest = -1.0f;
-                    mesh = tri = ent_hit = -1;
-                    visits = 0;
-                    ent = -1;
-                    ents = tlas::begin<kTlas>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
-                    live = (r1.w > r0.w) && begin(r0, r1);
-                    if (!live) store(r0, r1, false);
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
+                    base = __shfl_sync(kFull, base, 0);
+                    if (rank >= avail) mine = base + (rank - avail);
+                    pool_next = base + (cnt - avail);
+                    pool_end = base + kPoolRays;
+                }
+                if (!live && !exhausted) {
+                    if (static_cast<int64_t>(mine) >= n) {
+                        exhausted = true;
+                    } else {
+                        id = static_cast<int64_t>(mine);
+                        float4 r0, r1;
+                        load_ray(rays, id, r0, r1);
+                        tmin = r0.w;
+                        tmax = r1.w;
+                        closest = -1.0f;
+                        mesh = tri = ent_hit = -1;
+                        visits = 0;
+                        ent = -1;
+                        ents = tlas::begin<kTlas>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
+                        live = (r1.w > r0.w) && begin(r0, r1);
+                        if (!live) store(r0, r1, false);
+                    }
                 }
             }
+            if (!__any_sync(kFull, live)) break;
+            if (!live) continue;
+            if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
+            // the walk of entity `ent` has ended
+            visits += w.visits;
+            const float T = h.closest;
+            bool done = false;
+            if (kAny) {
+                done = T > 0.0f;
+            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+                tmax = T;
+                closest = T;
+                mesh = h.mesh;
+                tri = h.tri;
+                ent_hit = ent;
+            }
+            float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
+            if (!done) {
+                load_ray(rays, id, r0, r1);
+                if (begin(r0, r1)) continue;
+            }
+            if (!kAny) load_ray(rays, id, r0, r1);
+            store(r0, r1, done);
+            live = false;
         }
-        if (!__any_sync(kFull, live)) break;
-        if (!live) continue;
-        if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
-        // the walk of entity `ent` has ended
-        visits += w.visits;
-        const float T = h.closest;
-        bool done = false;
-        if (kAny) {
-            done = T > 0.0f;
-        } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
-            tmax = T;
-            closest = T;
-            mesh = h.mesh;
-            tri = h.tri;
-            ent_hit = ent;
-        }
-        float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
-        if (!done) {
-            load_ray(rays, id, r0, r1);
-            if (begin(r0, r1)) continue;
-        }
-        if (!kAny) load_ray(rays, id, r0, r1);
-        store(r0, r1, done);
-        live = false;
     }
 }
 

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, cons
                                                            unsigned long long* queue,
                                                            unsigned long long* counters) {
     if (s.ray_count && static_cast<int64_t>(*s.ray_count) < n) n = static_cast<int64_t>(*s.ray_count);
-    persist::StrictRay<kAny, kStackless, kTieLower, kTlas> R;
+    persist::StrictRay<kAny, kStackless, kTieLower, kTlas> R{};
     int32_t stack[kStackless ? 1 : 64];
     int64_t id = -1;
     bool need = true;
@@ -125,25 +125,24 @@ __global__ void __launch_bounds__(128, kM) k_persistent_strict(SceneView s, cons
                 }
             }
         }
-        if (counters) count_work(counters, nodes, tests);
-        return;
-    }
-    while (true) {
-        const int64_t nid = persist::fetch(queue, need);
-        if (need) {
-            id = nid;
-            if (id >= n) break;
-            float4 r0, r1;
-            load_ray(rays, id, r0, r1);
-            if (!R.init(s, r0, r1, flags)) {
-                store();
-                continue;
+    } else {
+        while (true) {
+            const int64_t nid = persist::fetch(queue, need);
+            if (need) {
+                id = nid;
+                if (id >= n) break;
+                float4 r0, r1;
+                load_ray(rays, id, r0, r1);
+                if (!R.init(s, r0, r1, flags)) {
+                    store();
+                    continue;
+                }
+                need = false;
             }
-            need = false;
-        }
-        if (R.step(s, stack, tests) && !R.end_entity(s, flags)) {
-            store();
-            need = true;
+            if (R.step(s, stack, tests) && !R.end_entity(s, flags)) {
+                store();
+                need = true;
+            }
         }
     }
     if (counters) count_work(counters, nodes, tests);

@@ -17,6 +17,8 @@
 //    to the count (per-entity prefix counts give the number skipped between two candidates);
 //  * entities whose walk tests triangles without a box test first (a stack-layout root with a
 //    leaf child) or whose transform is singular or not finite are never skipped.
+// BVH8 closest-hit queries walk the same tree nearest box first instead (rq_tlas.cuh, near_next):
+// their hit is the lexicographic minimum of (t, triangle, entity), which no walk order changes.
 #pragma once
 #include <cstdint>
 #include <string>

@@ -273,7 +273,11 @@ rq_status rq_scene_bytes(const rq_scene* scene, int64_t* bytes);
  * the inverse of its inverse matrix, widened by a margin that covers float rounding) the ray
  * meets before TMax, and count one iteration for each entity passed over (the root visit the
  * loop would have made).  Hits, ties and iteration counts therefore equal the loop's
- * (RQ_FLAG_ENTITY_LOOP runs the loop itself).  Entities whose walk tests triangles without a box
+ * (RQ_FLAG_ENTITY_LOOP runs the loop itself).  The one exception is RQ_LAYOUT_BVH8Q closest
+ * hits: these take their candidates nearest box first and drop the ones that start beyond the
+ * running TMax.  The hit is the same, because it is the lexicographic minimum of (t, triangle,
+ * entity) in any order.  Only iters differs: BVH8 nodes visited plus one per entity not walked.
+ * Entities whose walk tests triangles without a box
  * test first (a stack-layout root with a leaf child) or whose transform is singular are never
  * passed over.  Not maintained by rq_scene_update_positions: after it every entity is walked
  * until the entities or the BVH8 are set again. */

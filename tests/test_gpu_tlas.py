@@ -145,7 +145,12 @@ def test_tlas_bvh8_and_fast_equal_their_loops(scenes):
         for flags in (0, L.FLAG_IGNORE_TRANSPARENT):
             got = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, flags=flags, **kw))
             loop = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, flags=flags | L.FLAG_ENTITY_LOOP, **kw))
-            assert_hits_identical(got, loop, f"bvh8 {kw} flags {flags}")  # iters = BVH8 visits
+            # closest hits through the top level walk their candidates nearest first: the records
+            # equal the loop's except the BVH8 visit count (fewer walks, each with its own TMax)
+            for f in ("t", "u", "v", "w", "tri", "mesh", "entity"):
+                np.testing.assert_array_equal(got[f].view(np.uint32), loop[f].view(np.uint32),
+                                              err_msg=f"bvh8 {kw} flags {flags} {f}")
+            assert got["iters"].sum() < 1.1 * loop["iters"].sum()
         # hits equal the strict BVH2 hits (iters count BVH8 nodes there) for generic rays.  For
         # origins 2000 units away, and for axis-aligned rays through a vertex of the tetrahedron
         # (zero direction components), the reference's slab test can round or NaN a node with
