@@ -131,7 +131,8 @@ enum {
                                         context's work counters (rq_counters_read) */
     RQ_FLAG_ENTITY_LOOP = 32         /* walk every entity in turn (the reference's loop) instead
                                         of skipping the ones the top-level BVH rules out; same
-                                        results either way */
+                                        results either way (for BVH8 closest hits, same hits
+                                        with a different iters: see rq_tlas_info) */
 };
 
 typedef struct rq_opts {
