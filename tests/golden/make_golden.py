@@ -8,6 +8,12 @@
   these hashes on any machine.
 * oracle_hits_hf32.npz — closest-hit / any-hit results of the CPU restatement (oracle/) on a small
   seeded scene, so a change in the oracle's arithmetic on any platform is caught.
+* glsl_pins.json — SHA-256 of the outputs of the reference's own shaders compiled as C++
+  (oracle/_ref/librefglsl.so, built by oracle/Makefile from the mounted reference tree) on seeded
+  inputs: closest hits and occlusion on both layouts, closest hits over transformed and
+  translucent entities, collision records, the diffuse and specular shading sums and three frames
+  of the probe update.  Needs the reference tree; tests/test_golden_glsl.py then checks that the
+  restatement reproduces every one of them, on any machine.
 """
 from __future__ import annotations
 
@@ -76,8 +82,134 @@ def make_oracle_hits():
                         hits=hits.view(np.uint8), ao_rays=ao.view(np.uint8), occluded=occ)
 
 
+def _canon_hits(h):
+    """Closest-hit records in a form both implementations share: triangle, mesh and entity only
+    where there is a hit (the shader leaves them unwritten otherwise)."""
+    hit = h["t"] > 0
+    return np.stack([h["t"].view(np.int32), h["u"].view(np.int32), h["v"].view(np.int32),
+                     h["w"].view(np.int32), np.where(hit, h["tri"], -1), np.where(hit, h["mesh"], -1),
+                     np.where(hit, h["entity"], -1)], 1).astype(np.int32)
+
+
+def glsl_case_outputs(reference: bool) -> dict:
+    """Outputs of the reference shaders compiled as C++ (reference=True) or of the restatement
+    with the reference's conventions (first-found ties, the tri-0 test), on the same seeded inputs."""
+    import candela_gb300 as R
+    from candela_gb300.engine import probe_params, probe_volumes
+    sys.path.insert(0, str(ROOT))
+    from tests.helpers import mesh, single_object  # noqa: E402
+
+    out = {}
+    layouts = (("stack", R.STACK, O.ORC_STACK), ("stackless", R.STACKLESS, O.ORC_STACKLESS))
+    edge = np.zeros(4, dtype=R.RAY_DTYPE)
+    edge["o"] = [[0, 0, 5], [0, 0, 5], [0.1, 0.2, 3], [-3, 0.1, 0.05]]
+    edge["d"] = [[np.nan, 0, -1], [0, 0, 0], [0, 0, -1], [1, 0, 0]]
+    edge["tmax"] = 1e6
+    for name in ("hf32", "ico2"):
+        rays = np.concatenate([S.sphere_rays(4000, (-1.5, -1.5, -0.3), (1.5, 1.5, 1.2), seed=21),
+                               S.camera_rays(48, 36, **S.C1_CAMERA), edge])
+        for lname, lay, olay in layouts:
+            bufs = single_object(name, lay)
+            if reference:
+                h = O.ref_glsl_closest(olay, *bufs, rays)
+                occ = O.ref_glsl_occluded(olay, *bufs, rays)
+            else:
+                osc = O.OracleScene(olay, *bufs)
+                h = osc.closest(rays, tie=O.ORC_TIE_FIRST_FOUND, flags=O.ORC_FLAG_REF_COMPAT)
+                occ = osc.anyhit(rays)
+            out[f"closest_{name}_{lname}"] = np.concatenate([_canon_hits(h), h["iters"][:, None]], 1)
+            out[f"occluded_{name}_{lname}"] = occ.astype(np.uint8)
+    # transformed, scaled and translucent entities (the shader's iteration output is the last
+    # entity's, so iterations are left out here)
+    ri = R.RayIntersector(R.STACK)
+    ri.add_object(1, [mesh("hf32")])
+    ri.add_object(2, [mesh("ico2")])
+    M = S.instance_transforms(8, (-3.0, -3.0, 0.0), (3.0, 3.0, 1.0), 0.4, 1.2, seed=5, anisotropic=0.3, tilt=0.1)
+    for i in range(8):
+        ri.push_entity(1 + (i % 2), model=M[i].astype(np.float64), translucency=0.5 if i % 4 == 1 else 0.0)
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    rays = np.concatenate([S.sphere_rays(4000, (-4.0, -4.0, -0.5), (4.0, 4.0, 2.0), seed=22), edge])
+    for ignore in (False, True):
+        if reference:
+            h = O.ref_glsl_closest(O.ORC_STACK, v, t, n, e, rays, ignore_transparent=ignore)
+        else:
+            flags = O.ORC_FLAG_REF_COMPAT | (O.ORC_FLAG_IGNORE_TRANSPARENT if ignore else 0)
+            h = O.OracleScene(O.ORC_STACK, v, t, n, e).closest(rays, tie=O.ORC_TIE_FIRST_FOUND, flags=flags)
+        out[f"closest_entities_ignore{int(ignore)}"] = _canon_hits(h)
+    # collision records on both layouts
+    rng = np.random.default_rng(31)
+    for lname, lay, olay in layouts:
+        bufs = single_object("ico2", lay)
+        pts = bufs[0]["pos"][:, :3][rng.integers(0, bufs[0].shape[0], 3000)]
+        c = (pts + rng.uniform(-0.05, 0.05, size=pts.shape)).astype(np.float32)  # IEEE-exact draws
+        hsz = rng.uniform(0.002, 0.04, size=(pts.shape[0], 1)).astype(np.float32)
+        boxes = np.zeros((pts.shape[0], 8), dtype=np.float32)
+        boxes[:, 0:3], boxes[:, 4:7] = c - hsz, c + hsz
+        if reference:
+            rec = O.ref_glsl_collide(olay, *bufs, boxes)
+        else:
+            rec = O.OracleScene(olay, *bufs).collide(boxes, flags=O.ORC_FLAG_REF_COMPAT)
+        rec = np.where(rec[:, :1] == 1, rec, np.int32([[0, -1, -1, -1]])).astype(np.int32)
+        out[f"collide_ico2_{lname}"] = rec
+    # shading sums and the probe update, fed the restatement's traversal and surface data (their
+    # own parity with the shader is the closest-hit / GetData pins)
+    bufs = single_object("hf32", R.STACK)
+    osc = O.OracleScene(O.ORC_STACK, *bufs)
+    model = np.float32([[0.7, 0.6, 0.5], [0.2, 0.8, 0.4]])
+    rays = S.sphere_rays(3000, (-1.2, -1.2, -0.2), (1.2, 1.2, 1.0), seed=23)
+    hits = osc.closest(rays)
+    hit = hits["t"] > 0
+    alb = np.zeros((rays.shape[0], 4), dtype=np.float32)
+    alb[hit, :3] = osc.hit_albedo(hits[hit], model)
+    nrm = np.full((rays.shape[0], 3), -1.0, dtype=np.float32)
+    nrm[hit] = osc.hit_normal(hits[hit], 0)
+    lit = (np.arange(rays.shape[0]) % 3 != 0).astype(np.uint8)
+    sun_dir, sun, sky, amb = (np.float32([0.3, 0.4, -0.866]), np.float32([4.0, 3.8, 3.5]),
+                              np.float32([0.45, 0.6, 0.95]), np.float32([0.1, 0.1, 0.12]))
+    if reference:
+        out["shade_diffuse"] = O.ref_glsl_shade(0, rays, hits, alb, nrm, lit, sun_dir, sun, sky)
+        out["shade_specular"] = O.ref_glsl_shade(1, rays, hits, alb, nrm, lit, sun_dir, sun, sky, amb, 0.35)
+    else:
+        out["shade_diffuse"] = osc.shade(rays, hits, lit, model, sun_dir, sun, sky * np.float32(2.0))
+        out["shade_specular"] = osc.spec_shade(rays, hits, lit, model, 0.35, sun, sky, amb)
+    origins = [(0.0, 0.0, 0.4), (0.07, -0.05, 0.42), (0.15, 0.02, 0.38)]
+    sh, raw, pmap = probe_volumes(probe_params(grid=(8, 8, 4)))
+    prev = origins[0]
+    for k, org in enumerate(origins):
+        p = probe_params(grid=(8, 8, 4), origin=org, prev_origin=prev, size=(1.2, 1.2, 0.6), seed=7 + k,
+                         temporal=k < 2, sky_color=(0.4, 0.55, 0.9))
+        prays = O.probe_raygen(p)
+        ph = osc.closest(prays)
+        phit = ph["t"] > 0
+        palb = np.zeros((prays.shape[0], 4), dtype=np.float32)
+        palb[phit, :3] = osc.hit_albedo(ph[phit], model)
+        pn = np.full((prays.shape[0], 3), -1.0, dtype=np.float32)
+        pn[phit] = osc.hit_normal(ph[phit], 0)
+        plit = 1 - osc.anyhit(osc.shadow_raygen(prays, ph, np.array(p.sun_dir, dtype=np.float32), p.shadow_offset, 0))
+        if reference:
+            sh, raw, pmap = O.ref_glsl_probe(p, prays, ph, palb, pn, plit, sh, raw, pmap)
+        else:
+            sh, raw, pmap = osc.probe_shade(p, prays, ph, plit, model, sh, raw, pmap)
+        out[f"probe_frame{k}"] = np.concatenate([sh.view(np.int32), raw.view(np.int32), pmap.view(np.int32)], 1)
+        prev = org
+    return out
+
+
+def make_glsl_pins():
+    if not O.ref_glsl_available():
+        raise SystemExit("the reference tree is needed to regenerate glsl_pins.json")
+    ref = glsl_case_outputs(reference=True)
+    ours = glsl_case_outputs(reference=False)
+    for k in ref:
+        if sha(ref[k]) != sha(ours[k]):
+            raise SystemExit(f"the restatement differs from the reference shader on {k}")
+    (HERE / "glsl_pins.json").write_text(json.dumps({k: sha(v) for k, v in ref.items()}, indent=1) + "\n")
+
+
 if __name__ == "__main__":
     O.build()
     make_builder()
     make_oracle_hits()
+    make_glsl_pins()
     print("golden fixtures written to", HERE)
