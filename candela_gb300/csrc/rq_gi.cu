@@ -715,11 +715,25 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
         rad = static_cast<float4*>(d_rad);
         thr = static_cast<float4*>(d_thr);
     }
-    // phase 1
-    if (h_prim)
+    // phase 1.  Host rays in pinned memory on the BVH8 layout: the primary launch reads them over
+    // the host link itself and stores the device copy the later kernels read, so the transfer
+    // overlaps the traversal; other host rays are copied in first.
+    SceneView pv = sc->view;
+    const rq_ray* src = prim;
+    if (h_prim && q.layout == RQ_LAYOUT_BVH8Q) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, h_prim) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+            at.devicePointer != nullptr) {
+            src = static_cast<const rq_ray*>(at.devicePointer);
+            pv.ray_copy = const_cast<rq_ray*>(prim);
+        } else {
+            (void)cudaGetLastError();  // not registered with CUDA: copy it in
+        }
+    }
+    if (h_prim && src == prim)
         RQ_CUDA(ctx, cudaMemcpyAsync(const_cast<rq_ray*>(prim), h_prim, sizeof(rq_ray) * n,
                                      cudaMemcpyHostToDevice, st));
-    RQ_CUDA(ctx, launch_closest(sc->view, qp, prim, n, phit, queue_counter(ctx, 0), st));
+    RQ_CUDA(ctx, launch_closest(pv, qp, src, n, phit, queue_counter(ctx, 0), st));
     if (stats) k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
     if ((!p.sort_rays && !p.unfused) || bounce) {
         k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count,

@@ -38,6 +38,10 @@ struct SceneView {
     const int4* tlas_pre;
     float tlas_margin;
     int32_t tlas_pad;
+    // Optional copy target of the rays (BVH8 one-thread-per-ray launches): each ray loaded is also
+    // stored here, so a launch that reads rays from pinned host memory leaves a device copy for the
+    // kernels after it.
+    rq_ray* ray_copy;
 };
 
 // Per-mesh surface data of the shading kernels: ModelColor per mesh id, and optional albedo

@@ -161,6 +161,11 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __re
     if (i < n) {
         float4 r0, r1;
         load_ray(rays, i, r0, r1);
+        if (s.ray_copy) {
+            float4* c = reinterpret_cast<float4*>(s.ray_copy) + 2 * i;
+            c[0] = r0;
+            c[1] = r1;
+        }
         rq_hit hh;
         bool occluded;
         bvh8_ray<kAny, kTlas>(s, r0, r1, flags, hh, occluded, visits, tests, status);

@@ -147,6 +147,13 @@ def test_gi_frame_per_pixel_host_buffers_and_ref_compat(ctx, query):
                                flags=flags, stats=True)
         got_host = sc.gi_frame(rays, gi_params(**kw), layout=L.LAYOUT_BVH8Q, flags=flags)
         np.testing.assert_array_equal(got_host.view(np.uint32), want.cpu().numpy().view(np.uint32))
+        # pinned host rays: the primary launch reads them over the host link and leaves the device
+        # copy the later kernels read; the pixels are the same
+        import torch
+        pinned = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
+        pinned_out = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory().numpy()
+        sc.gi_frame(pinned, gi_params(**kw), out=pinned_out, layout=L.LAYOUT_BVH8Q, flags=flags)
+        np.testing.assert_array_equal(pinned_out.view(np.uint32), want.cpu().numpy().view(np.uint32))
     ph = osc.closest(rays)
     sec = osc.gi_raygen(rays, ph, kw["spp"], kw["seed"], kw["origin_offset"], kw.get("ray_tmax", 1e6))
     _, st = sc.gi_frame(rays_to_device(rays), gi_params(**kw), layout=L.LAYOUT_BVH8Q, stats=True)
