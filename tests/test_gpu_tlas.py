@@ -217,3 +217,34 @@ def test_tlas_rebuilt_with_entities(ctx):
     want = O.OracleScene(O.ORC_STACKLESS, v, t, n, e[::-1].copy()).closest(rays, tie=O.ORC_TIE_FIRST_FOUND)
     assert_hits_identical(hits_from_device(sc.closest(rays_to_device(rays), tie=L.TIE_FIRST_FOUND)), want,
                           "reversed entities")
+
+
+def test_tlas_exact_ties_across_entities(ctx):
+    """Two instances of one object with identical transforms give equal (t, triangle) hits: the
+    lower entity must win, as in the reference's loop.  BVH8 closest hits walk the candidates
+    nearest first (the duplicates' boxes are equal), strict BVH2 in entity order; both equal the
+    oracle's loop."""
+    ri = R.RayIntersector(R.STACK)
+    ri.add_object(1, [mesh("ico2")])
+    ri.add_object(2, [mesh("hf32")])
+    M = S.instance_transforms(6, (-2.0, -2.0, 0.0), (2.0, 2.0, 0.5), 0.5, 1.0, seed=17, tilt=0.05)
+    order = [(2, 0), (1, 1), (2, 2), (1, 3), (1, 1), (2, 4)]   # entity 4 duplicates entity 1
+    for obj, k in order:
+        ri.push_entity(obj, model=M[k].astype(np.float64))
+    ri.buffer_entities()
+    v, t, n, e = ri.global_buffers()
+    osc = O.OracleScene(O.ORC_STACK, v, t, n, e)
+    sc = ctx.scene(R.STACK, v, t, n, e)
+    sc.build_bvh8()
+    assert sc.tlas_info()["nodes"] > 0
+    rays = S.sphere_rays(20_000, (-2.5, -2.5, -0.3), (2.5, 2.5, 1.5), seed=19)
+    want = osc.closest(rays)
+    hit_dup = np.isin(want["entity"], [1, 4])
+    assert hit_dup.sum() > 200 and not (want["entity"] == 4).any()    # the loop keeps entity 1
+    d = rays_to_device(rays)
+    for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1)):
+        got = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, **kw))
+        for f in ("t", "u", "v", "w", "tri", "mesh", "entity"):
+            np.testing.assert_array_equal(got[f].view(np.uint32), want[f].view(np.uint32), err_msg=f"{kw} {f}")
+        strict = hits_from_device(sc.closest(d, **kw))
+        assert_hits_identical(strict, want, f"strict {kw}")
