@@ -19,9 +19,9 @@ __device__ __forceinline__ void load_ray(const rq_ray* rays, int64_t i, float4& 
 
 __device__ __forceinline__ void store_hit(rq_hit* hits, int64_t i, const rq_hit& h) {
     float4* p = reinterpret_cast<float4*>(hits) + 2 * i;
-    p[0] = make_float4(h.t, h.u, h.v, h.w);
-    p[1] = make_float4(__int_as_float(h.tri), __int_as_float(h.mesh), __int_as_float(h.entity),
-                       __int_as_float(h.iters));
+    __stcs(p, make_float4(h.t, h.u, h.v, h.w));
+    __stcs(p + 1, make_float4(__int_as_float(h.tri), __int_as_float(h.mesh), __int_as_float(h.entity),
+                              __int_as_float(h.iters)));
 }
 
 // Closest-hit record of a BVH8 query: barycentrics from the hit point with the strict arithmetic
