@@ -299,3 +299,24 @@ def test_textured_shading_matches_oracle(ctx, srgb, wrap):
                                         mesh_texture=mesh_tex, albedo_of=alb_fn)
     got_px = sc.gi_frame(rays_to_device(rays), pb).cpu().numpy()
     np.testing.assert_allclose(got_px, want_px, rtol=SHADE_RTOL * 8, atol=1e-6)
+
+
+def test_gi_frame_pinned_large_equals_device_pass(ctx):
+    """A frame of several host chunks with pinned host rays on the BVH8 layout (the primary launch
+    reads them over the host link, the pixels return in chunks while later chunks are shaded):
+    pixels and ray counts equal the device frame."""
+    import torch
+    from candela_gb300 import _lib as L
+    bufs = single_object("ico2", R.STACK)
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(np.random.default_rng(2).uniform(0.2, 0.9, (7, 3)).astype(np.float32))
+    sc.build_bvh8()
+    rays = S.camera_rays(1024, 520, eye=(0.0, -4.0, 2.0), target=(0.0, 0.0, 0.3))    # 532,480 pixels
+    p = gi_params(spp=2, seed=5, origin_offset=0.05, shadow_rays=True)
+    want, st_want = sc.gi_frame(rays_to_device(rays), p, layout=L.LAYOUT_BVH8Q, stats=True)
+    pinned = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
+    out = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory().numpy()
+    _, st_got = sc.gi_frame(pinned, p, out=out, layout=L.LAYOUT_BVH8Q, stats=True)
+    np.testing.assert_array_equal(out.view(np.uint32), want.cpu().numpy().view(np.uint32))
+    assert st_got == st_want
+    assert 0.1 < st_want["primary_hits"] / len(rays) < 0.9
