@@ -11,8 +11,8 @@
 * glsl_pins.json — SHA-256 of the outputs of the reference's own shaders compiled as C++
   (oracle/_ref/librefglsl.so, built by oracle/Makefile from the mounted reference tree) on seeded
   inputs: closest hits and occlusion on both layouts, closest hits over transformed and
-  translucent entities, collision records, the diffuse and specular shading sums and three frames
-  of the probe update.  Needs the reference tree; tests/test_golden_glsl.py then checks that the
+  translucent entities, collision records, GetData's surface values, the diffuse and specular
+  shading sums and three frames of the probe update.  Needs the reference tree; tests/test_golden_glsl.py then checks that the
   restatement reproduces every one of them, on any machine.
 """
 from __future__ import annotations
@@ -152,6 +152,29 @@ def glsl_case_outputs(reference: bool) -> dict:
             rec = O.OracleScene(olay, *bufs).collide(boxes, flags=O.ORC_FLAG_REF_COMPAT)
         rec = np.where(rec[:, :1] == 1, rec, np.int32([[0, -1, -1, -1]])).astype(np.int32)
         out[f"collide_ico2_{lname}"] = rec
+    # GetData: interpolated normal, the UV a textured mesh samples at (the harness texture() reports
+    # (u, v, texture index)), the ModelColor of untextured meshes, emissive and alpha
+    m = S.heightfield(32, seed=5)
+    pos = m.positions().astype(np.float64)
+    verts = S.with_texcoords(m.vertices, np.stack([pos[:, 0] * 1.7 + 0.3, pos[:, 1] * -2.1], 1))
+    mids = (np.arange(m.n_tris) % 3).astype(np.int32)
+    b = R.build_bvh(verts, m.indices, mids, 0, layout=R.STACK)
+    ents = R.identity_entity(0, b.nodes.shape[0], emissive=0.25, alpha=0.75)
+    gsc = O.OracleScene(O.ORC_STACK, verts, b.tris, b.nodes, ents)
+    ghits = gsc.closest(S.camera_rays(64, 48, **S.C1_CAMERA))
+    ghits = ghits[ghits["t"] > 0]
+    gmodel = np.float32([[0.7, 0.6, 0.5], [0.2, 0.8, 0.4], [0.9, 0.9, 0.2]])
+    textured = np.isin(ghits["mesh"], [0, 2])
+    if reference:
+        g = O.ref_glsl_getdata(verts, b.tris, ents, gmodel, [5, -1, 9], ghits)
+    else:
+        g = np.zeros((ghits.shape[0], 8), dtype=np.float32)
+        g[:, :3] = gsc.hit_normal(ghits, 0)
+        g[textured, 3:5] = gsc.hit_uv(ghits[textured])
+        g[textured, 5] = np.where(ghits["mesh"][textured] == 0, 5.0, 9.0)
+        g[~textured, 3:6] = gsc.hit_albedo(ghits[~textured], gmodel)
+        g[:, 6], g[:, 7] = np.float32(0.25), np.float32(0.75)
+    out["getdata_hf32"] = g
     # shading sums and the probe update, fed the restatement's traversal and surface data (their
     # own parity with the shader is the closest-hit / GetData pins)
     bufs = single_object("hf32", R.STACK)

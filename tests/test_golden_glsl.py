@@ -1,5 +1,5 @@
 """The restatement against fixtures taken from the reference's own shaders: tests/golden/glsl_pins.json
-holds SHA-256 hashes of what TraverseBVHStack[less].glsl, CollideBVHStack[less].glsl, the shading
+holds SHA-256 hashes of what TraverseBVHStack[less].glsl (with GetData), CollideBVHStack[less].glsl, the shading
 statements of DiffuseTrace.glsl / SpecularTrace.glsl and UpdateRadianceProbes.glsl, compiled as C++
 from the reference tree, return on seeded inputs (tests/golden/make_golden.py).  The oracle must
 reproduce every hash; no reference tree is needed here."""
