@@ -449,10 +449,11 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
 __global__ void k_bounce_init(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                               const uint8_t* __restrict__ occl, const unsigned long long* count, int64_t n_max,
                               const Materials mat, GiArgs a,
-                              float4* __restrict__ rad, float4* __restrict__ thr) {
+                              float4* __restrict__ rad, float4* __restrict__ thr, float4* __restrict__ bnc) {
     const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= n) return;
+    bnc[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // Bounced = vec3(0.0f) (:499)
     float4 h0;
     int4 h1;
     get_hit(hits, c, h0, h1);
@@ -510,13 +511,14 @@ __global__ void k_bounce_raygen(SceneView s, const rq_ray* __restrict__ prev_ray
     out_slot[j] = c;
 }
 
-// Bounce shading of compact segment k (GI slot slot[k]): rad += (GetDirect + emissive) *
-// throughput, throughput *= albedo; a miss adds 1.1 x sky x throughput (nothing under ref_miss, as
-// the reference) and ends the path.
+// Bounce shading of compact segment k (GI slot slot[k]): Bounced += (GetDirect + emissive) *
+// throughput, throughput *= albedo (:524, :530); a miss adds 1.1 x sky x throughput (nothing under
+// ref_miss, as the reference) and ends the path.  Bounced joins the slot's radiance once, after the
+// last bounce (FinalRadiance += Bounced, :535), in k_gather_accumulate.
 __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                                const uint8_t* __restrict__ occl, const int32_t* __restrict__ slot,
                                const unsigned long long* count, int64_t n_max, const Materials mat, GiArgs a,
-                               int ref_miss, float4* __restrict__ rad, float4* __restrict__ thr,
+                               int ref_miss, float4* __restrict__ bnc, float4* __restrict__ thr,
                                unsigned long long* hit_count) {
     const int64_t n = static_cast<int64_t>(*count) < n_max ? static_cast<int64_t>(*count) : n_max;
     const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -527,7 +529,7 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
         float4 h0;
         int4 h1;
         get_hit(hits, k, h0, h1);
-        float4 R = rad[c];
+        float4 R = bnc[c];
         if (h0.x > 0.0f) {
             const f3 rd = strict::xyz(__ldg(reinterpret_cast<const float4*>(rays) + 2 * k + 1));
             const float l = occl ? (occl[k] ? 0.0f : 1.0f) : 1.0f;
@@ -546,7 +548,7 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
             }
             T.w = 0.0f;
         }
-        rad[c] = R;
+        bnc[c] = R;
         thr[c] = T;
     }
     if (hit_count) {
@@ -555,15 +557,24 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
     }
 }
 
-// Per-pixel mean of the slots' radiance (summed in sample order; inactive samples add 0).
-__global__ void k_gather_accumulate(const float4* __restrict__ rad, const int32_t* __restrict__ comp_of,
-                                    int64_t n, int32_t spp, float4* __restrict__ pixels) {
+// Per-pixel mean of the slots' radiance (summed in sample order; inactive samples add 0), each
+// slot's radiance being its first hit's plus the bounces' (FinalRadiance += Bounced).
+__global__ void k_gather_accumulate(const float4* __restrict__ rad, const float4* __restrict__ bnc,
+                                    const int32_t* __restrict__ comp_of, int64_t n, int32_t spp,
+                                    float4* __restrict__ pixels) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int k = 0; k < spp; ++k) {
         const int32_t c = __ldg(comp_of + i * spp + k);
-        const float4 v = c >= 0 ? __ldg(rad + c) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (c >= 0) {
+            v = __ldg(rad + c);
+            const float4 b = __ldg(bnc + c);
+            v.x = __fadd_rn(v.x, b.x);
+            v.y = __fadd_rn(v.y, b.y);
+            v.z = __fadd_rn(v.z, b.z);
+        }
         acc.x = __fadd_rn(acc.x, v.x);
         acc.y = __fadd_rn(acc.y, v.y);
         acc.z = __fadd_rn(acc.z, v.z);
@@ -705,15 +716,17 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     // RT second-bounce loop: per compact slot its sample index, radiance and path throughput
     const bool bounce = p.query == 0 && p.bounces > 0;
     int32_t* samp_of = nullptr;
-    float4 *rad = nullptr, *thr = nullptr;
+    float4 *rad = nullptr, *thr = nullptr, *bnc = nullptr;
     if (bounce) {
         void *d_samp = nullptr, *d_rad = nullptr, *d_thr = nullptr;
+        void* d_bnc = nullptr;
         if ((s = scratch(ctx, 8, 4 * m, &d_samp)) != RQ_OK || (s = scratch(ctx, 10, 16 * m, &d_rad)) != RQ_OK ||
-            (s = scratch(ctx, 15, 16 * m, &d_thr)) != RQ_OK)
+            (s = scratch(ctx, 15, 16 * m, &d_thr)) != RQ_OK || (s = scratch(ctx, 12, 16 * m, &d_bnc)) != RQ_OK)
             return s;
         samp_of = static_cast<int32_t*>(d_samp);
         rad = static_cast<float4*>(d_rad);
         thr = static_cast<float4*>(d_thr);
+        bnc = static_cast<float4*>(d_bnc);
     }
     // phase 1.  Host rays in pinned memory on the BVH8 layout: the primary launch reads them over
     // the host link itself and stores the device copy the later kernels read, so the transfer
@@ -784,7 +797,8 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
             return s;
         unsigned long long* bcount = static_cast<unsigned long long*>(d_bc);
         RQ_CUDA(ctx, cudaMemsetAsync(bcount, 0, sizeof(unsigned long long) * p.bounces, st));
-        k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, materials_of(sc), a, rad, thr);
+        k_bounce_init<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, vis, count, m, materials_of(sc), a, rad, thr,
+                                                    bnc);
         RQ_CUDA(ctx, cudaGetLastError());
         QueryConfig qb = q;  // bounces use IntersectRay, not the ignore-transparent variant
         qb.flags &= ~RQ_FLAG_IGNORE_TRANSPARENT;
@@ -813,7 +827,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
                 bvis = occ;
             }
             k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, brays, shit, bvis, bslot, bc, m, materials_of(sc), a,
-                                                         (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0, rad, thr,
+                                                         (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0, bnc, thr,
                                                          stats ? cnt + 7 : nullptr);
             RQ_CUDA(ctx, cudaGetLastError());
             prev_rays = brays;
@@ -831,7 +845,8 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     for (int64_t off = 0; off < n; off += chunk) {
         const int64_t c = std::min(chunk, n - off);
         if (bounce)
-            k_gather_accumulate<<<grid(c, 256), 256, 0, st>>>(rad, comp_of + off * p.spp, c, p.spp, pixels4 + off);
+            k_gather_accumulate<<<grid(c, 256), 256, 0, st>>>(rad, bnc, comp_of + off * p.spp, c, p.spp,
+                                                              pixels4 + off);
         else if (p.unfused)
             k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, pixels4 + off);
         else

@@ -146,6 +146,7 @@ def orc() -> C.CDLL:
         L.orc_probe_raygen.argtypes = [pp, C.c_int, P]
         L.orc_probe_direction.argtypes = [C.c_uint32, P, I64, P]
         L.orc_probe_shade.argtypes = [sp, pp, P, P, P, C.POINTER(OrcMaterials), P, P, P, P, P, C.c_int]
+        L.orc_bounce_accumulate.argtypes = [P, P, P, I64, I32, P, P, P, C.c_int, P]
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
         L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -355,6 +356,21 @@ def pcg_hash(x: int) -> int:
     return orc().orc_pcg_hash(x & 0xFFFFFFFF)
 
 
+def bounce_accumulate(fr, thr0, inputs, sun_dir, sun_color, sky, ref_miss):
+    """FinalRadiance + Bounced of the RT second-bounce loop (DiffuseTrace.glsl:499-535) per GI slot:
+    fr, thr0 (n, 3); inputs (n, bounces, 12) {t, albedo rgb, emissive, normal xyz, direction xyz,
+    sun visibility}."""
+    fr = np.ascontiguousarray(fr, dtype=np.float32)
+    th = np.ascontiguousarray(thr0, dtype=np.float32)
+    x = np.ascontiguousarray(inputs, dtype=np.float32)
+    f3 = lambda v: np.ascontiguousarray(v, dtype=np.float32)  # noqa: E731
+    sd, sc, sk = f3(sun_dir), f3(sun_color), f3(sky)
+    out = np.empty((fr.shape[0], 3), dtype=np.float32)
+    orc().orc_bounce_accumulate(_p(fr), _p(th), _p(x), fr.shape[0], x.shape[1], _p(sd), _p(sc), _p(sk),
+                                int(bool(ref_miss)), _p(out))
+    return out
+
+
 def pcg_hash_np(x):
     """pcg_hash over a uint32 array (numpy arithmetic wraps like the C one)."""
     x = np.asarray(x, dtype=np.uint32)
@@ -546,6 +562,24 @@ def ref_glsl_probe(p, rays, hits, albedo, normals, lit, prev_sh, prev_raw, probe
     L.ref_glsl_probe(_p(grid), _p(org), _p(prev), _p(size), int(p.temporal), _p(sd), _p(sc), _p(sk), _p(x), _p(psh),
                      _p(praw), _p(pmap), _p(osh), _p(oraw))
     return osh, oraw, pmap
+
+
+def ref_glsl_bounce(slot, per_bounce, sun_dir, sun_color, sky):
+    """The RT second-bounce loop (DiffuseTrace.glsl:499-535) compiled as C++ per GI slot: slot
+    (n, 20) {GI ray origin, direction, TUVW, Albedo, faced normal, FinalRadiance}; per_bounce
+    (n, bounces, 15) {direction, TUVW, Albedo, normal, sun visibility}.  Returns (FinalRadiance
+    (n, 3), bounce ray origins (n, bounces, 3))."""
+    L = C.CDLL(str(REF_GLSL_SO))
+    L.ref_glsl_bounce.restype = None
+    L.ref_glsl_bounce.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_int64] + [C.c_void_p] * 5
+    sl = np.ascontiguousarray(slot, dtype=np.float32)
+    pb = np.ascontiguousarray(per_bounce, dtype=np.float32)
+    f3 = lambda v: np.ascontiguousarray(v, dtype=np.float32)  # noqa: E731
+    sd, sc, sk = f3(sun_dir), f3(sun_color), f3(sky)
+    fr = np.empty((sl.shape[0], 3), dtype=np.float32)
+    org = np.empty((sl.shape[0], pb.shape[1], 3), dtype=np.float32)
+    L.ref_glsl_bounce(pb.shape[1], _p(sl), _p(pb), sl.shape[0], _p(sd), _p(sc), _p(sk), _p(fr), _p(org))
+    return fr, org
 
 
 def ref_glsl_lambert_direction(h):

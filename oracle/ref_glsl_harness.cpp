@@ -330,6 +330,44 @@ extern "C" void ref_glsl_probe_sun_color(float* out3) {
     out3[2] = c.z;
 }
 
+// The RT second-bounce loop (DiffuseTrace.glsl:499-535) per GI slot.  slot: 20 floats {GI ray
+// origin, direction, TUVW, Albedo (rgb, emissive), faced normal, FinalRadiance before the loop};
+// per bounce (n_bounces <= 8): 15 floats {direction, TUVW, Albedo, normal as GetData returns it,
+// sun visibility}.  out_fr: FinalRadiance after the loop; out_org: the origin of each bounce ray.
+extern "C" void ref_glsl_bounce(int32_t n_bounces, const float* slot, const float* per_bounce, int64_t n,
+                                const float* sun_dir, const float* sun, const float* sky, float* out_fr,
+                                float* out_org) {
+    namespace G = glsl_bounce;
+    G::u_SunDirection = glsl::vec3(sun_dir[0], sun_dir[1], sun_dir[2]);
+    G::g_sun = glsl::vec3(sun[0], sun[1], sun[2]);
+    G::g_sky = glsl::vec3(sky[0], sky[1], sky[2]);
+    G::u_SecondaryBounces = n_bounces;
+    for (int64_t i = 0; i < n; ++i) {
+        const float* x = slot + 20 * i;
+        for (int k = 0; k < n_bounces; ++k) {
+            const float* y = per_bounce + (i * n_bounces + k) * 15;
+            G::g_dir[k] = glsl::vec3(y[0], y[1], y[2]);
+            G::g_tuvw[k] = glsl::vec4(y[3], y[4], y[5], y[6]);
+            G::g_alb[k] = glsl::vec4(y[7], y[8], y[9], y[10]);
+            G::g_nrm[k] = glsl::vec3(y[11], y[12], y[13]);
+            G::g_lit[k] = y[14];
+            G::g_org[k] = glsl::vec3(0.0f);
+        }
+        G::g_k = 0;
+        glsl::vec3 fr(x[17], x[18], x[19]);
+        G::bounce(glsl::vec3(x[0], x[1], x[2]), glsl::vec3(x[3], x[4], x[5]), glsl::vec4(x[6], x[7], x[8], x[9]),
+                  glsl::vec4(x[10], x[11], x[12], x[13]), glsl::vec3(x[14], x[15], x[16]), fr);
+        out_fr[3 * i] = fr.x;
+        out_fr[3 * i + 1] = fr.y;
+        out_fr[3 * i + 2] = fr.z;
+        for (int k = 0; k < n_bounces; ++k) {
+            out_org[(i * n_bounces + k) * 3] = G::g_org[k].x;
+            out_org[(i * n_bounces + k) * 3 + 1] = G::g_org[k].y;
+            out_org[(i * n_bounces + k) * 3 + 2] = G::g_org[k].z;
+        }
+    }
+}
+
 // SUN_COLOR_DIFF and SUN_COLOR_SPEC of ColorConstants.h as the shaders evaluate them.
 extern "C" void ref_glsl_sun_colors(float* out6) {
     const glsl::vec3 a = glsl_diffuse_shade::sun_color_constant(), b = glsl_specular_shade::sun_color_constant();

@@ -24,6 +24,8 @@
 //    and the specular pass's (SpecularTrace.glsl:554-563, 588-596 with SampleLighting, Sky,
 //    IsValid, the clamp and the t / 48 store), compiled the same way with the renderer state they
 //    read (shadow-map lookup, probe volume, sky textures) given as values: bit for bit;
+//  * the RT second-bounce loop (DiffuseTrace.glsl:499-535) the same way, fed the restatement's
+//    per-bounce hits: bounce ray origins and FinalRadiance + Bounced bit for bit;
 //  * the BVH constructor (ref_bvh_harness.cpp), byte for byte.
 // Parity unpinned for the texture filter only: the reference samples through bindless GL
 // samplers, which cannot run here, so bilinear filtering, wrap modes and the sRGB decode are
@@ -1459,6 +1461,45 @@ void orc_probe_shade(const orc_scene* sc, const orc_probe_params* p, const orc_r
             r[3] = 0.0f;
         }
     });
+}
+
+}  // extern "C"
+
+// ---- RT second-bounce loop accumulation (DiffuseTrace.glsl:499-535) -----------------------
+
+extern "C" {
+
+// Per GI slot: fr = the first hit's radiance (FinalRadiance), thr0 = its albedo (Throughput);
+// per bounce b < n_bounces of slot i, in = 12 floats {t (< 0: miss), albedo rgb, emissive,
+// GetData normal xyz, direction xyz, sun visibility}.  Bounced starts at 0; a hit adds
+// (GetDirect + albedo x emissive) x Throughput (:524) and multiplies Throughput by the albedo
+// (:530); a miss adds nothing under ref_miss (the shader's GetDirect of a zero albedo) or
+// 1.1 x sky x Throughput otherwise, and ends the path.  out = FinalRadiance + Bounced (:535).
+void orc_bounce_accumulate(const float* fr, const float* thr0, const float* in, int64_t n, int32_t n_bounces,
+                           const float sun_dir[3], const float sun_color[3], const float sky[3], int ref_miss,
+                           float* out3) {
+    const V3 sd = ld3(sun_dir), sun = ld3(sun_color), sk = ld3(sky);
+    for (int64_t i = 0; i < n; ++i) {
+        V3 b = {0.0f, 0.0f, 0.0f}, t = ld3(thr0 + 3 * i);
+        for (int32_t k = 0; k < n_bounces; ++k) {
+            const float* x = in + (i * n_bounces + k) * 12;
+            if (!(x[0] > 0.0f)) {
+                if (!ref_miss) b = add(b, mul(muls(sk, 1.1f), t));
+                break;
+            }
+            const V3 alb = ld3(x + 1), d = ld3(x + 8);
+            V3 nrm = ld3(x + 5);
+            if (dot(nrm, d) > 0.0001f) nrm = neg(nrm);
+            const float ndl = clamp01(dot(nrm, neg(sd)));
+            const V3 v = add(muls(muls(mul(alb, sun), x[11]), ndl), muls(alb, x[4]));
+            b = add(b, mul(v, t));
+            t = mul(t, alb);
+        }
+        const V3 f = add(ld3(fr + 3 * i), b);
+        out3[3 * i] = f.x;
+        out3[3 * i + 1] = f.y;
+        out3[3 * i + 2] = f.z;
+    }
 }
 
 }  // extern "C"

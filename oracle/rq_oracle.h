@@ -149,6 +149,13 @@ void orc_probe_shade(const orc_scene* s, const orc_probe_params* p, const orc_ra
                      const uint8_t* lit, const orc_materials* mat, const uint32_t* prev_sh, const float* prev_raw,
                      float* probe_map, uint32_t* out_sh, float* out_raw, int nthreads);
 
+// The RT second-bounce loop's accumulation for n GI slots (DiffuseTrace.glsl:499-535): fr and thr0
+// 3 floats per slot, in 12 floats per slot and bounce {t, albedo rgb, emissive, normal xyz,
+// direction xyz, sun visibility}; out3 = FinalRadiance + Bounced.
+void orc_bounce_accumulate(const float* fr, const float* thr0, const float* in, int64_t n, int32_t n_bounces,
+                           const float sun_dir[3], const float sun_color[3], const float sky[3], int ref_miss,
+                           float* out3);
+
 uint32_t orc_pcg_hash(uint32_t x);
 void orc_sincos_turns(float x, float* s, float* c);
 // CosWeightedHemisphere (Sampling.glsl:1-12) with the turn-based sine / cosine, n normals.

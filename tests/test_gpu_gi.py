@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import candela_gb300 as R
+from oracle import oracle as O
 from candela_gb300 import scenes as S
 from candela_gb300.engine import gi_params
 
@@ -189,8 +190,9 @@ def test_gi_frame_host_chunks_equal_device_pass(ctx, query):
 
 def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0, textures=None,
                         mesh_texture=None, albedo_of=None):
-    """The GI pass with the RT second-bounce loop, composed from the oracle's pieces in the
-    kernels' operation order (float32 numpy arithmetic, one rounding per operation)."""
+    """The GI pass with the RT second-bounce loop, composed from the oracle's pieces: rays, hits and
+    shading per bounce, then the loop's accumulation (FinalRadiance + Bounced,
+    oracle.bounce_accumulate, pinned to the shader's loop) and the per-pixel mean."""
     f = np.float32
     spp, seed = p.spp, p.seed
     sd, sc_, sky = np.array(p.sun_dir), np.array(p.sun_color), np.array(p.sky_color, np.float32)
@@ -201,8 +203,11 @@ def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0, textur
     tex = dict(textures=textures, mesh_texture=mesh_texture)
     rad = osc.shade(sec, sh, lit, albedo, sd, sc_, sky, **tex).astype(np.float32)
     alb_of = albedo_of or (lambda hits: osc.hit_albedo(hits, albedo))  # noqa: E731
+    emissive = osc.entities["data"][:, 0].view(np.float32)
     alive = sh["t"] > 0
-    thr = np.where(alive[:, None], alb_of(sh), f(0)).astype(np.float32)
+    thr0 = np.where(alive[:, None], alb_of(sh), f(0)).astype(np.float32)
+    inputs = np.zeros((len(sec), max(bounces, 1), 12), dtype=np.float32)
+    inputs[:, :, 0] = -1.0
     prev_r, prev_h = sec, sh
     sid = np.arange(len(sec), dtype=np.uint32)
     bflags = flags & ~R.engine.L.FLAG_IGNORE_TRANSPARENT
@@ -210,18 +215,22 @@ def _oracle_bounce_pass(osc, rays, p, albedo, bounces, ref_miss, flags=0, textur
     for b in range(bounces):
         br = osc.bounce_raygen(prev_r, prev_h, alive, sid, seed, b, 0.02, p.ray_tmax)
         bh = osc.closest(br, flags=bflags)
-        blit = 1 - osc.anyhit(osc.shadow_raygen(br, bh, sd, p.shadow_offset)) if p.shadow_rays else None
-        v = osc.shade(br, bh, blit, albedo, sd, sc_, sky, **tex).astype(np.float32)
+        blit = (1 - osc.anyhit(osc.shadow_raygen(br, bh, sd, p.shadow_offset))) if p.shadow_rays \
+            else np.ones(len(br), np.uint8)
         hit = alive & (bh["t"] > 0)
-        miss = alive & ~(bh["t"] > 0)
         n_rays += int(alive.sum())
         n_hits += int(hit.sum())
-        rad[hit, :3] = rad[hit, :3] + v[hit, :3] * thr[hit]
-        if not ref_miss:
-            rad[miss, :3] = rad[miss, :3] + (sky * f(1.1)) * thr[miss]
-        thr[hit] = thr[hit] * alb_of(bh[hit])
+        x = inputs[:, b]
+        x[hit, 0] = bh["t"][hit]
+        x[hit, 1:4] = alb_of(bh[hit])
+        x[hit, 4] = emissive[bh["entity"][hit]]
+        x[hit, 5:8] = osc.hit_normal(bh[hit], p.normal_mode)
+        x[hit, 8:11] = br["d"][hit]
+        x[hit, 11] = blit[hit]
         alive = hit
         prev_r, prev_h = br, bh
+    if bounces:
+        rad[:, :3] = O.bounce_accumulate(rad[:, :3], thr0, inputs[:, :bounces], sd, sc_, sky, ref_miss)
     rad = np.where((sec["tmax"] > sec["tmin"])[:, None], rad, f(0))
     acc = np.zeros((len(rays), 4), np.float32)
     r3 = rad.reshape(len(rays), spp, 4)

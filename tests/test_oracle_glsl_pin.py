@@ -312,3 +312,62 @@ def test_probe_direction_matches_reference_sampler():
         h = np.stack([O.sample_u01(seed, ids, 0), O.sample_u01(seed, ids, 1), np.full(ids.shape, 0.5, np.float32)], 1)
         d = np.abs(ours - O.ref_glsl_lambert_direction(h)).max(1)
         assert d.max() < 1e-6 and np.median(d) < 1e-7
+
+
+def test_bounce_loop_matches_reference_shader():
+    """The RT second-bounce loop (DiffuseTrace.glsl:499-535) compiled as C++, fed the restatement's
+    GI hits, bounce directions, bounce hits (GetData values) and shadow answers: the bounce ray
+    origins (HitPosition + iNormal * 0.02) and FinalRadiance + Bounced equal the restatement's
+    (orc_bounce_raygen, orc_bounce_accumulate with the reference's silent misses) bit for bit."""
+    osc, rays, hits, model, alb, nrm, lit = _shading_scene()
+    sd, sun, sky = np.float32([0.3, 0.4, -0.866]), np.float32([4.0, 3.8, 3.5]), np.float32([0.45, 0.6, 0.95])
+    bounces, seed = 3, 13
+    sec = osc.gi_raygen(rays, hits, 1, seed, 0.05)
+    sh = osc.closest(sec)
+    emissive = osc.entities["data"][:, 0].view(np.float32)
+    glit = 1 - osc.anyhit(osc.shadow_raygen(sec, sh, sd, 1e-3))
+    fr = osc.shade(sec, sh, glit, model, sd, sun, sky)[:, :3]
+    alive = sh["t"] > 0
+    n = len(sec)
+    slot = np.zeros((n, 20), dtype=np.float32)
+    slot[:, 0:3], slot[:, 3:6] = sec["o"], sec["d"]
+    slot[:, 6], slot[:, 7], slot[:, 8], slot[:, 9] = sh["t"], sh["u"], sh["v"], sh["w"]
+    gn = np.full((n, 3), -1.0, dtype=np.float32)
+    gn[alive] = osc.hit_normal(sh[alive], 0)
+    flip = (gn * sec["d"]).astype(np.float32)
+    facing = (flip[:, 0] + flip[:, 1]) + flip[:, 2] > np.float32(0.0001)
+    gn[facing] = -gn[facing]
+    thr0 = np.zeros((n, 3), dtype=np.float32)
+    thr0[alive] = osc.hit_albedo(sh[alive], model)
+    slot[alive, 10:13] = thr0[alive]
+    slot[alive, 13] = emissive[sh["entity"][alive]]
+    slot[:, 14:17], slot[:, 17:20] = gn, fr
+    per = np.zeros((n, bounces, 15), dtype=np.float32)
+    per[:, :, 3:7] = -1.0
+    per[:, :, 11:14] = -1.0
+    ours_in = np.zeros((n, bounces, 12), dtype=np.float32)
+    ours_in[:, :, 0] = -1.0
+    prev_r, prev_h, live = sec, sh, alive.copy()
+    origins = []
+    for b in range(bounces):
+        br = osc.bounce_raygen(prev_r, prev_h, live, np.arange(n, dtype=np.uint32), seed, b, 0.02, 1e6)
+        bh = osc.closest(br)
+        blit = 1 - osc.anyhit(osc.shadow_raygen(br, bh, sd, 1e-3))
+        hit = live & (bh["t"] > 0)
+        per[live, b, 0:3] = br["d"][live]
+        per[hit, b, 3], per[hit, b, 4], per[hit, b, 5], per[hit, b, 6] = (bh["t"][hit], bh["u"][hit], bh["v"][hit],
+                                                                          bh["w"][hit])
+        balb = osc.hit_albedo(bh[hit], model)
+        per[hit, b, 7:10], per[hit, b, 10] = balb, emissive[bh["entity"][hit]]
+        bn = osc.hit_normal(bh[hit], 0)
+        per[hit, b, 11:14], per[:, b, 14] = bn, blit
+        ours_in[hit, b, 0], ours_in[hit, b, 1:4], ours_in[hit, b, 4] = bh["t"][hit], balb, emissive[bh["entity"][hit]]
+        ours_in[hit, b, 5:8], ours_in[hit, b, 8:11], ours_in[hit, b, 11] = bn, br["d"][hit], blit[hit]
+        origins.append((live.copy(), br["o"].copy()))
+        prev_r, prev_h, live = br, bh, hit
+    ours = O.bounce_accumulate(fr, thr0, ours_in, sd, sun, sky, ref_miss=True)
+    ref_fr, ref_org = O.ref_glsl_bounce(slot, per, sd, sun, sky)
+    np.testing.assert_array_equal(ours.view(np.uint32), ref_fr.view(np.uint32))
+    for b, (traced, o) in enumerate(origins):
+        np.testing.assert_array_equal(ref_org[traced, b].view(np.uint32), o[traced].view(np.uint32), err_msg=f"b{b}")
+    assert alive.sum() > 2000 and (ours != fr).any(1).mean() > 0.05 and origins[1][0].sum() > 100
