@@ -12,7 +12,7 @@
   (oracle/_ref/librefglsl.so, built by oracle/Makefile from the mounted reference tree) on seeded
   inputs: closest hits and occlusion on both layouts, closest hits over transformed and
   translucent entities, collision records, GetData's surface values, the diffuse and specular
-  shading sums and three frames of the probe update.  Needs the reference tree; tests/test_golden_glsl.py then checks that the
+  shading sums, the RT second-bounce loop and three frames of the probe update.  Needs the reference tree; tests/test_golden_glsl.py then checks that the
   restatement reproduces every one of them, on any machine.
 """
 from __future__ import annotations
@@ -196,6 +196,55 @@ def glsl_case_outputs(reference: bool) -> dict:
     else:
         out["shade_diffuse"] = osc.shade(rays, hits, lit, model, sun_dir, sun, sky * np.float32(2.0))
         out["shade_specular"] = osc.spec_shade(rays, hits, lit, model, 0.35, sun, sky, amb)
+    # the RT second-bounce loop: GI rays from the hits above, three bounces, the reference's silent
+    # misses; the bounce ray origins and FinalRadiance + Bounced
+    emissive = bufs[3]["data"][:, 0].view(np.float32)
+    sec = osc.gi_raygen(rays, hits, 1, 13, 0.05)
+    gh = osc.closest(sec)
+    glit = 1 - osc.anyhit(osc.shadow_raygen(sec, gh, sun_dir, 1e-3))
+    fr = osc.shade(sec, gh, glit, model, sun_dir, sun, sky)[:, :3]
+    live = gh["t"] > 0
+    nb, ns = 3, len(sec)
+    thr0 = np.zeros((ns, 3), dtype=np.float32)
+    thr0[live] = osc.hit_albedo(gh[live], model)
+    slot = np.zeros((ns, 20), dtype=np.float32)
+    slot[:, 0:3], slot[:, 3:6] = sec["o"], sec["d"]
+    slot[:, 6], slot[:, 7], slot[:, 8], slot[:, 9] = gh["t"], gh["u"], gh["v"], gh["w"]
+    gn = np.full((ns, 3), -1.0, dtype=np.float32)
+    gn[live] = osc.hit_normal(gh[live], 0)
+    pr = (gn * sec["d"]).astype(np.float32)
+    gn[(pr[:, 0] + pr[:, 1]) + pr[:, 2] > np.float32(0.0001)] *= np.float32(-1.0)
+    slot[live, 10:13], slot[live, 13] = thr0[live], emissive[gh["entity"][live]]
+    slot[:, 14:17], slot[:, 17:20] = gn, fr
+    per = np.zeros((ns, nb, 15), dtype=np.float32)
+    per[:, :, 3:7], per[:, :, 11:14] = -1.0, -1.0
+    acc_in = np.zeros((ns, nb, 12), dtype=np.float32)
+    acc_in[:, :, 0] = -1.0
+    org = np.zeros((ns, nb, 3), dtype=np.float32)
+    prev_r, prev_h = sec, gh
+    for b in range(nb):
+        br = osc.bounce_raygen(prev_r, prev_h, live, np.arange(ns, dtype=np.uint32), 13, b, 0.02, 1e6)
+        bh = osc.closest(br)
+        blit = 1 - osc.anyhit(osc.shadow_raygen(br, bh, sun_dir, 1e-3))
+        hit = live & (bh["t"] > 0)
+        org[live, b] = br["o"][live]
+        per[live, b, 0:3] = br["d"][live]
+        per[hit, b, 3], per[hit, b, 4], per[hit, b, 5], per[hit, b, 6] = (bh["t"][hit], bh["u"][hit],
+                                                                          bh["v"][hit], bh["w"][hit])
+        balb, bn = osc.hit_albedo(bh[hit], model), osc.hit_normal(bh[hit], 0)
+        per[hit, b, 7:10], per[hit, b, 10], per[hit, b, 11:14] = balb, emissive[bh["entity"][hit]], bn
+        per[:, b, 14] = blit
+        acc_in[hit, b, 0], acc_in[hit, b, 1:4], acc_in[hit, b, 4] = bh["t"][hit], balb, emissive[bh["entity"][hit]]
+        acc_in[hit, b, 5:8], acc_in[hit, b, 8:11], acc_in[hit, b, 11] = bn, br["d"][hit], blit[hit]
+        prev_r, prev_h, live_next = br, bh, hit
+        live = live_next
+    traced = per[:, :, 0:3].any(2)
+    if reference:
+        bfr, borg = O.ref_glsl_bounce(slot, per, sun_dir, sun, sky)
+    else:
+        bfr, borg = O.bounce_accumulate(fr, thr0, acc_in, sun_dir, sun, sky, True), org
+    out["bounce_loop"] = np.concatenate([bfr.view(np.int32),
+                                         np.where(traced[:, :, None], borg, np.float32(0)).reshape(ns, -1).view(np.int32)], 1)
     origins = [(0.0, 0.0, 0.4), (0.07, -0.05, 0.42), (0.15, 0.02, 0.38)]
     sh, raw, pmap = probe_volumes(probe_params(grid=(8, 8, 4)))
     prev = origins[0]
