@@ -169,9 +169,20 @@ def combine_ranks(total_ms: float, rays_per_step: int, steps: int, world: int, d
     return total_ms, rays_per_step * steps * world / (total_ms / 1e3) / 1e6
 
 
-def make_workload(config: str):
-    import candela_gb300 as R
+class _OracleBVH:
+    """The BVH buffers of the oracle's restatement of the reference constructor, shaped like the
+    product's BVH objects (nodes, tris) for the CPU arms."""
+
+    def __init__(self, nodes, tris, info):
+        self.nodes, self.tris, self.info = nodes, tris, info
+
+
+def make_workload(config: str, builder: str = "product"):
+    """Scene, BVHs, rays and parameters of a workload.  builder "oracle": the BVHs come from the
+    oracle's restatement of the reference constructor (the CPU reference arm, which loads nothing of
+    the product); "product": from rq_build_bvh (the same bytes)."""
     from candela_gb300 import scenes as S
+    from candela_gb300.engine import identity_entity
     if config == "c1":
         mesh = S.c1_heightfield_scene()
         rays = S.camera_rays(512, 512, **S.C1_CAMERA)
@@ -186,11 +197,18 @@ def make_workload(config: str):
                 "closest-hit + 4 cosine diffuse-GI closest-hit rays per hit, Lambert shading, "
                 "stack BVH leaf 2, strict")
     t0 = time.perf_counter()
-    bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
-    build_s = time.perf_counter() - t0
-    ent = R.identity_entity(0, bvh.nodes.shape[0])
-    bvh_sl = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACKLESS)
-    ent_sl = R.identity_entity(0, bvh_sl.nodes.shape[0])
+    if builder == "oracle":
+        from oracle import oracle as O
+        bvh = _OracleBVH(*O.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, stackless=False))
+        build_s = time.perf_counter() - t0
+        bvh_sl = _OracleBVH(*O.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, stackless=True))
+    else:
+        import candela_gb300 as R
+        bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
+        build_s = time.perf_counter() - t0
+        bvh_sl = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACKLESS)
+    ent = identity_entity(0, bvh.nodes.shape[0])
+    ent_sl = identity_entity(0, bvh_sl.nodes.shape[0])
     n_mesh = int(mesh.mesh_ids.max()) + 1
     albedo = (0.25 + 0.65 * S.uniform(17, 5, n_mesh * 3)).astype(np.float32).reshape(-1, 3)
     return dict(mesh=mesh, bvh=bvh, ent=ent, bvh_sl=bvh_sl, ent_sl=ent_sl, rays=rays,
@@ -276,7 +294,7 @@ def cpu_baseline(wl, seconds: float):
         if time.perf_counter() - t0 >= seconds:
             break
     dt = time.perf_counter() - t0
-    return {"value": rays_done / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+    return {"value": rays_done / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port", "seconds": dt,
             "sample": f"{reps} whole GI passes over {len(prim)} of the primary rays (every "
                       f"{max(1, len(wl['rays']) // n)}th pixel), same scene/BVH/params, "
                       f"{dt:.1f} s on {nthreads} threads"}
@@ -288,6 +306,7 @@ def run_reference(args, wl, rank, world):
     res = cpu_baseline(wl, max(args.cpu_seconds, 1.0) * max(1, args.steps) / 10.0)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(res["seconds"] * 1e3 / max(1, args.steps), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": wl["name"]},
             "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -785,7 +804,7 @@ def main():
             return
         from oracle import oracle as O
         O.build(reference=False)
-        wl = make_workload(args.config)
+        wl = make_workload(args.config, builder="oracle")
         run_reference(args, wl, rank, world)
         return
 

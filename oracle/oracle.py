@@ -151,12 +151,42 @@ def orc() -> C.CDLL:
         L.orc_pcg_hash.restype = C.c_uint32
         L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.orc_cos_hemisphere.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        L.orc_brute_closest.argtypes = [sp, P, I64, P, P, C.c_int, C.c_int]
+        L.orc_build_bvh.restype = C.c_void_p
+        L.orc_build_bvh.argtypes = [P, I64, P, I64, P, I32, I32, I32, I32, C.c_uint32]
+        L.orc_bvh_info.argtypes = [P] + [C.POINTER(C.c_int64)] * 3
+        L.orc_bvh_copy.argtypes = [P, P, P]
+        L.orc_bvh_free.argtypes = [P]
         _orc = L
     return _orc
 
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def build_bvh(vertices, indices, mesh_ids=None, tri_offset=0, stackless=False, leaf_size=2,
+              swap_children=False, swap_seed=0):
+    """The restatement of the reference SAH constructor (orc_build.cpp): (nodes float32 (n, 16) or
+    (n, 8), triangles int32 (n_tris, 4), {"leaf_count", "split_fails"})."""
+    v = np.ascontiguousarray(vertices)
+    idx = np.ascontiguousarray(indices, dtype=np.uint32).ravel()
+    mid = None if mesh_ids is None else np.ascontiguousarray(mesh_ids, dtype=np.int32)
+    L = orc()
+    h = L.orc_build_bvh(_p(v), v.shape[0], _p(idx), idx.size, _p(mid), tri_offset, 1 if stackless else 0,
+                        leaf_size, 1 if swap_children else 0, swap_seed & 0xFFFFFFFF)
+    if not h:
+        raise ValueError("oracle BVH build rejected its input")
+    try:
+        vals = [C.c_int64() for _ in range(3)]
+        L.orc_bvh_info(h, *[C.byref(x) for x in vals])
+        n_nodes, leaves, fails = (x.value for x in vals)
+        nodes = np.empty((n_nodes, 8 if stackless else 16), dtype=np.float32)
+        tris = np.empty((idx.size // 3, 4), dtype=np.int32)
+        L.orc_bvh_copy(h, _p(nodes), _p(tris))
+    finally:
+        L.orc_bvh_free(h)
+    return nodes, tris, {"leaf_count": leaves, "split_fails": fails}
 
 
 class OracleScene:
@@ -187,6 +217,16 @@ class OracleScene:
         orc().orc_anyhit(C.byref(self.s), _p(rays), rays.shape[0], _p(occ),
                          nthreads or os.cpu_count() or 1, _p(it), _p(tt))
         return (occ, it, tt) if counters else occ
+
+    def brute_closest(self, rays, flags=0, nthreads=None):
+        """Every triangle of every entity tested (no box tests): (hits, occluded), the hit being the
+        lexicographic minimum of (t, triangle, entity).  Decides between two walks that disagree."""
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.empty(rays.shape[0], dtype=HIT_DTYPE)
+        occ = np.empty(rays.shape[0], dtype=np.uint8)
+        orc().orc_brute_closest(C.byref(self.s), _p(rays), rays.shape[0], _p(hits), _p(occ), flags,
+                                nthreads or os.cpu_count() or 1)
+        return hits, occ
 
     def gi_raygen(self, primary, hits, spp, seed, origin_offset, ray_tmax=1000000.0,
                   normal_mode=0, nthreads=None):

@@ -43,6 +43,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -1500,6 +1501,84 @@ void orc_bounce_accumulate(const float* fr, const float* thr0, const float* in, 
         out3[3 * i + 1] = f.y;
         out3[3 * i + 2] = f.z;
     }
+}
+
+
+// Brute force over every triangle of every entity (no box tests): the lexicographic minimum of
+// (t, triangle, entity) over tmin < t < tmax with the strict triangle test of RayTriangle
+// (TraverseBVHStack.glsl:87-105) on the entity-transformed ray, barycentrics as IntersectScene
+// reports them (:351-360).  A BVH walk can only lose hits to its box tests, so where a walk and
+// this disagree the brute force says which answer the triangle test supports.  occluded (nullable)
+// receives whether any such triangle exists.  flags: ORC_FLAG_IGNORE_TRANSPARENT.
+void orc_brute_closest(const orc_scene* sc, const orc_ray* rays, int64_t n, orc_hit* hits, uint8_t* occluded,
+                       int flags, int nthreads) {
+    const Scene s = make_scene(sc);
+    // leaf triangle ranges per entity, collected from every node of the entity's range
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> leaves(s.n_ents);
+    for (int i = 0; i < s.n_ents; ++i) {
+        const orc_entity& e = s.ents[i];
+        for (int64_t k = e.node_offset; k < (int64_t)e.node_offset + e.node_count && k < s.n_nodes; ++k) {
+            if (s.layout == ORC_STACK) {
+                const float* nd = s.nodes + k * 16;
+                for (int side = 0; side < 2; ++side) {
+                    const int32_t kind = f2i(nd[side * 8 + 3]);
+                    if (kind != -1 && (kind & 15) > 0) leaves[i].push_back({kind >> 4, kind & 15});
+                }
+            } else {
+                const int32_t kind = f2i(s.nodes[k * 8 + 3]);
+                if (kind != -1 && (kind & 15) > 0) leaves[i].push_back({kind >> 4, kind & 15});
+            }
+        }
+    }
+    parallel_for(n, nthreads, [&](int64_t b0, int64_t e0) {
+        for (int64_t r = b0; r < e0; ++r) {
+            const orc_ray& ray = rays[r];
+            orc_hit& h = hits[r];
+            h.t = h.u = h.v = h.w = -1.0f;
+            h.tri = h.mesh = h.entity = -1;
+            h.iters = 0;
+            if (occluded) occluded[r] = 0;
+            if (!(ray.tmax > ray.tmin)) continue;
+            const V3 o = ld3(ray.o), d = ld3(ray.d);
+            float bt = ray.tmax;
+            int32_t btri = -1, bent = -1, bmesh = -1;
+            bool any = false;
+            for (int i = 0; i < s.n_ents; ++i) {
+                const orc_entity& e = s.ents[i];
+                if ((flags & ORC_FLAG_IGNORE_TRANSPARENT) && ent_alpha(e) < 0.99f) continue;
+                const V3 ro = xform(e.inverse, o, 1.0f), rd = xform(e.inverse, d, 0.0f);
+                for (const auto& lf : leaves[i]) {
+                    for (int32_t idx = lf.first; idx < lf.first + lf.second; ++idx) {
+                        const int32_t* tr = s.tris + (int64_t)idx * 4;
+                        float t, u, v;
+                        ray_triangle(ro, rd, vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), t, u, v);
+                        if (!(t > ray.tmin) || !(t < ray.tmax)) continue;
+                        any = true;
+                        if (t < bt || (t == bt && (idx < btri || (idx == btri && i < bent)))) {
+                            bt = t;
+                            btri = idx;
+                            bent = i;
+                            bmesh = tr[3];
+                        }
+                    }
+                }
+            }
+            if (occluded) occluded[r] = any ? 1 : 0;
+            if (btri < 0) continue;
+            const orc_entity& e = s.ents[bent];
+            const V3 ro = xform(e.inverse, o, 1.0f), rd = xform(e.inverse, d, 0.0f);
+            const int32_t* tr = s.tris + (int64_t)btri * 4;
+            float u, v, w;
+            barycentrics(add(ro, muls(rd, bt)), vpos(s, tr[0]), vpos(s, tr[1]), vpos(s, tr[2]), u, v, w);
+            h.t = bt;
+            h.u = u;
+            h.v = v;
+            h.w = w;
+            h.tri = btri;
+            h.mesh = bmesh;
+            h.entity = bent;
+        }
+    });
 }
 
 }  // extern "C"

@@ -161,6 +161,12 @@ void orc_sincos_turns(float x, float* s, float* c);
 // CosWeightedHemisphere (Sampling.glsl:1-12) with the turn-based sine / cosine, n normals.
 void orc_cos_hemisphere(const float* normals, const float* r, int64_t n, float* out);
 
+// Brute force over every triangle of every entity, no box tests: the lexicographic minimum of
+// (t, triangle, entity) with tmin < t < tmax (strict triangle test); occluded (nullable) = any such
+// triangle.  Used to decide hits where two walks disagree.  flags: ORC_FLAG_IGNORE_TRANSPARENT.
+void orc_brute_closest(const orc_scene* s, const orc_ray* rays, int64_t n, orc_hit* hits, uint8_t* occluded,
+                       int flags, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,22 @@ def test_builder_matches_reference_golden_hashes(case):
     assert sha(b.nodes) == g["nodes_sha256"]
 
 
+@pytest.mark.parametrize("case", BUILDER_CASES, ids=[c[0] for c in BUILDER_CASES])
+def test_oracle_builder_matches_reference_golden_hashes(case):
+    """The oracle's restatement of the reference constructor (oracle/orc_build.cpp, which the CPU
+    reference arm of the benchmark builds with) reproduces the reference's output hashes."""
+    name, fn, stackless, leaf4, seed, off = case
+    m = fn()
+    g = GOLDEN[name]
+    nodes, tris, info = O.build_bvh(m.vertices, m.indices, m.mesh_ids, off, stackless=stackless,
+                                    leaf_size=4 if leaf4 else 2, swap_children=seed is not None,
+                                    swap_seed=seed or 0)
+    assert nodes.shape[0] == g["n_nodes"]
+    assert info["leaf_count"] == g["leaf_count"] and info["split_fails"] == g["split_fails"]
+    assert sha(tris) == g["tris_sha256"]
+    assert sha(nodes) == g["nodes_sha256"]
+
+
 needs_ref = pytest.mark.skipif(not O.ref_available(leaf4=True),
                                reason="reference tree not mounted (builder golden hashes still run)")
 
@@ -51,6 +67,11 @@ def test_builder_byte_identical_live_reference(layout, leaf, seed):
     assert np.array_equal(b.nodes.view(np.uint32), nodes.view(np.uint32))
     assert np.array_equal(b.tris, tris)
     assert b.leaf_count == info["leaf_count"] and b.split_fails == info["split_fails"]
+    o_nodes, o_tris, o_info = O.build_bvh(m.vertices, m.indices, m.mesh_ids, 123,
+                                          stackless=layout == R.STACKLESS, leaf_size=leaf,
+                                          swap_children=seed is not None, swap_seed=seed or 0)
+    assert np.array_equal(o_nodes.view(np.uint32), nodes.view(np.uint32))
+    assert np.array_equal(o_tris, tris) and o_info["split_fails"] == info["split_fails"]
 
 
 @needs_ref
@@ -71,6 +92,9 @@ def test_builder_signed_zero_and_degenerate_geometry():
         assert np.array_equal(b.nodes.view(np.uint32), nodes.view(np.uint32))
         assert np.array_equal(b.tris, tris)
         assert b.split_fails == info["split_fails"]
+        o_nodes, o_tris, o_info = O.build_bvh(v, idx, None, 0, stackless=layout == R.STACKLESS)
+        assert np.array_equal(o_nodes.view(np.uint32), nodes.view(np.uint32))
+        assert np.array_equal(o_tris, tris) and o_info["split_fails"] == info["split_fails"]
 
 
 def test_builder_multithreaded_equals_single_threaded():
