@@ -172,6 +172,9 @@ SIGNATURES = {
     "rq_scene_set_textures": (_S, [_P, _P, _I32, _P, _I32]),
     "rq_specular_frame": (_S, [_P, _P, _P, _I64, C.POINTER(RqSpecularParams), C.POINTER(RqOpts), _P, _P]),
     "rq_probe_update": (_S, [_P, _P, C.POINTER(RqProbeParams), _P, _P, _P, _P, _P, C.POINTER(RqOpts), _P]),
+    "rq_measure_read_gbs": (_S, [_P, _I64, _I32, C.POINTER(C.c_double)]),
+    "rq_hit_attribs": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
+    "rq_closest_attribs": (_S, [_P, _P, _P, _I64, _P, _P, C.POINTER(RqOpts), _P]),
 }
 
 NOALLOC_MAX_RAYS = 65536

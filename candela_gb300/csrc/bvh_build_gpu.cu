@@ -1172,7 +1172,7 @@ rq_status build_bvh_gpu(rq_ctx* ctx, const BuildInput& in, BuildOutput& out, std
         Arena m;
         carve(m, B, n, in.n_verts, in.mesh_ids != nullptr, in.layout);
         void* base = nullptr;
-        rq_status s = scratch(ctx, kBuildScratchSlot, m.used, &base);
+        rq_status s = scratch(ctx, rq::kSlotBuild, m.used, &base);
         if (s != RQ_OK) {
             why = "device allocation failed during GPU BVH build";
             return RQ_ENOMEM;

@@ -427,8 +427,8 @@ rq_status forward(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t n
     void* d_lpp = nullptr;
     void* d_part = nullptr;
     rq_status s;
-    if ((s = scratch(ctx, 16, sizeof(float) * n, &d_lpp)) != RQ_OK ||
-        (s = scratch(ctx, 17, sizeof(float) * 256, &d_part)) != RQ_OK)
+    if ((s = scratch(ctx, rq::kSlotLossPerPixel, sizeof(float) * n, &d_lpp)) != RQ_OK ||
+        (s = scratch(ctx, rq::kSlotLossPartials, sizeof(float) * 256, &d_part)) != RQ_OK)
         return s;
     k_diff_fwd<<<grid(n, 128), 128, 0, st>>>(sc->view, rays, n, reinterpret_cast<const float2*>(target),
                                               a, reinterpret_cast<float2*>(image), hits, gimg,
@@ -500,7 +500,7 @@ rq_status rq_fwd(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t n,
     t->bytes = static_cast<int64_t>(sizeof(float2) * n + (p->recompute ? 0 : 2 * sizeof(float4) * n));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     void* hits = t->d_hits;
-    if (p->recompute && (s = rq::scratch(ctx, 18, 2 * sizeof(float4) * n, &hits)) != RQ_OK) {
+    if (p->recompute && (s = rq::scratch(ctx, rq::kSlotTapeHits, 2 * sizeof(float4) * n, &hits)) != RQ_OK) {
         rq_tape_free(t);
         return s;
     }
@@ -527,10 +527,10 @@ rq_status rq_bwd(rq_ctx* ctx, rq_tape* t, float* grad, void* stream) {
     if (t->p.recompute) {  // re-trace: hits only (image and dloss/dimage are already known)
         void* h = nullptr;
         void *img = nullptr, *g2 = nullptr, *tg = nullptr;
-        if ((s = rq::scratch(ctx, 18, 2 * sizeof(float4) * n, &h)) != RQ_OK ||
-            (s = rq::scratch(ctx, 19, sizeof(float2) * n, &img)) != RQ_OK ||
-            (s = rq::scratch(ctx, 20, sizeof(float2) * n, &g2)) != RQ_OK ||
-            (s = rq::scratch(ctx, 21, sizeof(float2) * n, &tg)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotTapeHits, 2 * sizeof(float4) * n, &h)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotTapeImage, sizeof(float2) * n, &img)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotTapeGrad, sizeof(float2) * n, &g2)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotTapeTarget, sizeof(float2) * n, &tg)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaMemsetAsync(tg, 0, sizeof(float2) * n, st));
         if ((s = rq::forward(ctx, sc, t->rays, n, static_cast<float*>(tg), a, static_cast<float*>(img),
@@ -540,12 +540,12 @@ rq_status rq_bwd(rq_ctx* ctx, rq_tape* t, float* grad, void* stream) {
     }
     const int64_t nb = (n + rq::kTile - 1) / rq::kTile;
     void *contrib, *ka, *va, *kb, *vb, *hist, *segs, *sege;
-    if ((s = rq::scratch(ctx, 22, 9 * sizeof(float) * n, &contrib)) != RQ_OK ||
-        (s = rq::scratch(ctx, 23, 4 * n, &ka)) != RQ_OK || (s = rq::scratch(ctx, 24, 4 * n, &va)) != RQ_OK ||
-        (s = rq::scratch(ctx, 25, 4 * n, &kb)) != RQ_OK || (s = rq::scratch(ctx, 26, 4 * n, &vb)) != RQ_OK ||
-        (s = rq::scratch(ctx, 27, 4 * 256 * nb, &hist)) != RQ_OK ||
-        (s = rq::scratch(ctx, 28, 4 * (sc->n_tris + 1), &segs)) != RQ_OK ||
-        (s = rq::scratch(ctx, 29, 4 * (sc->n_tris + 1), &sege)) != RQ_OK)
+    if ((s = rq::scratch(ctx, rq::kSlotAdjContrib, 9 * sizeof(float) * n, &contrib)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotAdjKeysA, 4 * n, &ka)) != RQ_OK || (s = rq::scratch(ctx, rq::kSlotAdjValsA, 4 * n, &va)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotAdjKeysB, 4 * n, &kb)) != RQ_OK || (s = rq::scratch(ctx, rq::kSlotAdjValsB, 4 * n, &vb)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotAdjHist, 4 * 256 * nb, &hist)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotAdjSegStart, 4 * (sc->n_tris + 1), &segs)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotAdjSegEnd, 4 * (sc->n_tris + 1), &sege)) != RQ_OK)
         return s;
     const int32_t miss_key = static_cast<int32_t>(sc->n_tris);
     rq::k_adj_pixel<<<rq::grid(n, 128), 128, 0, st>>>(sc->view, t->rays, n, hits, t->d_gimg, a, miss_key,

@@ -284,6 +284,7 @@ rq_status rq_create(int device, rq_ctx** out) {
         rq_destroy(ctx);
         return s;
     }
+    rq::noalloc_resolve(ctx);  // reserves rq_gi_frame_noalloc's fixed array on this device
     *out = ctx;
     return RQ_OK;
 }
@@ -679,7 +680,7 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, 
     if (s != RQ_OK) return s;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
     void* out_buf = nullptr;
-    if ((s = rq::scratch(ctx, 9, query == 0 ? sizeof(rq_hit) * n : n, &out_buf)) != RQ_OK) return s;
+    if ((s = rq::scratch(ctx, rq::kSlotTuneOut, query == 0 ? sizeof(rq_hit) * n : n, &out_buf)) != RQ_OK) return s;
     cudaEvent_t a, b;
     RQ_CUDA(ctx, cudaEventCreate(&a));
     RQ_CUDA(ctx, cudaEventCreate(&b));

@@ -108,7 +108,7 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
     if (s != RQ_OK) return s;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
     void* d = nullptr;
-    if ((s = rq::scratch(ctx, 30, sizeof(rq::QueryDesc) * desc.size(), &d)) != RQ_OK) return s;
+    if ((s = rq::scratch(ctx, rq::kSlotBatchDesc, sizeof(rq::QueryDesc) * desc.size(), &d)) != RQ_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // Pageable source: the copy completes before the call returns, so `desc` may go out of scope.
     RQ_CUDA(ctx, cudaMemcpyAsync(d, desc.data(), sizeof(rq::QueryDesc) * desc.size(),

@@ -199,8 +199,8 @@ rq_status rq_collide(rq_ctx* ctx, const rq_scene* sc, const rq_box* boxes, int64
     if (host) {
         void *a = nullptr, *b = nullptr;
         rq_status s;
-        if ((s = rq::scratch(ctx, 13, sizeof(rq_box) * n, &a)) != RQ_OK ||
-            (s = rq::scratch(ctx, 14, sizeof(rq_collision) * n, &b)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotCollideBoxes, sizeof(rq_box) * n, &a)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotCollideOut, sizeof(rq_collision) * n, &b)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaMemcpyAsync(a, boxes, sizeof(rq_box) * n, cudaMemcpyHostToDevice, st));
         d_boxes = static_cast<const float4*>(a);

@@ -624,17 +624,6 @@ __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_h
     out[j] = shade_one(s, mat, a, strict::xyz(r1), h0, h1, l);
 }
 
-// AO query: visibility 1 - occluded for active rays, 0 for inactive ones.
-__global__ void k_ao_shade(const rq_ray* __restrict__ rays, const uint8_t* __restrict__ occ, int64_t n,
-                           float4* __restrict__ out) {
-    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * j;
-    const float tmin = __ldg(pr).w, tmax = __ldg(pr + 1).w;
-    const float vis = (tmax > tmin) ? (occ[j] ? 0.0f : 1.0f) : 0.0f;
-    out[j] = make_float4(0.0f, 0.0f, 0.0f, vis);
-}
-
 // Per-pixel mean over the spp secondary samples (summed in sample order).
 __global__ void k_accumulate(const float4* __restrict__ shaded, int64_t n, int32_t spp,
                              float4* __restrict__ pixels) {
@@ -688,19 +677,19 @@ __global__ void k_add_count(unsigned long long* dst, const unsigned long long* s
 // the caller).
 rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const rq_gi_params& p,
                   const rq_ray* prim, int64_t n, float4* pixels4, cudaStream_t st, bool stats,
-                  const rq_ray* h_prim, float* h_pix) {
+                  const rq_ray* h_prim, float* h_pix, GiArena& arena) {
     rq_status s;
     const int64_t m = n * p.spp;
     void *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr, *d_shade = nullptr,
          *d_shadow = nullptr, *d_comp = nullptr;
-    if ((s = scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
-        (s = scratch(ctx, 2, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
-        (s = scratch(ctx, 3, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
-        (s = scratch(ctx, 4, m, &d_occ)) != RQ_OK ||
-        (s = scratch(ctx, 11, 4 * m, &d_comp)) != RQ_OK)
+    if ((s = arena.get(rq::kSlotPrimaryHits, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
+        (s = arena.get(rq::kSlotRays, sizeof(rq_ray) * m, &d_sec)) != RQ_OK ||
+        (s = arena.get(rq::kSlotHits, sizeof(rq_hit) * m, &d_shit)) != RQ_OK ||
+        (s = arena.get(rq::kSlotOccluded, m, &d_occ)) != RQ_OK ||
+        (s = arena.get(rq::kSlotCompactOf, 4 * m, &d_comp)) != RQ_OK)
         return s;
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
-    unsigned long long* count = frame_counter(ctx);  // compact (active) secondary rays
+    unsigned long long* count = arena.count();  // compact (active) secondary rays
     RQ_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
     const GiArgs a = to_args(p);
     rq_hit* phit = static_cast<rq_hit*>(d_phit);
@@ -720,8 +709,8 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     if (bounce) {
         void *d_samp = nullptr, *d_rad = nullptr, *d_thr = nullptr;
         void* d_bnc = nullptr;
-        if ((s = scratch(ctx, 8, 4 * m, &d_samp)) != RQ_OK || (s = scratch(ctx, 10, 16 * m, &d_rad)) != RQ_OK ||
-            (s = scratch(ctx, 15, 16 * m, &d_thr)) != RQ_OK || (s = scratch(ctx, 12, 16 * m, &d_bnc)) != RQ_OK)
+        if ((s = arena.get(rq::kSlotSampleOf, 4 * m, &d_samp)) != RQ_OK || (s = arena.get(rq::kSlotRadiance, 16 * m, &d_rad)) != RQ_OK ||
+            (s = arena.get(rq::kSlotThroughput, 16 * m, &d_thr)) != RQ_OK || (s = arena.get(rq::kSlotBounced, 16 * m, &d_bnc)) != RQ_OK)
             return s;
         samp_of = static_cast<int32_t*>(d_samp);
         rad = static_cast<float4*>(d_rad);
@@ -746,14 +735,14 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     if (h_prim && src == prim)
         RQ_CUDA(ctx, cudaMemcpyAsync(const_cast<rq_ray*>(prim), h_prim, sizeof(rq_ray) * n,
                                      cudaMemcpyHostToDevice, st));
-    RQ_CUDA(ctx, launch_closest(pv, qp, src, n, phit, queue_counter(ctx, 0), st));
+    RQ_CUDA(ctx, launch_closest(pv, qp, src, n, phit, arena.queue(0), st));
     if (stats) k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
     if ((!p.sort_rays && !p.unfused) || bounce) {
         k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count,
                                                         samp_of);
     } else if (p.sort_rays) {
         void* d_oct = nullptr;
-        if ((s = scratch(ctx, 31, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
+        if ((s = arena.get(rq::kSlotOctants, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
         unsigned long long* counts = static_cast<unsigned long long*>(d_oct);
         RQ_CUDA(ctx, cudaMemsetAsync(counts, 0, 16 * sizeof(unsigned long long), st));
         k_gi_octant_count<<<grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, counts);
@@ -769,19 +758,19 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     cv.ray_count = count;
     const uint8_t* vis = nullptr;
     if (p.query == 1) {
-        RQ_CUDA(ctx, launch_anyhit(cv, q, sec, m, occ, queue_counter(ctx, 1), st));
+        RQ_CUDA(ctx, launch_anyhit(cv, q, sec, m, occ, arena.queue(1), st));
         if (stats) k_count_bytes_c<<<grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 2);
         vis = occ;
     } else {
-        RQ_CUDA(ctx, launch_closest(cv, q, sec, m, shit, queue_counter(ctx, 1), st));
+        RQ_CUDA(ctx, launch_closest(cv, q, sec, m, shit, arena.queue(1), st));
         if (stats) k_count_hits_c<<<grid(m, 256), 256, 0, st>>>(shit, m, count, cnt + 2);
         if (p.shadow_rays) {
-            if ((s = scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
+            if ((s = arena.get(rq::kSlotShadowRays, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
             rq_ray* sh = static_cast<rq_ray*>(d_shadow);
             k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, m, a, sh, count,
                                                             stats ? cnt + 3 : nullptr);
             RQ_CUDA(ctx, cudaGetLastError());
-            RQ_CUDA(ctx, launch_anyhit(cv, q, sh, m, occ, queue_counter(ctx, 2), st));
+            RQ_CUDA(ctx, launch_anyhit(cv, q, sh, m, occ, arena.queue(2), st));
             if (stats) k_count_bytes_c<<<grid(m, 256), 256, 0, st>>>(occ, m, count, cnt + 4);
             vis = occ;
         }
@@ -791,9 +780,9 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
         // the (no longer needed) GI rays, the hits reuse the GI hit buffer, and per segment the
         // GI slot it belongs to is kept.
         void *d_bray = nullptr, *d_sa = nullptr, *d_sb = nullptr, *d_bc = nullptr;
-        if ((s = scratch(ctx, 32, sizeof(rq_ray) * m, &d_bray)) != RQ_OK ||
-            (s = scratch(ctx, 33, 4 * m, &d_sa)) != RQ_OK || (s = scratch(ctx, 34, 4 * m, &d_sb)) != RQ_OK ||
-            (s = scratch(ctx, 35, 8 * sizeof(unsigned long long) + 8 * p.bounces, &d_bc)) != RQ_OK)
+        if ((s = arena.get(rq::kSlotBounceRays, sizeof(rq_ray) * m, &d_bray)) != RQ_OK ||
+            (s = arena.get(rq::kSlotBounceSlotA, 4 * m, &d_sa)) != RQ_OK || (s = arena.get(rq::kSlotBounceSlotB, 4 * m, &d_sb)) != RQ_OK ||
+            (s = arena.get(rq::kSlotBounceCounts, 8 * sizeof(unsigned long long) + 8 * p.bounces, &d_bc)) != RQ_OK)
             return s;
         unsigned long long* bcount = static_cast<unsigned long long*>(d_bc);
         RQ_CUDA(ctx, cudaMemsetAsync(bcount, 0, sizeof(unsigned long long) * p.bounces, st));
@@ -816,14 +805,14 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
             RQ_CUDA(ctx, cudaGetLastError());
             SceneView bv = sc->view;
             bv.ray_count = bc;
-            RQ_CUDA(ctx, launch_closest(bv, qb, brays, m, shit, queue_counter(ctx, 1), st));
+            RQ_CUDA(ctx, launch_closest(bv, qb, brays, m, shit, arena.queue(1), st));
             const uint8_t* bvis = nullptr;
             if (p.shadow_rays) {
-                if ((s = scratch(ctx, 7, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
+                if ((s = arena.get(rq::kSlotShadowRays, sizeof(rq_ray) * m, &d_shadow)) != RQ_OK) return s;
                 rq_ray* sh = static_cast<rq_ray*>(d_shadow);
                 k_shadow_raygen_c<<<grid(m, 256), 256, 0, st>>>(sc->view, brays, shit, m, a, sh, bc, nullptr);
                 RQ_CUDA(ctx, cudaGetLastError());
-                RQ_CUDA(ctx, launch_anyhit(bv, qb, sh, m, occ, queue_counter(ctx, 2), st));
+                RQ_CUDA(ctx, launch_anyhit(bv, qb, sh, m, occ, arena.queue(2), st));
                 bvis = occ;
             }
             k_bounce_shade<<<grid(m, 256), 256, 0, st>>>(sc->view, brays, shit, bvis, bslot, bc, m, materials_of(sc), a,
@@ -838,7 +827,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     // phase 3
     float4* shade = nullptr;
     if (p.unfused && !bounce) {  // per-sample shading into a scratch buffer, then the per-pixel mean
-        if ((s = scratch(ctx, 5, 16 * m, &d_shade)) != RQ_OK) return s;
+        if ((s = arena.get(rq::kSlotShaded, 16 * m, &d_shade)) != RQ_OK) return s;
         shade = static_cast<float4*>(d_shade);
         k_shade_c<<<grid(m, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of, m, vis, p.query, materials_of(sc), a, shade);
     }
@@ -865,40 +854,6 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
         RQ_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev, 0));
     }
     return RQ_OK;
-}
-
-// The GI pass over caller-provided intermediate buffers: the kernel sequence of rq_gi_frame
-// without its ray-count statistics.  Used by the no-allocation entry point (rq_noalloc.cu).
-cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
-                               const Materials& mat, const rq_ray* prim,
-                               int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st) {
-    const GiArgs a = to_args(p);
-    const int64_t m = n * p.spp;
-    cudaError_t e = launch_closest(s, q, prim, n, b.primary_hits, nullptr, st);
-    if (e != cudaSuccess) return e;
-    k_gi_raygen<<<grid(m, 256), 256, 0, st>>>(s, prim, b.primary_hits, n, a, b.secondary, nullptr);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (p.query == 1) {
-        if ((e = launch_anyhit(s, q, b.secondary, m, b.occluded, nullptr, st)) != cudaSuccess) return e;
-        k_ao_shade<<<grid(m, 256), 256, 0, st>>>(b.secondary, b.occluded, m, b.shaded);
-    } else {
-        if ((e = launch_closest(s, q, b.secondary, m, b.secondary_hits, nullptr, st)) != cudaSuccess)
-            return e;
-        const uint8_t* lit = nullptr;
-        if (p.shadow_rays) {
-            k_shadow_raygen<<<grid(m, 256), 256, 0, st>>>(s, b.secondary, b.secondary_hits, m, a,
-                                                          b.shadow, nullptr);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            if ((e = launch_anyhit(s, q, b.shadow, m, b.occluded, nullptr, st)) != cudaSuccess)
-                return e;
-            lit = b.occluded;
-        }
-        k_shade<<<grid(m, 256), 256, 0, st>>>(s, b.secondary, b.secondary_hits, m, lit, lit ? 1 : 0,
-                                              mat, a, b.shaded);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_accumulate<<<grid(n, 256), 256, 0, st>>>(b.shaded, n, p.spp, reinterpret_cast<float4*>(pixels4));
-    return cudaGetLastError();
 }
 
 }  // namespace rq
@@ -1044,17 +999,18 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     q.flags &= ~RQ_FLAG_HOST_BUFFERS;
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ctx->counters);
     if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
+    rq::CtxGiArena arena(ctx);
     if (!host) {
         if ((s = rq::gi_pass(ctx, sc, q, *p, primary, n, reinterpret_cast<float4*>(pixels4), st,
-                             stats != nullptr, nullptr, nullptr)) != RQ_OK)
+                             stats != nullptr, nullptr, nullptr, arena)) != RQ_OK)
             return s;
     } else {
         void *d_prim = nullptr, *d_pix = nullptr;
-        if ((s = rq::scratch(ctx, 0, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
-            (s = rq::scratch(ctx, 6, 16 * n, &d_pix)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotStageRays, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotStageOut, 16 * n, &d_pix)) != RQ_OK)
             return s;
         if ((s = rq::gi_pass(ctx, sc, q, *p, static_cast<const rq_ray*>(d_prim), n,
-                             static_cast<float4*>(d_pix), st, stats != nullptr, primary, pixels4)) != RQ_OK)
+                             static_cast<float4*>(d_pix), st, stats != nullptr, primary, pixels4, arena)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
     }

@@ -123,19 +123,4 @@ enum BatchFamily { kFamilyBvh8 = 0, kFamilyStrict = 1, kFamilyFast = 2 };
 cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
                          unsigned long long* queue, unsigned* status, cudaStream_t st);
 
-// Intermediate buffers of one GI pass (n primary rays, n*spp secondary rays).
-struct GiBuffers {
-    rq_hit* primary_hits;    // n
-    rq_ray* secondary;       // n*spp
-    rq_hit* secondary_hits;  // n*spp
-    uint8_t* occluded;       // n*spp (AO or shadow any-hit results)
-    float4* shaded;          // n*spp
-    rq_ray* shadow;          // n*spp (shadow rays, GI with shadow_rays only)
-};
-
-// The GI pass over caller-provided intermediate buffers (rq_gi.cu).
-cudaError_t gi_pass_on_buffers(const SceneView& s, const QueryConfig& q, const rq_gi_params& p,
-                               const Materials& mat, const rq_ray* prim,
-                               int64_t n, const GiBuffers& b, float* pixels4, cudaStream_t st);
-
 }  // namespace rq

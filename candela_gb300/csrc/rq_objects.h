@@ -9,7 +9,59 @@
 #include "bvh_build.h"
 #include "rq_internal.h"
 
-constexpr int kScratchSlots = 40;
+namespace rq {
+
+// Grow-only device scratch buffers of a context (rq_ctx::scratch), one per purpose.  Calls that run
+// one after another on the context's streams reuse them; each slot has one owner per kind of call,
+// so that two kinds of work that may overlap on the GPU never share bytes.
+enum ScratchSlot : int {
+    kSlotStageRays = 0,      // host-buffer passes: primary rays staged on the device
+    kSlotPrimaryHits = 1,    // GI / specular passes: primary hits
+    kSlotRays = 2,           // secondary, reflection or probe rays
+    kSlotHits = 3,           // their hits
+    kSlotOccluded = 4,       // any-hit results of a pass
+    kSlotShaded = 5,         // per-sample shading (unfused GI pass)
+    kSlotStageOut = 6,       // host-buffer passes: pixels staged on the device; probe raw radiance
+    kSlotShadowRays = 7,
+    kSlotSampleOf = 8,       // GI bounce loop: sample index per compact slot
+    kSlotTuneOut = 9,        // rq_autotune output
+    kSlotRadiance = 10,      // GI bounce loop: first-hit radiance per slot
+    kSlotCompactOf = 11,     // GI pass: compact slot of every sample
+    kSlotBuild = 12,         // GPU BVH build arena
+    kSlotCollideBoxes = 13,
+    kSlotCollideOut = 14,
+    kSlotThroughput = 15,    // GI bounce loop: path throughput per slot
+    kSlotLossPerPixel = 16,  // rq_fwd / rq_bwd (16..29)
+    kSlotLossPartials = 17,
+    kSlotTapeHits = 18,
+    kSlotTapeImage = 19,
+    kSlotTapeGrad = 20,
+    kSlotTapeTarget = 21,
+    kSlotAdjContrib = 22,
+    kSlotAdjKeysA = 23,
+    kSlotAdjValsA = 24,
+    kSlotAdjKeysB = 25,
+    kSlotAdjValsB = 26,
+    kSlotAdjHist = 27,
+    kSlotAdjSegStart = 28,
+    kSlotAdjSegEnd = 29,
+    kSlotBatchDesc = 30,     // rq_batch descriptor table
+    kSlotOctants = 31,       // GI pass with octant binning
+    kSlotBounceRays = 32,    // GI bounce loop (32..35)
+    kSlotBounceSlotA = 33,
+    kSlotBounceSlotB = 34,
+    kSlotBounceCounts = 35,
+    kSlotProbeStageSh = 36,  // rq_probe_update on host buffers (36..39)
+    kSlotProbeStageRaw = 37,
+    kSlotProbeStageMap = 38,
+    kSlotProbeStageOutSh = 39,
+    kSlotBounced = 40,       // GI bounce loop: Bounced radiance per slot
+    kNumScratchSlots = 41
+};
+
+}  // namespace rq
+
+constexpr int kScratchSlots = rq::kNumScratchSlots;
 
 struct rq_ctx {
     int device = 0;
@@ -23,6 +75,10 @@ struct rq_ctx {
     int* counters = nullptr;  // device work counters for persistent kernels (64 ints)
     void* scratch[kScratchSlots] = {};
     size_t scratch_bytes[kScratchSlots] = {};
+    // device address of rq_gi_frame_noalloc's fixed array on this context's device (resolved by
+    // rq_create), or null with the reason in noalloc_error
+    void* noalloc_base = nullptr;
+    std::string noalloc_error;
     std::string err;
 };
 
@@ -118,10 +174,39 @@ inline unsigned long long* queue_counter(rq_ctx* ctx, int k) {
 // GPU build of one object's BVH2 (bvh_build_gpu.cu): the buffers build_bvh produces, from host
 // input arrays, on the context's device.  RQ_OK, or a status with `why` set.
 rq_status build_bvh_gpu(rq_ctx* ctx, const BuildInput& in, BuildOutput& out, std::string& why);
-// Scratch slot holding the GPU BVH build's buffers.
-constexpr int kBuildScratchSlot = 12;
 // Grow-only device scratch buffer of the context (slot < kScratchSlots).
 rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out);
+
+// Where a GI pass takes its intermediate buffers and its device counters: the context's grow-only
+// scratch slots (rq_gi_frame), or fixed slices of a library array (rq_gi_frame_noalloc).
+struct GiArena {
+    virtual ~GiArena() = default;
+    // A device buffer of at least `bytes` for `slot` (a ScratchSlot).
+    virtual rq_status get(int slot, size_t bytes, void** out) = 0;
+    // The device word that counts the pass's compact (active) secondary rays.
+    virtual unsigned long long* count() = 0;
+    // Ray-queue counter k (0..2) of the persistent traversal launches.
+    virtual unsigned long long* queue(int k) = 0;
+};
+struct CtxGiArena final : GiArena {
+    rq_ctx* ctx;
+    explicit CtxGiArena(rq_ctx* c) : ctx(c) {}
+    rq_status get(int slot, size_t bytes, void** out) override { return scratch(ctx, slot, bytes, out); }
+    unsigned long long* count() override { return frame_counter(ctx); }
+    unsigned long long* queue(int k) override { return queue_counter(ctx, k); }
+};
+
+// Resolves the device address of rq_gi_frame_noalloc's fixed array for the context (rq_noalloc.cu);
+// called by rq_create with the context's device current.
+void noalloc_resolve(rq_ctx* ctx);
+
+// One GI / RTAO pass over n primary rays on stream st (rq_gi.cu): primary closest hits, secondary
+// ray generation, the secondary traversal (+ shadow rays), shading and the per-pixel mean, with
+// every intermediate buffer taken from `arena`.  h_prim / h_pix: host buffers (prim / pixels4 are
+// then device staging buffers).  stats: add the ray counts to the context's frame counters.
+rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const rq_gi_params& p,
+                  const rq_ray* prim, int64_t n, float4* pixels4, cudaStream_t st, bool stats,
+                  const rq_ray* h_prim, float* h_pix, GiArena& arena);
 
 }  // namespace rq
 

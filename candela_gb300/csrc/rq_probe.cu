@@ -395,8 +395,8 @@ rq_status rq_probe_update(rq_ctx* ctx, const rq_scene* sc, const rq_probe_params
     const size_t b_map = 512 * static_cast<size_t>(n);
     void *d_ray = nullptr, *d_hit = nullptr, *d_sh = nullptr, *d_occ = nullptr;
     // scratch: the GI pass's slots (passes on one context are stream-ordered, never concurrent)
-    if ((s = rq::scratch(ctx, 2, sizeof(rq_ray) * n, &d_ray)) != RQ_OK ||
-        (s = rq::scratch(ctx, 3, sizeof(rq_hit) * n, &d_hit)) != RQ_OK)
+    if ((s = rq::scratch(ctx, rq::kSlotRays, sizeof(rq_ray) * n, &d_ray)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotHits, sizeof(rq_hit) * n, &d_hit)) != RQ_OK)
         return s;
     const uint32_t* psh = prev_sh;
     const float* praw = prev_raw;
@@ -405,9 +405,9 @@ rq_status rq_probe_update(rq_ctx* ctx, const rq_scene* sc, const rq_probe_params
     float* oraw = out_raw;
     if (host) {
         void *a = nullptr, *b = nullptr, *c = nullptr, *d = nullptr, *e = nullptr;
-        if ((s = rq::scratch(ctx, 36, b_sh, &a)) != RQ_OK || (s = rq::scratch(ctx, 37, b_raw, &b)) != RQ_OK ||
-            (s = rq::scratch(ctx, 38, b_map, &c)) != RQ_OK || (s = rq::scratch(ctx, 39, b_sh, &d)) != RQ_OK ||
-            (s = rq::scratch(ctx, 6, b_raw, &e)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotProbeStageSh, b_sh, &a)) != RQ_OK || (s = rq::scratch(ctx, rq::kSlotProbeStageRaw, b_raw, &b)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotProbeStageMap, b_map, &c)) != RQ_OK || (s = rq::scratch(ctx, rq::kSlotProbeStageOutSh, b_sh, &d)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotStageOut, b_raw, &e)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaMemcpyAsync(a, prev_sh, b_sh, cudaMemcpyHostToDevice, st));
         RQ_CUDA(ctx, cudaMemcpyAsync(b, prev_raw, b_raw, cudaMemcpyHostToDevice, st));
@@ -437,7 +437,7 @@ rq_status rq_probe_update(rq_ctx* ctx, const rq_scene* sc, const rq_probe_params
     RQ_CUDA(ctx, rq::launch_closest(sc->view, q, ray, n, hit, rq::queue_counter(ctx, 1), st));
     const uint8_t* occ = nullptr;
     if (p->shadow_rays) {
-        if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * n, &d_sh)) != RQ_OK || (s = rq::scratch(ctx, 4, n, &d_occ)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotShadowRays, sizeof(rq_ray) * n, &d_sh)) != RQ_OK || (s = rq::scratch(ctx, rq::kSlotOccluded, n, &d_occ)) != RQ_OK)
             return s;
         rq::k_probe_shadow<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, ray, hit, n, a, static_cast<rq_ray*>(d_sh));
         RQ_CUDA(ctx, cudaGetLastError());

@@ -167,15 +167,15 @@ rq_status rq_specular_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* prima
     void *d_prim = nullptr, *d_out = nullptr, *d_phit = nullptr, *d_ray = nullptr, *d_hit = nullptr,
          *d_sh = nullptr, *d_occ = nullptr;
     // scratch: the GI pass's slots (a specular pass never overlaps one on the same context)
-    if ((s = rq::scratch(ctx, 1, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
-        (s = rq::scratch(ctx, 2, sizeof(rq_ray) * n, &d_ray)) != RQ_OK ||
-        (s = rq::scratch(ctx, 3, sizeof(rq_hit) * n, &d_hit)) != RQ_OK)
+    if ((s = rq::scratch(ctx, rq::kSlotPrimaryHits, sizeof(rq_hit) * n, &d_phit)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotRays, sizeof(rq_ray) * n, &d_ray)) != RQ_OK ||
+        (s = rq::scratch(ctx, rq::kSlotHits, sizeof(rq_hit) * n, &d_hit)) != RQ_OK)
         return s;
     const rq_ray* prim = primary;
     float4* out = reinterpret_cast<float4*>(out4);
     if (host) {
-        if ((s = rq::scratch(ctx, 0, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
-            (s = rq::scratch(ctx, 6, 16 * n, &d_out)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotStageRays, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotStageOut, 16 * n, &d_out)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaMemcpyAsync(d_prim, primary, sizeof(rq_ray) * n, cudaMemcpyHostToDevice, st));
         prim = static_cast<const rq_ray*>(d_prim);
@@ -193,8 +193,8 @@ rq_status rq_specular_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* prima
     RQ_CUDA(ctx, rq::launch_closest(sc->view, q, ray, n, hit, rq::queue_counter(ctx, 1), st));
     const uint8_t* vis = nullptr;
     if (p->shadow_rays) {
-        if ((s = rq::scratch(ctx, 7, sizeof(rq_ray) * n, &d_sh)) != RQ_OK ||
-            (s = rq::scratch(ctx, 4, n, &d_occ)) != RQ_OK)
+        if ((s = rq::scratch(ctx, rq::kSlotShadowRays, sizeof(rq_ray) * n, &d_sh)) != RQ_OK ||
+            (s = rq::scratch(ctx, rq::kSlotOccluded, n, &d_occ)) != RQ_OK)
             return s;
         rq::k_spec_shadow<<<rq::grid(n, 256), 256, 0, st>>>(sc->view, ray, hit, n, a, static_cast<rq_ray*>(d_sh));
         RQ_CUDA(ctx, cudaGetLastError());

@@ -147,6 +147,12 @@ class Context:
         check(lib().rq_counters_read(self.handle, C.byref(c), int(reset)), self.handle)
         return {"node_visits": c[0], "triangle_tests": c[1]}
 
+    def read_bandwidth(self, nbytes: int, reps: int = 50) -> float:
+        """Measured read bandwidth (GB/s) over a device buffer of nbytes (rq_measure_read_gbs)."""
+        g = C.c_double()
+        check(lib().rq_measure_read_gbs(self.handle, int(nbytes), int(reps), C.byref(g)), self.handle)
+        return g.value
+
     def scene(self, layout, vertices, tris, nodes, entities) -> "Scene":
         return Scene(self, layout, vertices, tris, nodes, entities)
 
@@ -245,6 +251,34 @@ class Scene:
         check(lib().rq_closest(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), C.byref(o),
                                _stream(rays, stream)), self.ctx.handle)
         return hits
+
+    def hit_attribs(self, hits, out=None, *, stream=None):
+        """GetData over hit records: (n, 8) float32 = normal xyz, alpha, albedo rgb, emissive
+        (rq_hit_attribs).  numpy hits -> host path."""
+        host = isinstance(hits, np.ndarray)
+        n = hits.shape[0] if host else hits.numel() * hits.element_size() // 32
+        if out is None:
+            out = np.empty((n, 8), dtype=np.float32) if host else _empty_like_dev(hits, (n, 8), __import__("torch").float32)
+        o = _opts(0, 0, 0, L.FLAG_HOST_BUFFERS if host else 0)
+        check(lib().rq_hit_attribs(self.ctx.handle, self.handle, ptr(hits), n, ptr(out), C.byref(o),
+                                   _stream(hits, stream)), self.ctx.handle)
+        return out
+
+    def closest_attribs(self, rays, *, layout=0, mode=0, tie=0, flags=0, block_size=0, min_blocks=0,
+                        persistent=0, stream=None):
+        """Closest hit + GetData (rq_closest_attribs): (hits, attribs)."""
+        host = isinstance(rays, np.ndarray)
+        n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
+        if host:
+            hits, att = np.empty(n, dtype=HIT_DTYPE), np.empty((n, 8), dtype=np.float32)
+        else:
+            import torch
+            hits = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
+            att = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size, min_blocks, persistent)
+        check(lib().rq_closest_attribs(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), ptr(att), C.byref(o),
+                                       _stream(rays, stream)), self.ctx.handle)
+        return hits, att
 
     def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, min_blocks=0,
                persistent=0, stream=None):

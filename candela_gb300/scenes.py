@@ -399,6 +399,15 @@ def c2_icosphere_scene(n_spheres: int = 64) -> Mesh:
     return icosphere_set(n_spheres=n_spheres, subdiv=5, seed=2)
 
 
+def c4_icosphere_scene() -> Mesh:
+    """256 displaced subdivision-5 icospheres over [-8,8]^2 x [0,4], no ground (5,242,880 triangles:
+    256 x 20,480; the precision workload's stated 4,194,304 does not match that shape)."""
+    return icosphere_set(n_spheres=256, subdiv=5, seed=4, lo=(-8.0, -8.0, 0.0), hi=(8.0, 8.0, 4.0),
+                         ground=None)
+
+
+C4_BOUNDS = ((-8.0, -8.0, 0.0), (8.0, 8.0, 4.0))
+
 C5_CAMERA = dict(eye=(0.0, -1.6, 2.2), target=(0.0, 0.0, 0.0), vfov_deg=60.0)
 
 

@@ -175,6 +175,13 @@ rq_status rq_counters_read(rq_ctx* ctx, rq_counters* out, int reset);
  * return the best hit found so far; the bits make that visible.  0 = clean. */
 rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset);
 
+/* Read bandwidth of the context's device in GB/s (no counterpart in the reference): 16-byte loads
+ * that bypass L1, from every SM, over a device buffer of `bytes` (allocated and freed inside the
+ * call), re-read `reps` times back to back after three warm-up passes.  A buffer well under the
+ * L2 size measures L2 read bandwidth, the roof of the traversal kernels, whose scenes stay
+ * L2-resident; one well above it measures HBM.  Synchronises the context's stream. */
+rq_status rq_measure_read_gbs(rq_ctx* ctx, int64_t bytes, int32_t reps, double* gbs);
+
 /* ---- BVH construction (host) ------------------------------------------------------------ */
 
 typedef struct rq_bvh rq_bvh;
@@ -299,6 +306,35 @@ rq_status rq_scene_destroy(rq_scene* scene);
  * TraverseBVHStackless.glsl:280-319).  opts may be NULL (strict, lower-index ties). */
 rq_status rq_closest(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
                      rq_hit* hits, const rq_opts* opts, void* stream);
+
+/* Surface attributes of a hit (32 bytes), the outputs of the reference's GetData
+ * (TraverseBVHStack.glsl:422-455) that its IntersectRay overloads return beside TUVW, Mesh and
+ * TriangleIdx: normal = the normalised barycentric mix of the three vertices' half-packed normals
+ * (UnpackNormal :417-420), albedo = the mesh's albedo texture at the interpolated half-packed UV
+ * when it has one (rq_scene_set_textures), else its ModelColor (rq_scene_set_materials; 0.8 grey
+ * for a mesh without an entry), emissive and alpha = the hit entity's Data[0] and Data[1].  A miss
+ * (t < 0 or mesh < 0) gives normal = -1, albedo = 0, emissive = 0 as GetData does, and alpha = 0
+ * (GetData returns before writing it). */
+typedef struct rq_hit_attrib {
+    float normal[3];
+    float alpha;
+    float albedo[3];
+    float emissive;
+} rq_hit_attrib;
+
+/* GetData over n hit records (from rq_closest or any other source), stackless and stack scenes
+ * alike: attribs[i] for hits[i].  RQ_FLAG_HOST_BUFFERS in opts: hits and attribs are host memory. */
+rq_status rq_hit_attribs(rq_ctx* ctx, const rq_scene* scene, const rq_hit* hits, int64_t n,
+                         rq_hit_attrib* attribs, const rq_opts* opts, void* stream);
+
+/* Closest hit plus surface attributes for n rays: replaces the overloads IntersectRay(o, d, out
+ * TUVW, out Mesh, out TriangleIdx, out Albedo, out Normal[, out Alpha[, out Iters]]) and
+ * IntersectRayIgnoreTransparent (TraverseBVHStack.glsl:458-502; TraverseBVHStackless.glsl the
+ * same), Albedo.xyz = attribs.albedo and Albedo.w = attribs.emissive as there.  The query is
+ * rq_closest's with the same opts (RQ_FLAG_IGNORE_TRANSPARENT gives the IgnoreTransparent form),
+ * followed by rq_hit_attribs over its hits. */
+rq_status rq_closest_attribs(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, int64_t n,
+                             rq_hit* hits, rq_hit_attrib* attribs, const rq_opts* opts, void* stream);
 
 /* Autotuner: times every compiled launch variant of the traversal kernel for `query` (0 =
  * closest hit, 1 = any hit) and `layout` on the caller's device rays (3 timed launches each, after
@@ -616,16 +652,21 @@ rq_status rq_scene_update_positions(rq_scene* scene, const float* xyz, void* str
  * images).  cudaMalloc can synchronise the device and can fail under memory pressure, so frame
  * loops that must keep their timing, and host applications that own all device memory through
  * their own allocator and forbid plugins from allocating, cannot call rq_gi_frame, which grows
- * its scratch on demand.  This variant allocates nothing: its intermediates live in one fixed
- * __device__ array (about 9 MiB, held by every GPU that loads librq.so until the process exits).
- *  - Device buffers only (RQ_FLAG_HOST_BUFFERS is rejected); no statistics.
+ * its scratch on demand.  This variant allocates nothing: it runs rq_gi_frame's kernels (fused
+ * per-pixel ray generation and shading, the autotuned or requested launch variant, persistent ray
+ * queues included) with every intermediate buffer and counter in one fixed __device__ array of
+ * about 8.3 MiB.
+ *  - The array is reserved on a device when the first context is created on it: rq_create looks
+ *    up its device address (cudaGetSymbolAddress, which also loads the module that holds it) and
+ *    keeps it in the context.  It stays reserved until the process exits.  After cudaDeviceReset,
+ *    create a new context (the old one's address, like its streams and buffers, is gone).
+ *  - Device buffers only (RQ_FLAG_HOST_BUFFERS is rejected); no statistics; bounces = 0;
+ *    sort_rays and unfused are ignored (they change the kernel arrangement, not the pixels).
  *  - n > RQ_NOALLOC_MAX_RAYS or n * spp > RQ_NOALLOC_MAX_RAYS is rejected with RQ_EINVAL.
- *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
- *    that device current; make that first call before any stream capture.
  *  - All calls share the array: calls whose work overlaps on the GPU (different streams or host
  *    threads) race and must be serialised by the caller.  Each call overwrites everything it
  *    reads, so nothing from an earlier call leaks into its result.
- * Results equal rq_gi_frame's for the same inputs. */
+ * Pixels equal rq_gi_frame's bit for bit for the same inputs and options. */
 rq_status rq_gi_frame_noalloc(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,
                               const rq_gi_params* params, const rq_opts* opts, float* pixels4,
                               void* stream);

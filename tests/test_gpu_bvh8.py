@@ -1,5 +1,8 @@
-"""BVH8 with quantised boxes on the GPU: hits equal the strict BVH2 kernel's (t, barycentrics,
-triangle, mesh, entity; `iters` counts different nodes), any-hit bits equal, no status bits."""
+"""BVH8 with quantised boxes on the GPU: hit records equal the oracle's strict BVH2 records (t,
+barycentrics, triangle, mesh, entity; `iters` counts different nodes) and any-hit bits are equal,
+except rays where a brute force over every triangle proves the BVH8 answer (the reference's slab
+test can round a node with the closest hit away; the conservative BVH8 boxes keep it).  No status
+bits."""
 import numpy as np
 import pytest
 
@@ -7,7 +10,8 @@ import candela_gb300 as R
 from candela_gb300 import _lib as L
 from candela_gb300 import scenes as S
 
-from .helpers import hits_from_device, mesh, oracle_scene, rays_to_device, single_object
+from .helpers import (assert_equal_or_proven, assert_occlusion_equal_or_proven, hits_from_device, mesh,
+                      oracle_scene, rays_to_device, single_object)
 
 pytestmark = pytest.mark.gpu
 
@@ -30,13 +34,15 @@ def test_bvh8_equals_strict(ctx, name, layout, leaf):
     rays = np.concatenate([S.camera_rays(384, 256, **S.C1_CAMERA),
                            S.sphere_rays(100_000, (-1.5, -1.5, -0.3), (1.5, 1.5, 1.2), seed=41)])
     d = rays_to_device(rays)
+    osc = oracle_scene(bufs, layout)
+    want = osc.closest(rays)
     strict = hits_from_device(sc.closest(d))
-    b8 = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q))
-    same = _same(strict, b8)
-    assert same.mean() >= 0.9999, f"{(~same).sum()} of {len(rays)} rays differ"
-    occ_s = sc.anyhit(d).cpu().numpy()
-    occ_8 = sc.anyhit(d, layout=L.LAYOUT_BVH8Q).cpu().numpy()
-    assert (occ_s == occ_8).mean() >= 0.9999
+    assert _same(strict, want).all()
+    for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1)):
+        b8 = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, **kw))
+        assert_equal_or_proven(b8, want, osc, rays, what=f"{name} layout {layout} {kw}")
+        occ_8 = sc.anyhit(d, layout=L.LAYOUT_BVH8Q, **kw).cpu().numpy()
+        assert_occlusion_equal_or_proven(occ_8, osc.anyhit(rays), osc, rays, what=f"{name} any {kw}")
     assert ctx.device_status() == 0
 
 
@@ -54,15 +60,17 @@ def test_bvh8_multi_entity_and_oracle(ctx):
     sc.build_bvh8()
     rays = S.sphere_rays(100_000, (-1.5, -1.5, -0.5), (1.5, 1.5, 1.5), seed=22)
     from oracle import oracle as O
-    want = O.OracleScene(O.ORC_STACK, *ri.global_buffers()).closest(rays)
+    osc = O.OracleScene(O.ORC_STACK, *ri.global_buffers())
+    want = osc.closest(rays)
     got = hits_from_device(sc.closest(rays_to_device(rays), layout=L.LAYOUT_BVH8Q))
-    assert _same(got, want).mean() >= 0.9999
+    assert_equal_or_proven(got, want, osc, rays, what="multi-entity")
     # entities changed after the build: the BVH8 follows
     ri.push_entity(1, model=T)
     ri.buffer_entities()
-    want2 = O.OracleScene(O.ORC_STACK, *ri.global_buffers()).closest(rays)
+    osc2 = O.OracleScene(O.ORC_STACK, *ri.global_buffers())
+    want2 = osc2.closest(rays)
     got2 = hits_from_device(sc.closest(rays_to_device(rays), layout=L.LAYOUT_BVH8Q))
-    assert _same(got2, want2).mean() >= 0.9999
+    assert_equal_or_proven(got2, want2, osc2, rays, what="multi-entity after set_entities")
     assert ctx.device_status() == 0
 
 

@@ -1,4 +1,4 @@
-"""Fast mode against strict mode, and batched queries against per-query calls."""
+"""Fast mode against the oracle's strict hits, and batched queries against per-query calls."""
 import numpy as np
 import pytest
 
@@ -6,18 +6,22 @@ import candela_gb300 as R
 from candela_gb300 import _lib as L
 from candela_gb300 import scenes as S
 
-from .helpers import hits_from_device, rays_to_device, single_object
+from .helpers import hits_from_device, oracle_scene, rays_to_device, single_object
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name,layout", [("c1", R.STACK), ("c1", R.STACKLESS), ("ico2", R.STACK)])
-def test_fast_mode_agrees_with_strict(ctx, name, layout):
-    sc = ctx.scene(layout, *single_object(name, layout))
+def test_fast_mode_agrees_with_oracle(ctx, name, layout):
+    """Fast mode: identical hit/miss and triangle IDs against the oracle's strict hits on >= 99.99 %
+    of rays, |dt| <= 1e-5 t on >= 99.99 % of the shared hits; occlusion bits likewise."""
+    bufs = single_object(name, layout)
+    sc = ctx.scene(layout, *bufs)
+    osc = oracle_scene(bufs, layout)
     rays = np.concatenate([S.camera_rays(384, 256, **S.C1_CAMERA),
                            S.sphere_rays(200_000, (-1.5, -1.5, -0.3), (1.5, 1.5, 1.2), seed=7)])
     d = rays_to_device(rays)
-    st = hits_from_device(sc.closest(d))
+    st = osc.closest(rays)
     fa = hits_from_device(sc.closest(d, mode=L.MODE_FAST))
     same_hit = (st["t"] > 0) == (fa["t"] > 0)
     same_id = same_hit & (st["tri"] == fa["tri"])
@@ -25,7 +29,7 @@ def test_fast_mode_agrees_with_strict(ctx, name, layout):
     both = same_id & (st["t"] > 0)
     rel = np.abs(fa["t"][both] - st["t"][both]) / st["t"][both]
     assert (rel <= 1e-5).mean() >= 0.9999 and rel.max() < 1e-3
-    oc_s = sc.anyhit(d).cpu().numpy()
+    oc_s = osc.anyhit(rays)
     oc_f = sc.anyhit(d, mode=L.MODE_FAST).cpu().numpy()
     assert (oc_s == oc_f).mean() >= 0.9999
 
