@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--profile-probe", action="store_true",
                     help="run two probe-volume frames on the 128 x 128 x 64 grid over the C2 scene and "
                          "exit (the case the ncu capture of k_probe_shade uses)")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the batched (C3), precision (C4) and differentiation (C5) sub-records")
     ap.add_argument("--profile", action="store_true",
                     help="run one GI pass and exit (the case the ncu captures use: the 2nd "
                          "traversal launch is the full-size secondary closest-hit launch; with "
@@ -358,13 +360,39 @@ def c3_workload(seed: int = 3):
     return scenes, queries
 
 
-def run_c3(args):
+def _event_timer(stream, flush, warmup):
+    """fn -> mean CUDA-event ms over `reps` runs on `stream`, L2 flushed (512 MB write) before each."""
+    import torch
+
+    def timed(fn, reps):
+        for _ in range(max(1, warmup)):
+            fn()
+        torch.cuda.synchronize()
+        evs = []
+        for i in range(reps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+    return timed
+
+
+def batched_record(args, ctx=None, flush=None):
+    """The metric's batched leg (C3): 64 queries over 8 scenes in ONE persistent launch replayed as
+    a captured CUDA graph, on the autotuned BVH8q layout, against the plain FP32 BVH2 kernel with
+    one launch per query; hits equal per-query calls; the CPU restatement on a sample of every
+    query's rays beside it."""
     import torch
     import candela_gb300 as R
     from candela_gb300 import _lib as L
-    torch.cuda.set_device(0)
+    from oracle import oracle as O
+    t_setup = time.perf_counter()
     scenes, queries = c3_workload()
-    ctx = R.Context(0)
+    ctx = ctx or R.Context(0)
     dev_scenes = []
     for s_ in scenes:
         sc = ctx.scene(R.STACK, s_["mesh"].vertices, s_["bvh"].tris, s_["bvh"].nodes,
@@ -380,109 +408,118 @@ def run_c3(args):
         qs.append((dev_scenes[q["scene"]], d, q["kind"], out))
     total = sum(len(q["rays"]) for q in queries)
     stream = torch.cuda.current_stream()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    flush.fill_(0)  # loads torch's fill kernel before any timed region
-
-    def timed(fn, reps):
-        for _ in range(max(1, args.warmup)):
-            fn()
-        torch.cuda.synchronize()
-        ms = []
-        for i in range(reps):
-            flush.fill_(i & 0xFF)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            torch.cuda.synchronize()
-            ms.append(a.elapsed_time(b))
-        return statistics.mean(ms)
+    if flush is None:
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+        flush.fill_(0)  # loads torch's fill kernel before any timed region
+    timed = _event_timer(stream, flush, args.warmup)
 
     def per_query(layout):
         def fn():
             for sc, d, kind, out in qs:
-                (sc.closest if kind == 0 else sc.anyhit)(d, out, layout=layout,
-                                                          block_size=128, min_blocks=1)
+                (sc.closest if kind == 0 else sc.anyhit)(d, out, layout=layout, block_size=128, min_blocks=1)
         return fn
 
-    plain_ms = timed(per_query(0), args.steps)          # plain FP32 BVH2, one launch per query
-    b8_ms = timed(per_query(L.LAYOUT_BVH8Q), args.steps)  # BVH8q, one launch per query
     plan = R.engine.BatchPlan(ctx, qs, layout=L.LAYOUT_BVH8Q)
     tune = plan.autotune(allow_bvh8=True)
-    batched_ms = timed(plan.launch, args.steps)
+    setup_s = time.perf_counter() - t_setup
+    with ClockSampler(0) as clk:
+        clk.ready()
+        plan.launch()
+        torch.cuda.synchronize()
+        clk.mark_timed(True)
+        batched_ms = timed(plan.launch, args.steps)
+        clk.mark_timed(False)
+    plain_ms = timed(per_query(0), args.steps)          # plain FP32 BVH2, one launch per query
+    b8_ms = timed(per_query(L.LAYOUT_BVH8Q), args.steps)  # BVH8q, one launch per query
+    plan.launch()
+    torch.cuda.synchronize()
     want = [out.cpu().numpy().copy() for _, _, _, out in qs]
     per_query(L.LAYOUT_BVH8Q if tune["family"] == 0 else 0)()
     torch.cuda.synchronize()
     same = all(np.array_equal(w.view(np.uint8)[:, :28] if w.ndim == 2 else w,
                               out.cpu().numpy().view(np.uint8)[:, :28] if w.ndim == 2 else out.cpu().numpy())
                for w, (_, _, _, out) in zip(want, qs))
+    plan.close()
+    # CPU restatement of the same queries on a sample (every 16th ray of every query), all host cores
+    nthreads = os.cpu_count() or 1
+    oscs = [O.OracleScene(O.ORC_STACK, s_["mesh"].vertices, s_["bvh"].tris, s_["bvh"].nodes,
+                          R.identity_entity(0, s_["bvh"].nodes.shape[0])) for s_ in scenes]
+    c0 = time.perf_counter()
+    n_cpu = 0
+    for q in queries:
+        r = np.ascontiguousarray(q["rays"][::16])
+        (oscs[q["scene"]].closest if q["kind"] == 0 else oscs[q["scene"]].anyhit)(r, nthreads=nthreads)
+        n_cpu += len(r)
+    cpu_s = time.perf_counter() - c0
     v = total / (batched_ms / 1e3) / 1e6
-    line = {"metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(batched_ms, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (8 seeded scenes, 64 seeded queries)",
-            "config": {"workload": "batching: 64 queries (1k-2M rays, log-uniform; half camera, "
-                                   "half uniform-sphere rays; 50/50 closest/any) over 8 scenes "
-                                   "(10k-2M triangles); step = the whole batch",
-                       "total_rays": int(total), "scene_triangles": [s_["tris"] for s_ in scenes],
-                       "query_rays": [len(q["rays"]) for q in queries],
-                       "l2": "flushed before each timed step"},
+    return {"workload": "batching: 64 queries (1k-2M rays, log-uniform; half camera, half uniform-sphere "
+                        "rays; 50/50 closest/any) over 8 scenes (10k-2M triangles); step = the whole batch",
+            "total_rays": int(total), "scene_triangles": [s_["tris"] for s_ in scenes],
+            "value": round(v, 2), "unit": UNIT, "ms_per_step": round(batched_ms, 4),
+            "form": "one persistent launch replayed as a CUDA graph, autotuned layout / block / occupancy",
+            "picked": tune,
             "plain_fp32_bvh2_one_launch_per_query": {"mrays_s": round(total / (plain_ms / 1e3) / 1e6, 2),
                                                      "ms": round(plain_ms, 4)},
-            "bvh8q_one_launch_per_query": {"mrays_s": round(total / (b8_ms / 1e3) / 1e6, 2),
-                                           "ms": round(b8_ms, 4)},
-            "batched_graph_autotuned": {"mrays_s": round(v, 2), "ms": round(batched_ms, 4),
-                                        "picked": tune, "hits_equal_per_query": bool(same)},
-            "speedup_batched_bvh8q_over_plain": round(plain_ms / batched_ms, 3)}
+            "bvh8q_one_launch_per_query": {"mrays_s": round(total / (b8_ms / 1e3) / 1e6, 2), "ms": round(b8_ms, 4)},
+            "speedup_batched_bvh8q_over_plain": round(plain_ms / batched_ms, 3),
+            "hits_equal_per_query": bool(same), "device_status": ctx.device_status(),
+            "l2": "flushed before each timed step", "setup_s": round(setup_s, 2),
+            "cpu_baseline": {"value": round(n_cpu / cpu_s / 1e6, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"every 16th ray of all 64 queries ({n_cpu} rays), {cpu_s:.2f} s"},
+            "clocks": clk.summary()}
+
+
+def run_c3(args):
+    import torch
+    torch.cuda.set_device(0)
+    rec = batched_record(args)
+    line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (8 seeded scenes, 64 seeded queries)",
+            "config": {"workload": rec["workload"], "total_rays": rec["total_rays"],
+                       "scene_triangles": rec["scene_triangles"], "l2": rec["l2"]},
+            "batched": rec, "cpu_baseline": rec["cpu_baseline"], "clocks": rec["clocks"]}
     print(json.dumps(line), flush=True)
 
 
-def run_c4(args):
-    """Precision workload: 256 displaced subdivision-5 icospheres over [-8,8]^2 x [0,4]
+def precision_record(args, ctx=None, flush=None, n_rays=1 << 23):
+    """Precision workload (C4): 256 displaced subdivision-5 icospheres over [-8,8]^2 x [0,4]
     (5,242,880 triangles: the stated 4,194,304 does not match 256 x 20,480), 2^23 rays with origins
-    uniform in the scene bounds and directions uniform on the sphere; closest hit with the BVH8q
-    and with the strict FP32 BVH2; triangle-ID agreement and t / barycentric error against the FP64
-    recomputation of each winning hit."""
+    uniform in the scene bounds and directions uniform on the sphere; closest hit with the BVH8q and
+    with the strict FP32 BVH2; triangle-ID agreement and t / barycentric error against the FP64
+    recomputation of each winning hit (rq_verify_hits)."""
     import torch
     import candela_gb300 as R
     from candela_gb300 import _lib as L
     from candela_gb300 import scenes as S
-    torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    mesh = S.icosphere_set(n_spheres=256, subdiv=5, seed=4, lo=(-8.0, -8.0, 0.0), hi=(8.0, 8.0, 4.0),
-                           ground=None)
+    mesh = S.c4_icosphere_scene()
     gen_s = time.perf_counter() - t0
     bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
-    ctx = R.Context(0)
+    ctx = ctx or R.Context(0)
     sc = ctx.scene(R.STACK, mesh.vertices, bvh.tris, bvh.nodes, R.identity_entity(0, bvh.nodes.shape[0]))
     b8 = sc.build_bvh8()
-    n = 1 << 23
-    rays = S.sphere_rays(n, (-8.0, -8.0, 0.0), (8.0, 8.0, 4.0), seed=44)
+    n = n_rays
+    rays = S.sphere_rays(n, *S.C4_BOUNDS, seed=44)
     d = torch.from_numpy(rays.view(np.uint8)).cuda()
     stream = torch.cuda.current_stream()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    flush.fill_(0)  # loads torch's fill kernel before any timed region
+    if flush is None:
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+        flush.fill_(0)
+    timed = _event_timer(stream, flush, args.warmup)
     tune8 = sc.autotune(d, query=0, layout=L.LAYOUT_BVH8Q)
     tune2 = sc.autotune(d, query=0, layout=R.STACK)
-
-    def timed(fn):
-        for _ in range(max(1, args.warmup)):
-            fn()
-        evs = []
-        for i in range(args.steps):
-            flush.fill_(i & 0xFF)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            evs.append((a, b))
-        torch.cuda.synchronize()
-        return statistics.mean(a.elapsed_time(b) for a, b in evs)
-
     h2 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
     h8 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
-    ms2 = timed(lambda: sc.closest(d, h2))
-    ms8 = timed(lambda: sc.closest(d, h8, layout=L.LAYOUT_BVH8Q))
+    with ClockSampler(0) as clk:
+        clk.ready()
+        sc.closest(d, h8, layout=L.LAYOUT_BVH8Q)
+        torch.cuda.synchronize()
+        clk.mark_timed(True)
+        ms8 = timed(lambda: sc.closest(d, h8, layout=L.LAYOUT_BVH8Q), args.steps)
+        clk.mark_timed(False)
+    ms2 = timed(lambda: sc.closest(d, h2), args.steps)
     u2 = h2.cpu().numpy().view(np.uint32)
     u8 = h8.cpu().numpy().view(np.uint32)
     hit2 = h2[:, 0].cpu().numpy() > 0
@@ -497,23 +534,49 @@ def run_c4(args):
                 "t_rel_err_median": float(np.median(te[ok])),
                 "bary_err_max": float(be[ok].max()), "bary_err_median": float(np.median(be[ok]))}
 
-    line = {"metric": METRIC, "value": round(n / (ms8 / 1e3) / 1e6, 2), "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms8, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded icospheres and rays)",
-            "config": {"workload": "precision: 256 displaced subdiv-5 icospheres over [-8,8]^2x[0,4] "
-                                   f"({mesh.n_tris} tris), {n} incoherent rays (origins uniform in the "
-                                   "bounds, directions uniform on the sphere), closest hit",
-                       "scene_gen_s": round(gen_s, 2), "bvh2_build_ms": round(bvh.build_ms, 1),
-                       "bvh8": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()}},
-            "bvh8q": {"mrays_s": round(n / (ms8 / 1e3) / 1e6, 2), "ms": round(ms8, 4),
-                      "picked": (tune8["block_size"], tune8["min_blocks"]), "fp64": errs(h8)},
-            "bvh2_strict": {"mrays_s": round(n / (ms2 / 1e3) / 1e6, 2), "ms": round(ms2, 4),
-                            "picked": (tune2["block_size"], tune2["min_blocks"]), "fp64": errs(h2)},
-            "triangle_id_agreement": float(same_id.mean()),
-            "identical_hit_records": float(same_all.mean()),
-            "hit_rate": float(hit2.mean()), "device_status": ctx.device_status(),
-            "speedup_bvh8q_over_bvh2": round(ms2 / ms8, 3)}
+    # the oracle on a sample of the same rays: strict hits bit for bit, and the CPU time
+    from oracle import oracle as O
+    nthreads = os.cpu_count() or 1
+    osc = O.OracleScene(O.ORC_STACK, mesh.vertices, bvh.tris, bvh.nodes, R.identity_entity(0, bvh.nodes.shape[0]))
+    samp = np.ascontiguousarray(rays[::128])
+    c0 = time.perf_counter()
+    want = osc.closest(samp, nthreads=nthreads)
+    cpu_s = time.perf_counter() - c0
+    got = np.ascontiguousarray(u2[::128]).view(R.HIT_DTYPE).reshape(-1)
+    oracle_equal = float((np.ascontiguousarray(want).view(np.uint32).reshape(-1, 8)
+                          == np.ascontiguousarray(got).view(np.uint32).reshape(-1, 8)).all(1).mean())
+    rec = {"workload": "precision: 256 displaced subdiv-5 icospheres over [-8,8]^2x[0,4] "
+                       f"({mesh.n_tris} tris), {n} incoherent rays (origins uniform in the bounds, "
+                       "directions uniform on the sphere), closest hit",
+           "value": round(n / (ms8 / 1e3) / 1e6, 2), "unit": UNIT, "ms_per_step": round(ms8, 4),
+           "scene_gen_s": round(gen_s, 2), "bvh2_build_ms": round(bvh.build_ms, 1),
+           "bvh8": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in b8.items()},
+           "bvh8q": {"mrays_s": round(n / (ms8 / 1e3) / 1e6, 2), "ms": round(ms8, 4),
+                     "picked": (tune8["block_size"], tune8["min_blocks"], tune8["persistent"]), "fp64": errs(h8)},
+           "bvh2_strict": {"mrays_s": round(n / (ms2 / 1e3) / 1e6, 2), "ms": round(ms2, 4),
+                           "picked": (tune2["block_size"], tune2["min_blocks"], tune2["persistent"]),
+                           "fp64": errs(h2)},
+           "triangle_id_agreement": float(same_id.mean()),
+           "identical_hit_records": float(same_all.mean()),
+           "strict_equals_oracle_on_sample": oracle_equal,
+           "hit_rate": float(hit2.mean()), "device_status": ctx.device_status(),
+           "speedup_bvh8q_over_bvh2": round(ms2 / ms8, 3), "l2": "flushed before each timed step",
+           "cpu_baseline": {"value": round(len(samp) / cpu_s / 1e6, 3), "unit": UNIT, "cores": nthreads,
+                            "kind": "port", "sample": f"every 128th ray ({len(samp)} rays), {cpu_s:.2f} s"},
+           "clocks": clk.summary()}
+    sc.close()
+    return rec
+
+
+def run_c4(args):
+    import torch
+    torch.cuda.set_device(0)
+    rec = precision_record(args)
+    line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded icospheres and rays)", "config": {"workload": rec["workload"]},
+            "precision": rec, "cpu_baseline": rec["cpu_baseline"], "clocks": rec["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -658,28 +721,31 @@ def run_c6(args):
     print(json.dumps(line), flush=True)
 
 
-def run_c5(args):
-    """Differentiation workload: heightfield 512x512 (524,288 tris, vertex z = parameters), 1024x1024
-    depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a second-seed
-    heightfield; timed step = rq_fwd + rq_bwd; central FD check (h = 1e-3) on 256 random vertices
-    whose pixels do not switch triangles; 100 Adam steps (lr 1e-3) with BVH refit per step."""
+def differentiation_record(args, ctx=None):
+    """Differentiation workload (C5): heightfield 512x512 (524,288 tris, vertex z = parameters),
+    1024x1024 depth + Lambert image with a shadow any-hit ray, L2 loss against the image of a
+    second-seed heightfield; timed step = rq_fwd + rq_bwd; central FD check (h = 1e-3, and h/2 for a
+    Richardson column) on 256 random vertices whose pixels do not switch triangles; 100 Adam steps
+    (lr 1e-3) with BVH refit per step."""
     import torch
     import candela_gb300 as R
+    from candela_gb300 import _lib as L
     from candela_gb300 import scenes as S
     from candela_gb300.engine import diff_params
-    torch.cuda.set_device(0)
     mesh = S.c5_heightfield_scene(5)
     tmesh = S.c5_heightfield_scene(6)
     bvh = R.build_bvh(mesh.vertices, mesh.indices, mesh.mesh_ids, 0, layout=R.STACK)
     tb = R.build_bvh(tmesh.vertices, tmesh.indices, tmesh.mesh_ids, 0, layout=R.STACK)
-    ctx = R.Context(0)
+    ctx = ctx or R.Context(0)
     sc = ctx.scene(R.STACK, mesh.vertices, bvh.tris, bvh.nodes, R.identity_entity(0, bvh.nodes.shape[0]))
     tsc = ctx.scene(R.STACK, tmesh.vertices, tb.tris, tb.nodes, R.identity_entity(0, tb.nodes.shape[0]))
+    b8 = sc.build_bvh8()  # refitted by every update_positions below
     rays = S.camera_rays(1024, 1024, **S.C5_CAMERA)
     n = len(rays)
     d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
-    p = diff_params(shadow_rays=True)
-    target, _, t0 = tsc.forward(d_rays, torch.zeros((n, 2), device="cuda"), p)
+    p2 = diff_params(shadow_rays=True)
+    p = diff_params(shadow_rays=True, layout=L.LAYOUT_BVH8Q)  # same hits as the strict BVH2 walk
+    target, _, t0 = tsc.forward(d_rays, torch.zeros((n, 2), device="cuda"), p2)
     t0.close()
     grad = torch.empty((mesh.vertices.shape[0], 3), dtype=torch.float32, device="cuda")
     image = torch.empty((n, 2), dtype=torch.float32, device="cuda")
@@ -690,15 +756,32 @@ def run_c5(args):
         tape.close()
     torch.cuda.synchronize()
     evs = []
+    with ClockSampler(0) as clk:
+        clk.ready()
+        clk.mark_timed(True)
+        for i in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            _, _, tape = sc.forward(d_rays, target, p, image=image, want_loss=False)
+            tape.backward(grad)
+            b.record(stream)
+            evs.append((a, b, tape))
+        torch.cuda.synchronize()
+        clk.mark_timed(False)
+    step_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in evs)
+    for _, _, t in evs:
+        t.close()
+    # the same step tracing the strict BVH2
+    evs = []
     for i in range(args.steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        _, _, tape = sc.forward(d_rays, target, p, image=image, want_loss=False)
+        _, _, tape = sc.forward(d_rays, target, p2, image=image, want_loss=False)
         tape.backward(grad)
         b.record(stream)
         evs.append((a, b, tape))
     torch.cuda.synchronize()
-    step_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in evs)
+    step2_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in evs)
     for _, _, t in evs:
         t.close()
     # central finite differences on 256 vertices away from triangle switches
@@ -723,26 +806,29 @@ def run_c5(args):
         return ld, lr_, tri
 
     # depth-only gradient for the depth-only FD comparison (w_radiance = 0)
-    pd = diff_params(shadow_rays=True, w_radiance=0.0)
+    pd = diff_params(shadow_rays=True, w_radiance=0.0, layout=L.LAYOUT_BVH8Q)
     _, _, tape = sc.forward(d_rays, target, pd)
     gz_depth = tape.backward().cpu().numpy()[:, 2]
     tape.close()
     rng = np.random.default_rng(11)
     cand = np.nonzero(np.abs(gz) > 1e-3 * np.abs(gz).max())[0]
     rng.shuffle(cand)
-    plain, rich, depth_only, tried = [], [], [], 0
+    plain, rich, rich2, depth_only, tried = [], [], [], [], 0
     for v in cand:
         tried += 1
-        r = {dz: render(dz, v) for dz in (h, -h, h / 2, -h / 2)}
-        if not all(np.array_equal(r[h][2], r[dz][2]) for dz in (-h, h / 2, -h / 2)):
+        r = {dz: render(dz, v) for dz in (h, -h, h / 2, -h / 2, h / 4, -h / 4)}
+        if not all(np.array_equal(r[h][2], r[dz][2]) for dz in (-h, h / 2, -h / 2, h / 4, -h / 4)):
             continue  # a pixel switches triangle: not differentiable there
         tot = {dz: (r[dz][0] + r[dz][1]).sum() for dz in r}
         fd_h = (tot[h] - tot[-h]) / (2 * h)
         fd_h2 = (tot[h / 2] - tot[-h / 2]) / h
+        fd_h4 = (tot[h / 4] - tot[-h / 4]) / (h / 2)
         fd_rich = (4 * fd_h2 - fd_h) / 3
+        fd_rich2 = (16 * ((4 * fd_h4 - fd_h2) / 3) - fd_rich) / 15
         fd_d = (r[h][0].sum() - r[-h][0].sum()) / (2 * h)
         plain.append(abs(fd_h - gz[v]) / max(abs(fd_h), 1e-12))
         rich.append(abs(fd_rich - gz[v]) / max(abs(fd_rich), 1e-12))
+        rich2.append(abs(fd_rich2 - gz[v]) / max(abs(fd_rich2), 1e-12))
         depth_only.append(abs(fd_d - gz_depth[v]) / max(abs(fd_d), 1e-12))
         if len(plain) == 256 or tried > 3000:
             break
@@ -756,6 +842,7 @@ def run_c5(args):
                 "frac_within_1e-3": float((x <= 1e-3).mean()) if len(x) else None}
 
     fd_check = {"h": h, "central": stats(plain), "richardson_h_h2": stats(rich),
+                "richardson_h_h2_h4": stats(rich2),
                 "depth_only_central": stats(depth_only),
                 "note": "h = 1e-3 is 26% of a triangle edge on the 512x512 grid (cell 2/512), so the "
                         "central difference of the Lambert term carries an O(h^2) truncation error of "
@@ -780,17 +867,29 @@ def run_c5(args):
         z -= lr * (m1 / (1 - b1 ** k)) / ((m2 / (1 - b2 ** k)).sqrt() + eps)
     torch.cuda.synchronize()
     adam_s = time.perf_counter() - t_adam
-    line = {"metric": METRIC, "value": round(n / (step_ms / 1e3) / 1e6, 2), "unit": UNIT,
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded heightfields and camera rays)",
-            "config": {"workload": "differentiation: heightfield 512x512 (524,288 tris), 1024x1024 "
-                                   "depth + Lambert + shadow any-hit, L2 vs second-seed image; step = "
-                                   "rq_fwd + rq_bwd (primary rays counted)"},
+    sc.close()
+    tsc.close()
+    return {"workload": "differentiation: heightfield 512x512 (524,288 tris), 1024x1024 depth + Lambert "
+                        "+ shadow any-hit, L2 vs second-seed image; step = rq_fwd + rq_bwd (primary rays "
+                        "counted)",
+            "value": round(n / (step_ms / 1e3) / 1e6, 2), "unit": UNIT, "ms_per_step": round(step_ms, 4),
+            "traversal": "BVH8q (refitted after every position update; same hits as strict BVH2)",
+            "bvh8_nodes": b8["nodes"], "strict_bvh2_ms_per_step": round(step2_ms, 4),
             "fd_check": fd_check,
             "adam": {"steps": 100, "lr": lr, "loss_first": losses[0], "loss_last": losses[-1],
-                     "seconds": round(adam_s, 3)},
-            "initial_loss": loss0}
+                     "seconds": round(adam_s, 3), "traversal": "BVH8q refitted each step"},
+            "initial_loss": loss0, "device_status": ctx.device_status(), "clocks": clk.summary()}
+
+
+def run_c5(args):
+    import torch
+    torch.cuda.set_device(0)
+    rec = differentiation_record(args)
+    line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded heightfields and camera rays)", "config": {"workload": rec["workload"]},
+            "differentiation": rec, "clocks": rec["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -1090,23 +1189,39 @@ def main():
     c8 = breakdown[dom]["counts"]
     fetched8 = 80 * c8["node_visits"] + 64 * c8["triangle_tests"]
     k_ms = breakdown[dom]["ms"]
-    peak, peak_kind = load_peaks()
+    hbm_peak, peak_kind = load_peaks()
+    # the scene (about 90 MB of BVH8 nodes and triangle records) stays in the 129 MB L2, so the
+    # memory roof of the traversal is L2 read bandwidth, measured here with the same kind of loads
+    l2_peak = ctx.read_bandwidth(32 << 20, reps=500)
+    hbm_read = ctx.read_bandwidth(4 << 30, reps=6)  # the same probe over 4 GiB: HBM reads
     achieved = algo_bytes / (k_ms / 1e3) / 1e9
-    traffic = None
+    traffic = l2_bytes = None
     prof = ROOT / "profiles" / "ncu_traffic.txt"
     if prof.exists():
         for ln in prof.read_text().splitlines():
             f = ln.split()
-            if len(f) == 3 and not ln.startswith("#") and f[0] == args.config:
+            if len(f) >= 3 and not ln.startswith("#") and f[0] == args.config:
                 traffic = int(f[2])
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                l2_bytes = int(f[3]) if len(f) >= 4 else None
+    roofline = {"bound": "l2", "achieved": round(achieved, 1), "peak": round(l2_peak, 1), "unit": "GB/s",
+                "frac": round(achieved / l2_peak, 4), "traffic": traffic,
+                "peak_kind": "L2 read bandwidth measured in this run (rq_measure_read_gbs: 16-byte L1-bypassing "
+                             "loads from every SM over a 32 MiB buffer, 500 passes)",
+                "hbm_read_gbs_same_probe": round(hbm_read, 1),
                 "kernel": dom.replace("_", " ") + (" (k_bvh8_persistent)" if dom_persistent else " (k_bvh8)"),
                 "kernel_ms": k_ms,
                 "algorithmic_bytes_per_launch": int(algo_bytes),
                 "algorithmic_bytes_basis": "strict BVH2 work for the same rays: 64 B per node visit "
                                            "+ 64 B per triangle test",
                 "bvh8_fetched_bytes_per_launch": int(fetched8),
+                "frac_bvh8_fetched_of_l2": round(fetched8 / (k_ms / 1e3) / 1e9 / l2_peak, 4),
+                "l2_bytes_per_launch_ncu": l2_bytes,
+                "frac_l2_ncu": None if l2_bytes is None else round(l2_bytes / (k_ms / 1e3) / 1e9 / l2_peak, 4),
+                "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind,
+                "frac_hbm_ncu_dram": None if traffic is None else round(traffic / (k_ms / 1e3) / 1e9 / hbm_peak, 4),
+                "frac_hbm_algorithmic": round(achieved / hbm_peak, 4),
+                "limiter": "instruction issue and fetch latency of divergent warps (neither L2 nor DRAM "
+                           "bandwidth is near its roof); see profiles/k_bvh8_persistent_c2_secondary.md",
                 "active_rays": n_sec}
     for k in list(breakdown):
         breakdown[k].pop("counts", None)
@@ -1144,6 +1259,12 @@ def main():
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+        if not args.no_legs and args.config == "c2":
+            # the metric's batched leg and the precision / differentiation workloads, each timed with
+            # CUDA events inside its own clock-sampled window
+            line["batched"] = batched_record(args, ctx, flush)
+            line["precision"] = precision_record(args, ctx, flush)
+            line["differentiation"] = differentiation_record(args, ctx)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

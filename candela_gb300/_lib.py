@@ -37,14 +37,19 @@ assert ENTITY_DTYPE.itemsize == 192 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.i
 class RqOpts(C.Structure):
     _fields_ = [("layout", C.c_int32), ("mode", C.c_int32), ("tie", C.c_int32),
                 ("flags", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
-                ("persistent", C.c_int32), ("reserved", C.c_int32)]
+                ("persistent", C.c_int32), ("stack_depth", C.c_int32)]
+
+
+MAX_VARIANTS = 10
+MAX_BATCH_COMBOS = 16
 
 
 class RqTuneResult(C.Structure):
     _fields_ = [("variant", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
-                ("persistent", C.c_int32), ("n_variants", C.c_int32), ("ms", C.c_float * 8),
-                ("block", C.c_int32 * 8), ("min_blocks_of", C.c_int32 * 8),
-                ("persistent_of", C.c_int32 * 8)]
+                ("persistent", C.c_int32), ("n_variants", C.c_int32), ("depth", C.c_int32),
+                ("ms", C.c_float * MAX_VARIANTS), ("block", C.c_int32 * MAX_VARIANTS),
+                ("min_blocks_of", C.c_int32 * MAX_VARIANTS), ("persistent_of", C.c_int32 * MAX_VARIANTS),
+                ("depth_of", C.c_int32 * MAX_VARIANTS)]
 
 
 class RqBuildOpts(C.Structure):
@@ -66,7 +71,8 @@ class RqBvh8Info(C.Structure):
 class RqDiffParams(C.Structure):
     _fields_ = [("sun_dir", C.c_float * 3), ("sun_color", C.c_float), ("albedo", C.c_float),
                 ("w_depth", C.c_float), ("w_radiance", C.c_float), ("shadow_rays", C.c_int32),
-                ("shadow_offset", C.c_float), ("recompute", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("shadow_offset", C.c_float), ("recompute", C.c_int32), ("layout", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class RqQuery(C.Structure):
@@ -76,8 +82,9 @@ class RqQuery(C.Structure):
 
 class RqBatchTune(C.Structure):
     _fields_ = [("family", C.c_int32), ("block_size", C.c_int32), ("min_blocks", C.c_int32),
-                ("n", C.c_int32), ("ms", C.c_float * 12), ("family_of", C.c_int32 * 12),
-                ("block_of", C.c_int32 * 12), ("min_blocks_of", C.c_int32 * 12)]
+                ("n", C.c_int32), ("depth", C.c_int32), ("ms", C.c_float * MAX_BATCH_COMBOS),
+                ("family_of", C.c_int32 * MAX_BATCH_COMBOS), ("block_of", C.c_int32 * MAX_BATCH_COMBOS),
+                ("min_blocks_of", C.c_int32 * MAX_BATCH_COMBOS), ("depth_of", C.c_int32 * MAX_BATCH_COMBOS)]
 
 
 class RqGiParams(C.Structure):
@@ -86,7 +93,12 @@ class RqGiParams(C.Structure):
                 ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
                 ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3),
                 ("sky_color", C.c_float * 3), ("sort_rays", C.c_int32), ("unfused", C.c_int32),
-                ("bounces", C.c_int32)]
+                ("bounces", C.c_int32), ("compact_below", C.c_float)]
+
+
+class RqGiTune(C.Structure):
+    _fields_ = [("compact_below", C.c_float), ("live_fraction", C.c_float), ("ms_compact", C.c_float),
+                ("ms_in_place", C.c_float)]
 
 
 class RqTexture(C.Structure):
@@ -175,6 +187,7 @@ SIGNATURES = {
     "rq_measure_read_gbs": (_S, [_P, _I64, _I32, C.POINTER(C.c_double)]),
     "rq_hit_attribs": (_S, [_P, _P, _P, _I64, _P, C.POINTER(RqOpts), _P]),
     "rq_closest_attribs": (_S, [_P, _P, _P, _I64, _P, _P, C.POINTER(RqOpts), _P]),
+    "rq_gi_autotune": (_S, [_P, _P, _P, _I64, C.POINTER(RqGiParams), C.POINTER(RqOpts), _P, C.POINTER(RqGiTune)]),
 }
 
 NOALLOC_MAX_RAYS = 65536

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "rq_bvh8_walk.cuh"
 #include "rq_objects.h"
 #include "rq_strict.cuh"
 
@@ -44,6 +45,7 @@ struct DiffArgs {
     float w_depth, w_rad;
     int shadow;
     float shadow_offset;
+    int bvh8;  // trace the BVH8q (same hits as the strict BVH2 walk)
 };
 
 DiffArgs to_args(const rq_diff_params& p) {
@@ -54,6 +56,7 @@ DiffArgs to_args(const rq_diff_params& p) {
     a.w_rad = p.w_radiance;
     a.shadow = p.shadow_rays;
     a.shadow_offset = p.shadow_offset;
+    a.bvh8 = p.layout == RQ_LAYOUT_BVH8Q ? 1 : 0;
     return a;
 }
 
@@ -63,18 +66,26 @@ __device__ __forceinline__ f3 fcross(f3 a, f3 b) {
 }
 __device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-// Forward: strict closest hit, geometric-normal Lambert, optional strict any-hit shadow ray.
+// Forward: strict closest hit, geometric-normal Lambert, optional strict any-hit shadow ray; on the
+// BVH8q (kBvh8) the walks give the same hits and occlusion (strict leaf test, conservative boxes).
+template <bool kBvh8>
 __global__ void k_diff_fwd(SceneView s, const rq_ray* __restrict__ rays, int64_t n,
                            const float2* __restrict__ target, DiffArgs a, float2* __restrict__ image,
                            float4* __restrict__ hits, float2* __restrict__ gimg,
-                           float* __restrict__ loss_pp) {
+                           float* __restrict__ loss_pp, unsigned* status_out) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * i;
     const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
     rq_hit h;
-    int32_t tests = 0;
-    strict::scene_closest<false, true>(s, r0, r1, 0, h, tests);
+    int32_t tests = 0, visits = 0;
+    unsigned status = 0;
+    if (kBvh8) {
+        bool occ;
+        bvh8_ray<false>(s, r0, r1, 0, h, occ, visits, tests, status);
+    } else {
+        strict::scene_closest<false, true>(s, r0, r1, 0, h, tests);
+    }
     float depth = 0.0f, rad = 0.0f, lit = 0.0f;
     float2 g = make_float2(0.0f, 0.0f);
     float l = 0.0f;
@@ -95,7 +106,14 @@ __global__ void k_diff_fwd(SceneView s, const rq_ray* __restrict__ rays, int64_t
                                           P.z + N.z * a.shadow_offset, 0.0f);
             const float4 s1 = make_float4(a.m.x, a.m.y, a.m.z, 1000000.0f);
             int32_t it = 0, te = 0;
-            lit = strict::scene_any<false>(s, s0, s1, it, te) ? 0.0f : 1.0f;
+            if (kBvh8) {
+                rq_hit hs;
+                bool occ = false;
+                bvh8_ray<true>(s, s0, s1, 0, hs, occ, it, te, status);
+                lit = occ ? 0.0f : 1.0f;
+            } else {
+                lit = strict::scene_any<false>(s, s0, s1, it, te) ? 0.0f : 1.0f;
+            }
         }
         depth = h.t;
         rad = a.c * lit * fmaxf(f, 0.0f);
@@ -111,6 +129,7 @@ __global__ void k_diff_fwd(SceneView s, const rq_ray* __restrict__ rays, int64_t
         hits[2 * i] = make_float4(h.t, h.u, h.v, h.w);
         hits[2 * i + 1] = make_float4(__int_as_float(h.t > 0.0f ? h.tri : -1), lit, 0.0f, 0.0f);
     }
+    if (status) atomicOr(status_out, status);
 }
 
 // Deterministic sum: each block sums a contiguous range in a fixed tree order.
@@ -417,6 +436,10 @@ rq_status prepare_scene(rq_ctx* ctx, rq_scene* sc) {
 rq_status check_diff(rq_ctx* ctx, const rq_scene* sc, const rq_diff_params* p) {
     if (!p) return fail(ctx, RQ_EINVAL, "NULL diff params");
     if (!sc->view.all_identity) return fail(ctx, RQ_ENOTSUP, "the adjoint needs identity entities");
+    if (p->layout != 0 && p->layout != RQ_LAYOUT_BVH8Q && p->layout != sc->layout)
+        return fail(ctx, RQ_EINVAL, "diff params: layout must be 0, the scene's BVH2 layout or RQ_LAYOUT_BVH8Q");
+    if (p->layout == RQ_LAYOUT_BVH8Q && !sc->bvh8)
+        return fail(ctx, RQ_ENOTSUP, "BVH8 not built: call rq_scene_build_bvh8");
     if (sc->n_tris >= (int64_t(1) << 30)) return fail(ctx, RQ_EINVAL, "too many triangles");
     return RQ_OK;
 }
@@ -430,9 +453,14 @@ rq_status forward(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, int64_t n
     if ((s = scratch(ctx, rq::kSlotLossPerPixel, sizeof(float) * n, &d_lpp)) != RQ_OK ||
         (s = scratch(ctx, rq::kSlotLossPartials, sizeof(float) * 256, &d_part)) != RQ_OK)
         return s;
-    k_diff_fwd<<<grid(n, 128), 128, 0, st>>>(sc->view, rays, n, reinterpret_cast<const float2*>(target),
-                                              a, reinterpret_cast<float2*>(image), hits, gimg,
-                                              static_cast<float*>(d_lpp));
+    if (a.bvh8)
+        k_diff_fwd<true><<<grid(n, 128), 128, 0, st>>>(sc->view, rays, n, reinterpret_cast<const float2*>(target),
+                                                        a, reinterpret_cast<float2*>(image), hits, gimg,
+                                                        static_cast<float*>(d_lpp), status_word(ctx));
+    else
+        k_diff_fwd<false><<<grid(n, 128), 128, 0, st>>>(sc->view, rays, n, reinterpret_cast<const float2*>(target),
+                                                         a, reinterpret_cast<float2*>(image), hits, gimg,
+                                                         static_cast<float*>(d_lpp), status_word(ctx));
     RQ_CUDA(ctx, cudaGetLastError());
     if (loss) {
         k_sum_blocks<<<256, 256, 0, st>>>(static_cast<float*>(d_lpp), n, static_cast<float*>(d_part));
@@ -470,9 +498,9 @@ rq_status rq_scene_update_positions(rq_scene* sc, const float* xyz, void* stream
     }
     RQ_CUDA(ctx, rq::launch_tri_fast(sc->d_tris, sc->n_tris, sc->d_verts, sc->d_tri_fast, st));
     RQ_CUDA(ctx, cudaGetLastError());
-    sc->bvh8 = false;          // quantised boxes are not refitted
-    sc->view.tlas = nullptr;   // nor are the top-level boxes: every entity is walked until the
-                               // entities or the BVH8 are set again
+    if ((s = rq::refit_bvh8(sc, st)) != RQ_OK) return s;  // quantised boxes refitted, topology kept
+    sc->view.tlas = nullptr;   // the top-level boxes are not refitted: every entity is walked until
+                               // the entities or the BVH8 are set again
     sc->host_stale = true;     // host copies of vertices / nodes are refreshed on demand
     return RQ_OK;
 }

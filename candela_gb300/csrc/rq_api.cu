@@ -57,14 +57,21 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
     q.block = o->block_size;
     q.counters = (o->flags & RQ_FLAG_COUNT) ? work_counters(ctx) : nullptr;
     q.variant_closest = q.variant_any = -1;
-    if (o->block_size || o->min_blocks || o->persistent) {
+    int di = 0;
+    rq_status ds = depth_index_of(ctx, o, di);
+    if (ds != RQ_OK) return ds;
+    if (o->block_size || o->min_blocks || o->persistent || o->stack_depth) {
+        // stack_depth 0 (or 48) names the default-depth variant
+        const int want_depth = di == 0 ? 0 : bvh8_depth(di);
         int found = -1;
         for (int v = 0; v < kNumLaunchVariants; ++v)
             if (kLaunchVariants[v].block == o->block_size &&
                 kLaunchVariants[v].min_blocks == o->min_blocks &&
-                kLaunchVariants[v].persistent == (o->persistent ? 1 : 0))
+                kLaunchVariants[v].persistent == (o->persistent ? 1 : 0) &&
+                kLaunchVariants[v].depth == want_depth)
                 found = v;
-        if (found < 0) return fail(ctx, RQ_EINVAL, "no compiled launch variant with that block size / min_blocks");
+        if (found < 0)
+            return fail(ctx, RQ_EINVAL, "no compiled launch variant with that block size / min_blocks / stack depth");
         q.variant_closest = q.variant_any = found;
     } else if (q.layout >= 0 && q.layout < 4) {
         q.variant_closest = sc->tuned[q.layout][0];
@@ -89,15 +96,64 @@ rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, Query
     return RQ_OK;
 }
 
+rq_status depth_index_of(rq_ctx* ctx, const rq_opts* o, int& index) {
+    index = 0;
+    if (!o || o->stack_depth == 0) return RQ_OK;
+    for (int k = 0; k < 3; ++k)
+        if (kBvh8Depths[k] == o->stack_depth) {
+            index = k;
+            return RQ_OK;
+        }
+    return fail(ctx, RQ_EINVAL, "stack_depth must be 0, 48, 32 or 24");
+}
+
 rq_status refresh_host(rq_scene* sc) {
-    if (!sc->host_stale) return RQ_OK;
     rq_ctx* ctx = sc->ctx;
-    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
-    RQ_CUDA(ctx, cudaDeviceSynchronize());
-    RQ_CUDA(ctx, cudaMemcpy(sc->h_nodes.data(), sc->d_nodes, sc->h_nodes.size() * 4, cudaMemcpyDeviceToHost));
-    RQ_CUDA(ctx, cudaMemcpy(sc->h_verts.data(), sc->d_verts, sc->h_verts.size() * 4, cudaMemcpyDeviceToHost));
-    sc->host_stale = false;
+    if (sc->host_stale) {
+        RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+        RQ_CUDA(ctx, cudaDeviceSynchronize());
+        RQ_CUDA(ctx, cudaMemcpy(sc->h_nodes.data(), sc->d_nodes, sc->h_nodes.size() * 4, cudaMemcpyDeviceToHost));
+        RQ_CUDA(ctx, cudaMemcpy(sc->h_verts.data(), sc->d_verts, sc->h_verts.size() * 4, cudaMemcpyDeviceToHost));
+        sc->host_stale = false;
+    }
+    if (sc->bvh8 && sc->b8_bounds_stale) {
+        // the root nodes of the refitted BVH8, copied back one by one (a handful per scene)
+        RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+        RQ_CUDA(ctx, cudaDeviceSynchronize());
+        std::vector<uint32_t> roots(sc->h_b8roots.size() * kBvh8NodeWords, 0u);
+        for (size_t i = 0; i < sc->h_b8roots.size(); ++i)
+            if (sc->h_b8roots[i] >= 0)
+                RQ_CUDA(ctx, cudaMemcpy(roots.data() + i * kBvh8NodeWords,
+                                        reinterpret_cast<const uint32_t*>(sc->d_b8nodes) +
+                                            static_cast<int64_t>(sc->h_b8roots[i]) * kBvh8NodeWords,
+                                        kBvh8NodeWords * 4, cudaMemcpyDeviceToHost));
+        bvh8_root_bounds(sc, roots);
+        sc->b8_bounds_stale = false;
+    }
     return RQ_OK;
+}
+
+// b8_bounds[6 i ..]: the union of entity i's BVH8 root child boxes, one grid step wider (the kernel
+// pads its slab test by half a step plus rounding); root_nodes holds each entity's root node.
+void bvh8_root_bounds(rq_scene* sc, const std::vector<uint32_t>& root_nodes) {
+    sc->b8_bounds.assign(6 * sc->h_ents.size(), 0.0);
+    for (size_t i = 0; i < sc->h_ents.size() && i < sc->h_b8roots.size(); ++i) {
+        double* bb = &sc->b8_bounds[6 * i];
+        bb[0] = bb[1] = bb[2] = 1e300;
+        bb[3] = bb[4] = bb[5] = -1e300;
+        if (sc->h_b8roots[i] < 0) continue;
+        const uint32_t* nd = root_nodes.data() + i * kBvh8NodeWords;
+        for (int c = 0; c < 8; ++c) {
+            float lo[3], hi[3];
+            bvh8_decode_child(nd, c, lo, hi);
+            if (!(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2])) continue;  // empty slot
+            for (int a = 0; a < 3; ++a) {
+                const double step = std::ldexp(1.0, static_cast<int>((nd[3] >> (8 * a)) & 0xFFu) - 127);
+                bb[a] = std::min(bb[a], double(lo[a]) - step);
+                bb[3 + a] = std::max(bb[3 + a], double(hi[a]) + step);
+            }
+        }
+    }
 }
 
 rq_status rebuild_tlas(rq_scene* sc) {
@@ -637,26 +693,57 @@ rq_status rq_scene_build_bvh8(rq_scene* sc, rq_bvh8_info* info) {
     sc->view.b8_tris = sc->d_b8tris;
     sc->view.b8_roots = sc->d_b8roots;
     sc->bvh8 = true;
-    // object-space bounds of each entity's BVH8 root children, one grid step wider (the kernel
-    // pads its slab test by half a step plus rounding)
     sc->h_b8roots = b.roots;
-    sc->b8_bounds.assign(6 * sc->h_ents.size(), 0.0);
-    for (size_t i = 0; i < sc->h_ents.size() && i < b.roots.size(); ++i) {
-        double* bb = &sc->b8_bounds[6 * i];
-        bb[0] = bb[1] = bb[2] = 1e300;
-        bb[3] = bb[4] = bb[5] = -1e300;
-        if (b.roots[i] < 0) continue;
-        const uint32_t* nd = b.nodes.data() + static_cast<size_t>(b.roots[i]) * rq::kBvh8NodeWords;
-        for (int c = 0; c < 8; ++c) {
-            float lo[3], hi[3];
-            rq::bvh8_decode_child(nd, c, lo, hi);
-            if (!(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2])) continue;  // empty slot
-            for (int a = 0; a < 3; ++a) {
-                const double step = std::ldexp(1.0, static_cast<int>((nd[3] >> (8 * a)) & 0xFFu) - 127);
-                bb[a] = std::min(bb[a], double(lo[a]) - step);
-                bb[3 + a] = std::max(bb[3 + a], double(hi[a]) + step);
+    {
+        std::vector<uint32_t> roots(b.roots.size() * rq::kBvh8NodeWords, 0u);
+        for (size_t i = 0; i < b.roots.size(); ++i)
+            if (b.roots[i] >= 0)
+                std::memcpy(roots.data() + i * rq::kBvh8NodeWords,
+                            b.nodes.data() + static_cast<size_t>(b.roots[i]) * rq::kBvh8NodeWords,
+                            rq::kBvh8NodeWords * 4);
+        rq::bvh8_root_bounds(sc, roots);
+    }
+    sc->b8_bounds_stale = false;
+    // refit plan: nodes level by level from each distinct root down (children of node x are
+    // child_base + 0 .. popc(imask) - 1)
+    {
+        std::vector<int32_t> level(static_cast<size_t>(b.n_nodes), -1);
+        std::vector<int32_t> cur, next;
+        for (int32_t r : b.roots)
+            if (r >= 0 && level[r] < 0) {
+                level[r] = 0;
+                cur.push_back(r);
             }
+        std::vector<int32_t> order;
+        sc->b8_level_off.assign(1, 0);
+        while (!cur.empty()) {
+            order.insert(order.end(), cur.begin(), cur.end());
+            sc->b8_level_off.push_back(static_cast<int64_t>(order.size()));
+            next.clear();
+            for (int32_t x : cur) {
+                const uint32_t* nd = b.nodes.data() + static_cast<size_t>(x) * rq::kBvh8NodeWords;
+                const int ni = __builtin_popcount(nd[3] >> 24);
+                for (int i = 0; i < ni; ++i) {
+                    const int32_t c = static_cast<int32_t>(nd[4]) + i;
+                    if (c >= 0 && c < b.n_nodes && level[c] < 0) {
+                        level[c] = level[x] + 1;
+                        next.push_back(c);
+                    }
+                }
+            }
+            cur.swap(next);
         }
+        if (sc->d_b8_order) cudaFree(sc->d_b8_order);
+        if (sc->d_b8box) cudaFree(sc->d_b8box);
+        sc->d_b8_order = nullptr;
+        sc->d_b8box = nullptr;
+        if (cudaMalloc(&sc->d_b8_order, sizeof(int32_t) * std::max<size_t>(1, order.size())) != cudaSuccess ||
+            cudaMalloc(&sc->d_b8box, sizeof(float) * 6 * std::max<int64_t>(1, b.n_nodes)) != cudaSuccess)
+            return fail(ctx, RQ_ENOMEM, "BVH8 refit plan allocation failed");
+        if (!order.empty())
+            RQ_CUDA(ctx, cudaMemcpy(sc->d_b8_order, order.data(), sizeof(int32_t) * order.size(),
+                                    cudaMemcpyHostToDevice));
+        sc->b8_bytes += static_cast<int64_t>(sizeof(int32_t) * order.size() + sizeof(float) * 6 * b.n_nodes);
     }
     if ((st0 = rq::rebuild_tlas(sc)) != RQ_OK) return st0;
     if (info) {
@@ -689,13 +776,21 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, 
     float best = 1e30f;
     int best_v = 0;
     cudaStream_t st = ctx->stream;
+    // status bits of earlier work are kept aside; a trial that overflows its group stack is rejected
+    unsigned prior = 0;
+    RQ_CUDA(ctx, cudaDeviceSynchronize());
+    RQ_CUDA(ctx, cudaMemcpy(&prior, rq::status_word(ctx), sizeof(unsigned), cudaMemcpyDeviceToHost));
     for (int v = 0; v < kNumLaunchVariants; ++v) {
         out->block[v] = kLaunchVariants[v].block;
         out->min_blocks_of[v] = kLaunchVariants[v].min_blocks;
         out->persistent_of[v] = kLaunchVariants[v].persistent;
+        out->depth_of[v] = kLaunchVariants[v].depth ? kLaunchVariants[v].depth : rq::bvh8_depth(0);
         out->ms[v] = -1.0f;
         if (kLaunchVariants[v].persistent && q.mode == RQ_MODE_FAST) continue;
+        // the group-stack depth is a BVH8 knob: the BVH2 walks keep the reference's stack
+        if (kLaunchVariants[v].depth && q.layout != RQ_LAYOUT_BVH8Q) continue;
         q.variant_closest = q.variant_any = v;
+        RQ_CUDA(ctx, cudaMemsetAsync(rq::status_word(ctx), 0, sizeof(unsigned), st));
         float vbest = 1e30f;
         for (int rep = 0; rep < 4; ++rep) {
             RQ_CUDA(ctx, cudaEventRecord(a, st));
@@ -709,12 +804,19 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, 
             RQ_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
             if (rep > 0) vbest = std::min(vbest, ms);  // rep 0 is the warm-up
         }
+        unsigned bits = 0;
+        RQ_CUDA(ctx, cudaMemcpy(&bits, rq::status_word(ctx), sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (bits & rq::kStatusOverflowBit) {
+            out->ms[v] = -2.0f;  // the stack overflowed on these rays: not usable
+            continue;
+        }
         out->ms[v] = vbest;
         if (vbest < best) {
             best = vbest;
             best_v = v;
         }
     }
+    RQ_CUDA(ctx, cudaMemcpy(rq::status_word(ctx), &prior, sizeof(unsigned), cudaMemcpyHostToDevice));
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     sc->tuned[q.layout][query] = static_cast<int8_t>(best_v);
@@ -722,6 +824,7 @@ rq_status rq_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* rays, int64_t n, 
     out->block_size = kLaunchVariants[best_v].block;
     out->min_blocks = kLaunchVariants[best_v].min_blocks;
     out->persistent = kLaunchVariants[best_v].persistent;
+    out->depth = out->depth_of[best_v];
     return RQ_OK;
 }
 
@@ -766,6 +869,8 @@ rq_status rq_scene_destroy(rq_scene* sc) {
     if (sc->d_b8nodes) cudaFree(sc->d_b8nodes);
     if (sc->d_b8tris) cudaFree(sc->d_b8tris);
     if (sc->d_b8roots) cudaFree(sc->d_b8roots);
+    if (sc->d_b8_order) cudaFree(sc->d_b8_order);
+    if (sc->d_b8box) cudaFree(sc->d_b8box);
     if (sc->d_refit) cudaFree(sc->d_refit);
     if (sc->d_tri_fast) cudaFree(sc->d_tri_fast);
     if (sc->d_adj_off) cudaFree(sc->d_adj_off);

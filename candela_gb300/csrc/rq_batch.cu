@@ -14,6 +14,7 @@ struct rq_batch_plan {
     rq_opts opts{};
     int32_t family = rq::kFamilyStrict;
     int32_t variant = 0;
+    int32_t depth_index = 0;  // BVH8 group-stack depth (bvh8::kStackDepths)
     int64_t total = 0;
     rq::QueryDesc* d_desc = nullptr;
     unsigned long long* d_queue = nullptr;
@@ -66,12 +67,12 @@ rq_status capture(rq_batch_plan* p) {
     p->exec = nullptr;
     p->graph = nullptr;
     // occupancy queries happen here, before the capture starts
-    RQ_CUDA(ctx, launch_batch(p->d_desc, 1, 1, p->family, p->variant, nullptr, nullptr, nullptr));
+    RQ_CUDA(ctx, launch_batch(p->d_desc, 1, 1, p->family, p->variant, nullptr, nullptr, nullptr, p->depth_index));
     RQ_CUDA(ctx, cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned long long), p->cap);
     if (e == cudaSuccess)
         e = launch_batch(p->d_desc, static_cast<int>(p->desc.size()), p->total, p->family, p->variant,
-                         p->d_queue, status_word(ctx), p->cap);
+                         p->d_queue, status_word(ctx), p->cap, p->depth_index);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(p->cap, &g);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch capture");
@@ -124,8 +125,10 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
                 variant = v;
         if (variant < 0) return fail(ctx, RQ_EINVAL, "no compiled batch variant with that block size");
     }
+    int di = 0;
+    if ((s = rq::depth_index_of(ctx, opts, di)) != RQ_OK) return s;
     RQ_CUDA(ctx, rq::launch_batch(static_cast<rq::QueryDesc*>(d), n_queries, total, family, variant,
-                                  queue, rq::status_word(ctx), st));
+                                  queue, rq::status_word(ctx), st, di));
     return RQ_OK;
 }
 
@@ -144,6 +147,10 @@ rq_status rq_batch_plan_create(rq_ctx* ctx, const rq_query* queries, int32_t n_q
     if (n_queries < 1 || n_queries > rq::kMaxBatchQueries) {
         delete p;
         return fail(ctx, RQ_EINVAL, "1..1024 queries per batch");
+    }
+    if ((s = rq::depth_index_of(ctx, opts, p->depth_index)) != RQ_OK) {
+        delete p;
+        return s;
     }
     if (cudaMalloc(&p->d_desc, sizeof(rq::QueryDesc) * n_queries) != cudaSuccess ||
         cudaMalloc(&p->d_queue, sizeof(unsigned long long)) != cudaSuccess ||
@@ -177,50 +184,70 @@ rq_status rq_batch_plan_autotune(rq_batch_plan* p, int32_t allow_bvh8, rq_batch_
     cudaEvent_t a, b;
     RQ_CUDA(ctx, cudaEventCreate(&a));
     RQ_CUDA(ctx, cudaEventCreate(&b));
+    // the status bits of earlier work are kept aside: a stack overflow during a trial marks that
+    // depth as unusable for this batch
+    unsigned prior = 0;
+    RQ_CUDA(ctx, cudaDeviceSynchronize());
+    RQ_CUDA(ctx, cudaMemcpy(&prior, rq::status_word(ctx), sizeof(unsigned), cudaMemcpyDeviceToHost));
     float best = 1e30f;
-    int best_f = p->family, best_v = p->variant;
+    int best_f = p->family, best_v = p->variant, best_d = p->depth_index;
     int k = 0;
     for (int fi = 0; fi < 2; ++fi) {
-        for (int v = 0; v < rq::kNumBatchVariants; ++v, ++k) {
-            out->family_of[k] = fams[fi];
-            out->block_of[k] = rq::kBatchVariants[v].block;
-            out->min_blocks_of[k] = rq::kBatchVariants[v].min_blocks;
-            out->ms[k] = -1.0f;
-            if (fams[fi] == rq::kFamilyBvh8 && !all_b8) continue;
-            p->family = fams[fi];
-            rq_status s = rq::upload(p);
-            if (s != RQ_OK) return s;
-            float vbest = 1e30f;
-            for (int rep = 0; rep < 4; ++rep) {
-                RQ_CUDA(ctx, cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned long long), p->cap));
-                RQ_CUDA(ctx, cudaEventRecord(a, p->cap));
-                RQ_CUDA(ctx, rq::launch_batch(p->d_desc, static_cast<int>(p->desc.size()), p->total,
-                                              p->family, v, p->d_queue, rq::status_word(ctx), p->cap));
-                RQ_CUDA(ctx, cudaEventRecord(b, p->cap));
-                RQ_CUDA(ctx, cudaEventSynchronize(b));
-                float ms = 0.0f;
-                RQ_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
-                if (rep > 0) vbest = std::min(vbest, ms);
-            }
-            out->ms[k] = vbest;
-            if (vbest < best) {
-                best = vbest;
-                best_f = fams[fi];
-                best_v = v;
+        const int n_depths = fams[fi] == rq::kFamilyBvh8 ? rq::kNumBatchDepths : 1;
+        for (int di = 0; di < n_depths; ++di) {
+            for (int v = 0; v < rq::kNumBatchVariants; ++v, ++k) {
+                out->family_of[k] = fams[fi];
+                out->block_of[k] = rq::kBatchVariants[v].block;
+                out->min_blocks_of[k] = rq::kBatchVariants[v].min_blocks;
+                out->depth_of[k] = fams[fi] == rq::kFamilyBvh8 ? rq::bvh8_depth(di) : 0;
+                out->ms[k] = -1.0f;
+                if (fams[fi] == rq::kFamilyBvh8 && !all_b8) continue;
+                p->family = fams[fi];
+                rq_status s = rq::upload(p);
+                if (s != RQ_OK) return s;
+                RQ_CUDA(ctx, cudaMemset(rq::status_word(ctx), 0, sizeof(unsigned)));
+                float vbest = 1e30f;
+                for (int rep = 0; rep < 4; ++rep) {
+                    RQ_CUDA(ctx, cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned long long), p->cap));
+                    RQ_CUDA(ctx, cudaEventRecord(a, p->cap));
+                    RQ_CUDA(ctx, rq::launch_batch(p->d_desc, static_cast<int>(p->desc.size()), p->total,
+                                                  p->family, v, p->d_queue, rq::status_word(ctx), p->cap, di));
+                    RQ_CUDA(ctx, cudaEventRecord(b, p->cap));
+                    RQ_CUDA(ctx, cudaEventSynchronize(b));
+                    float ms = 0.0f;
+                    RQ_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+                    if (rep > 0) vbest = std::min(vbest, ms);
+                }
+                unsigned bits = 0;
+                RQ_CUDA(ctx, cudaMemcpy(&bits, rq::status_word(ctx), sizeof(unsigned), cudaMemcpyDeviceToHost));
+                if (bits & rq::kStatusOverflowBit) {
+                    out->ms[k] = -2.0f;  // overflowed: results would be incomplete
+                    continue;
+                }
+                out->ms[k] = vbest;
+                if (vbest < best) {
+                    best = vbest;
+                    best_f = fams[fi];
+                    best_v = v;
+                    best_d = di;
+                }
             }
         }
     }
+    RQ_CUDA(ctx, cudaMemcpy(rq::status_word(ctx), &prior, sizeof(unsigned), cudaMemcpyHostToDevice));
     out->n = k;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     p->family = best_f;
     p->variant = best_v;
+    p->depth_index = best_f == rq::kFamilyBvh8 ? best_d : 0;
     rq_status s = rq::upload(p);
     if (s != RQ_OK) return s;
     if ((s = rq::capture(p)) != RQ_OK) return s;
     out->family = best_f;
     out->block_size = rq::kBatchVariants[best_v].block;
     out->min_blocks = rq::kBatchVariants[best_v].min_blocks;
+    out->depth = best_f == rq::kFamilyBvh8 ? rq::bvh8_depth(p->depth_index) : 0;
     return RQ_OK;
 }
 

@@ -23,7 +23,11 @@ namespace bvh8 {
 
 using strict::f3;
 
-constexpr int kStack = 48;         // group stack entries per lane
+constexpr int kStack = 48;         // group stack entries per lane (the default depth)
+// Group-stack depths the launch variants are compiled for (the autotuner picks among them; a
+// walk that would push beyond its depth sets kStatusStackOverflow, and the tuner rejects that
+// variant).  A shallower stack is a smaller local-memory frame per lane.
+constexpr int kStackDepths[3] = {48, 32, 24};
 constexpr int kMaxVisits = 1 << 16;  // node visits per ray and entity before RQ_EBUDGET
 
 enum : unsigned { kStatusStackOverflow = 1u, kStatusBudget = 2u };
@@ -92,8 +96,8 @@ __device__ __forceinline__ Walk walk_begin(int32_t root) { return Walk{0ull, roo
 
 // Visits node w.node (box tests of its eight children, then its leaf triangles) and selects the
 // node after it.  Returns false when the walk has ended (stack empty, any-hit found, or an
-// overflow/budget status bit set).
-template <bool kAny, bool kTieLower>
+// overflow/budget status bit set).  `stack` holds kDepth entries.
+template <bool kAny, bool kTieLower, int kDepth = kStack>
 __device__ __forceinline__ bool step(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                      const Ray8& r, float tmin, Hit8& h, Walk& w, uint64_t* stack,
                                      int32_t& tests, unsigned& status) {
@@ -218,7 +222,7 @@ __device__ __forceinline__ bool step(const uint4* __restrict__ nodes, const floa
             }
             if (hits_oct) {
                 if (static_cast<uint32_t>(group >> 32) & 0xFFu) {
-                    if (sp >= kStack) {
+                    if (sp >= kDepth) {
                         status |= kStatusStackOverflow;
                         return false;
                     }
@@ -247,13 +251,13 @@ __device__ __forceinline__ bool step(const uint4* __restrict__ nodes, const floa
 }
 
 // Visits the BVH8 rooted at `root`.  Returns the node-visit count; sets *status bits on overflow.
-template <bool kAny, bool kTieLower>
+template <bool kAny, bool kTieLower, int kDepth = kStack>
 __device__ int32_t traverse(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                             int32_t root, const Ray8& r, float tmin, Hit8& h, int32_t& tests,
                             unsigned& status) {
-    uint64_t stack[kStack];
+    uint64_t stack[kDepth];
     Walk w = walk_begin(root);
-    while (step<kAny, kTieLower>(nodes, tris, r, tmin, h, w, stack, tests, status)) {
+    while (step<kAny, kTieLower, kDepth>(nodes, tris, r, tmin, h, w, stack, tests, status)) {
     }
     return w.visits;
 }

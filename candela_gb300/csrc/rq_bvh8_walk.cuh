@@ -55,7 +55,7 @@ __device__ __forceinline__ void bvh8_finish(const SceneView& s, int flags, const
 }
 
 // BVH8 traversal of one ray with the strict scene loop around it.
-template <bool kAny, bool kTlas = true>
+template <bool kAny, bool kTlas = true, int kDepth = bvh8::kStack>
 __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, const float4 r1, int flags,
                                          rq_hit& hh, bool& occluded, int32_t& visits,
                                          int32_t& tests, unsigned& status) {
@@ -85,7 +85,7 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
                                                     strict::xform(E.inverse, d, 0.0f));
                 // an equal (t, triangle) from a lower entity wins: let the walk take it
                 bvh8::Hit8 h{tmax, -1.0f, (ent >= 0 && e < ent) ? tri + 1 : tri, -1};
-                visits += bvh8::traverse<false, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests, status);
+                visits += bvh8::traverse<false, true, kDepth>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests, status);
                 const float T = h.closest;
                 if (T > 0.0f && (T < tmax || (T == tmax && (h.tri < tri || (h.tri == tri && e < ent))))) {
                     tmax = T;
@@ -108,7 +108,7 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
             const bvh8::Ray8 r = bvh8::make_ray(strict::xform(E.inverse, o, 1.0f),
                                                 strict::xform(E.inverse, d, 0.0f));
             bvh8::Hit8 h{kAny ? rtmax : tmax, -1.0f, kAny ? -1 : tri, -1};
-            visits += bvh8::traverse<kAny, true>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests,
+            visits += bvh8::traverse<kAny, true, kDepth>(s.b8_nodes, s.b8_tris, root, r, rtmin, h, tests,
                                                  status);
             const float T = h.closest;
             if (kAny) {
@@ -141,14 +141,14 @@ __device__ __forceinline__ void bvh8_ray(const SceneView& s, const float4 r0, co
 // entity or the final record needs it, which keeps it out of the loop's registers.
 constexpr int kPoolRays = 64;
 
-template <bool kAny, class Sink, bool kTlas = true>
+template <bool kAny, class Sink, bool kTlas = true, int kDepth = bvh8::kStack>
 __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const rq_ray* __restrict__ rays,
                                                      int64_t n, int flags, unsigned long long* queue,
                                                      const Sink& sink, int32_t& tests,
                                                      int32_t& nodes_total, unsigned& status) {
     const unsigned kFull = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
-    uint64_t stack[bvh8::kStack];
+    uint64_t stack[kDepth];
     bvh8::Ray8 r;
     bvh8::Hit8 h;
     bvh8::Walk w;
@@ -280,7 +280,7 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                 }
                 continue;
             }
-            if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
+            if (bvh8::step<kAny, true, kDepth>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
             // the walk of entity `ent` has ended
             visits += w.visits;
             const float T = h.closest;
@@ -341,7 +341,7 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
             }
             if (!__any_sync(kFull, live)) break;
             if (!live) continue;
-            if (bvh8::step<kAny, true>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
+            if (bvh8::step<kAny, true, kDepth>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
             // the walk of entity `ent` has ended
             visits += w.visits;
             const float T = h.closest;

@@ -178,7 +178,7 @@ __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int 
     if (!(rtmax > rtmin)) return;
     const f3 o = strict::xyz(r0), d = strict::xyz(r1);
     Best best{rtmax, -1.0f, 0.0f, 0.0f, -1, -1};
-    int32_t ent = -1;
+    int32_t ent = -1, last_walked = -1, last_count = 0;
     const bool skip_transparent = !kAny && (flags & RQ_FLAG_IGNORE_TRANSPARENT);
     const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
     int32_t cur = tlas::begin<kTlas>(s, wo, wd);
@@ -190,8 +190,11 @@ __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int 
         Best bb = best;
         bb.closest = -1.0f;
         if (kAny) bb.tmax = rtmax;
-        h.iters += kStackless ? bvh_stackless<kAny>(s, r, e.node_offset, e.node_count, rtmin, bb, tests)
-                              : bvh_stack<kAny>(s, r, e.node_offset, e.node_count, rtmin, bb, tests);
+        const int32_t it = kStackless ? bvh_stackless<kAny>(s, r, e.node_offset, e.node_count, rtmin, bb, tests)
+                                      : bvh_stack<kAny>(s, r, e.node_offset, e.node_count, rtmin, bb, tests);
+        h.iters += it;
+        last_walked = i;
+        last_count = it;
         if (kAny) {
             if (bb.closest > 0.0f) {
                 occluded = true;
@@ -202,6 +205,7 @@ __device__ void scene(const SceneView& s, const float4 r0, const float4 r1, int 
             ent = i;
         }
     }
+    if (!kAny && (flags & RQ_FLAG_REF_COMPAT)) h.iters = strict::last_entity_iters(s, flags, last_walked, last_count);
     if (!kAny && best.closest > 0.0f) {
         h.tri = best.tri;
         h.mesh = best.mesh;

@@ -276,14 +276,24 @@ __global__ void __launch_bounds__(256) k_gi_raygen_compact(
     }
 }
 
+// Whether a pass traces its secondary rays compacted: always without a live count, else when the
+// fraction of primary rays with a hit is below the threshold.
+__device__ __forceinline__ bool compact_rays(const unsigned long long* live, int64_t n, float compact_below) {
+    if (!live) return true;
+    return __fdiv_rn(static_cast<float>(*live), static_cast<float>(n)) < compact_below;
+}
+
 // Per-pixel form of k_gi_raygen_compact: one thread per primary ray i computes the hit point and
 // faced normal once and writes the spp secondary rays of slots j = i*spp + k.  Compaction is
 // block-aggregated and pixel-major within the block, the order k_gi_raygen_compact gives, with the
-// same slot map; every value is computed with the same functions.
+// same slot map; every value is computed with the same functions.  With a live count (the primary
+// hits, counted by k_count_live) at or above the compaction threshold the rays stay in place
+// instead: slot j holds sample j (an inactive ray for a pixel without a hit), the slot map is the
+// identity and *count = n * spp, so the secondary launch covers every slot.
 __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
     SceneView s, const rq_ray* __restrict__ prim, const rq_hit* __restrict__ hits, int64_t n,
     GiArgs a, rq_ray* __restrict__ out, int32_t* __restrict__ comp_of, unsigned long long* count,
-    int32_t* __restrict__ samp_of) {
+    int32_t* __restrict__ samp_of, const unsigned long long* __restrict__ live, float compact_below) {
     __shared__ unsigned warp_hits[8];
     __shared__ unsigned long long block_base;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -291,6 +301,33 @@ __global__ void __launch_bounds__(256) k_gi_raygen_pixel(
     int4 h1 = make_int4(-1, -1, -1, 0);
     if (i < n) get_hit(hits, i, h0, h1);
     const bool hit = i < n && h0.x > 0.0f;
+    if (!compact_rays(live, n, compact_below)) {  // in place
+        if (i == 0) *count = static_cast<unsigned long long>(n) * a.spp;
+        if (i >= n) return;
+        if (!hit) {
+            for (int k = 0; k < a.spp; ++k) {
+                put_ray(out, i * a.spp + k, f3{0.0f, 0.0f, 0.0f}, 0.0f, f3{0.0f, 0.0f, 1.0f}, -1.0f);
+                comp_of[i * a.spp + k] = -1;
+            }
+            return;
+        }
+        const float4* pr = reinterpret_cast<const float4*>(prim) + 2 * i;
+        const float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+        const f3 ro = strict::xyz(r0), rd = strict::xyz(r1);
+        const f3 P = strict::add(ro, strict::muls(rd, h0.x));
+        f3 N = gi::hit_normal(s, h1.x, h0.y, h0.z, h0.w, a.normal_mode);
+        if (strict::dot(N, rd) > 0.0001f) N = strict::neg(N);
+        const f3 org = strict::add(P, strict::muls(N, a.origin_offset));
+        for (int k = 0; k < a.spp; ++k) {
+            const int64_t j = i * a.spp + k;
+            const uint32_t rid = static_cast<uint32_t>(j);
+            const float u0 = gi::u01(gi::sample_key(a.seed, rid, 0u));
+            const float u1 = gi::u01(gi::sample_key(a.seed, rid, 1u));
+            put_ray(out, j, org, 0.0f, gi::cos_weighted_hemisphere(N, u0, u1), a.ray_tmax);
+            comp_of[j] = static_cast<int32_t>(j);
+        }
+        return;
+    }
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
     if (lane == 0) warp_hits[warp] = __popc(m);
@@ -663,8 +700,12 @@ rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
 
 }  // namespace
 
-// Adds the compact ray count of a pass to the frame statistics.
-__global__ void k_add_count(unsigned long long* dst, const unsigned long long* src) { *dst += *src; }
+// Adds the active secondary ray count of a pass to the frame statistics: the compact count, or
+// live x spp when the rays stayed in place.
+__global__ void k_add_count(unsigned long long* dst, const unsigned long long* src,
+                            const unsigned long long* live, int64_t n, int32_t spp, float compact_below) {
+    *dst += compact_rays(live, n, compact_below) ? *src : *live * static_cast<unsigned long long>(spp);
+}
 
 // One GI pass over n primary rays on stream st, in three phases: (1) primary closest hits and
 // secondary ray generation, (2) one secondary traversal over all compact rays (+ shadow rays),
@@ -737,9 +778,20 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
                                      cudaMemcpyHostToDevice, st));
     RQ_CUDA(ctx, launch_closest(pv, qp, src, n, phit, arena.queue(0), st));
     if (stats) k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, cnt + 0);
+    // Compaction threshold: the per-pixel form keeps the rays in place when the fraction of primary
+    // rays with a hit is at or above it (counted on the device: no host round trip); the bounce
+    // loop, octant binning and the per-sample form always compact.
+    const float compact_below = p.compact_below > 0.0f ? p.compact_below : sc->gi_compact_below;
+    const unsigned long long* live = nullptr;
+    if (compact_below <= 1.0f && !bounce && !p.sort_rays && !p.unfused) {
+        unsigned long long* lw = arena.live();
+        RQ_CUDA(ctx, cudaMemsetAsync(lw, 0, sizeof(unsigned long long), st));
+        k_count_hits<<<grid(n, 256), 256, 0, st>>>(phit, n, lw);
+        live = lw;
+    }
     if ((!p.sort_rays && !p.unfused) || bounce) {
         k_gi_raygen_pixel<<<grid(n, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count,
-                                                        samp_of);
+                                                        samp_of, live, compact_below);
     } else if (p.sort_rays) {
         void* d_oct = nullptr;
         if ((s = arena.get(rq::kSlotOctants, 16 * sizeof(unsigned long long), &d_oct)) != RQ_OK) return s;
@@ -752,7 +804,7 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
         k_gi_raygen_compact<<<grid(m, 256), 256, 0, st>>>(sc->view, prim, phit, n, a, sec, comp_of, count);
     }
     RQ_CUDA(ctx, cudaGetLastError());
-    if (stats) k_add_count<<<1, 1, 0, st>>>(cnt + 5, count);
+    if (stats) k_add_count<<<1, 1, 0, st>>>(cnt + 5, count, live, n, p.spp, compact_below);
     // phase 2
     SceneView cv = sc->view;  // secondary launches cover only the compact prefix
     cv.ray_count = count;
@@ -979,6 +1031,51 @@ rq_status rq_shade(rq_ctx* ctx, const rq_scene* sc, const rq_ray* rays, const rq
                                                   rq::to_args(*p),
                                                   reinterpret_cast<float4*>(out4));
     RQ_CUDA(ctx, cudaGetLastError());
+    return RQ_OK;
+}
+
+rq_status rq_gi_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* primary, int64_t n, const rq_gi_params* p,
+                         const rq_opts* opts, float* pixels4, rq_gi_tune* out) {
+    if (!ctx || !sc || !out || n <= 0 || !primary || !pixels4) return fail(ctx, RQ_EINVAL, "bad arguments");
+    rq_status s = rq::check_params(ctx, p);
+    if (s != RQ_OK) return s;
+    rq::QueryConfig q{};
+    if ((s = rq::resolve_query(ctx, sc, opts, q)) != RQ_OK) return s;
+    if (q.flags & RQ_FLAG_HOST_BUFFERS) return fail(ctx, RQ_EINVAL, "rq_gi_autotune takes device buffers");
+    RQ_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    rq::CtxGiArena arena(ctx);
+    cudaEvent_t a, b;
+    RQ_CUDA(ctx, cudaEventCreate(&a));
+    RQ_CUDA(ctx, cudaEventCreate(&b));
+    float ms[2] = {1e30f, 1e30f};
+    unsigned long long live = 0;
+    for (int form = 0; form < 2; ++form) {  // 0: always compact, 1: in place
+        rq_gi_params pp = *p;
+        pp.bounces = 0;
+        pp.sort_rays = 0;
+        pp.unfused = 0;
+        pp.compact_below = form == 0 ? 2.0f : 1e-30f;
+        for (int rep = 0; rep < 4; ++rep) {
+            RQ_CUDA(ctx, cudaEventRecord(a, st));
+            if ((s = rq::gi_pass(ctx, sc, q, pp, primary, n, reinterpret_cast<float4*>(pixels4), st, false, nullptr,
+                                 nullptr, arena)) != RQ_OK)
+                return s;
+            RQ_CUDA(ctx, cudaEventRecord(b, st));
+            RQ_CUDA(ctx, cudaEventSynchronize(b));
+            float t = 0.0f;
+            RQ_CUDA(ctx, cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) ms[form] = std::min(ms[form], t);
+        }
+        if (form == 1) RQ_CUDA(ctx, cudaMemcpy(&live, arena.live(), sizeof(live), cudaMemcpyDeviceToHost));
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    out->live_fraction = static_cast<float>(static_cast<double>(live) / static_cast<double>(n));
+    out->ms_compact = ms[0];
+    out->ms_in_place = ms[1];
+    sc->gi_compact_below = ms[1] < ms[0] ? std::max(out->live_fraction, 1e-30f) : 2.0f;
+    out->compact_below = sc->gi_compact_below;
     return RQ_OK;
 }
 

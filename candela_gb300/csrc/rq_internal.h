@@ -79,11 +79,12 @@ struct QueryConfig {
 };
 
 // Compiled launch variants of the traversal kernels: threads per block, minimum resident blocks
-// per SM (the register cap follows from it), and the persistent ray-queue form.
+// per SM (the register cap follows from it), the persistent ray-queue form, and the BVH8 group-stack
+// depth (0 = the default, 48; the BVH2 walks keep the reference's 64-entry stack whatever it says).
 struct LaunchVariant {
-    int32_t block, min_blocks, persistent;
+    int32_t block, min_blocks, persistent, depth;
 };
-constexpr int kNumLaunchVariants = 8;
+constexpr int kNumLaunchVariants = 10;
 extern const LaunchVariant kLaunchVariants[kNumLaunchVariants];
 // The one-thread-per-ray variant with the same block size and occupancy target as variant v
 // (v itself when it is not persistent).
@@ -119,8 +120,11 @@ constexpr int kMaxBatchQueries = 1024;
 constexpr int kNumBatchVariants = 4;
 extern const LaunchVariant kBatchVariants[kNumBatchVariants];
 enum BatchFamily { kFamilyBvh8 = 0, kFamilyStrict = 1, kFamilyFast = 2 };
+// BVH8 group-stack depths of the batch kernel (index into bvh8::kStackDepths: 48, 32, 24).
+constexpr int kNumBatchDepths = 3;
 // One persistent launch over every query (rq_kernels.cu).  queue is zeroed by the caller.
+// depth_index selects the BVH8 family's group-stack depth.
 cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
-                         unsigned long long* queue, unsigned* status, cudaStream_t st);
+                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index = 0);
 
 }  // namespace rq

@@ -2,6 +2,7 @@
 // triangle records.  The per-variant kernels and launchers are in rq_kernels.cuh; the top-level
 // form is instantiated in rq_kernels_tlas.cu.
 #include "rq_kernels.cuh"
+#include "rq_objects.h"
 
 namespace rq {
 
@@ -32,7 +33,7 @@ namespace {
 
 // Batched queries: one persistent launch; each warp takes 32 consecutive work items from a global
 // counter, and every item finds its query by binary search over the queries' first work index.
-template <int kB, int kM, int kFamily>
+template <int kB, int kM, int kFamily, int kDepth = bvh8::kStack>
 __global__ void __launch_bounds__(kB, kM) k_batch(const QueryDesc* __restrict__ qd, int nq, int64_t total,
                                                   unsigned long long* queue, unsigned* status_out) {
     __shared__ int64_t base[kMaxBatchQueries + 1];
@@ -60,8 +61,8 @@ __global__ void __launch_bounds__(kB, kM) k_batch(const QueryDesc* __restrict__ 
         bool oc = false;
         int32_t visits = 0, tests = 0;
         if (kFamily == kFamilyBvh8) {
-            if (Q.kind) bvh8_ray<true>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
-            else bvh8_ray<false>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
+            if (Q.kind) bvh8_ray<true, true, kDepth>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
+            else bvh8_ray<false, true, kDepth>(Q.s, r0, r1, Q.flags, h, oc, visits, tests, status);
         } else if (kFamily == kFamilyFast) {
             const bool sl = Q.s.layout == RQ_LAYOUT_BVH2_STACKLESS;
             if (Q.kind) {
@@ -104,8 +105,14 @@ __global__ void k_tri_fast(const int4* __restrict__ tris, int64_t n, const float
 
 }  // namespace
 
+static_assert(bvh8::kStackDepths[0] == kBvh8Depths[0] && bvh8::kStackDepths[1] == kBvh8Depths[1] &&
+                  bvh8::kStackDepths[2] == kBvh8Depths[2] && bvh8::kStack == kBvh8Depths[0],
+              "the host's list of BVH8 stack depths must match the kernels'");
+static_assert(bvh8::kStatusStackOverflow == kStatusOverflowBit, "status bit of a stack overflow");
+
 const LaunchVariant kLaunchVariants[kNumLaunchVariants] = {
-    {128, 1, 0}, {128, 4, 0}, {128, 6, 0}, {128, 8, 0}, {256, 3, 0}, {64, 12, 0}, {128, 1, 1}, {128, 8, 1}};
+    {128, 1, 0, 0}, {128, 4, 0, 0}, {128, 6, 0, 0}, {128, 8, 0, 0}, {256, 3, 0, 0}, {64, 12, 0, 0},
+    {128, 1, 1, 0}, {128, 8, 1, 0}, {128, 8, 1, bvh8::kStackDepths[1]}, {128, 8, 1, bvh8::kStackDepths[2]}};
 
 int non_persistent_variant(int v) {
     if (v < 0 || v >= kNumLaunchVariants || !kLaunchVariants[v].persistent) return v;
@@ -116,47 +123,72 @@ int non_persistent_variant(int v) {
     return 0;
 }
 
-const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1}, {128, 8, 1}, {64, 12, 1}, {256, 3, 1}};
+const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1, 0}, {128, 8, 1, 0}, {64, 12, 1, 0},
+                                                         {256, 3, 1, 0}};
 
 namespace {
+// The BVH8 family's kernel for depth index di (bvh8::kStackDepths).
+template <int kB, int kM>
+int batch_bvh8_grid(int di) {
+    switch (di) {
+        case 1: return persistent_grid(k_batch<kB, kM, kFamilyBvh8, bvh8::kStackDepths[1]>, kB);
+        case 2: return persistent_grid(k_batch<kB, kM, kFamilyBvh8, bvh8::kStackDepths[2]>, kB);
+        default: return persistent_grid(k_batch<kB, kM, kFamilyBvh8>, kB);
+    }
+}
+
 template <int kB, int kM>
 cudaError_t batch_variant(const QueryDesc* d, int nq, int64_t total, int family,
-                          unsigned long long* queue, unsigned* status, cudaStream_t st) {
+                          unsigned long long* queue, unsigned* status, cudaStream_t st, int di) {
     int g = 0;
     switch (family) {
-        case kFamilyBvh8: g = persistent_grid(k_batch<kB, kM, kFamilyBvh8>, kB); break;
+        case kFamilyBvh8: g = batch_bvh8_grid<kB, kM>(di); break;
         case kFamilyFast: g = persistent_grid(k_batch<kB, kM, kFamilyFast>, kB); break;
         default: g = persistent_grid(k_batch<kB, kM, kFamilyStrict>, kB); break;
     }
     const int64_t need = (total + 31) / 32 * 32 / kB + 1;
     if (need < g) g = static_cast<int>(need);
-    if (family == kFamilyBvh8)
-        k_batch<kB, kM, kFamilyBvh8><<<g, kB, 0, st>>>(d, nq, total, queue, status);
-    else if (family == kFamilyFast)
+    if (family == kFamilyBvh8) {
+        if (di == 1)
+            k_batch<kB, kM, kFamilyBvh8, bvh8::kStackDepths[1]><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+        else if (di == 2)
+            k_batch<kB, kM, kFamilyBvh8, bvh8::kStackDepths[2]><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+        else
+            k_batch<kB, kM, kFamilyBvh8><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+    } else if (family == kFamilyFast) {
         k_batch<kB, kM, kFamilyFast><<<g, kB, 0, st>>>(d, nq, total, queue, status);
-    else
+    } else {
         k_batch<kB, kM, kFamilyStrict><<<g, kB, 0, st>>>(d, nq, total, queue, status);
+    }
     return cudaGetLastError();
+}
+
+template <int kB, int kM>
+void batch_grids() {
+    for (int di = 0; di < kNumBatchDepths; ++di) batch_bvh8_grid<kB, kM>(di);
+    persistent_grid(k_batch<kB, kM, kFamilyStrict>, kB);
+    persistent_grid(k_batch<kB, kM, kFamilyFast>, kB);
 }
 }  // namespace
 
 cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
-                         unsigned long long* queue, unsigned* status, cudaStream_t st) {
+                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index) {
     if (total <= 0 || nq <= 0) return cudaSuccess;
+    const int di = (depth_index >= 0 && depth_index < kNumBatchDepths) ? depth_index : 0;
     if (!st && !queue) {  // grid-size query only (fills the occupancy cache outside stream capture)
         switch (variant) {
-            case 1: persistent_grid(k_batch<128, 8, kFamilyBvh8>, 128); persistent_grid(k_batch<128, 8, kFamilyStrict>, 128); persistent_grid(k_batch<128, 8, kFamilyFast>, 128); break;
-            case 2: persistent_grid(k_batch<64, 12, kFamilyBvh8>, 64); persistent_grid(k_batch<64, 12, kFamilyStrict>, 64); persistent_grid(k_batch<64, 12, kFamilyFast>, 64); break;
-            case 3: persistent_grid(k_batch<256, 3, kFamilyBvh8>, 256); persistent_grid(k_batch<256, 3, kFamilyStrict>, 256); persistent_grid(k_batch<256, 3, kFamilyFast>, 256); break;
-            default: persistent_grid(k_batch<128, 1, kFamilyBvh8>, 128); persistent_grid(k_batch<128, 1, kFamilyStrict>, 128); persistent_grid(k_batch<128, 1, kFamilyFast>, 128); break;
+            case 1: batch_grids<128, 8>(); break;
+            case 2: batch_grids<64, 12>(); break;
+            case 3: batch_grids<256, 3>(); break;
+            default: batch_grids<128, 1>(); break;
         }
         return cudaGetLastError();
     }
     switch (variant) {
-        case 1: return batch_variant<128, 8>(d_desc, nq, total, family, queue, status, st);
-        case 2: return batch_variant<64, 12>(d_desc, nq, total, family, queue, status, st);
-        case 3: return batch_variant<256, 3>(d_desc, nq, total, family, queue, status, st);
-        default: return batch_variant<128, 1>(d_desc, nq, total, family, queue, status, st);
+        case 1: return batch_variant<128, 8>(d_desc, nq, total, family, queue, status, st, di);
+        case 2: return batch_variant<64, 12>(d_desc, nq, total, family, queue, status, st, di);
+        case 3: return batch_variant<256, 3>(d_desc, nq, total, family, queue, status, st, di);
+        default: return batch_variant<128, 1>(d_desc, nq, total, family, queue, status, st, di);
     }
 }
 

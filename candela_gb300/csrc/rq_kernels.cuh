@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8(SceneView s, const rq_ray* __re
 
 // Persistent BVH8 traversal (bvh8_persistent_loop in rq_bvh8_walk.cuh), results as hit records
 // or occlusion bytes.
-template <bool kAny, int kB, int kM, bool kTlas>
+template <bool kAny, int kB, int kM, bool kTlas, int kDepth = bvh8::kStack>
 __global__ void __launch_bounds__(kB, kM) k_bvh8_persistent(SceneView s, const rq_ray* __restrict__ rays,
                                                             int64_t n, rq_hit* __restrict__ hits,
                                                             uint8_t* __restrict__ occ, int flags,
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kB, kM) k_bvh8_persistent(SceneView s, const r
     int32_t tests = 0, nodes_total = 0;
     unsigned status = 0;
     const QuerySink sink{s, flags, hits, occ};
-    bvh8_persistent_loop<kAny, QuerySink, kTlas>(s, rays, n, flags, queue, sink, tests, nodes_total, status);
+    bvh8_persistent_loop<kAny, QuerySink, kTlas, kDepth>(s, rays, n, flags, queue, sink, tests, nodes_total, status);
     if (status) atomicOr(status_out, status);
     if (counters) count_work(counters, nodes_total, tests);
 }
@@ -254,12 +254,12 @@ cudaError_t launch_persistent(const SceneView& s, const QueryConfig& q, const rq
     return cudaGetLastError();
 }
 
-template <bool kAny, int kM, bool kTlas>
+template <bool kAny, int kM, bool kTlas, int kDepth>
 cudaError_t launch_bvh8_persistent(const SceneView& s, const QueryConfig& q, const rq_ray* rays,
                                    int64_t n, rq_hit* hits, uint8_t* occ, unsigned long long* queue,
                                    cudaStream_t st) {
     const int block = 128;
-    auto k = k_bvh8_persistent<kAny, 128, kM, kTlas>;
+    auto k = k_bvh8_persistent<kAny, 128, kM, kTlas, kDepth>;
     const int64_t g = std::min<int64_t>(persistent_grid(k, block), (n + block - 1) / block);
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
@@ -267,11 +267,13 @@ cudaError_t launch_bvh8_persistent(const SceneView& s, const QueryConfig& q, con
     return cudaGetLastError();
 }
 
-// Persistent launch of variant kM (min blocks per SM) for the query's layout.
-template <bool kAny, int kM, bool kTlas>
+// Persistent launch of variant kM (min blocks per SM) for the query's layout; kDepth is the BVH8
+// group-stack depth (the BVH2 walks keep the reference's 64-entry stack).
+template <bool kAny, int kM, bool kTlas, int kDepth = bvh8::kStack>
 cudaError_t persistent_variant(const SceneView& s, const QueryConfig& q, const rq_ray* rays, int64_t n,
                                rq_hit* hits, uint8_t* occ, unsigned long long* queue, cudaStream_t st) {
-    if (q.layout == RQ_LAYOUT_BVH8Q) return launch_bvh8_persistent<kAny, kM, kTlas>(s, q, rays, n, hits, occ, queue, st);
+    if (q.layout == RQ_LAYOUT_BVH8Q)
+        return launch_bvh8_persistent<kAny, kM, kTlas, kDepth>(s, q, rays, n, hits, occ, queue, st);
     const bool sl = q.layout == RQ_LAYOUT_BVH2_STACKLESS;
     if (kAny)
         return sl ? launch_persistent<true, true, false, kM, kTlas>(s, q, rays, n, nullptr, occ, queue, st)
@@ -341,6 +343,8 @@ cudaError_t launch_closest_t(const SceneView& s, const QueryConfig& q, const rq_
         case 5: return closest_variant<64, 12, kTlas>(s, q, rays, n, hits, st);
         case 6: return persistent_variant<false, 1, kTlas>(s, q, rays, n, hits, nullptr, queue, st);
         case 7: return persistent_variant<false, 8, kTlas>(s, q, rays, n, hits, nullptr, queue, st);
+        case 8: return persistent_variant<false, 8, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, hits, nullptr, queue, st);
+        case 9: return persistent_variant<false, 8, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, hits, nullptr, queue, st);
         default: return closest_variant<128, 1, kTlas>(s, q, rays, n, hits, st);
     }
 }
@@ -359,6 +363,8 @@ cudaError_t launch_anyhit_t(const SceneView& s, const QueryConfig& q, const rq_r
         case 5: return anyhit_variant<64, 12, kTlas>(s, q, rays, n, occluded, st);
         case 6: return persistent_variant<true, 1, kTlas>(s, q, rays, n, nullptr, occluded, queue, st);
         case 7: return persistent_variant<true, 8, kTlas>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 8: return persistent_variant<true, 8, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 9: return persistent_variant<true, 8, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, nullptr, occluded, queue, st);
         default: return anyhit_variant<128, 1, kTlas>(s, q, rays, n, occluded, st);
     }
 }

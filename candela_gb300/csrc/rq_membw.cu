@@ -13,21 +13,32 @@
 
 namespace {
 
-// Grid-stride read of n16 16-byte words; the XOR of what was read is stored only when it equals a
-// value the data cannot produce, so the loads stay live without a store per thread.
-__global__ void __launch_bounds__(512) k_read(const uint4* __restrict__ buf, int64_t n16,
+// `passes` grid-stride reads of n16 16-byte words (each pass starts at a different rotation so that
+// a thread does not re-read its own words from L1); the XOR of what was read is stored only when it
+// equals a value the data cannot produce, so the loads stay live without a store per thread.
+__global__ void __launch_bounds__(512) k_read(const uint4* __restrict__ buf, int64_t n16, int passes,
                                               unsigned* __restrict__ sink) {
     uint32_t acc = 0;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    for (; i + 3 * stride < n16; i += 4 * stride) {
-        const uint4 a = __ldcg(buf + i), b = __ldcg(buf + i + stride);
-        const uint4 c = __ldcg(buf + i + 2 * stride), d = __ldcg(buf + i + 3 * stride);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
-    }
-    for (; i < n16; i += stride) {
-        const uint4 a = __ldcg(buf + i);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w;
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (int p = 0; p < passes; ++p) {
+        int64_t i = t;
+        const int64_t rot = (static_cast<int64_t>(p) * 7919 * 32) % n16;
+        for (; i + 3 * stride < n16; i += 4 * stride) {
+            int64_t j0 = i + rot, j1 = i + stride + rot, j2 = i + 2 * stride + rot, j3 = i + 3 * stride + rot;
+            j0 -= j0 >= n16 ? n16 : 0;
+            j1 -= j1 >= n16 ? n16 : 0;
+            j2 -= j2 >= n16 ? n16 : 0;
+            j3 -= j3 >= n16 ? n16 : 0;
+            const uint4 a = __ldcg(buf + j0), b = __ldcg(buf + j1), c = __ldcg(buf + j2), d = __ldcg(buf + j3);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+        }
+        for (; i < n16; i += stride) {
+            int64_t j = i + rot;
+            j -= j >= n16 ? n16 : 0;
+            const uint4 a = __ldcg(buf + j);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w;
+        }
     }
     if (acc == 0x9E3779B9u) atomicAdd(sink, 1u);
 }
@@ -60,9 +71,11 @@ rq_status rq_measure_read_gbs(rq_ctx* ctx, int64_t bytes, int32_t reps, double* 
         (e = cudaEventCreate(&e0)) == cudaSuccess && (e = cudaEventCreate(&e1)) == cudaSuccess) {
         const unsigned grid = static_cast<unsigned>(sms) * 4;  // 4 blocks of 512 threads per SM
         k_fill<<<grid, 512, 0, st>>>(static_cast<uint4*>(buf), n16);
-        for (int w = 0; w < 3; ++w) k_read<<<grid, 512, 0, st>>>(static_cast<const uint4*>(buf), n16, sink);
+        k_read<<<grid, 512, 0, st>>>(static_cast<const uint4*>(buf), n16, 3, sink);  // warm-up
+        // many passes per launch, so that launch gaps do not count against the bandwidth
         cudaEventRecord(e0, st);
-        for (int r = 0; r < reps; ++r) k_read<<<grid, 512, 0, st>>>(static_cast<const uint4*>(buf), n16, sink);
+        for (int r = 0; r < reps; r += 50)
+            k_read<<<grid, 512, 0, st>>>(static_cast<const uint4*>(buf), n16, reps - r < 50 ? reps - r : 50, sink);
         cudaEventRecord(e1, st);
         if ((e = cudaEventSynchronize(e1)) == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
     }

@@ -77,6 +77,7 @@ struct FixedArena final : rq::GiArena {
     unsigned long long* queue(int k) override {
         return reinterpret_cast<unsigned long long*>(base + kCountersOff) + 1 + k;
     }
+    unsigned long long* live() override { return reinterpret_cast<unsigned long long*>(base + kCountersOff) + 4; }
 };
 
 }  // namespace

@@ -124,6 +124,13 @@ struct rq_scene {
     double b8_build_ms = 0.0;
     std::vector<int32_t> h_b8roots;  // per entity: BVH8 root (-1: none)
     std::vector<double> b8_bounds;   // per entity: object-space bounds its BVH8 root can box-test
+    // BVH8 refit plan (rq_refit8.cu): node indices level by level from the roots down, the level
+    // offsets, and a per-node FP32 box (6 floats) written during a refit; b8_bounds is recomputed
+    // from the device roots after a refit
+    int32_t* d_b8_order = nullptr;
+    std::vector<int64_t> b8_level_off;
+    float* d_b8box = nullptr;
+    bool b8_bounds_stale = false;
     // top level over the entities (tlas.h); rebuilt with the entities and the BVH8
     float4* d_tlas = nullptr;
     int4* d_tlas_pre = nullptr;
@@ -137,6 +144,9 @@ struct rq_scene {
     int32_t* d_adj = nullptr;
     // autotuned launch variant per [layout][query kind] (-1 = default)
     int8_t tuned[4][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+    // GI compaction threshold used when rq_gi_params.compact_below is 0 (rq_gi_autotune); above 1 =
+    // always compact
+    float gi_compact_below = 2.0f;
 };
 
 namespace rq {
@@ -149,8 +159,13 @@ inline Materials materials_of(const rq_scene* sc) {
 rq_status fail(rq_ctx* ctx, rq_status s, const std::string& msg);
 // Rebuilds the top level over the scene's entities (none below kTlasMinEntities entities).
 rq_status rebuild_tlas(rq_scene* sc);
-// Copies device-updated node and vertex buffers back to the host copies.
+// Copies device-updated node and vertex buffers back to the host copies (and recomputes the BVH8
+// root bounds after a BVH8 refit).
 rq_status refresh_host(rq_scene* sc);
+// Refits the scene's BVH8 to the current device vertex positions, topology kept (rq_refit8.cu).
+rq_status refit_bvh8(rq_scene* sc, cudaStream_t st);
+// Object-space bounds of each entity's BVH8 root children from host copies of the root nodes.
+void bvh8_root_bounds(rq_scene* sc, const std::vector<uint32_t>& root_nodes);
 rq_status cuda_fail(rq_ctx* ctx, cudaError_t e, const char* what);
 // Resolves rq_opts (NULL = defaults) against the scene into a kernel configuration.
 rq_status resolve_query(rq_ctx* ctx, const rq_scene* sc, const rq_opts* o, QueryConfig& q);
@@ -174,6 +189,14 @@ inline unsigned long long* queue_counter(rq_ctx* ctx, int k) {
 // GPU build of one object's BVH2 (bvh_build_gpu.cu): the buffers build_bvh produces, from host
 // input arrays, on the context's device.  RQ_OK, or a status with `why` set.
 rq_status build_bvh_gpu(rq_ctx* ctx, const BuildInput& in, BuildOutput& out, std::string& why);
+// BVH8 group-stack depths selectable by rq_opts.stack_depth (0 = the default).
+constexpr int kBvh8Depths[3] = {48, 32, 24};
+inline int bvh8_depth(int index) { return kBvh8Depths[(index >= 0 && index < 3) ? index : 0]; }
+// The index of opts->stack_depth in kBvh8Depths (0 for 0 or NULL opts); RQ_EINVAL for any other depth.
+rq_status depth_index_of(rq_ctx* ctx, const rq_opts* o, int& index);
+// Status bit a BVH8 walk raises when its group stack overflows (bvh8::kStatusStackOverflow).
+constexpr unsigned kStatusOverflowBit = 1u;
+
 // Grow-only device scratch buffer of the context (slot < kScratchSlots).
 rq_status scratch(rq_ctx* ctx, int slot, size_t bytes, void** out);
 
@@ -187,6 +210,8 @@ struct GiArena {
     virtual unsigned long long* count() = 0;
     // Ray-queue counter k (0..2) of the persistent traversal launches.
     virtual unsigned long long* queue(int k) = 0;
+    // The device word that counts the primary rays with a hit (the compaction decision).
+    virtual unsigned long long* live() = 0;
 };
 struct CtxGiArena final : GiArena {
     rq_ctx* ctx;
@@ -194,6 +219,7 @@ struct CtxGiArena final : GiArena {
     rq_status get(int slot, size_t bytes, void** out) override { return scratch(ctx, slot, bytes, out); }
     unsigned long long* count() override { return frame_counter(ctx); }
     unsigned long long* queue(int k) override { return queue_counter(ctx, k); }
+    unsigned long long* live() override { return reinterpret_cast<unsigned long long*>(ctx->counters) + 13; }
 };
 
 // Resolves the device address of rq_gi_frame_noalloc's fixed array for the context (rq_noalloc.cu);

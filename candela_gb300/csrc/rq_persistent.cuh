@@ -26,6 +26,7 @@ struct StrictRay {
     // scene-level result (IntersectScene, TraverseBVHStack.glsl:327-366)
     float tmax, closest;
     int32_t mesh, tri, ent_hit, iters_total;
+    int32_t last_walked, last_count;  // the last entity walked and its count (RQ_FLAG_REF_COMPAT)
     // current entity traversal (IntersectBVHStack / IntersectBVHStackless)
     int32_t ent, start, count, cur, sp, iters;
     int32_t ents;  // entity cursor (rq_tlas.cuh); `ent` is the last entity it gave
@@ -85,6 +86,8 @@ struct StrictRay {
         closest = -1.0f;
         mesh = tri = ent_hit = -1;
         iters_total = 0;
+        last_walked = -1;
+        last_count = 0;
         occluded = false;
         ent = -1;
         if (!(rtmax > rtmin)) return false;  // inactive ray
@@ -99,6 +102,8 @@ struct StrictRay {
     // Scene-level acceptance at the end of an entity's walk; false when the ray is done (any hit).
     __device__ __forceinline__ bool accept_entity() {
         iters_total += iters;
+        last_walked = ent;
+        last_count = iters;
         const float T = bb.closest;
         if (kAny) {
             if (T > 0.0f) {
@@ -198,6 +203,8 @@ struct StrictRay {
         h.t = h.u = h.v = h.w = -1.0f;
         h.tri = h.mesh = h.entity = -1;
         h.iters = iters_total;
+        if ((flags & RQ_FLAG_REF_COMPAT) && rtmax > rtmin)
+            h.iters = strict::last_entity_iters(s, flags, last_walked, last_count);
         if (closest > 0.0f) {
             h.tri = tri;
             h.mesh = mesh;

@@ -243,6 +243,20 @@ __device__ int32_t bvh_stackless(const SceneView& s, f3 ro, f3 rd, int32_t start
 
 __device__ __forceinline__ float ent_alpha(const rq_entity& e) { return __int_as_float(e.data[1]); }
 
+// IntersectScene's Iters under RQ_FLAG_REF_COMPAT: the shader hands one `out int Iters` to every
+// entity's walk (TraverseBVHStack.glsl:337-349, :380-398), so it reports the iteration count of the
+// last entity its loop walks: the last entity, or under IgnoreTransparent the last opaque one.
+// `last_walked` / `last_count`: the last entity walked here and its count; an entity the top level
+// passed over would have visited its root only (one iteration).  0 when the loop walks nothing.
+__device__ __forceinline__ int32_t last_entity_iters(const SceneView& s, int flags, int32_t last_walked,
+                                                     int32_t last_count) {
+    int32_t L = s.n_ents - 1;
+    if (flags & RQ_FLAG_IGNORE_TRANSPARENT)
+        while (L >= 0 && ent_alpha(s.ents[L]) < 0.99f) --L;
+    if (L < 0) return 0;
+    return last_walked == L ? last_count : 1;
+}
+
 // IntersectScene / IntersectSceneIgnoreTransparent (:327-413; stackless :280-366).
 template <bool kStackless, bool kTieLower, bool kTlas = true>
 __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 r1, int flags,
@@ -255,7 +269,7 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
     const f3 o = xyz(r0), d = xyz(r1);
     float tmax = rtmax;
     float closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent = -1;
+    int32_t mesh = -1, tri = -1, ent = -1, last_walked = -1, last_count = 0;
     const float3 wo = make_float3(o.x, o.y, o.z), wd = make_float3(d.x, d.y, d.z);
     int32_t cur = tlas::begin<kTlas>(s, wo, wd);
     const int counted = (flags & RQ_FLAG_IGNORE_TRANSPARENT) ? tlas::kOpaque : tlas::kAll;
@@ -269,6 +283,8 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
             kStackless ? bvh_stackless<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests)
                        : bvh_stack<false, kTieLower>(s, ro, rd, e.node_offset, e.node_count, rtmin, bb, tests);
         h.iters += it;
+        last_walked = i;
+        last_count = it;
         const float T = bb.closest;
         if (T > 0.0f && (T < tmax || (kTieLower && T == tmax && bb.tri < tri))) {
             tmax = T;
@@ -278,6 +294,7 @@ __device__ void scene_closest(const SceneView& s, const float4 r0, const float4 
             ent = i;
         }
     }
+    if (flags & RQ_FLAG_REF_COMPAT) h.iters = last_entity_iters(s, flags, last_walked, last_count);
     if (closest > 0.0f) {
         h.tri = tri;
         h.mesh = mesh;

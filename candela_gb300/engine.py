@@ -166,8 +166,8 @@ def _stream(t, stream):
     return torch.cuda.current_stream(t.device).cuda_stream
 
 
-def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0, min_blocks=0, persistent=0) -> L.RqOpts:
-    return L.RqOpts(layout, mode, tie, flags, block_size, min_blocks, persistent, 0)
+def _opts(layout=0, mode=0, tie=0, flags=0, block_size=0, min_blocks=0, persistent=0, stack_depth=0) -> L.RqOpts:
+    return L.RqOpts(layout, mode, tie, flags, block_size, min_blocks, persistent, stack_depth)
 
 
 class Scene:
@@ -197,10 +197,10 @@ class Scene:
         check(lib().rq_autotune(self.ctx.handle, self.handle, ptr(rays), n, query,
                                 layout or self.layout, C.byref(r)), self.ctx.handle)
         variants = [dict(block=r.block[i], min_blocks=r.min_blocks_of[i],
-                         persistent=r.persistent_of[i], ms=round(r.ms[i], 4))
+                         persistent=r.persistent_of[i], stack_depth=r.depth_of[i], ms=round(r.ms[i], 4))
                     for i in range(r.n_variants)]
         return dict(variant=r.variant, block_size=r.block_size, min_blocks=r.min_blocks,
-                    persistent=r.persistent, variants=variants)
+                    persistent=r.persistent, stack_depth=r.depth, variants=variants)
 
     def verify(self, rays, hits, stream=None):
         """rq_verify_hits: FP64 relative t error and barycentric error per hit ((n, 2), NaN = miss)."""
@@ -235,7 +235,7 @@ class Scene:
 
     # -- queries -----------------------------------------------------------------------------
     def closest(self, rays, hits=None, *, layout=0, mode=0, tie=0, flags=0, block_size=0,
-                min_blocks=0, persistent=0, stream=None):
+                min_blocks=0, persistent=0, stack_depth=0, stream=None):
         """Closest hit.  `rays` is a numpy RAY_DTYPE array (host path, copies inside the call)
         or a torch uint8/float tensor on the device holding 32-byte rays."""
         host = isinstance(rays, np.ndarray)
@@ -247,7 +247,7 @@ class Scene:
                 import torch
                 hits = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
-        o = _opts(layout, mode, tie, f, block_size, min_blocks, persistent)
+        o = _opts(layout, mode, tie, f, block_size, min_blocks, persistent, stack_depth)
         check(lib().rq_closest(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), C.byref(o),
                                _stream(rays, stream)), self.ctx.handle)
         return hits
@@ -265,7 +265,7 @@ class Scene:
         return out
 
     def closest_attribs(self, rays, *, layout=0, mode=0, tie=0, flags=0, block_size=0, min_blocks=0,
-                        persistent=0, stream=None):
+                        persistent=0, stack_depth=0, stream=None):
         """Closest hit + GetData (rq_closest_attribs): (hits, attribs)."""
         host = isinstance(rays, np.ndarray)
         n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
@@ -275,13 +275,14 @@ class Scene:
             import torch
             hits = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
             att = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
-        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size, min_blocks, persistent)
+        o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size, min_blocks, persistent,
+                  stack_depth)
         check(lib().rq_closest_attribs(self.ctx.handle, self.handle, ptr(rays), n, ptr(hits), ptr(att), C.byref(o),
                                        _stream(rays, stream)), self.ctx.handle)
         return hits, att
 
     def anyhit(self, rays, out=None, *, layout=0, mode=0, flags=0, block_size=0, min_blocks=0,
-               persistent=0, stream=None):
+               persistent=0, stack_depth=0, stream=None):
         host = isinstance(rays, np.ndarray)
         n = rays.shape[0] if host else rays.numel() * rays.element_size() // 32
         if out is None:
@@ -291,7 +292,7 @@ class Scene:
                 import torch
                 out = torch.empty(n, dtype=torch.uint8, device=rays.device)
         f = flags | (L.FLAG_HOST_BUFFERS if host else 0)
-        o = _opts(layout, mode, 0, f, block_size, min_blocks, persistent)
+        o = _opts(layout, mode, 0, f, block_size, min_blocks, persistent, stack_depth)
         check(lib().rq_anyhit(self.ctx.handle, self.handle, ptr(rays), n, ptr(out), C.byref(o),
                               _stream(rays, stream)), self.ctx.handle)
         return out
@@ -343,15 +344,16 @@ class Scene:
 def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode=0, query=0,
               shadow_rays=False, shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866),
               sun_color=(4.0, 3.8, 3.5), sky_color=(0.5, 0.7, 1.0), sort_rays=False,
-              unfused=False, bounces=0) -> L.RqGiParams:
+              unfused=False, bounces=0, compact_below=0.0) -> L.RqGiParams:
     """rq_gi_params for the diffuse-GI (query=0) or RTAO (query=1) pass; `bounces` further
-    bounces per GI hit (the RT second-bounce loop)."""
+    bounces per GI hit (the RT second-bounce loop); `compact_below` the compaction threshold (0 =
+    the scene's tuned value)."""
     sd = np.asarray(sun_dir, dtype=np.float64)
     sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
     f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
     return L.RqGiParams(spp, seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode, query,
                         int(shadow_rays), shadow_offset, f3(sd), f3(sun_color), f3(sky_color),
-                        int(sort_rays), int(unfused), int(bounces))
+                        int(sort_rays), int(unfused), int(bounces), float(compact_below))
 
 
 def specular_params(seed=0, roughness=0.3, ray_tmax=1000000.0, normal_mode=0, shadow_rays=False,
@@ -454,7 +456,7 @@ class _GiMixin:
         return out
 
     def probe_update(self, params, prev_sh, prev_raw, probe_map, out_sh=None, out_raw=None, *, layout=0, mode=0,
-                     tie=0, flags=0, block_size=0, min_blocks=0, persistent=0, stream=None):
+                     tie=0, flags=0, block_size=0, min_blocks=0, persistent=0, stack_depth=0, stream=None):
         """One frame of the radiance-probe update (rq_probe_update).  numpy volumes -> host path.
         probe_map is updated in place; returns (out_sh, out_raw)."""
         host = isinstance(prev_sh, np.ndarray)
@@ -465,14 +467,27 @@ class _GiMixin:
             out_raw = (np.empty((n, 4), dtype=np.float32) if host
                        else _empty_like_dev(prev_raw, (n, 4), __import__("torch").float32))
         o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size, min_blocks,
-                  persistent)
+                  persistent, stack_depth)
         check(lib().rq_probe_update(self.ctx.handle, self.handle, C.byref(params), ptr(prev_sh), ptr(prev_raw),
                                     ptr(probe_map), ptr(out_sh), ptr(out_raw), C.byref(o),
                                     _stream(prev_sh, stream)), self.ctx.handle)
         return out_sh, out_raw
 
+    def gi_autotune(self, primary, params, out=None, *, layout=0, flags=0, block_size=0, min_blocks=0,
+                    persistent=0, stack_depth=0) -> dict:
+        """rq_gi_autotune on device primary rays: the compaction threshold of the GI pass."""
+        n = primary.numel() * primary.element_size() // 32
+        if out is None:
+            out = _empty_like_dev(primary, (n, 4), __import__("torch").float32)
+        r = L.RqGiTune()
+        o = _opts(layout, 0, 0, flags, block_size, min_blocks, persistent, stack_depth)
+        check(lib().rq_gi_autotune(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params), C.byref(o),
+                                   ptr(out), C.byref(r)), self.ctx.handle)
+        return dict(compact_below=r.compact_below, live_fraction=r.live_fraction, ms_compact=round(r.ms_compact, 4),
+                    ms_in_place=round(r.ms_in_place, 4))
+
     def gi_frame(self, primary, params, out=None, *, layout=0, mode=0, tie=0, flags=0,
-                 block_size=0, min_blocks=0, persistent=0, stats=False, stream=None):
+                 block_size=0, min_blocks=0, persistent=0, stack_depth=0, stats=False, stream=None):
         """Whole GI / AO pass.  numpy primary rays -> host path (copies inside the call)."""
         host = isinstance(primary, np.ndarray)
         n = primary.shape[0] if host else primary.numel() * primary.element_size() // 32
@@ -483,7 +498,7 @@ class _GiMixin:
                 out = _empty_like_dev(primary, (n, 4), __import__("torch").float32)
         st = L.RqFrameStats() if stats else None
         o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size,
-                  min_blocks, persistent)
+                  min_blocks, persistent, stack_depth)
         check(lib().rq_gi_frame(self.ctx.handle, self.handle, ptr(primary), n, C.byref(params),
                                 C.byref(o), ptr(out), C.byref(st) if st is not None else None,
                                 _stream(primary, stream)), self.ctx.handle)
@@ -498,12 +513,12 @@ for _name, _fn in list(vars(_GiMixin).items()):
 
 
 def diff_params(sun_dir=(0.4, 0.3, -0.866), sun_color=3.0, albedo=0.7, w_depth=1.0,
-                w_radiance=1.0, shadow_rays=True, shadow_offset=1e-3, recompute=False):
+                w_radiance=1.0, shadow_rays=True, shadow_offset=1e-3, recompute=False, layout=0):
+    """rq_diff_params; layout 0 = the scene's BVH2, BVH8Q = trace the (refitted) BVH8."""
     sd = np.asarray(sun_dir, dtype=np.float64)
     sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
     return L.RqDiffParams((C.c_float * 3)(*[float(x) for x in sd]), sun_color, albedo, w_depth,
-                          w_radiance, int(shadow_rays), shadow_offset, int(recompute),
-                          (C.c_int32 * 2)())
+                          w_radiance, int(shadow_rays), shadow_offset, int(recompute), int(layout), 0)
 
 
 class Tape:
@@ -573,10 +588,11 @@ def _queries(queries):
     return arr
 
 
-def batch(ctx: Context, queries, layout=0, mode=0, flags=0, block_size=0, min_blocks=0, stream=None):
+def batch(ctx: Context, queries, layout=0, mode=0, flags=0, block_size=0, min_blocks=0, stack_depth=0,
+          stream=None):
     """rq_batch: every query in one persistent launch."""
     arr = _queries(queries)
-    o = _opts(layout, mode, 0, flags, block_size, min_blocks, 0)
+    o = _opts(layout, mode, 0, flags, block_size, min_blocks, 0, stack_depth)
     st = stream
     if st is None and queries:
         st = _stream(queries[0][1], None)
@@ -603,8 +619,9 @@ class BatchPlan:
         r = L.RqBatchTune()
         check(lib().rq_batch_plan_autotune(self.handle, int(allow_bvh8), C.byref(r)), self.ctx.handle)
         combos = [dict(family=r.family_of[i], block=r.block_of[i], min_blocks=r.min_blocks_of[i],
-                       ms=round(r.ms[i], 4)) for i in range(r.n)]
-        return dict(family=r.family, block_size=r.block_size, min_blocks=r.min_blocks, combos=combos)
+                       stack_depth=r.depth_of[i], ms=round(r.ms[i], 4)) for i in range(r.n)]
+        return dict(family=r.family, block_size=r.block_size, min_blocks=r.min_blocks, stack_depth=r.depth,
+                    combos=combos)
 
     def close(self):
         if self.handle:

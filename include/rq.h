@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define RQ_ABI_VERSION 1
+#define RQ_ABI_VERSION 2
 
 typedef enum rq_status {
     RQ_OK = 0,
@@ -95,7 +95,8 @@ typedef struct rq_ray {
 /* Closest-hit result (32 bytes): the reference's TUVW = (t, u, v, w) with u + v + w = 1 and u
  * weighting vertex i0 (ComputeBarycentrics, TraverseBVHStack.glsl:150-166), plus the mesh id,
  * global triangle index and entity index.  A miss is t = u = v = w = -1, tri = mesh = entity =
- * -1.  iters = BVH nodes visited, summed over entities. */
+ * -1.  iters = BVH nodes visited, summed over entities (the last entity's under
+ * RQ_FLAG_REF_COMPAT). */
 typedef struct rq_hit {
     float t, u, v, w;
     int32_t tri, mesh, entity, iters;
@@ -122,7 +123,10 @@ typedef enum rq_tie {
 enum {
     RQ_FLAG_REF_COMPAT = 1,          /* reproduce IntersectScene's `TriangleIdx > 0` test
                                         (TraverseBVHStack.glsl:351): a hit on triangle 0 is
-                                        reported with t = u = v = w = -1 */
+                                        reported with t = u = v = w = -1; and its Iters, which
+                                        is the last walked entity's count (one `out int Iters`
+                                        serves every walk, :337-349) instead of the sum (BVH2
+                                        strict and fast walks; BVH8 iters count BVH8 nodes) */
     RQ_FLAG_IGNORE_TRANSPARENT = 2,  /* IntersectSceneIgnoreTransparent: skip entities with
                                         alpha < 0.99 (TraverseBVHStack.glsl:368-413) */
     RQ_FLAG_HOST_BUFFERS = 4,        /* ray/hit pointers are host memory */
@@ -146,7 +150,9 @@ typedef struct rq_opts {
     int32_t block_size;
     int32_t min_blocks;  /* minimum resident blocks per SM the kernel was compiled for */
     int32_t persistent;  /* 1 = persistent ray-queue kernel (strict mode, every layout) */
-    int32_t reserved;
+    int32_t stack_depth; /* BVH8 group-stack entries per lane of that variant: 0 (= 48), 32 or 24; a
+                            walk that would go deeper raises status bit 0 (rq_device_status) and
+                            returns the best hit found so far */
 } rq_opts;
 
 /* ---- Context ---------------------------------------------------------------------------- */
@@ -177,7 +183,7 @@ rq_status rq_device_status(rq_ctx* ctx, uint32_t* bits, int reset);
 
 /* Read bandwidth of the context's device in GB/s (no counterpart in the reference): 16-byte loads
  * that bypass L1, from every SM, over a device buffer of `bytes` (allocated and freed inside the
- * call), re-read `reps` times back to back after three warm-up passes.  A buffer well under the
+ * call), re-read `reps` times (up to 50 passes per launch) after three warm-up passes.  A buffer well under the
  * L2 size measures L2 read bandwidth, the roof of the traversal kernels, whose scenes stay
  * L2-resident; one well above it measures HBM.  Synchronises the context's stream. */
 rq_status rq_measure_read_gbs(rq_ctx* ctx, int64_t bytes, int32_t reps, double* gbs);
@@ -339,13 +345,19 @@ rq_status rq_closest_attribs(rq_ctx* ctx, const rq_scene* scene, const rq_ray* r
 /* Autotuner: times every compiled launch variant of the traversal kernel for `query` (0 =
  * closest hit, 1 = any hit) and `layout` on the caller's device rays (3 timed launches each, after
  * one warm-up), and records the fastest for the scene; later queries with an all-zero variant in
- * rq_opts use it.  out->ms[i] is variant i's best time in ms (-1 = not applicable to the layout). */
-#define RQ_MAX_VARIANTS 8
+ * rq_opts use it.  The variants span threads per block, minimum resident blocks per SM, one thread
+ * per ray or the persistent ray queue, and (BVH8 only) the group-stack depth.  out->ms[i] is
+ * variant i's best time in ms (-1 = not applicable to the layout, -2 = its stack overflowed on
+ * these rays, so it is never picked).  No counterpart in the reference (its traversal is one
+ * shader with a fixed 64-entry stack, TraverseBVHStack.glsl:168-324). */
+#define RQ_MAX_VARIANTS 10
 typedef struct rq_tune_result {
     int32_t variant, block_size, min_blocks, persistent;
     int32_t n_variants;
+    int32_t depth;  /* group-stack depth of the chosen variant (BVH8) */
     float ms[RQ_MAX_VARIANTS];
     int32_t block[RQ_MAX_VARIANTS], min_blocks_of[RQ_MAX_VARIANTS], persistent_of[RQ_MAX_VARIANTS];
+    int32_t depth_of[RQ_MAX_VARIANTS];
 } rq_tune_result;
 rq_status rq_autotune(rq_ctx* ctx, rq_scene* scene, const rq_ray* rays, int64_t n, int32_t query,
                       rq_layout layout, rq_tune_result* out);
@@ -393,14 +405,18 @@ typedef struct rq_batch_plan rq_batch_plan;
 rq_status rq_batch_plan_create(rq_ctx* ctx, const rq_query* queries, int32_t n_queries,
                                const rq_opts* opts, rq_batch_plan** out);
 rq_status rq_batch_plan_launch(rq_batch_plan* plan, void* stream);
-/* Times every batch launch variant (block size x occupancy target) for each usable layout family
- * (BVH8Q when every scene has one, the BVH2 layouts) on the plan's own queries, keeps the fastest
- * and re-captures the graph.  ms[i] = time of combination i, described by family_of[i] (0 =
- * BVH8Q, 1 = BVH2 strict, 2 = BVH2 fast), block_of[i], min_blocks_of[i]; -1 = not applicable. */
+/* Times every batch launch variant (block size x occupancy target, and for BVH8Q the group-stack
+ * depth 48 / 32 / 24) for each usable layout family (BVH8Q when every scene has one, the BVH2
+ * layouts) on the plan's own queries, keeps the fastest and re-captures the graph.  ms[i] = time
+ * of combination i, described by family_of[i] (0 = BVH8Q, 1 = BVH2 strict, 2 = BVH2 fast),
+ * block_of[i], min_blocks_of[i], depth_of[i]; -1 = not applicable, -2 = the stack overflowed. */
+#define RQ_MAX_BATCH_COMBOS 16
 typedef struct rq_batch_tune {
     int32_t family, block_size, min_blocks, n;
-    float ms[12];
-    int32_t family_of[12], block_of[12], min_blocks_of[12];
+    int32_t depth;
+    float ms[RQ_MAX_BATCH_COMBOS];
+    int32_t family_of[RQ_MAX_BATCH_COMBOS], block_of[RQ_MAX_BATCH_COMBOS], min_blocks_of[RQ_MAX_BATCH_COMBOS];
+    int32_t depth_of[RQ_MAX_BATCH_COMBOS];
 } rq_batch_tune;
 rq_status rq_batch_plan_autotune(rq_batch_plan* plan, int32_t allow_bvh8, rq_batch_tune* out);
 rq_status rq_batch_plan_destroy(rq_batch_plan* plan);
@@ -462,6 +478,13 @@ typedef struct rq_gi_params {
                               skymap against the first bounce's 2.0) and ends the path.  With
                               RQ_FLAG_REF_COMPAT a bounce miss adds nothing, as the reference's
                               loop does (it tests the first bounce's t for the sky) */
+    float compact_below;   /* rq_gi_frame: the secondary rays are traced compacted (active rays
+                              only) when the fraction of primary rays with a hit is below this
+                              value, else in place (one slot per sample, inactive slots included);
+                              the fraction is counted on the device.  > 1 = always compact; 0 = the
+                              scene's value from rq_gi_autotune (always compact until tuned).  The
+                              pixels are the same either way; the bounce loop, sort_rays and
+                              unfused always compact */
 } rq_gi_params;
 
 typedef struct rq_frame_stats {
@@ -519,6 +542,19 @@ rq_status rq_shade(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, const
 rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,
                       const rq_gi_params* params, const rq_opts* opts, float* pixels4,
                       rq_frame_stats* stats, void* stream);
+
+/* GI-pass autotuner (no counterpart in the reference): runs rq_gi_frame on the caller's device
+ * primary rays with the secondary rays compacted and in place (3 timed passes each after a
+ * warm-up; pixels4 receives the pixels), and records the threshold for the scene: the frame's
+ * fraction of primary hits when the in-place pass was faster (frames at least that full then run
+ * in place), else 2 (always compact).  Passes with rq_gi_params.compact_below = 0 use it. */
+typedef struct rq_gi_tune {
+    float compact_below;  /* the threshold recorded */
+    float live_fraction;  /* fraction of the frame's primary rays with a hit */
+    float ms_compact, ms_in_place;
+} rq_gi_tune;
+rq_status rq_gi_autotune(rq_ctx* ctx, rq_scene* scene, const rq_ray* primary, int64_t n,
+                         const rq_gi_params* params, const rq_opts* opts, float* pixels4, rq_gi_tune* out);
 
 /* ---- Specular reflections ---------------------------------------------------------------- */
 
@@ -620,7 +656,9 @@ typedef struct rq_diff_params {
     int32_t shadow_rays;
     float shadow_offset;
     int32_t recompute;  /* 1 = keep no hit records: rq_bwd re-traces the primary (and shadow) rays */
-    int32_t reserved[2];
+    int32_t layout;     /* 0 = the scene's BVH2 (strict walk), RQ_LAYOUT_BVH8Q = the BVH8 (same hits;
+                           refitted by rq_scene_update_positions) */
+    int32_t reserved;
 } rq_diff_params;
 
 typedef struct rq_tape rq_tape;
@@ -637,8 +675,11 @@ rq_status rq_tape_free(rq_tape* tape);
 rq_status rq_tape_bytes(const rq_tape* tape, int64_t* bytes);
 
 /* Replaces every vertex position (xyz: n_verts x 3 device floats) and refits the BVH2 boxes with
- * the topology kept (exact min/max per level, bottom-up).  Stack layout scenes; the BVH8 is
- * dropped (rebuild with rq_scene_build_bvh8). */
+ * the topology kept (exact min/max per level, bottom-up), and the BVH8 when one is built: its
+ * triangle records are recomputed and its quantised child boxes refitted level by level, rounded
+ * outward onto each node's new grid, so its hits stay those of the strict BVH2 walk.  Stack layout
+ * scenes.  The top level over the entities is not refitted: every entity is walked until the
+ * entities or the BVH8 are set again. */
 rq_status rq_scene_update_positions(rq_scene* scene, const float* xyz, void* stream);
 
 /* ---- Allocation-free GI pass ------------------------------------------------------------ */

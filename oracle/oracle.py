@@ -21,7 +21,18 @@ REF_SO = HERE / "_ref" / "librefbvh.so"
 REF_LEAF4_SO = HERE / "_ref" / "librefbvh_leaf4.so"
 REF_PHYSICS_SO = HERE / "_ref" / "librefphysics.so"
 REF_GLSL_SO = HERE / "_ref" / "librefglsl.so"
-REFERENCE_ROOT = Path(os.environ.get("RQ_REFERENCE_ROOT", "/root/reference"))
+# Where the reference source tree is: RQ_REFERENCE_ROOT, else the location the last reference build
+# recorded (oracle/_ref/REFERENCE_ROOT); None where it is not mounted (the GPU hosts).
+_ROOT_NOTE = HERE / "_ref" / "REFERENCE_ROOT"
+
+
+def reference_root() -> Path | None:
+    env = os.environ.get("RQ_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    if _ROOT_NOTE.exists():
+        return Path(_ROOT_NOTE.read_text().strip())
+    return None
 
 RAY_DTYPE = np.dtype([("o", "<f4", (3,)), ("tmin", "<f4"), ("d", "<f4", (3,)), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("w", "<f4"),
@@ -32,14 +43,26 @@ ORC_TIE_FIRST_FOUND, ORC_TIE_LOWER_INDEX = 0, 1
 ORC_FLAG_REF_COMPAT, ORC_FLAG_IGNORE_TRANSPARENT = 1, 2
 
 
-def build(reference: bool | None = None) -> None:
-    """Builds liboracle.so; also the reference-builder harness when the reference is present."""
-    targets = ["oracle"]
+def build(reference: bool | None = None, reference_root: str | os.PathLike | None = None) -> None:
+    """Builds liboracle.so; also the reference checkers (oracle/_ref) when the reference source tree
+    is given (reference_root, RQ_REFERENCE_ROOT or the location recorded by an earlier build) and
+    present.  The location is recorded in oracle/_ref/REFERENCE_ROOT for later sessions."""
+    root = Path(reference_root) if reference_root else reference_root_or_none()
+    have = root is not None and (root / "Source" / "Core" / "BVH" / "BVHConstructor.cpp").exists()
     if reference is None:
-        reference = (REFERENCE_ROOT / "Source" / "Core" / "BVH" / "BVHConstructor.cpp").exists()
+        reference = have
+    if reference and not have:
+        raise FileNotFoundError("the reference source tree is not available: set RQ_REFERENCE_ROOT")
+    targets = ["oracle"] + (["ref"] if reference else [])
+    args = ["make", "-s", "-C", str(HERE), *targets] + ([f"REF={root}"] if reference else [])
+    subprocess.run(args, check=True)
     if reference:
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", str(HERE), f"REF={REFERENCE_ROOT}", *targets], check=True)
+        _ROOT_NOTE.parent.mkdir(parents=True, exist_ok=True)
+        _ROOT_NOTE.write_text(str(root))
+
+
+def reference_root_or_none() -> Path | None:
+    return reference_root()
 
 
 class OrcScene(C.Structure):
@@ -361,6 +384,23 @@ class OracleScene:
         out = np.empty((hits.shape[0], 3), dtype=np.float32)
         orc().orc_hit_albedo(C.byref(self.s), _p(hits), hits.shape[0], C.byref(mat),
                              nthreads or os.cpu_count() or 1, _p(out))
+        return out
+
+    def getdata(self, hits, albedo, textures=None, mesh_texture=None):
+        """GetData (TraverseBVHStack.glsl:422-455) per hit record: (n, 8) float32 = Normal xyz,
+        Alpha, Albedo rgb, Emissivity; a miss (t < 0 or mesh < 0) gives Normal -1, Albedo 0,
+        Emissivity 0 and Alpha 0 (the shader returns before writing Alpha)."""
+        hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+        out = np.zeros((hits.shape[0], 8), dtype=np.float32)
+        out[:, 0:3] = -1.0
+        hit = (hits["t"] >= 0) & (hits["mesh"] >= 0)
+        h = np.ascontiguousarray(hits[hit])
+        if len(h):
+            out[hit, 0:3] = self.hit_normal(h, 0)
+            out[hit, 4:7] = self.hit_albedo(h, albedo, textures, mesh_texture)
+            data = self.entities["data"][h["entity"]]
+            out[hit, 7] = data[:, 0].view(np.float32)
+            out[hit, 3] = data[:, 1].view(np.float32)
         return out
 
 
@@ -688,7 +728,8 @@ def ref_collide_boxes(vertices, tris, nodes, entities, boxes) -> np.ndarray:
 
 def ref_available(leaf4: bool = False) -> bool:
     so = REF_LEAF4_SO if leaf4 else REF_SO
-    if not so.exists() and (REFERENCE_ROOT / "Source").exists():
+    root = reference_root()
+    if not so.exists() and root is not None and (root / "Source").exists():
         try:
             build(reference=True)
         except Exception:

@@ -384,7 +384,7 @@ void scene_closest(const Scene& s, const orc_ray& r, orc_hit& h, int tie, int fl
     const V3 o = ld3(r.o), d = ld3(r.d);
     float tmax = r.tmax;  // scene TMax (1000000.0 in the reference, :331)
     float closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent = -1;
+    int32_t mesh = -1, tri = -1, ent = -1, last = 0;
     for (int i = 0; i < s.n_ents; ++i) {
         const orc_entity& e = s.ents[i];
         if ((flags & ORC_FLAG_IGNORE_TRANSPARENT) && ent_alpha(e) < 0.99f) continue;
@@ -400,6 +400,7 @@ void scene_closest(const Scene& s, const orc_ray& r, orc_hit& h, int tie, int fl
                          : bvh_stackless_closest(s, ro, rd, e.node_offset, e.node_count, r.tmin,
                                                  bb, tie, tests);
         h.iters += it;
+        last = it;  // IntersectScene hands one `out int Iters` to every walk (:337-349)
         const float T = bb.closest;
         if (T > 0.0f && (T < tmax || (tie == ORC_TIE_LOWER_INDEX && T == tmax && bb.tri < tri))) {
             tmax = T;
@@ -409,6 +410,8 @@ void scene_closest(const Scene& s, const orc_ray& r, orc_hit& h, int tie, int fl
             ent = i;
         }
     }
+    // the reference reports the last walked entity's count; the sum over entities otherwise
+    if (flags & ORC_FLAG_REF_COMPAT) h.iters = last;
     if (closest > 0.0f) {
         h.tri = tri;
         h.mesh = mesh;

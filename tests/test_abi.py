@@ -35,7 +35,7 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 
 def test_abi_version_and_status_strings():
-    assert L.lib().rq_abi_version() == 1
+    assert L.lib().rq_abi_version() == 2
     assert L.lib().rq_status_string(L.RQ_EINVAL) == b"invalid argument"
 
 
@@ -46,7 +46,7 @@ def test_struct_sizes_match_reference_layouts():
     assert L.STACKLESS_NODE_DTYPE.itemsize == 32  # FlattenedNode
     assert L.ENTITY_DTYPE.itemsize == 192        # BVHEntity
     assert C.sizeof(L.RqOpts) == 32
-    assert C.sizeof(L.RqGiParams) == 80
+    assert C.sizeof(L.RqGiParams) == 84
     assert C.sizeof(L.RqProbeParams) == 108     # rq_probe_params, the oracle's orc_probe_params
     from oracle import oracle as O
     assert C.sizeof(O.OrcProbeParams) == C.sizeof(L.RqProbeParams)
@@ -64,3 +64,32 @@ def test_null_arguments_rejected():
     assert L.lib().rq_create(0, None) == L.RQ_EINVAL
     assert L.lib().rq_closest(None, None, None, 0, None, None, None) == L.RQ_EINVAL
     assert L.lib().rq_build_bvh(None, 0, None, 0, None, 0, 1, None, C.byref(h)) == L.RQ_EINVAL
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct the Python mirror declares has the size and field offsets the C compiler gives
+    include/rq.h (a small C program prints them)."""
+    import subprocess
+    from pathlib import Path
+    inc = Path(__file__).resolve().parents[1] / "include"
+    structs = {"rq_opts": L.RqOpts, "rq_tune_result": L.RqTuneResult, "rq_batch_tune": L.RqBatchTune,
+               "rq_gi_params": L.RqGiParams, "rq_gi_tune": L.RqGiTune, "rq_probe_params": L.RqProbeParams,
+               "rq_frame_stats": L.RqFrameStats, "rq_diff_params": L.RqDiffParams,
+               "rq_specular_params": L.RqSpecularParams}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "rq.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines += ['printf("rq_hit_attrib %zu\\n", sizeof(rq_hit_attrib));', "return 0; }"]
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                   check=True).stdout.splitlines())
+    for name, cls in structs.items():
+        assert int(got[name]) == C.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(got[f"{name}.{f}"]) == getattr(cls, f).offset, f"{name}.{f}"
+    assert int(got["rq_hit_attrib"]) == 32

@@ -10,11 +10,12 @@ import numpy as np
 import pytest
 
 import candela_gb300 as R
+from candela_gb300 import _lib as L
 from candela_gb300 import scenes as S
 from candela_gb300.engine import diff_params
 from oracle import oracle as O
 
-from .helpers import rays_to_device
+from .helpers import assert_hits_identical, hits_from_device, rays_to_device
 
 pytestmark = pytest.mark.gpu
 
@@ -187,3 +188,101 @@ def test_refit_tight_and_containing(ctx):
     want = osc.closest(rays)
     got = sc.closest(d_rays).cpu().numpy().view(np.uint32).reshape(-1, 8)
     assert np.array_equal(got, want.view(np.uint32).reshape(-1, 8))
+
+
+def _host_refit(b, P):
+    """The stack-layout BVH2 of b with every box recomputed from positions P (bottom-up, exact)."""
+    nodes = b.nodes.copy()
+    w = nodes.view(np.int32)
+
+    def box(j):
+        out = []
+        for s in (0, 8):
+            if w[j, s + 3] == -1:
+                lo, hi = box(w[j, s + 7])
+            else:
+                st, ln = w[j, s + 3] >> 4, w[j, s + 3] & 15
+                pts = P[b.tris[st:st + ln, :3].ravel()]
+                lo, hi = pts.min(0), pts.max(0)
+            nodes[j, s:s + 3] = lo
+            nodes[j, s + 4:s + 7] = hi
+            out.append((lo, hi))
+        return np.minimum(out[0][0], out[1][0]), np.maximum(out[0][1], out[1][1])
+
+    box(0)
+    return nodes
+
+
+def test_bvh8_refit_follows_vertex_moves(ctx):
+    """rq_scene_update_positions refits the BVH8 (records and quantised boxes, topology kept): after
+    three successive moves, small and large, BVH8q closest hits and occlusion equal the oracle's walk
+    over the host-refitted BVH2 (or are proven by a brute force), in one-thread-per-ray and
+    persistent launches at every group-stack depth, and equal a BVH8 built afresh from the moved
+    positions."""
+    import torch
+    from .helpers import assert_equal_or_proven, assert_occlusion_equal_or_proven, same_records
+    m = S.heightfield(64, seed=5)
+    b = R.build_bvh(m.vertices, m.indices, m.mesh_ids, 0, layout=R.STACK)
+    ent = R.identity_entity(0, b.nodes.shape[0])
+    sc = ctx.scene(R.STACK, m.vertices, b.tris, b.nodes, ent)
+    sc.build_bvh8()
+    rays = np.concatenate([S.camera_rays(160, 120, **CAM),
+                           S.sphere_rays(40_000, (-1.3, -1.3, -0.6), (1.3, 1.3, 1.0), seed=17)])
+    d_rays = rays_to_device(rays)
+    base = m.vertices["pos"][:, :3].astype(np.float64)
+    rng = np.random.default_rng(3)
+    for step, amp in enumerate((0.002, 0.05, 0.3)):
+        P = base.copy()
+        P[:, 2] += amp * np.sin(7.0 * base[:, 0] + step) * np.cos(5.0 * base[:, 1])
+        P[:, :2] += rng.uniform(-0.3, 0.3, (len(P), 2)) * (2.0 / 64) * (amp > 0.01)
+        P = P.astype(np.float32)
+        sc.update_positions(torch.from_numpy(P).cuda())
+        v2 = m.vertices.copy()
+        v2["pos"][:, :3] = P
+        osc = O.OracleScene(O.ORC_STACK, v2, b.tris, _host_refit(b, P), ent)
+        want = osc.closest(rays)
+        want_occ = osc.anyhit(rays)
+        assert_hits_identical(hits_from_device(sc.closest(d_rays)), want, f"strict after move {step}")
+        for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1),
+                   dict(block_size=128, min_blocks=8, persistent=1, stack_depth=24)):
+            got = hits_from_device(sc.closest(d_rays, layout=L.LAYOUT_BVH8Q, **kw))
+            assert_equal_or_proven(got, want, osc, rays, what=f"bvh8 refit move {step} {kw}")
+            occ = sc.anyhit(d_rays, layout=L.LAYOUT_BVH8Q, **kw).cpu().numpy()
+            assert_occlusion_equal_or_proven(occ, want_occ, osc, rays, what=f"bvh8 refit any {step} {kw}")
+        # a BVH8 built afresh over the moved positions (same BVH2 topology) finds the same hits
+        fresh = ctx.scene(R.STACK, v2, b.tris, _host_refit(b, P), ent)
+        fresh.build_bvh8()
+        f_hits = hits_from_device(fresh.closest(d_rays, layout=L.LAYOUT_BVH8Q))
+        assert same_records(got, f_hits).all()
+        fresh.close()
+        assert (want["t"] > 0).mean() > 0.3
+    assert ctx.device_status() == 0
+    sc.close()
+
+
+def test_adjoint_on_bvh8_equals_bvh2(ctx):
+    """rq_fwd / rq_bwd tracing the BVH8q give the BVH2 image, loss and gradients bit for bit, also
+    after a refit, taped and in recompute mode."""
+    import torch
+    m, b, ent, sc, rays, d_rays, tsc, zero = _setup(ctx, n=48)
+    sc.build_bvh8()
+    p2 = diff_params(shadow_rays=True)
+    target, _, t0 = tsc.forward(d_rays, zero, p2)
+    t0.close()
+    for moved in (False, True):
+        if moved:
+            xyz = torch.from_numpy(m.vertices["pos"][:, :3].copy()).cuda()
+            xyz[:, 2] += 0.05 * torch.sin(11.0 * xyz[:, 0])
+            sc.update_positions(xyz)
+        for recompute in (False, True):
+            img2, l2, tp2 = sc.forward(d_rays, target, diff_params(shadow_rays=True, recompute=recompute))
+            g2 = tp2.backward().cpu().numpy()
+            img8, l8, tp8 = sc.forward(d_rays, target, diff_params(shadow_rays=True, recompute=recompute,
+                                                                   layout=L.LAYOUT_BVH8Q))
+            g8 = tp8.backward().cpu().numpy()
+            np.testing.assert_array_equal(img8.cpu().numpy().view(np.uint32), img2.cpu().numpy().view(np.uint32))
+            assert l8 == l2
+            np.testing.assert_array_equal(g8.view(np.uint32), g2.view(np.uint32))
+            tp2.close()
+            tp8.close()
+    assert ctx.device_status() == 0

@@ -61,7 +61,9 @@ def test_closest_attribs_bit_exact(scene, flags):
     np.testing.assert_array_equal(a.cpu().numpy().view(np.uint32), want_a.view(np.uint32))
     hit = want_h["t"] > 0
     assert 0.2 < hit.mean() < 0.95
-    assert len(np.unique(want_a[hit, 7])) >= 3 and len(np.unique(want_a[hit, 3])) >= 2
+    assert len(np.unique(want_a[hit, 7])) >= 3
+    if not flags & L.FLAG_IGNORE_TRANSPARENT:
+        assert len(np.unique(want_a[hit, 3])) >= 2  # translucent entities hit
     # host buffers: the same records
     hh, ah = sc.closest_attribs(rays, flags=flags)
     assert_hits_identical(hh, want_h, "host buffers")

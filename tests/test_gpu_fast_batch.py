@@ -104,8 +104,16 @@ def test_batch_plan_graph_and_autotune(ctx):
         plan.launch()
         _check(qs, want)
     res = plan.autotune(allow_bvh8=True)
-    assert res["family"] in (0, 1) and len(res["combos"]) == 8
-    assert sum(c["ms"] > 0 for c in res["combos"]) == 8
+    # BVH8q: 4 launch shapes x group-stack depths 48 / 32 / 24; BVH2 strict: 4 launch shapes
+    assert res["family"] in (0, 1) and len(res["combos"]) == 16
+    assert sum(c["ms"] > 0 for c in res["combos"]) == 16
+    assert sorted({c["stack_depth"] for c in res["combos"] if c["family"] == 0}) == [24, 32, 48]
+    # every combination the tuner can pick gives the per-query results
+    for depth in (48, 32, 24):
+        for sc, d, kind, out in qs:
+            out.zero_()
+        R.engine.batch(ctx, qs, layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=8, stack_depth=depth)
+        _check(qs, want)
     for sc, d, kind, out in qs:
         out.zero_()
     plan.launch()
