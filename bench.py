@@ -846,7 +846,7 @@ def differentiation_record(args, ctx=None):
                 "depth_only_central": stats(depth_only),
                 "note": "h = 1e-3 is 26% of a triangle edge on the 512x512 grid (cell 2/512), so the "
                         "central difference of the Lambert term carries an O(h^2) truncation error of "
-                        "a few percent; Richardson extrapolation from h and h/2 removes it"}
+                        "a few percent; Richardson extrapolation from h and h/2 (and h/4) removes it"}
     # 100 Adam steps on vertex z with refit
     z = base[:, 2].clone().requires_grad_(False)
     m1 = torch.zeros_like(z)

@@ -606,7 +606,9 @@ rq_status rq_specular_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* pr
  *
  * Buffers, probe-major: prev_sh / out_sh 8 uint32 per probe (the u_PrevFrameSH / o_SHOutput
  * A.xyzw, B.xyzw texels), prev_raw / out_raw 4 floats per probe (radiance, 0: the o_CurrentRaw
- * texel, kept in float32 where the reference stores r11g11b10), probe_map 64 x 2 floats per probe
+ * texel, kept in float32 where the reference stores r11f_g11f_b10f, :17-18; with
+ * RQ_FLAG_REF_COMPAT rounded to what that format holds, the GL conversion with ties to even, so
+ * the next frame blends what the reference blends), probe_map 64 x 2 floats per probe
  * (the 8x8 octahedral depth / depth^2 map, MapData), updated in place at the pixel the ray's
  * direction maps to.  prev_sh and out_sh, and prev_raw and out_raw, must not overlap.
  * Differences from the shader, each deliberate: the map of probe (x, y, z) starts at p * 64 (the

@@ -255,7 +255,7 @@ def test_bvh8_refit_follows_vertex_moves(ctx):
         f_hits = hits_from_device(fresh.closest(d_rays, layout=L.LAYOUT_BVH8Q))
         assert same_records(got, f_hits).all()
         fresh.close()
-        assert (want["t"] > 0).mean() > 0.3
+        assert (want["t"] > 0).mean() > 0.2
     assert ctx.device_status() == 0
     sc.close()
 

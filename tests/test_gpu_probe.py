@@ -119,7 +119,8 @@ def test_probe_update_rejects_bad_arguments(ctx):
 def test_probe_update_textures_and_ref_compat(ctx, flags):
     """Textured albedo (a repeat and a clamped sRGB texture over a heightfield with texture
     coordinates) and the reference's conventions (RQ_FLAG_REF_COMPAT: a hit on global triangle 0
-    reads as a miss): the volume equals the oracle's bit for bit."""
+    reads as a miss, and the raw radiance is held as the reference's r11f_g11f_b10f images hold it,
+    which the next frame's temporal blend reads): the volume equals the oracle's bit for bit."""
     m = S.heightfield(48, seed=8)
     pos = m.positions().astype(np.float64)
     verts = S.with_texcoords(m.vertices, np.stack([pos[:, 0] * 1.5 + 0.2, pos[:, 1] * -1.3], 1))
@@ -146,6 +147,12 @@ def test_probe_update_textures_and_ref_compat(ctx, flags):
         np.testing.assert_array_equal(got_sh.cpu().numpy().view(np.uint32), want_sh, err_msg=f"frame {k} sh")
         np.testing.assert_array_equal(got_raw.cpu().numpy().view(np.uint32), want_raw.view(np.uint32))
         np.testing.assert_array_equal(d_map.cpu().numpy().view(np.uint32), want_map.view(np.uint32))
+        r11 = np.vectorize(lambda x, mb: O.small_ufloat(float(x), mb), otypes=[np.float32])
+        packed = np.stack([r11(want_raw[:, 0], 6), r11(want_raw[:, 1], 6), r11(want_raw[:, 2], 5)], 1)
+        if flags & L.FLAG_REF_COMPAT:  # every value representable in the packed format
+            np.testing.assert_array_equal(packed.view(np.uint32), want_raw[:, :3].view(np.uint32))
+        else:  # float32 keeps more than the packed format
+            assert (packed != want_raw[:, :3]).any()
         sh, raw, pmap = want_sh, want_raw, want_map
         d_sh, d_raw = got_sh, got_raw
         assert 0.2 < (hits["t"] > 0).mean() < 0.95
