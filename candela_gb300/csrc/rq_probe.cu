@@ -295,11 +295,35 @@ __global__ void k_probe_shadow(SceneView s, const rq_ray* __restrict__ rays, con
     put(out, i, strict::add(P, strict::muls(N, a.shadow_offset)), strict::neg(a.sun_dir), 1000000.0f);
 }
 
-// UpdateRadianceProbes.glsl main after the trace (:440-519), one thread per probe.
+// The value an unsigned float with a 5-bit exponent (bias 15) and `mbits` mantissa bits holds
+// for x: the R and G (6 bits) and B (5 bits) channels of GL_R11F_G11F_B10F, the format of the
+// reference's raw radiance images (UpdateRadianceProbes.glsl:17-18, ProbeGI.cpp:100, 110).  As the
+// GL specification converts: finite values to the closest representable one (ties to even here),
+// negative values and -inf to 0, values above the largest finite one to it, +inf and NaN kept.
+// Every step is an exact binary32 operation (power-of-two scaling, round to integer).
+__device__ __forceinline__ float to_small_ufloat(float x, int mbits) {
+    if (x != x || x == INFINITY) return x;
+    if (!(x > 0.0f)) return 0.0f;
+    const float maxf = ldexpf(2.0f - ldexpf(1.0f, -mbits), 15);
+    if (x >= maxf) return maxf;
+    int k;
+    frexpf(x, &k);                      // x in [2^(k-1), 2^k)
+    const int e = max(k - 1, -14);      // subnormals share the step of the smallest binade
+    const float step = ldexpf(1.0f, e - mbits);
+    const float q = __fmul_rn(rintf(__fdiv_rn(x, step)), step);
+    return q > maxf ? maxf : q;
+}
+__device__ __forceinline__ f3 to_r11g11b10(f3 v) {
+    return {to_small_ufloat(v.x, 6), to_small_ufloat(v.y, 6), to_small_ufloat(v.z, 5)};
+}
+
+// UpdateRadianceProbes.glsl main after the trace (:440-519), one thread per probe.  raw_r11: store
+// the raw radiance as the r11f_g11f_b10f image holds it (RQ_FLAG_REF_COMPAT).
 __global__ void k_probe_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_hit* __restrict__ hits,
                               const uint8_t* __restrict__ occl, int64_t n, const Materials mat, ProbeArgs a,
                               const uint4* __restrict__ prev_sh, const float4* __restrict__ prev_raw,
-                              float2* __restrict__ map, uint4* __restrict__ out_sh, float4* __restrict__ out_raw) {
+                              float2* __restrict__ map, uint4* __restrict__ out_sh, float4* __restrict__ out_raw,
+                              int raw_r11) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* pr = reinterpret_cast<const float4*>(rays) + 2 * i;
@@ -361,6 +385,7 @@ __global__ void k_probe_shade(SceneView s, const rq_ray* __restrict__ rays, cons
     B.w = static_cast<uint32_t>(frames);
     out_sh[2 * i] = A;
     out_sh[2 * i + 1] = B;
+    if (raw_r11) fr = to_r11g11b10(fr);
     out_raw[i] = make_float4(fr.x, fr.y, fr.z, 0.0f);
 }
 
@@ -448,7 +473,7 @@ rq_status rq_probe_update(rq_ctx* ctx, const rq_scene* sc, const rq_probe_params
     rq::k_probe_shade<<<rq::grid(n, 128), 128, 0, st>>>(
         sc->view, ray, hit, occ, n, rq::materials_of(sc), a, reinterpret_cast<const uint4*>(psh),
         reinterpret_cast<const float4*>(praw), reinterpret_cast<float2*>(pmap), reinterpret_cast<uint4*>(osh),
-        reinterpret_cast<float4*>(oraw));
+        reinterpret_cast<float4*>(oraw), (q.flags & RQ_FLAG_REF_COMPAT) ? 1 : 0);
     RQ_CUDA(ctx, cudaGetLastError());
     if (host) {
         RQ_CUDA(ctx, cudaMemcpyAsync(out_sh, osh, b_sh, cudaMemcpyDeviceToHost, st));

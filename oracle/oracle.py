@@ -168,7 +168,9 @@ def orc() -> C.CDLL:
         pp = C.POINTER(OrcProbeParams)
         L.orc_probe_raygen.argtypes = [pp, C.c_int, P]
         L.orc_probe_direction.argtypes = [C.c_uint32, P, I64, P]
-        L.orc_probe_shade.argtypes = [sp, pp, P, P, P, C.POINTER(OrcMaterials), P, P, P, P, P, C.c_int]
+        L.orc_probe_shade.argtypes = [sp, pp, P, P, P, C.POINTER(OrcMaterials), P, P, P, P, P, C.c_int, C.c_int]
+        L.orc_small_ufloat.argtypes = [C.c_float, C.c_int]
+        L.orc_small_ufloat.restype = C.c_float
         L.orc_bounce_accumulate.argtypes = [P, P, P, I64, I32, P, P, P, C.c_int, P]
         L.orc_pcg_hash.argtypes = [C.c_uint32]
         L.orc_pcg_hash.restype = C.c_uint32
@@ -330,10 +332,11 @@ class OracleScene:
         return out
 
     def probe_shade(self, p, rays, hits, lit, albedo, prev_sh, prev_raw, probe_map, textures=None,
-                    mesh_texture=None, nthreads=None):
+                    mesh_texture=None, nthreads=None, raw_r11=False):
         """Shading, bounce, SH encoding, temporal blend and packing of the probe rays
         (UpdateRadianceProbes.glsl:438-519).  Returns (out_sh (n, 8) uint32, out_raw (n, 4),
-        the updated probe map (n, 128))."""
+        the updated probe map (n, 128)).  raw_r11: the raw radiance rounded to what the reference's
+        r11f_g11f_b10f images hold."""
         q = probe_params(p)
         n = probe_count(q)
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
@@ -347,7 +350,8 @@ class OracleScene:
         osh = np.empty((n, 8), dtype=np.uint32)
         oraw = np.empty((n, 4), dtype=np.float32)
         orc().orc_probe_shade(C.byref(self.s), C.byref(q), _p(rays), _p(hits), _p(lit), C.byref(mat), _p(psh),
-                              _p(praw), _p(pmap), _p(osh), _p(oraw), nthreads or os.cpu_count() or 1)
+                              _p(praw), _p(pmap), _p(osh), _p(oraw), 1 if raw_r11 else 0,
+                              nthreads or os.cpu_count() or 1)
         return osh, oraw, pmap
 
     def probe_update(self, p, albedo, prev_sh, prev_raw, probe_map, flags=0, textures=None, mesh_texture=None):
@@ -362,7 +366,7 @@ class OracleScene:
                                     p.normal_mode)
             lit = 1 - self.anyhit(sr)
         osh, oraw, pmap = self.probe_shade(p, rays, hits, lit, albedo, prev_sh, prev_raw, probe_map,
-                                           textures, mesh_texture)
+                                           textures, mesh_texture, raw_r11=bool(flags & ORC_FLAG_REF_COMPAT))
         return osh, oraw, pmap, rays, hits
 
     def hit_normal(self, hits, normal_mode=0):
@@ -430,6 +434,11 @@ def barycentrics(p, a, b, c):
     out = np.zeros(3, dtype=np.float32)
     orc().orc_barycentrics(*[_p(v) for v in x], _p(out))
     return out
+
+
+def small_ufloat(x: float, mbits: int) -> float:
+    """The value a GL_R11F_G11F_B10F channel with mbits mantissa bits holds for x (restatement)."""
+    return orc().orc_small_ufloat(x, mbits)
 
 
 def pcg_hash(x: int) -> int:

@@ -809,6 +809,23 @@ uint32_t sample_key(uint32_t seed, uint32_t ray, uint32_t dim) {
     return pcg_hash(pcg_hash(pcg_hash(seed) + ray) + dim);
 }
 
+// The value GL_R11F_G11F_B10F holds for x in a channel with `mbits` mantissa bits (5-bit exponent,
+// bias 15, no sign), converted as the GL specification (section "Unsigned 11-Bit / 10-Bit
+// Floating-Point Numbers") describes: the closest representable finite value (ties to even),
+// negative values and -inf to 0, values above the largest finite one to it, +inf and NaN kept.
+float small_ufloat(float x, int mbits) {
+    if (std::isnan(x) || x == INFINITY) return x;
+    if (!(x > 0.0f)) return 0.0f;
+    const float maxf = std::ldexp(2.0f - std::ldexp(1.0f, -mbits), 15);
+    if (x >= maxf) return maxf;
+    int k;
+    std::frexp(x, &k);
+    const int e = std::max(k - 1, -14);
+    const float step = std::ldexp(1.0f, e - mbits);
+    const float q = std::nearbyint(x / step) * step;
+    return q > maxf ? maxf : q;
+}
+
 }  // namespace
 
 extern "C" {
@@ -857,6 +874,8 @@ void orc_barycentrics(const float p[3], const float a[3], const float b[3], cons
                       float out[3]) {
     barycentrics(ld3(p), ld3(a), ld3(b), ld3(c), out[0], out[1], out[2]);
 }
+
+float orc_small_ufloat(float x, int mbits) { return small_ufloat(x, mbits); }
 
 uint32_t orc_pcg_hash(uint32_t x) { return pcg_hash(x); }
 void orc_sincos_turns(float x, float* s, float* c) { sincos_turns(x, *s, *c); }
@@ -1400,10 +1419,11 @@ void orc_probe_direction(uint32_t seed, const uint32_t* ids, int64_t n, float* o
 }
 
 // UpdateRadianceProbes.glsl main (:408-520) after the trace: shading, the bounce from the previous
-// volume, SH encoding, temporal blend and packing; probe_map updated in place.
+// volume, SH encoding, temporal blend and packing; probe_map updated in place.  raw_r11: the raw
+// radiance as the reference's r11f_g11f_b10f images (:17-18) hold it.
 void orc_probe_shade(const orc_scene* sc, const orc_probe_params* p, const orc_ray* rays, const orc_hit* hits,
                      const uint8_t* lit, const orc_materials* mat, const uint32_t* prev_sh, const float* prev_raw,
-                     float* probe_map, uint32_t* out_sh, float* out_raw, int nthreads) {
+                     float* probe_map, uint32_t* out_sh, float* out_raw, int raw_r11, int nthreads) {
     const Scene s = make_scene(sc);
     const ProbeGrid g = probe_grid(*p);
     const V3 sun = ld3(p->sun_color), sky = ld3(p->sky_color), sdir = ld3(p->sun_dir);
@@ -1459,6 +1479,7 @@ void orc_probe_shade(const orc_scene* sc, const orc_probe_params* p, const orc_r
             pack_sh(sh, w);
             w[7] = uint32_t(frames);
             float* r = out_raw + 4 * i;
+            if (raw_r11) fr = V3{small_ufloat(fr.x, 6), small_ufloat(fr.y, 6), small_ufloat(fr.z, 5)};
             r[0] = fr.x;
             r[1] = fr.y;
             r[2] = fr.z;

@@ -147,7 +147,9 @@ void orc_probe_raygen(const orc_probe_params* p, int nthreads, orc_ray* out);
 void orc_probe_direction(uint32_t seed, const uint32_t* ids, int64_t n, float* out3);
 void orc_probe_shade(const orc_scene* s, const orc_probe_params* p, const orc_ray* rays, const orc_hit* hits,
                      const uint8_t* lit, const orc_materials* mat, const uint32_t* prev_sh, const float* prev_raw,
-                     float* probe_map, uint32_t* out_sh, float* out_raw, int nthreads);
+                     float* probe_map, uint32_t* out_sh, float* out_raw, int raw_r11, int nthreads);
+// The value a GL_R11F_G11F_B10F channel with `mbits` mantissa bits (6: R, G; 5: B) holds for x.
+float orc_small_ufloat(float x, int mbits);
 
 // The RT second-bounce loop's accumulation for n GI slots (DiffuseTrace.glsl:499-535): fr and thr0
 // 3 floats per slot, in 12 floats per slot and bounce {t, albedo rgb, emissive, normal xyz,
