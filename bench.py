@@ -179,6 +179,12 @@ class _OracleBVH:
         self.nodes, self.tris, self.info = nodes, tris, info
 
 
+def shared_config(wl) -> dict:
+    """The `config` both arms print (the same dict, so the two lines name the same workload)."""
+    return {"workload": wl["name"],
+            "l2": "GPU arm: flushed between timed steps (512 MB write); CPU arm: not applicable"}
+
+
 def make_workload(config: str, builder: str = "product"):
     """Scene, BVHs, rays and parameters of a workload.  builder "oracle": the BVHs come from the
     oracle's restatement of the reference constructor (the CPU reference arm, which loads nothing of
@@ -310,7 +316,7 @@ def run_reference(args, wl, rank, world):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(res["seconds"] * 1e3 / max(1, args.steps), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": wl["name"]},
+            "data": "synthetic", "config": shared_config(wl),
             "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -1230,8 +1236,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene and camera rays)",
-            "config": {"workload": wl["name"], "traversal": "BVH8q, autotuned launch, strict FP32 "
-                                                            "leaf test (hits identical to strict BVH2)",
+            "config": shared_config(wl),
+            "workload_detail": {"traversal": "BVH8q, autotuned launch, strict FP32 "
+                                             "leaf test (hits identical to strict BVH2)",
                        "rays_per_step": int(rays_per_step),
                        "primary_rays": int(st["primary_rays"]),
                        "secondary_rays": int(st["secondary_rays"]),
