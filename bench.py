@@ -618,7 +618,7 @@ def c6_scene():
     return ri, int(sum(m.n_tris for m in objs)), n_ent
 
 
-def run_c6(args):
+def instancing_record(args, ctx=None, flush=None):
     """Instancing workload (the top level over entities): 1920x1080 primary closest-hit rays plus one
     cosine GI closest-hit ray per hit over the 4096-entity scene of c6_scene; the GI pass with the
     top level against the reference's entity loop (RQ_FLAG_ENTITY_LOOP), same pixels."""
@@ -627,11 +627,10 @@ def run_c6(args):
     from candela_gb300 import _lib as L
     from candela_gb300 import scenes as S
     from candela_gb300.engine import gi_params
-    torch.cuda.set_device(0)
     t0 = time.perf_counter()
     ri, n_obj_tris, n_ent = c6_scene()
     build_s = time.perf_counter() - t0
-    ctx = R.Context(0)
+    ctx = ctx or R.Context(0)
     sc = ri.buffer_data(ctx)
     tl = sc.tlas_info()
     b8 = sc.build_bvh8()
@@ -641,8 +640,9 @@ def run_c6(args):
     pix = torch.empty((n, 4), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    flush.fill_(0)  # loads torch's fill kernel before any timed region
+    if flush is None:
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+        flush.fill_(0)  # loads torch's fill kernel before any timed region
     p = gi_params(spp=1, seed=1, origin_offset=1e-3, ray_tmax=1000000.0, query=0)
 
     def timed(fn, steps, warm):
@@ -680,8 +680,19 @@ def run_c6(args):
     st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr)[1]
     rays_per_step = int(st["primary_rays"]) + int(st["secondary_rays"])
     res = {}
+    clk = ClockSampler(0)
     for name, layout in (("bvh8q", L.LAYOUT_BVH8Q), ("strict_bvh2", R.STACK)):
-        ms_t = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, stream=sptr), args.steps, args.warmup)
+        if name == "bvh8q":
+            with clk:
+                clk.ready()
+                sc.gi_frame(d, p, out=pix, layout=layout, stream=sptr)
+                torch.cuda.synchronize()
+                clk.mark_timed(True)
+                ms_t = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, stream=sptr), args.steps,
+                             args.warmup)
+                clk.mark_timed(False)
+        else:
+            ms_t = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, stream=sptr), args.steps, args.warmup)
         a = pix.cpu().numpy().copy()
         ms_l = timed(lambda: sc.gi_frame(d, p, out=pix, layout=layout, flags=L.FLAG_ENTITY_LOOP, stream=sptr),
                      1, 1)
@@ -707,23 +718,35 @@ def run_c6(args):
     c0 = time.perf_counter()
     osc.closest(sample, nthreads=os.cpu_count() or 1)
     cpu_s = time.perf_counter() - c0
-    line = {"metric": METRIC, "value": res["bvh8q"]["top_level_mrays_s"], "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["bvh8q"]["top_level_ms"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded instanced scene and camera rays)",
-            "config": {"workload": f"instancing: {n_ent} entities of 3 objects ({n_obj_tris} object tris), "
-                                   "1920x1080 primary closest-hit + 1 cosine GI closest-hit ray per hit, "
-                                   "Lambert shading, stack BVH leaf 2, strict",
-                       "rays_per_step": rays_per_step, "scene_build_s": round(build_s, 2),
-                       "top_level": tl, "bvh8_nodes": b8["nodes"],
-                       "l2": "flushed between timed steps (512 MB write)"},
-            "gi_pass": res, "primary_launch_bvh8q": primary,
-            "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
-                             "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
-            "cpu_baseline": {"value": round(len(sample) / cpu_s / 1e6, 4), "unit": UNIT,
-                             "cores": os.cpu_count() or 1, "kind": "port",
-                             "sample": f"{len(sample)} primary rays, entity loop, {cpu_s:.2f} s"},
-            "device_status": ctx.device_status()}
+    rec = {"workload": f"instancing: {n_ent} entities of 3 objects ({n_obj_tris} object tris), "
+                       "1920x1080 primary closest-hit + 1 cosine GI closest-hit ray per hit, "
+                       "Lambert shading, stack BVH leaf 2, strict",
+           "value": res["bvh8q"]["top_level_mrays_s"], "unit": UNIT, "ms_per_step": res["bvh8q"]["top_level_ms"],
+           "rays_per_step": rays_per_step, "scene_build_s": round(build_s, 2), "top_level": tl,
+           "bvh8_nodes": b8["nodes"], "l2": "flushed between timed steps (512 MB write)",
+           "gi_pass": res, "primary_launch_bvh8q": primary,
+           "autotune": {k: {"picked": (v["block_size"], v["min_blocks"], v["persistent"]),
+                            "ms": [x["ms"] for x in v["variants"]]} for k, v in tuning.items()},
+           "cpu_baseline": {"value": round(len(sample) / cpu_s / 1e6, 4), "unit": UNIT,
+                            "cores": os.cpu_count() or 1, "kind": "port",
+                            "sample": f"{len(sample)} primary rays, entity loop, {cpu_s:.2f} s"},
+           "device_status": ctx.device_status(), "clocks": clk.summary()}
+    sc.close()
+    return rec
+
+
+def run_c6(args):
+    import torch
+    torch.cuda.set_device(0)
+    if args.profile:
+        instancing_record(args)
+        return
+    rec = instancing_record(args)
+    line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded instanced scene and camera rays)", "config": {"workload": rec["workload"]},
+            "instancing": rec, "cpu_baseline": rec["cpu_baseline"], "clocks": rec["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -1141,6 +1164,11 @@ def main():
 
     # ---- specular reflection pass (rq_specular_frame) over the same camera: primary + one GGX
     # reflection ray per pixel (roughness 0.3) + a shadow ray per reflection hit
+    # the consumer passes below are timed inside one clock-sampled window
+    legs_clk = ClockSampler(local)
+    legs_clk.__enter__()
+    legs_clk.ready()
+    legs_clk.mark_timed(True)
     from candela_gb300.engine import specular_params
     sp = specular_params(seed=1, roughness=0.3, shadow_rays=True)
     d_spec = torch.empty((n, 4), dtype=torch.float32, device=dev)
@@ -1164,8 +1192,6 @@ def main():
                "stackless_mboxes_s": round(n_box / (coll_sl_ms / 1e3) / 1e6, 1),
                "stackless_ms": round(coll_sl_ms, 4),
                "boxes_desc": "centred within 0.05 of a random vertex, half-extents 0.002-0.03"}
-    if rank == 0:
-        collide["cpu_baseline"] = cpu_collide(wl)
 
     # ---- radiance probe volume (rq_probe_update): the reference's default probe count (48 x 24 x
     # 48 = 55,296 probes), laid over the scene, and a 128 x 128 x 64 grid (1M probes); each frame
@@ -1183,7 +1209,12 @@ def main():
         n_pr = int(np.prod(grid))
         probe[name] = {"probes": n_pr, "ms": round(pr_ms, 4), "mprobes_s": round(n_pr / (pr_ms / 1e3) / 1e6, 1)}
         del vols
+    legs_clk.mark_timed(False)
+    legs_clk.__exit__(None, None, None)
+    legs_clocks = legs_clk.summary()
+    specular["clocks"] = collide["clocks"] = probe["clocks"] = legs_clocks
     if rank == 0:
+        collide["cpu_baseline"] = cpu_collide(wl)
         probe["cpu_baseline"] = cpu_probe(wl, wl["albedo"])
 
     # ---- roofline of the dominant kernel (secondary closest / AO any-hit on BVH8q)
@@ -1272,6 +1303,7 @@ def main():
             line["batched"] = batched_record(args, ctx, flush)
             line["precision"] = precision_record(args, ctx, flush)
             line["differentiation"] = differentiation_record(args, ctx)
+            line["instancing"] = instancing_record(args, ctx, flush)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
