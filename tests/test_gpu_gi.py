@@ -314,8 +314,9 @@ def test_textured_shading_matches_oracle(ctx, srgb, wrap):
 
 def test_gi_frame_pinned_large_equals_device_pass(ctx):
     """A frame of several host chunks with pinned host rays on the BVH8 layout (the primary launch
-    reads them over the host link, the pixels return in chunks while later chunks are shaded):
-    pixels and ray counts equal the device frame."""
+    reads them over the host link, the pixels return in chunks while later chunks are shaded; the
+    last chunk is short): pixels and ray counts equal the device frame.  Then RTAO on pageable
+    host buffers and the RT bounce loop on pinned ones."""
     import torch
     from candela_gb300 import _lib as L
     bufs = single_object("ico2", R.STACK)
@@ -331,3 +332,13 @@ def test_gi_frame_pinned_large_equals_device_pass(ctx):
     np.testing.assert_array_equal(out.view(np.uint32), want.cpu().numpy().view(np.uint32))
     assert st_got == st_want
     assert 0.1 < st_want["primary_hits"] / len(rays) < 0.9
+    pa = gi_params(spp=3, seed=9, origin_offset=0.05, ray_tmax=0.5, query=1)
+    want_a, st_a = sc.gi_frame(rays_to_device(rays), pa, layout=L.LAYOUT_BVH8Q, stats=True)
+    got_a, st_ga = sc.gi_frame(rays, pa, layout=L.LAYOUT_BVH8Q, stats=True)
+    np.testing.assert_array_equal(got_a.view(np.uint32), want_a.cpu().numpy().view(np.uint32))
+    assert st_ga == st_a and 0 < st_a["secondary_hits"] < st_a["secondary_rays"]
+    pb = gi_params(spp=1, seed=3, origin_offset=0.05, bounces=1)
+    want_b = sc.gi_frame(rays_to_device(rays), pb, layout=L.LAYOUT_BVH8Q)
+    np.testing.assert_array_equal(sc.gi_frame(pinned, pb, layout=L.LAYOUT_BVH8Q).view(np.uint32),
+                                  want_b.cpu().numpy().view(np.uint32))
+    assert sc.ctx.device_status() == 0
