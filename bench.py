@@ -194,16 +194,16 @@ def make_workload(config: str, builder: str = "product"):
     if config == "c1":
         mesh = S.c1_heightfield_scene()
         rays = S.camera_rays(512, 512, **S.C1_CAMERA)
-        params = dict(spp=1, seed=1, origin_offset=1e-3, ray_tmax=0.25, query=1)
+        params = dict(spp=1, seed=1, origin_offset=1e-3, ray_tmax=0.25, query=1, pixel_format=1)
         name = ("heightfield 256x256 (131,072 tris), 512x512 primary closest-hit + 1 cosine AO "
-                "any-hit ray per hit (tmax 0.25), stack BVH leaf 2, strict")
+                "any-hit ray per hit (tmax 0.25), stack BVH leaf 2, strict, rgba16f pixels")
     else:
         mesh = S.c2_icosphere_scene()
         rays = S.camera_rays(1920, 1080, **S.C2_CAMERA)
-        params = dict(spp=4, seed=1, origin_offset=1e-3, ray_tmax=1000000.0, query=0)
+        params = dict(spp=4, seed=1, origin_offset=1e-3, ray_tmax=1000000.0, query=0, pixel_format=1)
         name = ("64 displaced subdiv-5 icospheres + ground (1,310,722 tris), 1920x1080 primary "
                 "closest-hit + 4 cosine diffuse-GI closest-hit rays per hit, Lambert shading, "
-                "stack BVH leaf 2, strict")
+                "stack BVH leaf 2, strict, rgba16f pixels")
     t0 = time.perf_counter()
     if builder == "oracle":
         from oracle import oracle as O
@@ -962,7 +962,9 @@ def main():
     rays = wl["rays"]
     n = len(rays)
     d_rays = torch.from_numpy(rays.view(np.uint8)).to(dev)
-    d_pix = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    # pixels as the reference's output image stores them (rgba16f, DiffuseTrace.glsl:17)
+    pix_dtype = torch.float16 if wl["params"].get("pixel_format") == L.PIXELS_RGBA16F else torch.float32
+    d_pix = torch.empty((n, 4), dtype=pix_dtype, device=dev)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
@@ -1078,15 +1080,23 @@ def main():
 
     # ---- e2e: host buffers through the C ABI (pinned in, pinned out), host clock
     h_rays = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
-    h_pix = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
-    for _ in range(max(1, args.warmup)):
-        sc.gi_frame(h_rays, p, out=h_pix, layout=B8)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        sc.gi_frame(h_rays, p, out=h_pix, layout=B8)
-    e2e_s = time.perf_counter() - t0
+    def e2e_leg(params, dtype):
+        h_pix = torch.empty((n, 4), dtype=dtype).pin_memory().numpy()
+        for _ in range(max(1, args.warmup)):
+            sc.gi_frame(h_rays, params, out=h_pix, layout=B8)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sc.gi_frame(h_rays, params, out=h_pix, layout=B8)
+        return time.perf_counter() - t0, int(h_pix.nbytes)
+
+    e2e_s, d2h = e2e_leg(p, pix_dtype)
     e2e = {"value": round(rays_per_step * args.steps / e2e_s / 1e6, 2), "unit": UNIT,
-           "h2d_bytes_per_step": int(h_rays.nbytes), "d2h_bytes_per_step": int(h_pix.nbytes)}
+           "h2d_bytes_per_step": int(h_rays.nbytes), "d2h_bytes_per_step": d2h}
+    if pix_dtype == torch.float16:  # the same pass with float32 pixels (twice the bytes out)
+        p32 = gi_params(**{**wl["params"], "pixel_format": L.PIXELS_RGBA32F})
+        e2e32_s, d2h32 = e2e_leg(p32, torch.float32)
+        e2e["rgba32f_pixels"] = {"value": round(rays_per_step * args.steps / e2e32_s / 1e6, 2),
+                                 "d2h_bytes_per_step": d2h32}
 
     # ---- per-query breakdown (device rays, L2 flushed before each timed launch)
     def timed(fn, reps=max(3, min(args.steps, 10))):

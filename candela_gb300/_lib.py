@@ -21,6 +21,8 @@ TIE_LOWER_INDEX, TIE_FIRST_FOUND = 0, 1
 FLAG_REF_COMPAT, FLAG_IGNORE_TRANSPARENT, FLAG_HOST_BUFFERS, FLAG_NO_PERSISTENT = 1, 2, 4, 8
 FLAG_COUNT = 16
 FLAG_ENTITY_LOOP = 32
+PIXELS_RGBA32F, PIXELS_RGBA16F = 0, 1
+ABI_VERSION = 3
 
 VERTEX_DTYPE = np.dtype([("pos", "<f4", (4,)), ("packed", "<u4", (4,))])
 TRI_DTYPE = np.dtype(("<i4", (4,)))
@@ -93,7 +95,7 @@ class RqGiParams(C.Structure):
                 ("shadow_rays", C.c_int32), ("shadow_offset", C.c_float),
                 ("sun_dir", C.c_float * 3), ("sun_color", C.c_float * 3),
                 ("sky_color", C.c_float * 3), ("sort_rays", C.c_int32), ("unfused", C.c_int32),
-                ("bounces", C.c_int32), ("compact_below", C.c_float)]
+                ("bounces", C.c_int32), ("compact_below", C.c_float), ("pixel_format", C.c_int32)]
 
 
 class RqGiTune(C.Structure):

@@ -145,6 +145,11 @@ constexpr int kPoolRays = 64;
 // persistent): 1 (serve at once) 0.831 ms, 4: 0.823, 8: 0.791, 12: 0.777, 16: 0.780, 20: 0.789,
 // 24: 0.829, 32 (only when no lane walks) 1.26.
 constexpr int kServeBatch = 12;
+// Guided hand-out: once fewer than kTailPools x kPoolRays x (warps of the grid) rays remain past a
+// warp's last pool, the warp takes only the rays its idle lanes need, so that the warps run out of
+// work together.  C2 secondary launch: 0 (always pools) 0.769 ms, 1: 0.768, 2: 0.767, 4: 0.764,
+// 8: 0.767, 16: 0.763, always exact: 0.790.
+constexpr int kTailPools = 4;
 
 template <bool kAny, class Sink, bool kTlas = true, int kDepth = bvh8::kStack>
 __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const rq_ray* __restrict__ rays,
@@ -311,6 +316,8 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
         // lanes (or whenever no lane is walking), instead of for one or two lanes in every
         // iteration.  Rays and results are the same; only when they are stored changes.
         bool pending = false, pending_occ = false;
+        const unsigned long long tail_rays = static_cast<unsigned long long>(kTailPools) * kPoolRays *
+                                             (static_cast<unsigned long long>(gridDim.x) * blockDim.x / 32u);
         while (true) {
             const unsigned idle = __ballot_sync(kFull, !live && !exhausted);
             const unsigned walking = __ballot_sync(kFull, live);
@@ -333,12 +340,16 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
                     if (avail >= cnt) {
                         pool_next += cnt;
                     } else {
+                        // near the end of the queue a warp takes only the rays its idle lanes need
+                        const unsigned long long need = cnt - avail;
+                        const unsigned long long grab =
+                            pool_end + tail_rays >= static_cast<unsigned long long>(n) ? need : kPoolRays;
                         unsigned long long base = 0;
-                        if (lane == 0) base = atomicAdd(queue, static_cast<unsigned long long>(kPoolRays));
+                        if (lane == 0) base = atomicAdd(queue, grab);
                         base = __shfl_sync(kFull, base, 0);
                         if (rank >= avail) mine = base + (rank - avail);
-                        pool_next = base + (cnt - avail);
-                        pool_end = base + kPoolRays;
+                        pool_next = base + need;
+                        pool_end = base + grab;
                     }
                     if (!live && !exhausted) {
                         if (static_cast<int64_t>(mine) >= n) {

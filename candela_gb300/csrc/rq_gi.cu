@@ -1,5 +1,6 @@
 // Diffuse-GI / RTAO pass: secondary ray generation, shading and per-pixel accumulation, plus the
 // C ABI entry points that drive the whole pass (rq_gi_frame).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,25 @@ struct GiArgs {
     float shadow_offset;
     f3 sun_dir, sun_color, sky;
     int32_t bounces;
+};
+
+// Output pixels of a GI pass: 4 floats, or 4 binary16 values (rq_gi_params.pixel_format, the
+// reference's rgba16f output image) each rounded to nearest, ties to even.
+struct PixelOut {
+    void* base;
+    bool half;
+    __device__ __forceinline__ void put(int64_t i, float4 v) const {
+        if (half) {
+            const __half2 lo = __halves2half2(__float2half_rn(v.x), __float2half_rn(v.y));
+            const __half2 hi = __halves2half2(__float2half_rn(v.z), __float2half_rn(v.w));
+            uint2 w;
+            w.x = *reinterpret_cast<const uint32_t*>(&lo);
+            w.y = *reinterpret_cast<const uint32_t*>(&hi);
+            static_cast<uint2*>(base)[i] = w;
+        } else {
+            static_cast<float4*>(base)[i] = v;
+        }
+    }
 };
 
 // Origin offset of the bounce rays (HitPosition + iNormal * 0.02, DiffuseTrace.glsl:518).
@@ -448,7 +468,7 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
                                    const rq_hit* __restrict__ hits, const int32_t* __restrict__ comp_of,
                                    int64_t n, const uint8_t* __restrict__ occl, int query,
                                    const Materials mat, GiArgs a,
-                                   float4* __restrict__ pixels) {
+                                   const PixelOut pixels) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -474,8 +494,8 @@ __global__ void k_shade_accumulate(SceneView s, const rq_ray* __restrict__ rays,
         acc.w = __fadd_rn(acc.w, v.w);
     }
     const float inv = __fdiv_rn(1.0f, static_cast<float>(a.spp));
-    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
-                            __fmul_rn(acc.w, inv));
+    pixels.put(i, make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                              __fmul_rn(acc.w, inv)));
 }
 
 // ---- RT second-bounce loop (DiffuseTrace.glsl:502-536), per compact GI slot c ----------------
@@ -598,7 +618,7 @@ __global__ void k_bounce_shade(SceneView s, const rq_ray* __restrict__ rays, con
 // slot's radiance being its first hit's plus the bounces' (FinalRadiance += Bounced).
 __global__ void k_gather_accumulate(const float4* __restrict__ rad, const float4* __restrict__ bnc,
                                     const int32_t* __restrict__ comp_of, int64_t n, int32_t spp,
-                                    float4* __restrict__ pixels) {
+                                    const PixelOut pixels) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -618,8 +638,8 @@ __global__ void k_gather_accumulate(const float4* __restrict__ rad, const float4
         acc.w = __fadd_rn(acc.w, v.w);
     }
     const float inv = __fdiv_rn(1.0f, static_cast<float>(spp));
-    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
-                            __fmul_rn(acc.w, inv));
+    pixels.put(i, make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                              __fmul_rn(acc.w, inv)));
 }
 
 __global__ void k_count_hits_c(const rq_hit* __restrict__ hits, int64_t n_max,
@@ -663,7 +683,7 @@ __global__ void k_shade(SceneView s, const rq_ray* __restrict__ rays, const rq_h
 
 // Per-pixel mean over the spp secondary samples (summed in sample order).
 __global__ void k_accumulate(const float4* __restrict__ shaded, int64_t n, int32_t spp,
-                             float4* __restrict__ pixels) {
+                             const PixelOut pixels) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -675,8 +695,8 @@ __global__ void k_accumulate(const float4* __restrict__ shaded, int64_t n, int32
         acc.w = __fadd_rn(acc.w, v.w);
     }
     const float inv = __fdiv_rn(1.0f, static_cast<float>(spp));
-    pixels[i] = make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
-                            __fmul_rn(acc.w, inv));
+    pixels.put(i, make_float4(__fmul_rn(acc.x, inv), __fmul_rn(acc.y, inv), __fmul_rn(acc.z, inv),
+                              __fmul_rn(acc.w, inv)));
 }
 
 __global__ void k_count_hits(const rq_hit* __restrict__ hits, int64_t n, unsigned long long* cnt) {
@@ -695,6 +715,8 @@ rq_status check_params(rq_ctx* ctx, const rq_gi_params* p) {
     if (p->normal_mode != 0 && p->normal_mode != 1) return fail(ctx, RQ_EINVAL, "bad normal_mode");
     if (p->query != 0 && p->query != 1) return fail(ctx, RQ_EINVAL, "bad query kind");
     if (p->bounces < 0 || p->bounces > 8) return fail(ctx, RQ_EINVAL, "bounces must be 0..8");
+    if (p->pixel_format != RQ_PIXELS_RGBA32F && p->pixel_format != RQ_PIXELS_RGBA16F)
+        return fail(ctx, RQ_EINVAL, "bad pixel_format");
     return RQ_OK;
 }
 
@@ -717,8 +739,8 @@ __global__ void k_add_count(unsigned long long* dst, const unsigned long long* s
 // copies ran.)  With `stats`, the ray counts are added to the context's frame counters (cleared by
 // the caller).
 rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const rq_gi_params& p,
-                  const rq_ray* prim, int64_t n, float4* pixels4, cudaStream_t st, bool stats,
-                  const rq_ray* h_prim, float* h_pix, GiArena& arena) {
+                  const rq_ray* prim, int64_t n, void* pixels4, cudaStream_t st, bool stats,
+                  const rq_ray* h_prim, void* h_pix, GiArena& arena) {
     rq_status s;
     const int64_t m = n * p.spp;
     void *d_phit = nullptr, *d_sec = nullptr, *d_shit = nullptr, *d_occ = nullptr, *d_shade = nullptr,
@@ -739,6 +761,10 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     uint8_t* occ = static_cast<uint8_t*>(d_occ);
     int32_t* comp_of = static_cast<int32_t*>(d_comp);
     const int64_t chunk = h_pix ? kGiHostChunk : n;
+    const int64_t pix_bytes = p.pixel_format == RQ_PIXELS_RGBA16F ? 8 : 16;
+    auto px = [&](int64_t off) {
+        return PixelOut{static_cast<char*>(pixels4) + off * pix_bytes, pix_bytes == 8};
+    };
     // Camera rays are coherent and short (a few node visits): the one-thread-per-ray form of the
     // tuned launch shape beats the persistent ray queue there, which pays per-ray hand-over costs.
     QueryConfig qp = q;
@@ -886,19 +912,18 @@ rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const r
     for (int64_t off = 0; off < n; off += chunk) {
         const int64_t c = std::min(chunk, n - off);
         if (bounce)
-            k_gather_accumulate<<<grid(c, 256), 256, 0, st>>>(rad, bnc, comp_of + off * p.spp, c, p.spp,
-                                                              pixels4 + off);
+            k_gather_accumulate<<<grid(c, 256), 256, 0, st>>>(rad, bnc, comp_of + off * p.spp, c, p.spp, px(off));
         else if (p.unfused)
-            k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, pixels4 + off);
+            k_accumulate<<<grid(c, 256), 256, 0, st>>>(shade + off * p.spp, c, p.spp, px(off));
         else
             k_shade_accumulate<<<grid(c, 256), 256, 0, st>>>(sc->view, sec, shit, comp_of + off * p.spp, c, vis,
-                                                             p.query, materials_of(sc), a, pixels4 + off);
+                                                             p.query, materials_of(sc), a, px(off));
         RQ_CUDA(ctx, cudaGetLastError());
         if (h_pix) {
             RQ_CUDA(ctx, cudaEventRecord(ctx->ev, st));
             RQ_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[1], ctx->ev, 0));
-            RQ_CUDA(ctx, cudaMemcpyAsync(h_pix + 4 * off, pixels4 + off, 16 * c, cudaMemcpyDeviceToHost,
-                                         ctx->pipe[1]));
+            RQ_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(h_pix) + off * pix_bytes, px(off).base, pix_bytes * c,
+                                         cudaMemcpyDeviceToHost, ctx->pipe[1]));
         }
     }
     if (h_pix) {
@@ -1058,8 +1083,7 @@ rq_status rq_gi_autotune(rq_ctx* ctx, rq_scene* sc, const rq_ray* primary, int64
         pp.compact_below = form == 0 ? 2.0f : 1e-30f;
         for (int rep = 0; rep < 4; ++rep) {
             RQ_CUDA(ctx, cudaEventRecord(a, st));
-            if ((s = rq::gi_pass(ctx, sc, q, pp, primary, n, reinterpret_cast<float4*>(pixels4), st, false, nullptr,
-                                 nullptr, arena)) != RQ_OK)
+            if ((s = rq::gi_pass(ctx, sc, q, pp, primary, n, pixels4, st, false, nullptr, nullptr, arena)) != RQ_OK)
                 return s;
             RQ_CUDA(ctx, cudaEventRecord(b, st));
             RQ_CUDA(ctx, cudaEventSynchronize(b));
@@ -1098,16 +1122,16 @@ rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* sc, const rq_ray* primary, in
     if (stats) RQ_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned long long), st));
     rq::CtxGiArena arena(ctx);
     if (!host) {
-        if ((s = rq::gi_pass(ctx, sc, q, *p, primary, n, reinterpret_cast<float4*>(pixels4), st,
-                             stats != nullptr, nullptr, nullptr, arena)) != RQ_OK)
+        if ((s = rq::gi_pass(ctx, sc, q, *p, primary, n, pixels4, st, stats != nullptr, nullptr, nullptr, arena)) !=
+            RQ_OK)
             return s;
     } else {
         void *d_prim = nullptr, *d_pix = nullptr;
         if ((s = rq::scratch(ctx, rq::kSlotStageRays, sizeof(rq_ray) * n, &d_prim)) != RQ_OK ||
             (s = rq::scratch(ctx, rq::kSlotStageOut, 16 * n, &d_pix)) != RQ_OK)
             return s;
-        if ((s = rq::gi_pass(ctx, sc, q, *p, static_cast<const rq_ray*>(d_prim), n,
-                             static_cast<float4*>(d_pix), st, stats != nullptr, primary, pixels4, arena)) != RQ_OK)
+        if ((s = rq::gi_pass(ctx, sc, q, *p, static_cast<const rq_ray*>(d_prim), n, d_pix, st, stats != nullptr,
+                             primary, pixels4, arena)) != RQ_OK)
             return s;
         RQ_CUDA(ctx, cudaStreamSynchronize(st));
     }

@@ -137,7 +137,7 @@ rq_status rq_gi_frame_noalloc(rq_ctx* ctx, const rq_scene* sc, const rq_ray* pri
     pp.sort_rays = 0;
     pp.unfused = 0;
     FixedArena arena(ctx, static_cast<unsigned char*>(ctx->noalloc_base));
-    return rq::gi_pass(ctx, sc, q, pp, primary, n, reinterpret_cast<float4*>(pixels4),
+    return rq::gi_pass(ctx, sc, q, pp, primary, n, pixels4,
                        static_cast<cudaStream_t>(stream), false, nullptr, nullptr, arena);
 }
 

@@ -231,8 +231,8 @@ void noalloc_resolve(rq_ctx* ctx);
 // every intermediate buffer taken from `arena`.  h_prim / h_pix: host buffers (prim / pixels4 are
 // then device staging buffers).  stats: add the ray counts to the context's frame counters.
 rq_status gi_pass(rq_ctx* ctx, const rq_scene* sc, const QueryConfig& q, const rq_gi_params& p,
-                  const rq_ray* prim, int64_t n, float4* pixels4, cudaStream_t st, bool stats,
-                  const rq_ray* h_prim, float* h_pix, GiArena& arena);
+                  const rq_ray* prim, int64_t n, void* pixels4, cudaStream_t st, bool stats,
+                  const rq_ray* h_prim, void* h_pix, GiArena& arena);
 
 }  // namespace rq
 

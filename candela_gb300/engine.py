@@ -344,16 +344,17 @@ class Scene:
 def gi_params(spp=4, seed=0, origin_offset=0.05, ray_tmax=1000000.0, normal_mode=0, query=0,
               shadow_rays=False, shadow_offset=1e-3, sun_dir=(0.3, 0.4, -0.866),
               sun_color=(4.0, 3.8, 3.5), sky_color=(0.5, 0.7, 1.0), sort_rays=False,
-              unfused=False, bounces=0, compact_below=0.0) -> L.RqGiParams:
+              unfused=False, bounces=0, compact_below=0.0, pixel_format=0) -> L.RqGiParams:
     """rq_gi_params for the diffuse-GI (query=0) or RTAO (query=1) pass; `bounces` further
     bounces per GI hit (the RT second-bounce loop); `compact_below` the compaction threshold (0 =
-    the scene's tuned value)."""
+    the scene's tuned value); `pixel_format` L.PIXELS_RGBA32F or L.PIXELS_RGBA16F (the output
+    pixels as float16, the reference's rgba16f output image)."""
     sd = np.asarray(sun_dir, dtype=np.float64)
     sd = (sd / np.sqrt(sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2])).astype(np.float32)
     f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
     return L.RqGiParams(spp, seed & 0xFFFFFFFF, origin_offset, ray_tmax, normal_mode, query,
                         int(shadow_rays), shadow_offset, f3(sd), f3(sun_color), f3(sky_color),
-                        int(sort_rays), int(unfused), int(bounces), float(compact_below))
+                        int(sort_rays), int(unfused), int(bounces), float(compact_below), int(pixel_format))
 
 
 def specular_params(seed=0, roughness=0.3, ray_tmax=1000000.0, normal_mode=0, shadow_rays=False,
@@ -492,10 +493,12 @@ class _GiMixin:
         host = isinstance(primary, np.ndarray)
         n = primary.shape[0] if host else primary.numel() * primary.element_size() // 32
         if out is None:
+            half = params.pixel_format == L.PIXELS_RGBA16F
             if host:
-                out = np.empty((n, 4), dtype=np.float32)
+                out = np.empty((n, 4), dtype=np.float16 if half else np.float32)
             else:
-                out = _empty_like_dev(primary, (n, 4), __import__("torch").float32)
+                torch = __import__("torch")
+                out = _empty_like_dev(primary, (n, 4), torch.float16 if half else torch.float32)
         st = L.RqFrameStats() if stats else None
         o = _opts(layout, mode, tie, flags | (L.FLAG_HOST_BUFFERS if host else 0), block_size,
                   min_blocks, persistent, stack_depth)

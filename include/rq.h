@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define RQ_ABI_VERSION 2
+#define RQ_ABI_VERSION 3
 
 typedef enum rq_status {
     RQ_OK = 0,
@@ -485,7 +485,15 @@ typedef struct rq_gi_params {
                               scene's value from rq_gi_autotune (always compact until tuned).  The
                               pixels are the same either way; the bounce loop, sort_rays and
                               unfused always compact */
+    int32_t pixel_format;  /* rq_gi_frame / rq_gi_frame_noalloc / rq_gi_autotune output pixels:
+                              RQ_PIXELS_RGBA32F (0): 4 floats per pixel; RQ_PIXELS_RGBA16F (1): 4
+                              IEEE binary16 values per pixel (8 bytes), the format of the
+                              reference's output image (layout(rgba16f) o_OutputData,
+                              DiffuseTrace.glsl:17), each the float pixel rounded to nearest, ties
+                              to even */
 } rq_gi_params;
+
+enum { RQ_PIXELS_RGBA32F = 0, RQ_PIXELS_RGBA16F = 1 };
 
 typedef struct rq_frame_stats {
     int64_t primary_rays, primary_hits;
@@ -536,7 +544,8 @@ rq_status rq_shade(rq_ctx* ctx, const rq_scene* scene, const rq_ray* rays, const
                    void* stream);
 /* Whole GI / RTAO pass for n primary rays (pixels): primary closest hit, secondary ray
  * generation, secondary queries (closest + optional shadow any-hit, or AO any-hit), shading, and
- * the per-pixel mean over spp written to pixels4 (rgb radiance, AO or visibility).  With
+ * the per-pixel mean over spp written to pixels4 (rgb radiance, AO or visibility): n x 4 floats,
+ * or n x 4 binary16 values with params->pixel_format = RQ_PIXELS_RGBA16F.  With
  * RQ_FLAG_HOST_BUFFERS in opts, `primary` and `pixels4` are host memory.  `stats` (nullable)
  * synchronises the stream to read the ray counts. */
 rq_status rq_gi_frame(rq_ctx* ctx, const rq_scene* scene, const rq_ray* primary, int64_t n,

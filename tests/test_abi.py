@@ -35,7 +35,7 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 
 def test_abi_version_and_status_strings():
-    assert L.lib().rq_abi_version() == 2
+    assert L.lib().rq_abi_version() == L.ABI_VERSION == 3
     assert L.lib().rq_status_string(L.RQ_EINVAL) == b"invalid argument"
 
 
@@ -46,7 +46,7 @@ def test_struct_sizes_match_reference_layouts():
     assert L.STACKLESS_NODE_DTYPE.itemsize == 32  # FlattenedNode
     assert L.ENTITY_DTYPE.itemsize == 192        # BVHEntity
     assert C.sizeof(L.RqOpts) == 32
-    assert C.sizeof(L.RqGiParams) == 84
+    assert C.sizeof(L.RqGiParams) == 88
     assert C.sizeof(L.RqProbeParams) == 108     # rq_probe_params, the oracle's orc_probe_params
     from oracle import oracle as O
     assert C.sizeof(O.OrcProbeParams) == C.sizeof(L.RqProbeParams)

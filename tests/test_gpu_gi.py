@@ -342,3 +342,56 @@ def test_gi_frame_pinned_large_equals_device_pass(ctx):
     np.testing.assert_array_equal(sc.gi_frame(pinned, pb, layout=L.LAYOUT_BVH8Q).view(np.uint32),
                                   want_b.cpu().numpy().view(np.uint32))
     assert sc.ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("query", [0, 1])
+def test_gi_frame_rgba16f_pixels(ctx, query):
+    """pixel_format = RGBA16F (the reference's rgba16f output image, DiffuseTrace.glsl:17): every
+    pixel is the float pixel rounded to binary16, nearest with ties to even (numpy's conversion),
+    bit for bit, on device buffers, pinned and pageable host buffers (several host chunks), the
+    BVH8 layout, the bounce loop and the no-alloc entry point; a bad format is rejected."""
+    import torch
+    from candela_gb300 import _lib as L
+    bufs = single_object("ico2", R.STACK)
+    sc = ctx.scene(R.STACK, *bufs)
+    sc.set_materials(np.random.default_rng(4).uniform(0.2, 0.9, (7, 3)).astype(np.float32))
+    sc.build_bvh8()
+    rays = S.camera_rays(768, 480, eye=(0.0, -4.0, 2.0), target=(0.0, 0.0, 0.3))  # 368,640 pixels
+    kw = dict(spp=2, seed=21, origin_offset=0.05, query=query)
+    if query == 1:
+        kw["ray_tmax"] = 0.5
+    else:
+        kw["shadow_rays"] = True
+    d = rays_to_device(rays)
+    pinned = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory().numpy().view(R.RAY_DTYPE)
+    for layout in (0, L.LAYOUT_BVH8Q):
+        want = sc.gi_frame(d, gi_params(**kw), layout=layout).cpu().numpy().astype(np.float16)
+        p16 = gi_params(**kw, pixel_format=L.PIXELS_RGBA16F)
+        got = sc.gi_frame(d, p16, layout=layout)
+        assert got.dtype == torch.float16
+        np.testing.assert_array_equal(got.cpu().numpy().view(np.uint16), want.view(np.uint16))
+        np.testing.assert_array_equal(sc.gi_frame(rays, p16, layout=layout).view(np.uint16), want.view(np.uint16))
+        out = torch.empty((len(rays), 4), dtype=torch.float16).pin_memory().numpy()
+        sc.gi_frame(pinned, p16, out=out, layout=layout)
+        np.testing.assert_array_equal(out.view(np.uint16), want.view(np.uint16))
+    assert np.abs(want.astype(np.float32)).sum() > 0
+    if query == 0:
+        pb = gi_params(spp=1, seed=3, origin_offset=0.05, bounces=2)
+        wb = sc.gi_frame(d, pb).cpu().numpy().astype(np.float16)
+        gb = sc.gi_frame(d, gi_params(spp=1, seed=3, origin_offset=0.05, bounces=2, pixel_format=L.PIXELS_RGBA16F))
+        np.testing.assert_array_equal(gb.cpu().numpy().view(np.uint16), wb.view(np.uint16))
+    # the no-alloc entry point (at most NOALLOC_MAX_RAYS secondary rays)
+    small = rays_to_device(S.camera_rays(128, 96, eye=(0.0, -4.0, 2.0), target=(0.0, 0.0, 0.3)))
+    want_s = sc.gi_frame(small, gi_params(**kw)).cpu().numpy().astype(np.float16)
+    out_s = torch.empty((128 * 96, 4), dtype=torch.float16, device="cuda")
+    import ctypes as C
+    from candela_gb300.engine import _opts
+    st = L.lib().rq_gi_frame_noalloc(ctx.handle, sc.handle, L.ptr(small), 128 * 96,
+                                     C.byref(gi_params(**kw, pixel_format=L.PIXELS_RGBA16F)), C.byref(_opts()),
+                                     L.ptr(out_s), torch.cuda.current_stream().cuda_stream)
+    L.check(st, ctx.handle)
+    np.testing.assert_array_equal(out_s.cpu().numpy().view(np.uint16), want_s.view(np.uint16))
+    with pytest.raises(R.RqError) as e:
+        sc.gi_frame(d, gi_params(**kw, pixel_format=2))
+    assert e.value.status == L.RQ_EINVAL
+    assert sc.ctx.device_status() == 0
