@@ -3,18 +3,22 @@
 
 Workload (default): 64 displaced subdivision-5 icospheres + ground plane, 1,310,722 triangles,
 SAH BVH (leaf 2, stack layout); 1920x1080 pinhole primary closest-hit rays plus 4 cosine-weighted
-diffuse-GI closest-hit rays per primary hit, Lambert shading and per-pixel accumulation.  One
-"step" is that whole pass (rq_gi_frame).  Metric: Mrays/s = (primary + active secondary rays) per
-second.  Synthetic seeded scene and rays (no dataset).
+diffuse-GI closest-hit rays per primary hit, Lambert shading and per-pixel accumulation into
+rgba16f pixels (the format of the reference's output image).  One "step" is that whole pass
+(rq_gi_frame).  Metric: Mrays/s = (primary + active secondary rays) per second.  Synthetic seeded
+scene and rays (no dataset).
 
   value      device-resident inputs, CUDA-event time per step, L2 flushed between steps
   e2e        same pass through the C ABI with host buffers: pinned primary rays copied in and the
-             pixel buffer copied out inside the timed region
+             pixel buffer copied out inside the timed region (also with float32 pixels)
   roofline   the dominant kernel (secondary closest-hit traversal): algorithmic bytes per launch
              (64 B per node visit + 64 B per triangle test, counted on the device) / its
-             CUDA-event launch time, against the measured HBM copy bandwidth
+             CUDA-event launch time, against the L2 read bandwidth measured in the run (HBM beside)
   cpu_baseline  the CPU restatement of the reference traversal (the reference has no CPU
-             intersector) on the host cores, on a bounded sample of the same workload
+             intersector) on the host cores, on a bounded sample of the same workload, and on one
+             thread on a smaller sample
+  bvh8q_vs_strict  hit agreement of the BVH8q and strict BVH2 walks on the GI rays, and how many
+             records the reference's first-found tie rule changes against the lower-index rule
 
 --impl reference times that CPU path alone (the reference's ray-query path restated on the host
 cores) on the same workload and prints its own line.
@@ -271,15 +275,16 @@ def cpu_probe(wl, albedo):
             "kind": "port"}
 
 
-def cpu_baseline(wl, seconds: float):
-    """The CPU restatement of the reference path on all host cores, on a bounded sample:
-    repeated whole-pass runs over a prefix of the primary rays until `seconds` elapse."""
+def cpu_baseline(wl, seconds: float, nthreads: int = 0, max_rays: int = 1 << 18):
+    """The CPU restatement of the reference path on all host cores (or `nthreads`), on a bounded
+    sample: repeated whole-pass runs over every k-th primary ray (at most `max_rays`) until
+    `seconds` elapse."""
     from oracle import oracle as O
-    nthreads = os.cpu_count() or 1
+    nthreads = nthreads or os.cpu_count() or 1
     osc = O.OracleScene(O.ORC_STACK, wl["mesh"].vertices, wl["bvh"].tris, wl["bvh"].nodes,
                         wl["ent"])
     p = wl["params"]
-    n = min(len(wl["rays"]), 1 << 18)
+    n = min(len(wl["rays"]), max_rays)
     prim = wl["rays"][:: max(1, len(wl["rays"]) // n)][:n]
     rays_done = 0
     t0 = time.perf_counter()
@@ -1171,6 +1176,11 @@ def main():
     agreement = {"closest_hits_identical": float((h_strict == h_b8).all(1).mean()),
                  "anyhit_identical": float((o_strict == o_b8).mean()),
                  "rays": n_sec_slots, "device_status": ctx.device_status()}
+    # the reference's tie rule (the first hit found in traversal order keeps a tie in t) against
+    # the lower-triangle-index rule, strict BVH2 on the same GI rays
+    h_ff = sc.closest(d_sec, tie=L.TIE_FIRST_FOUND, stream=sptr).cpu().numpy().view(np.uint32)[:, :7]
+    agreement["tie_rules"] = {"rays": n_sec_slots, "records_differ": int((h_ff != h_strict).any(1).sum()),
+                              "triangles_differ": int((h_ff[:, 4] != h_strict[:, 4]).sum())}
 
     # ---- specular reflection pass (rq_specular_frame) over the same camera: primary + one GGX
     # reflection ray per pixel (roughness 0.3) + a shadow ray per reflection hit
@@ -1307,6 +1317,8 @@ def main():
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+        one = cpu_baseline(wl, max(1.0, args.cpu_seconds / 4), nthreads=1, max_rays=1 << 14)
+        line["cpu_baseline"]["single_thread"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
         if not args.no_legs and args.config == "c2":
             # the metric's batched leg and the precision / differentiation workloads, each timed with
             # CUDA events inside its own clock-sampled window
