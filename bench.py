@@ -670,7 +670,7 @@ def instancing_record(args, ctx=None, flush=None):
         # two BVH8q GI passes with the top level and the launch variant the autotuner picks here on
         # GB300 (persistent ray queue, 128 threads, 8 blocks per SM): the ncu captures of the
         # instancing row; the second k_bvh8_persistent launch is the second pass's GI rays
-        launch = dict(block_size=128, min_blocks=8, persistent=1)
+        launch = dict(block_size=128, min_blocks=7, persistent=1)
         st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr, **launch)[1]
         rays_per_step = int(st["primary_rays"]) + int(st["secondary_rays"])
         sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stream=sptr, **launch)
@@ -711,7 +711,7 @@ def instancing_record(args, ctx=None, flush=None):
     h_p = torch.empty((n, 8), dtype=torch.float32, device="cuda")
     primary = {}
     for name, kw in (("one_thread_per_ray_ms", dict(block_size=128, min_blocks=8, persistent=0)),
-                     ("persistent_ms", dict(block_size=128, min_blocks=8, persistent=1))):
+                     ("persistent_ms", dict(block_size=128, min_blocks=7, persistent=1))):
         primary[name] = round(timed(lambda: sc.closest(d, h_p, layout=L.LAYOUT_BVH8Q, stream=sptr, **kw),
                                     args.steps, args.warmup), 4)
     del h_p
@@ -995,7 +995,7 @@ def main():
         sc.build_bvh8()
         pp = probe_params(grid=(128, 128, 64), origin=PROBE_ORIGIN, size=PROBE_SIZE, seed=2)
         vols = [probe_volumes(pp, device=dev) for _ in range(2)]
-        launch = dict(layout=B8, block_size=128, min_blocks=8, persistent=1)
+        launch = dict(layout=B8, block_size=128, min_blocks=7, persistent=1)
         sc.probe_update(pp, vols[0][0], vols[0][1], vols[0][2], out_sh=vols[1][0], out_raw=vols[1][1],
                         stream=sptr, **launch)
         sc.probe_update(pp, vols[1][0], vols[1][1], vols[1][2], out_sh=vols[0][0], out_raw=vols[0][1],
@@ -1014,7 +1014,7 @@ def main():
         h = sc.closest(d_rays, stream=sptr)
         sec = sc.gi_raygen(d_rays, h, p, stream=sptr)
         fn = sc.anyhit if q_any else sc.closest
-        fn(sec, layout=B8, block_size=128, min_blocks=8, persistent=1, stream=sptr)
+        fn(sec, layout=B8, block_size=128, min_blocks=7, persistent=1, stream=sptr)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": wl["name"], "pixels": n, "bvh8_nodes": b8["nodes"]}))
         return
@@ -1135,18 +1135,18 @@ def main():
         ("primary_closest_bvh8q_128x8",
          lambda: sc.closest(d_rays, layout=B8, stream=sptr, block_size=128, min_blocks=8), n, None),
         ("primary_closest_bvh8q_persistent",
-         lambda: sc.closest(d_rays, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         lambda: sc.closest(d_rays, layout=B8, stream=sptr, block_size=128, min_blocks=7, persistent=1),
          n, None),
         ("secondary_closest_bvh8q_128x8",
          lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8), n_sec, None),
         ("secondary_closest_bvh8q_persistent",
-         lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=7, persistent=1),
          n_sec, None),
         ("secondary_closest_bvh8q_persistent_m1",
          lambda: sc.closest(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=1, persistent=1),
          n_sec, None),
         ("secondary_anyhit_bvh8q_persistent",
-         lambda: sc.anyhit(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=8, persistent=1),
+         lambda: sc.anyhit(d_sec, layout=B8, stream=sptr, block_size=128, min_blocks=7, persistent=1),
          n_sec, None),
     ]
     sc_sl = ctx.scene(R.STACKLESS, wl["mesh"].vertices, wl["bvh_sl"].tris, wl["bvh_sl"].nodes,

@@ -1,6 +1,8 @@
 // Ray-query launchers (the plain-loop kernel form), the batched-query kernel and the fast-mode
 // triangle records.  The per-variant kernels and launchers are in rq_kernels.cuh; the top-level
 // form is instantiated in rq_kernels_tlas.cu.
+#include <cstdlib>
+
 #include "rq_kernels.cuh"
 #include "rq_objects.h"
 
@@ -112,15 +114,21 @@ static_assert(bvh8::kStatusStackOverflow == kStatusOverflowBit, "status bit of a
 
 const LaunchVariant kLaunchVariants[kNumLaunchVariants] = {
     {128, 1, 0, 0}, {128, 4, 0, 0}, {128, 6, 0, 0}, {128, 8, 0, 0}, {256, 3, 0, 0}, {64, 12, 0, 0},
-    {128, 1, 1, 0}, {128, 8, 1, 0}, {128, 8, 1, bvh8::kStackDepths[1]}, {128, 8, 1, bvh8::kStackDepths[2]}};
+    {128, 1, 1, 0}, {128, 7, 1, 0}, {128, 7, 1, bvh8::kStackDepths[1]}, {128, 7, 1, bvh8::kStackDepths[2]}};
 
 int non_persistent_variant(int v) {
     if (v < 0 || v >= kNumLaunchVariants || !kLaunchVariants[v].persistent) return v;
-    for (int k = 0; k < kNumLaunchVariants; ++k)
-        if (!kLaunchVariants[k].persistent && kLaunchVariants[k].block == kLaunchVariants[v].block &&
-            kLaunchVariants[k].min_blocks == kLaunchVariants[v].min_blocks)
-            return k;
-    return 0;
+    // same block size, the nearest occupancy target (the higher one on a tie)
+    int best = 0, best_d = 1 << 30;
+    for (int k = 0; k < kNumLaunchVariants; ++k) {
+        if (kLaunchVariants[k].persistent || kLaunchVariants[k].block != kLaunchVariants[v].block) continue;
+        const int d = std::abs(kLaunchVariants[k].min_blocks - kLaunchVariants[v].min_blocks);
+        if (d < best_d || (d == best_d && kLaunchVariants[k].min_blocks > kLaunchVariants[best].min_blocks)) {
+            best = k;
+            best_d = d;
+        }
+    }
+    return best;
 }
 
 const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1, 0}, {128, 8, 1, 0}, {64, 12, 1, 0},

@@ -342,9 +342,9 @@ cudaError_t launch_closest_t(const SceneView& s, const QueryConfig& q, const rq_
         case 4: return closest_variant<256, 3, kTlas>(s, q, rays, n, hits, st);
         case 5: return closest_variant<64, 12, kTlas>(s, q, rays, n, hits, st);
         case 6: return persistent_variant<false, 1, kTlas>(s, q, rays, n, hits, nullptr, queue, st);
-        case 7: return persistent_variant<false, 8, kTlas>(s, q, rays, n, hits, nullptr, queue, st);
-        case 8: return persistent_variant<false, 8, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, hits, nullptr, queue, st);
-        case 9: return persistent_variant<false, 8, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, hits, nullptr, queue, st);
+        case 7: return persistent_variant<false, 7, kTlas>(s, q, rays, n, hits, nullptr, queue, st);
+        case 8: return persistent_variant<false, 7, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, hits, nullptr, queue, st);
+        case 9: return persistent_variant<false, 7, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, hits, nullptr, queue, st);
         default: return closest_variant<128, 1, kTlas>(s, q, rays, n, hits, st);
     }
 }
@@ -362,9 +362,9 @@ cudaError_t launch_anyhit_t(const SceneView& s, const QueryConfig& q, const rq_r
         case 4: return anyhit_variant<256, 3, kTlas>(s, q, rays, n, occluded, st);
         case 5: return anyhit_variant<64, 12, kTlas>(s, q, rays, n, occluded, st);
         case 6: return persistent_variant<true, 1, kTlas>(s, q, rays, n, nullptr, occluded, queue, st);
-        case 7: return persistent_variant<true, 8, kTlas>(s, q, rays, n, nullptr, occluded, queue, st);
-        case 8: return persistent_variant<true, 8, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, nullptr, occluded, queue, st);
-        case 9: return persistent_variant<true, 8, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 7: return persistent_variant<true, 7, kTlas>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 8: return persistent_variant<true, 7, kTlas, bvh8::kStackDepths[1]>(s, q, rays, n, nullptr, occluded, queue, st);
+        case 9: return persistent_variant<true, 7, kTlas, bvh8::kStackDepths[2]>(s, q, rays, n, nullptr, occluded, queue, st);
         default: return anyhit_variant<128, 1, kTlas>(s, q, rays, n, occluded, st);
     }
 }

@@ -243,8 +243,8 @@ def test_bvh8_refit_follows_vertex_moves(ctx):
         want = osc.closest(rays)
         want_occ = osc.anyhit(rays)
         assert_hits_identical(hits_from_device(sc.closest(d_rays)), want, f"strict after move {step}")
-        for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1),
-                   dict(block_size=128, min_blocks=8, persistent=1, stack_depth=24)):
+        for kw in (dict(), dict(block_size=128, min_blocks=7, persistent=1),
+                   dict(block_size=128, min_blocks=7, persistent=1, stack_depth=24)):
             got = hits_from_device(sc.closest(d_rays, layout=L.LAYOUT_BVH8Q, **kw))
             assert_equal_or_proven(got, want, osc, rays, what=f"bvh8 refit move {step} {kw}")
             occ = sc.anyhit(d_rays, layout=L.LAYOUT_BVH8Q, **kw).cpu().numpy()

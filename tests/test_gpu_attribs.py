@@ -79,7 +79,7 @@ def test_hit_attribs_over_given_hits_and_bvh8(scene):
     np.testing.assert_array_equal(sc.hit_attribs(want_h).view(np.uint32), want_a.view(np.uint32))
     if layout == R.STACK:
         sc.build_bvh8()
-        h8, a8 = sc.closest_attribs(rays_to_device(rays), layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=8,
+        h8, a8 = sc.closest_attribs(rays_to_device(rays), layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=7,
                                     persistent=1)
         h8 = hits_from_device(h8)
         same = np.ones(len(rays), bool)

@@ -38,7 +38,7 @@ def test_bvh8_equals_strict(ctx, name, layout, leaf):
     want = osc.closest(rays)
     strict = hits_from_device(sc.closest(d))
     assert _same(strict, want).all()
-    for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1)):
+    for kw in (dict(), dict(block_size=128, min_blocks=7, persistent=1)):
         b8 = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, **kw))
         assert_equal_or_proven(b8, want, osc, rays, what=f"{name} layout {layout} {kw}")
         occ_8 = sc.anyhit(d, layout=L.LAYOUT_BVH8Q, **kw).cpu().numpy()

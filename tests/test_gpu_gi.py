@@ -119,7 +119,7 @@ def test_gi_frame_forms_identical(ctx, query):
     for sort in (False, True):
         for unfused in (False, True):
             p = gi_params(sort_rays=sort, unfused=unfused, **kw)
-            for launch in (dict(block_size=128, min_blocks=8), dict(block_size=128, min_blocks=8, persistent=1),
+            for launch in (dict(block_size=128, min_blocks=8), dict(block_size=128, min_blocks=7, persistent=1),
                            dict(block_size=128, min_blocks=1, persistent=1)):
                 got, st2 = sc.gi_frame(rays, p, layout=L.LAYOUT_BVH8Q, stats=True, **launch)
                 got = got.cpu().numpy()

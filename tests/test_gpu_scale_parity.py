@@ -25,7 +25,7 @@ from .helpers import (assert_equal_or_proven, assert_hits_identical, assert_occl
 pytestmark = pytest.mark.gpu
 
 SHADE_RTOL = 2e-6  # the GI tests' shading tolerance (the AO pow is the only non-exact operation)
-TUNED = dict(block_size=128, min_blocks=8, persistent=1)  # the launch the autotuner picks for BVH8q
+TUNED = dict(block_size=128, min_blocks=7, persistent=1)  # the launch the autotuner picks for BVH8q
 
 
 def _c2_rays():

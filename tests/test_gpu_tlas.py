@@ -115,7 +115,7 @@ def test_tlas_closest_equals_entity_loop(scenes, layout, flags):
     hit = want["t"] > 0
     assert hit.mean() > 0.2 and len(np.unique(want["entity"][hit])) > 100
     # the persistent forms
-    for bs, mb in ((128, 1), (128, 8)):
+    for bs, mb in ((128, 1), (128, 7)):
         got = hits_from_device(sc.closest(d, flags=flags, block_size=bs, min_blocks=mb, persistent=1))
         assert_hits_identical(got, osc.closest(rays, flags=flags), f"persistent {bs}x{mb}")
 
@@ -130,7 +130,7 @@ def test_tlas_anyhit_equals_entity_loop(scenes, layout):
         d = rays_to_device(r)
         want = osc.anyhit(r)
         np.testing.assert_array_equal(sc.anyhit(d).cpu().numpy(), want)
-        np.testing.assert_array_equal(sc.anyhit(d, block_size=128, min_blocks=8, persistent=1).cpu().numpy(),
+        np.testing.assert_array_equal(sc.anyhit(d, block_size=128, min_blocks=7, persistent=1).cpu().numpy(),
                                       want)
         assert 0.05 < want.mean() < 0.95
 
@@ -142,7 +142,7 @@ def test_tlas_bvh8_and_fast_equal_their_loops(scenes):
     rays = _rays(M, seed=3)
     d = rays_to_device(rays)
     strict = osc.closest(rays)
-    for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1), dict(block_size=128, min_blocks=1)):
+    for kw in (dict(), dict(block_size=128, min_blocks=7, persistent=1), dict(block_size=128, min_blocks=1)):
         for flags in (0, L.FLAG_IGNORE_TRANSPARENT):
             got = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, flags=flags, **kw))
             loop = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, flags=flags | L.FLAG_ENTITY_LOOP, **kw))
@@ -238,7 +238,7 @@ def test_tlas_exact_ties_across_entities(ctx):
     hit_dup = np.isin(want["entity"], [1, 4])
     assert hit_dup.sum() > 200 and not (want["entity"] == 4).any()    # the loop keeps entity 1
     d = rays_to_device(rays)
-    for kw in (dict(), dict(block_size=128, min_blocks=8, persistent=1)):
+    for kw in (dict(), dict(block_size=128, min_blocks=7, persistent=1)):
         got = hits_from_device(sc.closest(d, layout=L.LAYOUT_BVH8Q, **kw))
         for f in ("t", "u", "v", "w", "tri", "mesh", "entity"):
             np.testing.assert_array_equal(got[f].view(np.uint32), want[f].view(np.uint32), err_msg=f"{kw} {f}")

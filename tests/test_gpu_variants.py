@@ -14,7 +14,7 @@ from .helpers import hits_from_device, rays_to_device, single_object
 pytestmark = pytest.mark.gpu
 
 VARIANTS = [(128, 1, 0, 0), (128, 4, 0, 0), (128, 6, 0, 0), (128, 8, 0, 0), (256, 3, 0, 0), (64, 12, 0, 0),
-            (128, 1, 1, 0), (128, 8, 1, 0), (128, 8, 1, 32), (128, 8, 1, 24)]
+            (128, 1, 1, 0), (128, 7, 1, 0), (128, 7, 1, 32), (128, 7, 1, 24)]
 
 
 @pytest.mark.parametrize("layout", [R.STACK, R.STACKLESS, L.LAYOUT_BVH8Q])
@@ -36,7 +36,7 @@ def test_all_variants_identical(ctx, layout):
     with pytest.raises(R.RqError):
         sc.closest(rays, layout=layout, block_size=96, min_blocks=1)
     with pytest.raises(R.RqError):
-        sc.closest(rays, layout=layout, block_size=128, min_blocks=8, persistent=1, stack_depth=40)
+        sc.closest(rays, layout=layout, block_size=128, min_blocks=7, persistent=1, stack_depth=40)
 
 
 def test_autotune_records_choice(ctx):
@@ -72,8 +72,8 @@ def test_gi_compaction_threshold_and_tuner(ctx):
         want, st_w = sc.gi_frame(rays, gi_params(**kw, compact_below=2.0), stats=True)
         want = want.cpu().numpy()
         assert 0.2 < st_w["primary_hits"] / st_w["primary_rays"] < 0.999
-        for launch in (dict(), dict(layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=8, persistent=1),
-                       dict(layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=8, persistent=1, stack_depth=24)):
+        for launch in (dict(), dict(layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=7, persistent=1),
+                       dict(layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=7, persistent=1, stack_depth=24)):
             for cb in (2.0, 1e-30, 0.5, 0.99):
                 got, st = sc.gi_frame(rays, gi_params(**kw, compact_below=cb), stats=True, **launch)
                 np.testing.assert_array_equal(got.cpu().numpy().view(np.uint32), want.view(np.uint32))
