@@ -16,6 +16,7 @@ struct rq_batch_plan {
     int32_t variant = 0;
     int32_t depth_index = 0;  // BVH8 group-stack depth (bvh8::kStackDepths)
     int64_t total = 0;
+    int64_t total_c = -1;  // rays of the closest-hit queries when the lane-refill kernel applies, else -1
     rq::QueryDesc* d_desc = nullptr;
     unsigned long long* d_queue = nullptr;
     cudaStream_t cap = nullptr;
@@ -26,20 +27,31 @@ struct rq_batch_plan {
 namespace rq {
 namespace {
 
-// Validates queries and fills device descriptors for `family`.
+// Validates queries and fills device descriptors for `family`: the closest-hit queries first, then
+// the any-hit queries (each in the caller's order; every query writes its own outputs).  total_c:
+// the closest-hit queries' rays when the BVH8 lane-refill kernel applies (BVH8 family, no scene
+// with a top level), else -1.
 rq_status describe(rq_ctx* ctx, const rq_query* q, int32_t nq, const rq_opts* o, int family,
-                   std::vector<QueryDesc>& out, int64_t& total) {
+                   std::vector<QueryDesc>& out, int64_t& total, int64_t& total_c) {
     if (nq < 1 || nq > kMaxBatchQueries) return fail(ctx, RQ_EINVAL, "1..1024 queries per batch");
     out.assign(nq, QueryDesc{});
     total = 0;
-    for (int32_t k = 0; k < nq; ++k) {
+    total_c = 0;
+    bool plain = true;
+    std::vector<int32_t> order;
+    order.reserve(nq);
+    for (int kind = 0; kind < 2; ++kind)
+        for (int32_t k = 0; k < nq; ++k)
+            if (q[k].kind == kind || (kind == 1 && q[k].kind != 0)) order.push_back(k);
+    for (int32_t j = 0; j < nq; ++j) {
+        const int32_t k = order[j];
         const rq_query& x = q[k];
         if (!x.scene || x.scene->ctx != ctx || x.n < 0 || (x.kind != 0 && x.kind != 1) ||
             (x.n > 0 && (!x.rays || (x.kind == 0 ? !x.hits : !x.occluded))))
             return fail(ctx, RQ_EINVAL, "query " + std::to_string(k) + ": bad scene, rays or outputs");
         if (family == kFamilyBvh8 && !x.scene->bvh8)
             return fail(ctx, RQ_ENOTSUP, "query " + std::to_string(k) + ": scene has no BVH8");
-        QueryDesc& d = out[k];
+        QueryDesc& d = out[j];
         d.s = entity_view(x.scene->view, o ? o->flags : 0);
         d.rays = x.rays;
         d.hits = x.hits;
@@ -50,7 +62,10 @@ rq_status describe(rq_ctx* ctx, const rq_query* q, int32_t nq, const rq_opts* o,
         d.flags = o ? (o->flags & (RQ_FLAG_REF_COMPAT | RQ_FLAG_IGNORE_TRANSPARENT)) : 0;
         d.tie_lower = (!o || o->tie == RQ_TIE_LOWER_INDEX) ? 1 : 0;
         total += x.n;
+        if (x.kind == 0) total_c += x.n;
+        plain = plain && d.s.tlas == nullptr;
     }
+    if (family != kFamilyBvh8 || !plain) total_c = -1;
     return RQ_OK;
 }
 
@@ -69,10 +84,10 @@ rq_status capture(rq_batch_plan* p) {
     // occupancy queries happen here, before the capture starts
     RQ_CUDA(ctx, launch_batch(p->d_desc, 1, 1, p->family, p->variant, nullptr, nullptr, nullptr, p->depth_index));
     RQ_CUDA(ctx, cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned long long), p->cap);
+    cudaError_t e = cudaMemsetAsync(p->d_queue, 0, 2 * sizeof(unsigned long long), p->cap);
     if (e == cudaSuccess)
         e = launch_batch(p->d_desc, static_cast<int>(p->desc.size()), p->total, p->family, p->variant,
-                         p->d_queue, status_word(ctx), p->cap, p->depth_index);
+                         p->d_queue, status_word(ctx), p->cap, p->depth_index, p->total_c);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(p->cap, &g);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch capture");
@@ -85,7 +100,7 @@ rq_status capture(rq_batch_plan* p) {
 rq_status upload(rq_batch_plan* p) {
     rq_ctx* ctx = p->ctx;
     rq_status s = describe(ctx, p->queries.data(), static_cast<int32_t>(p->queries.size()), &p->opts,
-                           p->family, p->desc, p->total);
+                           p->family, p->desc, p->total, p->total_c);
     if (s != RQ_OK) return s;
     RQ_CUDA(ctx, cudaMemcpy(p->d_desc, p->desc.data(), sizeof(QueryDesc) * p->desc.size(),
                             cudaMemcpyHostToDevice));
@@ -104,8 +119,8 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
     if (!ctx || !queries) return fail(ctx, RQ_EINVAL, "NULL argument");
     const int family = rq::family_of(opts);
     std::vector<rq::QueryDesc> desc;
-    int64_t total = 0;
-    rq_status s = rq::describe(ctx, queries, n_queries, opts, family, desc, total);
+    int64_t total = 0, total_c = -1;
+    rq_status s = rq::describe(ctx, queries, n_queries, opts, family, desc, total, total_c);
     if (s != RQ_OK) return s;
     RQ_CUDA(ctx, cudaSetDevice(ctx->device));
     void* d = nullptr;
@@ -114,8 +129,8 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
     // Pageable source: the copy completes before the call returns, so `desc` may go out of scope.
     RQ_CUDA(ctx, cudaMemcpyAsync(d, desc.data(), sizeof(rq::QueryDesc) * desc.size(),
                                  cudaMemcpyHostToDevice, st));
-    unsigned long long* queue = rq::queue_counter(ctx, 10);
-    RQ_CUDA(ctx, cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st));
+    unsigned long long* queue = rq::queue_counter(ctx, 10);  // and counter 11 (the any-hit queue)
+    RQ_CUDA(ctx, cudaMemsetAsync(queue, 0, 2 * sizeof(unsigned long long), st));
     int variant = 0;
     if (opts && (opts->block_size || opts->min_blocks)) {
         variant = -1;
@@ -128,7 +143,7 @@ rq_status rq_batch(rq_ctx* ctx, const rq_query* queries, int32_t n_queries, cons
     int di = 0;
     if ((s = rq::depth_index_of(ctx, opts, di)) != RQ_OK) return s;
     RQ_CUDA(ctx, rq::launch_batch(static_cast<rq::QueryDesc*>(d), n_queries, total, family, variant,
-                                  queue, rq::status_word(ctx), st, di));
+                                  queue, rq::status_word(ctx), st, di, total_c));
     return RQ_OK;
 }
 
@@ -153,7 +168,7 @@ rq_status rq_batch_plan_create(rq_ctx* ctx, const rq_query* queries, int32_t n_q
         return s;
     }
     if (cudaMalloc(&p->d_desc, sizeof(rq::QueryDesc) * n_queries) != cudaSuccess ||
-        cudaMalloc(&p->d_queue, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&p->d_queue, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking) != cudaSuccess) {
         rq_batch_plan_destroy(p);
         return fail(ctx, RQ_ENOMEM, "plan device allocation failed");
@@ -208,10 +223,11 @@ rq_status rq_batch_plan_autotune(rq_batch_plan* p, int32_t allow_bvh8, rq_batch_
                 RQ_CUDA(ctx, cudaMemset(rq::status_word(ctx), 0, sizeof(unsigned)));
                 float vbest = 1e30f;
                 for (int rep = 0; rep < 4; ++rep) {
-                    RQ_CUDA(ctx, cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned long long), p->cap));
+                    RQ_CUDA(ctx, cudaMemsetAsync(p->d_queue, 0, 2 * sizeof(unsigned long long), p->cap));
                     RQ_CUDA(ctx, cudaEventRecord(a, p->cap));
                     RQ_CUDA(ctx, rq::launch_batch(p->d_desc, static_cast<int>(p->desc.size()), p->total,
-                                                  p->family, v, p->d_queue, rq::status_word(ctx), p->cap, di));
+                                                  p->family, v, p->d_queue, rq::status_word(ctx), p->cap, di,
+                                                  p->total_c));
                     RQ_CUDA(ctx, cudaEventRecord(b, p->cap));
                     RQ_CUDA(ctx, cudaEventSynchronize(b));
                     float ms = 0.0f;

@@ -400,6 +400,149 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
 }
 
 
+// Lane-refill walk of the batched BVH8 queries of one kind over scenes without a top level: the
+// batch's work items [lo, hi) (query q holds items base[q] .. base[q+1] - 1, the queries of one
+// kind contiguous), handed out from `queue` the way bvh8_persistent_loop hands out rays.  A lane
+// that takes an item finds its query by binary search over `base` and keeps the query's BVH8
+// pointers in registers.  Per ray the entity loop, the walk, the acceptance tests and the record
+// are those of bvh8_ray (the same step and finish functions), so results equal k_batch's.
+template <bool kAny, int kDepth>
+__device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd, const int64_t* base, int nq,
+                                                int64_t lo, int64_t hi, unsigned long long* queue,
+                                                unsigned& status) {
+    const int64_t n = hi - lo;
+    if (n <= 0) return;
+    const unsigned kFull = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    uint64_t stack[kDepth];
+    bvh8::Ray8 r;
+    bvh8::Hit8 h;
+    bvh8::Walk w;
+    float tmin = 0.0f, tmax = 0.0f, closest = -1.0f;
+    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = -1, visits = 0, tests = 0;
+    int32_t ents = tlas::kPlain;
+    int64_t id = -1;          // ray index within the lane's query
+    const QueryDesc* Q = qd;  // the lane's query
+    const uint4* nodes = nullptr;
+    const float4* recs = nullptr;
+    bool live = false, exhausted = false, pending = false, pending_occ = false;
+    unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
+    const unsigned long long tail_rays = static_cast<unsigned long long>(kTailPools) * kPoolRays *
+                                         (static_cast<unsigned long long>(gridDim.x) * blockDim.x / 32u);
+    // Starts the walk of entity `ent` or a later one of the lane's scene; false when none is left.
+    auto begin = [&](const float4 r0, const float4 r1) -> bool {
+        const SceneView& s = Q->s;
+        const bool skip_transparent = !kAny && (Q->flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const float3 wo = make_float3(r0.x, r0.y, r0.z), wd = make_float3(r1.x, r1.y, r1.z);
+        while ((ent = tlas::next<false>(s, ents, ent, wo, wd, kAny ? r1.w : tmax,
+                                        skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0) {
+            const rq_entity& E = s.ents[ent];
+            if (skip_transparent && strict::ent_alpha(E) < 0.99f) continue;
+            const int32_t root = s.b8_roots[ent];
+            if (root < 0) continue;
+            r = bvh8::make_ray(strict::xform(E.inverse, strict::xyz(r0), 1.0f),
+                               strict::xform(E.inverse, strict::xyz(r1), 0.0f));
+            h = bvh8::Hit8{kAny ? r1.w : tmax, -1.0f, kAny ? -1 : tri, -1};
+            w = bvh8::walk_begin(root);
+            return true;
+        }
+        return false;
+    };
+    auto store = [&](const float4 r0, const float4 r1, bool occluded) {
+        if (kAny) {
+            Q->occ[id] = occluded ? 1 : 0;
+        } else {
+            rq_hit hh;
+            bvh8_finish(Q->s, Q->flags, strict::xyz(r0), strict::xyz(r1), closest, tri, mesh, ent_hit, visits, hh);
+            store_hit(Q->hits, id, hh);
+        }
+    };
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !live && !exhausted);
+        const unsigned walking = __ballot_sync(kFull, live);
+        const bool serve = !(idle && walking && __popc(idle) < kServeBatch);
+        if (serve) {
+            if (pending) {
+                float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
+                if (!kAny) load_ray(Q->rays, id, r0, r1);
+                store(r0, r1, pending_occ);
+                pending = false;
+            }
+            while (true) {
+                const unsigned want = __ballot_sync(kFull, !live && !exhausted);
+                if (!want) break;
+                const unsigned cnt = __popc(want);
+                const unsigned rank = __popc(want & persist::lanemask_lt());
+                const unsigned long long avail = pool_end - pool_next;
+                unsigned long long mine = pool_next + rank;
+                if (avail >= cnt) {
+                    pool_next += cnt;
+                } else {
+                    const unsigned long long need = cnt - avail;
+                    const unsigned long long grab =
+                        pool_end + tail_rays >= static_cast<unsigned long long>(n) ? need : kPoolRays;
+                    unsigned long long b0 = 0;
+                    if (lane == 0) b0 = atomicAdd(queue, grab);
+                    b0 = __shfl_sync(kFull, b0, 0);
+                    if (rank >= avail) mine = b0 + (rank - avail);
+                    pool_next = b0 + need;
+                    pool_end = b0 + grab;
+                }
+                if (!live && !exhausted) {
+                    if (static_cast<int64_t>(mine) >= n) {
+                        exhausted = true;
+                    } else {
+                        const int64_t item = lo + static_cast<int64_t>(mine);
+                        int a = 0, z = nq - 1;
+                        while (a < z) {
+                            const int mid = (a + z + 1) >> 1;
+                            if (base[mid] <= item) a = mid; else z = mid - 1;
+                        }
+                        Q = qd + a;
+                        id = item - base[a];
+                        nodes = Q->s.b8_nodes;
+                        recs = Q->s.b8_tris;
+                        float4 r0, r1;
+                        load_ray(Q->rays, id, r0, r1);
+                        tmin = r0.w;
+                        tmax = r1.w;
+                        closest = -1.0f;
+                        mesh = tri = ent_hit = -1;
+                        visits = 0;
+                        ent = -1;
+                        ents = tlas::kPlain;
+                        live = (r1.w > r0.w) && begin(r0, r1);
+                        if (!live) store(r0, r1, false);
+                    }
+                }
+            }
+            if (!__any_sync(kFull, live)) break;  // every lane exhausted, every result stored
+        }
+        if (!live) continue;
+        if (bvh8::step<kAny, true, kDepth>(nodes, recs, r, tmin, h, w, stack, tests, status)) continue;
+        visits += w.visits;
+        const float T = h.closest;
+        bool done = false;
+        if (kAny) {
+            done = T > 0.0f;
+        } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
+            tmax = T;
+            closest = T;
+            mesh = h.mesh;
+            tri = h.tri;
+            ent_hit = ent;
+        }
+        if (!done) {
+            float4 r0, r1;
+            load_ray(Q->rays, id, r0, r1);
+            if (begin(r0, r1)) continue;
+        }
+        pending = true;
+        pending_occ = done;
+        live = false;
+    }
+}
+
 // Sink of the query kernels: hit records (closest) or occlusion bytes (any hit).
 struct QuerySink {
     const SceneView& s;

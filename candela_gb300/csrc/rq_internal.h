@@ -124,7 +124,11 @@ enum BatchFamily { kFamilyBvh8 = 0, kFamilyStrict = 1, kFamilyFast = 2 };
 constexpr int kNumBatchDepths = 3;
 // One persistent launch over every query (rq_kernels.cu).  queue is zeroed by the caller.
 // depth_index selects the BVH8 family's group-stack depth.
+// total_c >= 0 (BVH8 family, no scene with a top level, the closest-hit queries' descriptors first
+// with total_c rays in all): the lane-refill kernel, which takes two queue counters (queue[0],
+// queue[1]); otherwise the one-ray-per-thread kernel (one counter).
 cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
-                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index = 0);
+                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index = 0,
+                         int64_t total_c = -1);
 
 }  // namespace rq

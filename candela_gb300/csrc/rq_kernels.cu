@@ -93,6 +93,23 @@ __global__ void __launch_bounds__(kB, kM) k_batch(const QueryDesc* __restrict__ 
     if (status) atomicOr(status_out, status);
 }
 
+// Lane-refill form of the batched BVH8 queries when no scene of the batch has a top level: the
+// closest-hit queries' rays (work items [0, total_c): the descriptors list those queries first),
+// then the any-hit queries' rays, each kind from its own ray queue (queue[0], queue[1]).  Results
+// equal k_batch's (bvh8_batch_loop).
+template <int kB, int kM, int kDepth = bvh8::kStack>
+__global__ void __launch_bounds__(kB, kM) k_batch_b8(const QueryDesc* __restrict__ qd, int nq, int64_t total_c,
+                                                     int64_t total, unsigned long long* queue,
+                                                     unsigned* status_out) {
+    __shared__ int64_t base[kMaxBatchQueries + 1];
+    for (int k = threadIdx.x; k <= nq; k += blockDim.x) base[k] = k < nq ? qd[k].base : total;
+    __syncthreads();
+    unsigned status = 0;
+    bvh8_batch_loop<false, kDepth>(qd, base, nq, 0, total_c, queue, status);
+    bvh8_batch_loop<true, kDepth>(qd, base, nq, total_c, total, queue + 1, status);
+    if (status) atomicOr(status_out, status);
+}
+
 __global__ void k_tri_fast(const int4* __restrict__ tris, int64_t n, const float4* __restrict__ verts,
                            float4* __restrict__ out) {
     const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -131,7 +148,7 @@ int non_persistent_variant(int v) {
     return best;
 }
 
-const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1, 0}, {128, 8, 1, 0}, {64, 12, 1, 0},
+const LaunchVariant kBatchVariants[kNumBatchVariants] = {{128, 1, 1, 0}, {128, 7, 1, 0}, {64, 12, 1, 0},
                                                          {256, 3, 1, 0}};
 
 namespace {
@@ -144,19 +161,36 @@ int batch_bvh8_grid(int di) {
         default: return persistent_grid(k_batch<kB, kM, kFamilyBvh8>, kB);
     }
 }
+// The lane-refill kernel's grid for depth index di.
+template <int kB, int kM>
+int batch_b8_grid(int di) {
+    switch (di) {
+        case 1: return persistent_grid(k_batch_b8<kB, kM, bvh8::kStackDepths[1]>, kB);
+        case 2: return persistent_grid(k_batch_b8<kB, kM, bvh8::kStackDepths[2]>, kB);
+        default: return persistent_grid(k_batch_b8<kB, kM>, kB);
+    }
+}
 
 template <int kB, int kM>
 cudaError_t batch_variant(const QueryDesc* d, int nq, int64_t total, int family,
-                          unsigned long long* queue, unsigned* status, cudaStream_t st, int di) {
+                          unsigned long long* queue, unsigned* status, cudaStream_t st, int di, int64_t total_c) {
+    const bool refill = family == kFamilyBvh8 && total_c >= 0;
     int g = 0;
     switch (family) {
-        case kFamilyBvh8: g = batch_bvh8_grid<kB, kM>(di); break;
+        case kFamilyBvh8: g = refill ? batch_b8_grid<kB, kM>(di) : batch_bvh8_grid<kB, kM>(di); break;
         case kFamilyFast: g = persistent_grid(k_batch<kB, kM, kFamilyFast>, kB); break;
         default: g = persistent_grid(k_batch<kB, kM, kFamilyStrict>, kB); break;
     }
     const int64_t need = (total + 31) / 32 * 32 / kB + 1;
     if (need < g) g = static_cast<int>(need);
-    if (family == kFamilyBvh8) {
+    if (refill) {
+        if (di == 1)
+            k_batch_b8<kB, kM, bvh8::kStackDepths[1]><<<g, kB, 0, st>>>(d, nq, total_c, total, queue, status);
+        else if (di == 2)
+            k_batch_b8<kB, kM, bvh8::kStackDepths[2]><<<g, kB, 0, st>>>(d, nq, total_c, total, queue, status);
+        else
+            k_batch_b8<kB, kM><<<g, kB, 0, st>>>(d, nq, total_c, total, queue, status);
+    } else if (family == kFamilyBvh8) {
         if (di == 1)
             k_batch<kB, kM, kFamilyBvh8, bvh8::kStackDepths[1]><<<g, kB, 0, st>>>(d, nq, total, queue, status);
         else if (di == 2)
@@ -173,19 +207,23 @@ cudaError_t batch_variant(const QueryDesc* d, int nq, int64_t total, int family,
 
 template <int kB, int kM>
 void batch_grids() {
-    for (int di = 0; di < kNumBatchDepths; ++di) batch_bvh8_grid<kB, kM>(di);
+    for (int di = 0; di < kNumBatchDepths; ++di) {
+        batch_bvh8_grid<kB, kM>(di);
+        batch_b8_grid<kB, kM>(di);
+    }
     persistent_grid(k_batch<kB, kM, kFamilyStrict>, kB);
     persistent_grid(k_batch<kB, kM, kFamilyFast>, kB);
 }
 }  // namespace
 
 cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int family, int variant,
-                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index) {
+                         unsigned long long* queue, unsigned* status, cudaStream_t st, int depth_index,
+                         int64_t total_c) {
     if (total <= 0 || nq <= 0) return cudaSuccess;
     const int di = (depth_index >= 0 && depth_index < kNumBatchDepths) ? depth_index : 0;
     if (!st && !queue) {  // grid-size query only (fills the occupancy cache outside stream capture)
         switch (variant) {
-            case 1: batch_grids<128, 8>(); break;
+            case 1: batch_grids<128, 7>(); break;
             case 2: batch_grids<64, 12>(); break;
             case 3: batch_grids<256, 3>(); break;
             default: batch_grids<128, 1>(); break;
@@ -193,10 +231,10 @@ cudaError_t launch_batch(const QueryDesc* d_desc, int nq, int64_t total, int fam
         return cudaGetLastError();
     }
     switch (variant) {
-        case 1: return batch_variant<128, 8>(d_desc, nq, total, family, queue, status, st, di);
-        case 2: return batch_variant<64, 12>(d_desc, nq, total, family, queue, status, st, di);
-        case 3: return batch_variant<256, 3>(d_desc, nq, total, family, queue, status, st, di);
-        default: return batch_variant<128, 1>(d_desc, nq, total, family, queue, status, st, di);
+        case 1: return batch_variant<128, 7>(d_desc, nq, total, family, queue, status, st, di, total_c);
+        case 2: return batch_variant<64, 12>(d_desc, nq, total, family, queue, status, st, di, total_c);
+        case 3: return batch_variant<256, 3>(d_desc, nq, total, family, queue, status, st, di, total_c);
+        default: return batch_variant<128, 1>(d_desc, nq, total, family, queue, status, st, di, total_c);
     }
 }
 

@@ -88,8 +88,33 @@ def test_batch_equals_per_query(ctx, layout, mode):
     _check(qs, want)
     for sc, d, kind, out in qs:
         out.zero_()
-    R.engine.batch(ctx, qs, layout=layout, mode=mode, block_size=128, min_blocks=8)
+    R.engine.batch(ctx, qs, layout=layout, mode=mode, block_size=128, min_blocks=7)
     _check(qs, want)
+    assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("kinds", ["closest", "any", "alternating"])
+def test_batch_bvh8_lane_refill_kinds(ctx, kinds):
+    """The BVH8q batch on scenes without a top level runs the closest-hit queries' rays, then the
+    any-hit queries' rays, each from its own ray queue: batches of one kind (one phase empty) and
+    alternating kinds give the per-query records, in every launch shape and group-stack depth."""
+    import torch
+    scenes = _scenes(ctx)
+    qs = []
+    for k, n in enumerate([4000, 1, 0, 30_000, 777, 12_000]):
+        kind = {"closest": 0, "any": 1}.get(kinds, k % 2)
+        rays = S.sphere_rays(max(n, 1), (-1.5, -1.5, -0.3), (1.5, 1.5, 1.0), seed=300 + k)[:n]
+        d = rays_to_device(rays) if n else torch.zeros(0, dtype=torch.uint8, device="cuda")
+        out = (torch.empty((n, 8), dtype=torch.float32, device="cuda") if kind == 0
+               else torch.empty(n, dtype=torch.uint8, device="cuda"))
+        qs.append((scenes[k % len(scenes)], d, kind, out))
+    want = _per_query(qs, layout=L.LAYOUT_BVH8Q)
+    for kw in (dict(), dict(block_size=128, min_blocks=1), dict(block_size=64, min_blocks=12),
+               dict(block_size=256, min_blocks=3, stack_depth=24), dict(block_size=128, min_blocks=7, stack_depth=32)):
+        for sc, d, kind, out in qs:
+            out.zero_()
+        R.engine.batch(ctx, qs, layout=L.LAYOUT_BVH8Q, **kw)
+        _check(qs, want)
     assert ctx.device_status() == 0
 
 
@@ -112,7 +137,7 @@ def test_batch_plan_graph_and_autotune(ctx):
     for depth in (48, 32, 24):
         for sc, d, kind, out in qs:
             out.zero_()
-        R.engine.batch(ctx, qs, layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=8, stack_depth=depth)
+        R.engine.batch(ctx, qs, layout=L.LAYOUT_BVH8Q, block_size=128, min_blocks=7, stack_depth=depth)
         _check(qs, want)
     for sc, d, kind, out in qs:
         out.zero_()

@@ -193,6 +193,17 @@ def test_tlas_gi_frame_and_batch(scenes, ctx):
             assert_hits_identical(hits_from_device(out), osc.closest(r), "batch")
         else:
             np.testing.assert_array_equal(out.cpu().numpy(), osc.anyhit(r))
+    # BVH8q batch over a scene with a top level (the one-ray-per-thread batch kernel): the records
+    # of per-query BVH8q calls
+    sc.build_bvh8()
+    want = [(sc.closest(dr, layout=L.LAYOUT_BVH8Q) if kind == 0 else sc.anyhit(dr, layout=L.LAYOUT_BVH8Q))
+            .cpu().numpy().copy() for _, dr, kind, _, _ in qs]
+    for q in qs:
+        q[3].zero_()
+    R.engine.batch(ctx, [q[:4] for q in qs], layout=L.LAYOUT_BVH8Q)
+    for (_, _, _, out, _), w in zip(qs, want):
+        np.testing.assert_array_equal(out.cpu().numpy().view(np.uint8), w.view(np.uint8))
+    assert ctx.device_status() == 0
 
 
 def test_tlas_rebuilt_with_entities(ctx):
