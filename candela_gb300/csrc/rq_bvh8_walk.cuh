@@ -151,6 +151,12 @@ constexpr int kServeBatch = 12;
 // 8: 0.767, 16: 0.763, always exact: 0.790.
 constexpr int kTailPools = 4;
 
+template <class Sink>
+struct OneQuery;
+template <bool kAny, int kDepth, class Src>
+__device__ __forceinline__ void bvh8_plain_queue_loop(Src& src, int64_t n, unsigned long long* queue,
+                                                      int32_t& tests, int32_t& nodes_total, unsigned& status);
+
 template <bool kAny, class Sink, bool kTlas = true, int kDepth = bvh8::kStack>
 __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const rq_ray* __restrict__ rays,
                                                      int64_t n, int flags, unsigned long long* queue,
@@ -311,106 +317,24 @@ __device__ __forceinline__ void bvh8_persistent_loop(const SceneView& s, const r
             seek = true;
         }
     } else {
-        // A lane whose ray is finished keeps its result (`pending`) until the warp serves its idle
-        // lanes: the result stores and the refills then run together, with at least kServeBatch
-        // lanes (or whenever no lane is walking), instead of for one or two lanes in every
-        // iteration.  Rays and results are the same; only when they are stored changes.
-        bool pending = false, pending_occ = false;
-        const unsigned long long tail_rays = static_cast<unsigned long long>(kTailPools) * kPoolRays *
-                                             (static_cast<unsigned long long>(gridDim.x) * blockDim.x / 32u);
-        while (true) {
-            const unsigned idle = __ballot_sync(kFull, !live && !exhausted);
-            const unsigned walking = __ballot_sync(kFull, live);
-            const bool serve = !(idle && walking && __popc(idle) < kServeBatch);
-            if (serve) {
-                if (pending) {
-                    float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
-                    if (!kAny) load_ray(rays, id, r0, r1);
-                    store(r0, r1, pending_occ);
-                    pending = false;
-                }
-                // refill idle lanes (warp-uniform loop; inactive rays are answered here)
-                while (true) {
-                    const unsigned want = __ballot_sync(kFull, !live && !exhausted);
-                    if (!want) break;
-                    const unsigned cnt = __popc(want);
-                    const unsigned rank = __popc(want & persist::lanemask_lt());
-                    const unsigned long long avail = pool_end - pool_next;
-                    unsigned long long mine = pool_next + rank;
-                    if (avail >= cnt) {
-                        pool_next += cnt;
-                    } else {
-                        // near the end of the queue a warp takes only the rays its idle lanes need
-                        const unsigned long long need = cnt - avail;
-                        const unsigned long long grab =
-                            pool_end + tail_rays >= static_cast<unsigned long long>(n) ? need : kPoolRays;
-                        unsigned long long base = 0;
-                        if (lane == 0) base = atomicAdd(queue, grab);
-                        base = __shfl_sync(kFull, base, 0);
-                        if (rank >= avail) mine = base + (rank - avail);
-                        pool_next = base + need;
-                        pool_end = base + grab;
-                    }
-                    if (!live && !exhausted) {
-                        if (static_cast<int64_t>(mine) >= n) {
-                            exhausted = true;
-                        } else {
-                            id = static_cast<int64_t>(mine);
-                            float4 r0, r1;
-                            load_ray(rays, id, r0, r1);
-                            tmin = r0.w;
-                            tmax = r1.w;
-                            closest = -1.0f;
-                            mesh = tri = ent_hit = -1;
-                            visits = 0;
-                            ent = -1;
-                            ents = tlas::begin<kTlas>(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z));
-                            live = (r1.w > r0.w) && begin(r0, r1);
-                            if (!live) store(r0, r1, false);
-                        }
-                    }
-                }
-                if (!__any_sync(kFull, live)) break;  // every lane exhausted, every result stored
-            }
-            if (!live) continue;
-            if (bvh8::step<kAny, true, kDepth>(s.b8_nodes, s.b8_tris, r, tmin, h, w, stack, tests, status)) continue;
-            // the walk of entity `ent` has ended
-            visits += w.visits;
-            const float T = h.closest;
-            bool done = false;
-            if (kAny) {
-                done = T > 0.0f;
-            } else if (T > 0.0f && (T < tmax || (T == tmax && h.tri < tri))) {
-                tmax = T;
-                closest = T;
-                mesh = h.mesh;
-                tri = h.tri;
-                ent_hit = ent;
-            }
-            if (!done) {
-                float4 r0, r1;
-                load_ray(rays, id, r0, r1);
-                if (begin(r0, r1)) continue;
-            }
-            pending = true;  // stored when the warp next serves its idle lanes
-            pending_occ = done;
-            live = false;
-        }
+        OneQuery<Sink> src{s, rays, flags, sink, -1};
+        bvh8_plain_queue_loop<kAny, kDepth>(src, n, queue, tests, nodes_total, status);
     }
 }
 
 
-// Lane-refill walk of the batched BVH8 queries of one kind over scenes without a top level: the
-// batch's work items [lo, hi) (query q holds items base[q] .. base[q+1] - 1, the queries of one
-// kind contiguous), handed out from `queue` the way bvh8_persistent_loop hands out rays.  A lane
-// that takes an item finds its query by binary search over `base` and keeps the query's BVH8
-// pointers in registers.  Per ray the entity loop, the walk, the acceptance tests and the record
-// are those of bvh8_ray (the same step and finish functions), so results equal k_batch's.
-template <bool kAny, int kDepth>
-__device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd, const int64_t* base, int nq,
-                                                int64_t lo, int64_t hi, unsigned long long* queue,
-                                                unsigned& status) {
-    const int64_t n = hi - lo;
+// The plain lane-refill loop (scenes without a top level) over a ray source: the rays of one
+// query (OneQuery) or the rays of a batch's queries of one kind (BatchQueries).  Each warp hands
+// its idle lanes rays from a warp-private pool of consecutive indices refilled kPoolRays at a time
+// from `queue` (by need near the end of the queue); each lane walks its ray's entities one node
+// per iteration.  A lane whose ray is finished keeps its result (`pending`) until the warp serves
+// its idle lanes: the result stores and the refills then run together, with at least kServeBatch
+// lanes (or whenever no lane is walking), instead of for one or two lanes in every iteration.  Per
+// ray the entity loop, the walk, the acceptance tests and the record are those of bvh8_ray, so
+// results are identical whatever the assignment of rays to lanes.
+template <bool kAny, int kDepth, class Src>
+__device__ __forceinline__ void bvh8_plain_queue_loop(Src& src, int64_t n, unsigned long long* queue,
+                                                      int32_t& tests, int32_t& nodes_total, unsigned& status) {
     if (n <= 0) return;
     const unsigned kFull = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
@@ -419,20 +343,16 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
     bvh8::Hit8 h;
     bvh8::Walk w;
     float tmin = 0.0f, tmax = 0.0f, closest = -1.0f;
-    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = -1, visits = 0, tests = 0;
+    int32_t mesh = -1, tri = -1, ent_hit = -1, ent = -1, visits = 0;
     int32_t ents = tlas::kPlain;
-    int64_t id = -1;          // ray index within the lane's query
-    const QueryDesc* Q = qd;  // the lane's query
-    const uint4* nodes = nullptr;
-    const float4* recs = nullptr;
     bool live = false, exhausted = false, pending = false, pending_occ = false;
     unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
     const unsigned long long tail_rays = static_cast<unsigned long long>(kTailPools) * kPoolRays *
                                          (static_cast<unsigned long long>(gridDim.x) * blockDim.x / 32u);
     // Starts the walk of entity `ent` or a later one of the lane's scene; false when none is left.
     auto begin = [&](const float4 r0, const float4 r1) -> bool {
-        const SceneView& s = Q->s;
-        const bool skip_transparent = !kAny && (Q->flags & RQ_FLAG_IGNORE_TRANSPARENT);
+        const SceneView& s = src.scene();
+        const bool skip_transparent = !kAny && (src.flags() & RQ_FLAG_IGNORE_TRANSPARENT);
         const float3 wo = make_float3(r0.x, r0.y, r0.z), wd = make_float3(r1.x, r1.y, r1.z);
         while ((ent = tlas::next<false>(s, ents, ent, wo, wd, kAny ? r1.w : tmax,
                                         skip_transparent ? tlas::kBvh8Opaque : tlas::kBvh8, visits)) >= 0) {
@@ -449,13 +369,8 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
         return false;
     };
     auto store = [&](const float4 r0, const float4 r1, bool occluded) {
-        if (kAny) {
-            Q->occ[id] = occluded ? 1 : 0;
-        } else {
-            rq_hit hh;
-            bvh8_finish(Q->s, Q->flags, strict::xyz(r0), strict::xyz(r1), closest, tri, mesh, ent_hit, visits, hh);
-            store_hit(Q->hits, id, hh);
-        }
+        nodes_total += visits;
+        src.template put<kAny>(r0, r1, closest, tri, mesh, ent_hit, visits, occluded);
     };
     while (true) {
         const unsigned idle = __ballot_sync(kFull, !live && !exhausted);
@@ -464,10 +379,11 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
         if (serve) {
             if (pending) {
                 float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
-                if (!kAny) load_ray(Q->rays, id, r0, r1);
+                if (!kAny) src.load(r0, r1);
                 store(r0, r1, pending_occ);
                 pending = false;
             }
+            // refill idle lanes (warp-uniform loop; inactive rays are answered here)
             while (true) {
                 const unsigned want = __ballot_sync(kFull, !live && !exhausted);
                 if (!want) break;
@@ -478,32 +394,24 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
                 if (avail >= cnt) {
                     pool_next += cnt;
                 } else {
+                    // near the end of the queue a warp takes only the rays its idle lanes need
                     const unsigned long long need = cnt - avail;
                     const unsigned long long grab =
                         pool_end + tail_rays >= static_cast<unsigned long long>(n) ? need : kPoolRays;
-                    unsigned long long b0 = 0;
-                    if (lane == 0) b0 = atomicAdd(queue, grab);
-                    b0 = __shfl_sync(kFull, b0, 0);
-                    if (rank >= avail) mine = b0 + (rank - avail);
-                    pool_next = b0 + need;
-                    pool_end = b0 + grab;
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(queue, grab);
+                    base = __shfl_sync(kFull, base, 0);
+                    if (rank >= avail) mine = base + (rank - avail);
+                    pool_next = base + need;
+                    pool_end = base + grab;
                 }
                 if (!live && !exhausted) {
                     if (static_cast<int64_t>(mine) >= n) {
                         exhausted = true;
                     } else {
-                        const int64_t item = lo + static_cast<int64_t>(mine);
-                        int a = 0, z = nq - 1;
-                        while (a < z) {
-                            const int mid = (a + z + 1) >> 1;
-                            if (base[mid] <= item) a = mid; else z = mid - 1;
-                        }
-                        Q = qd + a;
-                        id = item - base[a];
-                        nodes = Q->s.b8_nodes;
-                        recs = Q->s.b8_tris;
+                        src.take(static_cast<int64_t>(mine));
                         float4 r0, r1;
-                        load_ray(Q->rays, id, r0, r1);
+                        src.load(r0, r1);
                         tmin = r0.w;
                         tmax = r1.w;
                         closest = -1.0f;
@@ -519,7 +427,8 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
             if (!__any_sync(kFull, live)) break;  // every lane exhausted, every result stored
         }
         if (!live) continue;
-        if (bvh8::step<kAny, true, kDepth>(nodes, recs, r, tmin, h, w, stack, tests, status)) continue;
+        if (bvh8::step<kAny, true, kDepth>(src.nodes(), src.recs(), r, tmin, h, w, stack, tests, status)) continue;
+        // the walk of entity `ent` has ended
         visits += w.visits;
         const float T = h.closest;
         bool done = false;
@@ -534,13 +443,87 @@ __device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd
         }
         if (!done) {
             float4 r0, r1;
-            load_ray(Q->rays, id, r0, r1);
+            src.load(r0, r1);
             if (begin(r0, r1)) continue;
         }
-        pending = true;
+        pending = true;  // stored when the warp next serves its idle lanes
         pending_occ = done;
         live = false;
     }
+}
+
+// Ray source of one query: ray `id` of `rays`, results through `sink` (QuerySink).
+template <class Sink>
+struct OneQuery {
+    const SceneView& s;
+    const rq_ray* __restrict__ rays;
+    int flags_;
+    const Sink& sink;
+    int64_t id;
+    __device__ __forceinline__ void take(int64_t item) { id = item; }
+    __device__ __forceinline__ void load(float4& r0, float4& r1) const { load_ray(rays, id, r0, r1); }
+    __device__ __forceinline__ const SceneView& scene() const { return s; }
+    __device__ __forceinline__ int flags() const { return flags_; }
+    __device__ __forceinline__ const uint4* nodes() const { return s.b8_nodes; }
+    __device__ __forceinline__ const float4* recs() const { return s.b8_tris; }
+    template <bool kAny>
+    __device__ __forceinline__ void put(const float4 r0, const float4 r1, float closest, int32_t tri, int32_t mesh,
+                                        int32_t ent, int32_t visits, bool occluded) const {
+        sink.template put<kAny>(id, r0, r1, closest, tri, mesh, ent, visits, occluded);
+    }
+};
+
+// Ray source of a batch's queries of one kind (scenes without a top level): work items
+// [lo, lo + n) of the batch, query q holding items base[q] .. base[q + 1] - 1.  A lane that takes
+// an item finds its query by binary search and keeps the query's BVH8 pointers in registers.
+struct BatchQueries {
+    const QueryDesc* __restrict__ qd;
+    const int64_t* base;
+    int nq;
+    int64_t lo;
+    const QueryDesc* q;  // the lane's query
+    int64_t id;          // ray index within it
+    const uint4* nodes_;
+    const float4* recs_;
+    __device__ __forceinline__ void take(int64_t item) {
+        item += lo;
+        int a = 0, z = nq - 1;
+        while (a < z) {
+            const int mid = (a + z + 1) >> 1;
+            if (base[mid] <= item) a = mid; else z = mid - 1;
+        }
+        q = qd + a;
+        id = item - base[a];
+        nodes_ = q->s.b8_nodes;
+        recs_ = q->s.b8_tris;
+    }
+    __device__ __forceinline__ void load(float4& r0, float4& r1) const { load_ray(q->rays, id, r0, r1); }
+    __device__ __forceinline__ const SceneView& scene() const { return q->s; }
+    __device__ __forceinline__ int flags() const { return q->flags; }
+    __device__ __forceinline__ const uint4* nodes() const { return nodes_; }
+    __device__ __forceinline__ const float4* recs() const { return recs_; }
+    template <bool kAny>
+    __device__ __forceinline__ void put(const float4 r0, const float4 r1, float closest, int32_t tri, int32_t mesh,
+                                        int32_t ent, int32_t visits, bool occluded) const {
+        if (kAny) {
+            q->occ[id] = occluded ? 1 : 0;
+        } else {
+            rq_hit hh;
+            bvh8_finish(q->s, q->flags, strict::xyz(r0), strict::xyz(r1), closest, tri, mesh, ent, visits, hh);
+            store_hit(q->hits, id, hh);
+        }
+    }
+};
+
+// The batched BVH8 queries of one kind over scenes without a top level: work items [lo, hi) of
+// the batch from `queue`, through bvh8_plain_queue_loop (results equal k_batch's).
+template <bool kAny, int kDepth>
+__device__ __forceinline__ void bvh8_batch_loop(const QueryDesc* __restrict__ qd, const int64_t* base, int nq,
+                                                int64_t lo, int64_t hi, unsigned long long* queue,
+                                                unsigned& status) {
+    BatchQueries src{qd, base, nq, lo, qd, -1, nullptr, nullptr};
+    int32_t tests = 0, nodes_total = 0;
+    bvh8_plain_queue_loop<kAny, kDepth>(src, hi - lo, queue, tests, nodes_total, status);
 }
 
 // Sink of the query kernels: hit records (closest) or occlusion bytes (any hit).
