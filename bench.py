@@ -668,7 +668,7 @@ def instancing_record(args, ctx=None, flush=None):
     # takes the tuned variant, its primary launch the one-thread-per-ray form of the same shape
     if args.profile:
         # two BVH8q GI passes with the top level and the launch variant the autotuner picks here on
-        # GB300 (persistent ray queue, 128 threads, 8 blocks per SM): the ncu captures of the
+        # GB300 (persistent ray queue, 128 threads, 7 blocks per SM): the ncu captures of the
         # instancing row; the second k_bvh8_persistent launch is the second pass's GI rays
         launch = dict(block_size=128, min_blocks=7, persistent=1)
         st = sc.gi_frame(d, p, out=pix, layout=L.LAYOUT_BVH8Q, stats=True, stream=sptr, **launch)[1]
