@@ -10,9 +10,31 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "rq_strict.cuh"
 
 namespace rq {
+
+// Resident-grid size of a persistent kernel (SM count x resident blocks), cached per device.
+template <class K>
+int persistent_grid(K kernel, int block) {
+    static std::mutex mu;
+    static std::unordered_map<long long, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long long key = (reinterpret_cast<long long>(reinterpret_cast<const void*>(kernel)) << 6) ^ dev;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    const int g = sms * (per_sm > 0 ? per_sm : 1);
+    cache[key] = g;
+    return g;
+}
 namespace persist {
 
 using strict::f3;
