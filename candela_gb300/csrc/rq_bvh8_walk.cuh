@@ -1,5 +1,6 @@
 // BVH8 walks over a batch of rays, shared by the query kernels and the fused GI kernels:
-// one ray per thread (bvh8_ray) or a persistent ray queue (bvh8_persistent_loop), with the
+// one ray per thread (bvh8_ray) or a persistent ray queue (bvh8_persistent_loop; its plain form,
+// bvh8_plain_queue_loop, also runs the batched queries through a per-lane ray source), with the
 // reference's entity loop (IntersectScene, TraverseBVHStack.glsl:327-366) around the walk.
 #pragma once
 #include <cuda_runtime.h>
@@ -143,7 +144,9 @@ constexpr int kPoolRays = 64;
 // Idle lanes a warp gathers before it stores their results and refills them while other lanes
 // are still walking.  Measured on the C2 secondary closest-hit launch (8.3M slots, 128 x 8
 // persistent): 1 (serve at once) 0.831 ms, 4: 0.823, 8: 0.791, 12: 0.777, 16: 0.780, 20: 0.789,
-// 24: 0.829, 32 (only when no lane walks) 1.26.
+// 24: 0.829, 32 (only when no lane walks) 1.26; at 128 x 7 (GI pass) 8: 1.001, 12: 0.989, 16:
+// 0.993, 20: 1.009 ms.  The top-level branch refills every iteration: serving there measured
+// slower.
 constexpr int kServeBatch = 12;
 // Guided hand-out: once fewer than kTailPools x kPoolRays x (warps of the grid) rays remain past a
 // warp's last pool, the warp takes only the rays its idle lanes need, so that the warps run out of
