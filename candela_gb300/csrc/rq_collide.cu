@@ -169,8 +169,11 @@ __device__ __forceinline__ int collide_stackless_step(const SceneView& s, Collid
 // tests are those of the shader's loops, so the records are those of one thread per box walking to
 // its end (measured against that form on C2's 1M boxes: the same records, stack layout 3.17 ->
 // 0.65 ms, stackless 1.49 -> 0.50 ms); only the assignment of boxes to lanes changes.
+// Occupancy target: 7 blocks per SM for the stack walk (72 registers; its 64-entry stack state
+// spilled at 8 blocks: 0.651 -> 0.596 ms on C2's 1M boxes), 8 for the pointer walk (0.498 ms; 7
+// blocks: 0.502, 6: 0.552).
 template <bool kStackless>
-__global__ void __launch_bounds__(128, 8) k_collide_queue(SceneView s, const float4* __restrict__ boxes, int64_t n,
+__global__ void __launch_bounds__(128, kStackless ? 8 : 7) k_collide_queue(SceneView s, const float4* __restrict__ boxes, int64_t n,
                                                           int4* __restrict__ out, int flags,
                                                           unsigned long long* queue) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
